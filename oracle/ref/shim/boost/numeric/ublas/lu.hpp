@@ -1,0 +1,2 @@
+// Forwarding header of the project-written uBLAS stand-in.
+#include "ublas_shim.hpp"
