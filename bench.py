@@ -1,0 +1,267 @@
+"""Benchmark of the GB300 implicit prism step.
+
+Workload: the 320k-prism sheet (200 x 200 cell grid, 4 layers, 202005 nodes,
+606015 DOF, E log-normal, internal viscosity 100 Pa s, Gaussian growth bump),
+one implicit time step of 60 s per bench step.
+
+Reported (one JSON line on rank 0):
+  value        prism K+f assemblies/s: prisms x assemblies / device time of
+               the assemblies, measured inside the timed Newton steps
+  ms_per_step  Newton-step device time (the whole updateStepNR: growth,
+               viscosity surfaces, every assembly and linear solve)
+  e2e          the same metric through the C ABI from host buffers: per step
+               tf_set_state (H2D of uk, un), tf_assemble, tf_get_residual (D2H)
+  roofline     element kernel: algorithmic bytes / kernel time vs measured HBM
+  cpu_baseline the reference's algorithm (oracle port, literal 3^6 tangent),
+               all host threads, on a bounded sample of prisms
+
+`--impl reference` times the CPU implementation alone on the same metric.
+Inputs (~1.3 GB of device data per assembly) exceed the 129 MB L2, so no
+flush is needed between timed iterations.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MEASURED = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+
+
+def peaks():
+    try:
+        with open(MEASURED) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index=0):
+        self.p = None
+        self.path = os.path.join("/tmp", f"tf_clocks_{os.getpid()}.csv")
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(nn, ne, nnz):
+    """Minimal unique traffic of one K+f assembly: per prism 6 int32 node ids,
+    18 FP64 reference coordinates, 9 FP64 InvFg, 3 FP64 material values and 36
+    int32 slot offsets (408 B); per node uk and un (48 B) and g (24 B); K
+    written once (8 B per nonzero)."""
+    return 408 * ne + 48 * nn + 24 * nn + 8 * nnz
+
+
+def cpu_sample(t, seconds_target=15.0, literal=True):
+    """The reference's algorithm on the host: element loop + serial scatter on
+    a bounded sample of prisms; returns (prisms/s, sample, threads)."""
+    from oracle.oracle import CLOSED, LITERAL, Port
+
+    p = Port(t)
+    uk, un = t.pos + 0.01, t.pos
+    mode = LITERAL if literal else CLOSED
+    n = 256
+    p.assemble_sample(uk, un, t.dt, 64, mode)   # warm-up
+    t0 = time.perf_counter()
+    p.assemble_sample(uk, un, t.dt, n, mode)
+    dt = time.perf_counter() - t0
+    rate = n / dt
+    n = int(min(t.n_elems, max(256, rate * seconds_target)))
+    t0 = time.perf_counter()
+    p.assemble_sample(uk, un, t.dt, n, mode)
+    dt = time.perf_counter() - t0
+    p.close()
+    return n / dt, n, dt, Port.threads()
+
+
+def run_reference(args, t):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle.oracle import Port
+
+    Port.set_threads(os.cpu_count() or 1)
+    rates = []
+    for _ in range(args.warmup):
+        cpu_sample(t, seconds_target=2.0)
+    samples = []
+    for _ in range(args.steps):
+        r, n, dt, th = cpu_sample(t, seconds_target=args.ref_seconds)
+        rates.append(r)
+        samples.append(n)
+    value = statistics.median(rates)
+    line = {
+        "impl": "reference", "metric": "prism K+f assemblies/s", "value": value, "unit": "prisms/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": t.name, "prisms": t.n_elems, "nodes": t.n_nodes, "dof": 3 * t.n_nodes,
+                   "l2": "inputs larger than L2"},
+        "ms_per_step": t.n_elems / value * 1e3,
+        "cpu_baseline": {"value": value, "unit": "prisms/s", "cores": Port.threads(), "kind": "port",
+                         "sample": f"element loop (literal 3^6 tangent, the reference's algorithm) + serial "
+                                   f"scatter over the first {samples[-1]} of {t.n_elems} prisms"},
+        "e2e": {"value": value, "unit": "prisms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args, t):
+    from tissuefolding_paperversion_gb300 import api
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        dist.init_process_group("gloo")
+    s = api.Solver(t, device=local if world > 1 else 0)
+    s.set_growth_rates(t.rates)
+    nn, ne, nnzb = s.sizes()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        s.newton_step(t.dt)
+    barrier()
+    l0 = s.launch_count()
+    clocks = Clocks(local)
+    w0 = time.perf_counter()
+    stats = [s.newton_step(t.dt) for _ in range(args.steps)]
+    wall = time.perf_counter() - w0
+    clk = clocks.stop()
+    launches = s.launch_count() - l0
+    ms_steps = [x["ms_total"] for x in stats]
+    ms_asm = sum(x["ms_assemble"] for x in stats)
+    n_asm = sum(x["iters"] for x in stats)
+    step_ms = sum(ms_steps) / len(ms_steps)
+    asm_rate = ne * n_asm / (ms_asm / 1e3)
+    if dist is not None:
+        import torch
+
+        v = torch.tensor([step_ms, ms_asm / n_asm], dtype=torch.float64)
+        dist.all_reduce(v, op=dist.ReduceOp.MAX)
+        step_ms, per_asm = float(v[0]), float(v[1])
+        asm_rate = ne * world / (per_asm / 1e3)
+
+    # element-kernel roofline (back-to-back assemblies at the converged state)
+    per_asm_ms, elem_ms = s.time_assembly(max(3, args.steps))
+    ia, ja, a = s.export_csr(0.0)
+    nnz = int(ia[-1])
+    alg = algorithmic_bytes(nn, ne, nnz)
+    hbm, how = peaks()
+    achieved = alg / (elem_ms / 1e3) / 1e9
+
+    # e2e through the C ABI with host buffers
+    uk = s.positions()
+    un = uk - 1e-3
+    for _ in range(2):
+        s.set_state(uk, un, t.dt)
+        s.assemble()
+        s.residual()
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        s.set_state(uk, un, t.dt)
+        s.assemble()
+        g = s.residual()
+    e2e_s = (time.perf_counter() - e0) / args.steps
+    s.close()
+
+    if rank != 0:
+        return
+    line = {
+        "metric": "prism K+f assemblies/s", "value": asm_rate, "unit": "prisms/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": t.name, "prisms": ne, "nodes": nn, "dof": 3 * nn, "block_nonzeros": nnzb,
+                   "dt_s": t.dt, "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single"},
+        "newton": {"ms_per_step": step_ms, "assemblies_per_step": n_asm / len(stats),
+                   "krylov_iters_per_step": sum(x["krylov_total"] for x in stats) / len(stats),
+                   "ms_assembly": ms_asm / n_asm, "wall_s": wall},
+        "e2e": {"value": ne / e2e_s, "unit": "prisms/s", "h2d_bytes_per_step": 2 * 8 * 3 * nn,
+                "d2h_bytes_per_step": 8 * 3 * nn},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "peak_source": how, "kernel": "k_element", "ms_per_launch": elem_ms,
+                     "algorithmic_bytes": alg},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        r, n, dt, th = cpu_sample(t, seconds_target=args.ref_seconds)
+        line["cpu_baseline"] = {"value": r, "unit": "prisms/s", "cores": th, "kind": "port",
+                                "sample": f"element loop (literal 3^6 tangent) + serial scatter over "
+                                          f"{n} of {ne} prisms, {dt:.1f} s"}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="large", choices=["large", "small"])
+    ap.add_argument("--ref-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    from tissuefolding_paperversion_gb300 import mesh
+
+    t = mesh.config_large(seed=0) if args.config == "large" else mesh.config_small(seed=0)
+    if args.impl == "reference":
+        run_reference(args, t)
+    else:
+        run_gpu(args, t)
+
+
+if __name__ == "__main__":
+    main()

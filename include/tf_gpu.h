@@ -1,0 +1,178 @@
+/*
+ * tf_gpu.h -- C ABI of the GB300 implicit prism time step.
+ *
+ * Drop-in for the reference's NewtonRaphsonSolver call sequence as driven by
+ * Simulation::updateStepNR (TissueFolding/TissueFolding/SourceCode/
+ * Simulation.cpp:6449-6590).  Every entry point returns a tf_status; none of
+ * them exits or throws.  Plain pointers and sizes only: host arrays are
+ * read/written in the reference's layouts (DOF index = 3*node + dim, prism
+ * nodes 0-2 basal and 3-5 apical, row-major 3x3 tensors).
+ *
+ * Citations below are relative to TissueFolding/TissueFolding/SourceCode/.
+ */
+#ifndef TF_GPU_H
+#define TF_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define TF_API __attribute__((visibility("default")))
+#else
+#define TF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum tf_status {
+    TF_OK = 0,
+    TF_NOT_CONVERGED = 1,        /* Newton hit its iteration cap; the reference prints
+                                    "did not converge" and carries on (Simulation.cpp:6568-6571) */
+    TF_KRYLOV_NOT_CONVERGED = 2, /* linear solve stopped at its iteration cap */
+    TF_KRYLOV_BREAKDOWN = 3,     /* a Krylov recurrence divided by zero / lost positivity */
+    TF_NAN_DETECTED = 4,         /* non-finite residual or update (the reference only prints) */
+    TF_BAD_INPUT = 5,            /* invalid argument, mesh or size */
+    TF_CUDA_ERROR = 6,           /* a CUDA runtime call failed; see tf_last_error() */
+    TF_NO_DEVICE = 7,            /* no usable GB300 device */
+    TF_OUT_OF_MEMORY = 8
+} tf_status;
+
+typedef struct tf_handle tf_handle;
+
+/* Mesh and node data, as the reference holds them in Simulation::Nodes /
+ * Elements after initiateSystem (Simulation.cpp:546-715). */
+typedef struct tf_mesh {
+    int32_t n_nodes;
+    int32_t n_elems;
+    const double* node_pos;        /* [3*n_nodes] reference (initial) positions, Node::Position */
+    const int32_t* conn;           /* [6*n_elems] prism node ids, ShapeBase::NodeIds */
+    const uint8_t* fixed;          /* [3*n_nodes] Node::FixedPos */
+    const double* ext_visc;        /* [3*n_nodes] Node::externalViscosity */
+    const int32_t* node_placement; /* [n_nodes] Node::tissuePlacement (0 basal, 1 apical, 2 mid) */
+} tf_mesh;
+
+/* Per-element material, Prism::setElasticProperties (Prism.cpp:491-516) and
+ * ShapeBase::setViscosity (ShapeBase.cpp:871-873). */
+typedef struct tf_material {
+    const double* E;   /* [n_elems] Young's modulus */
+    const double* nu;  /* [n_elems] Poisson ratio (clamped to [0, 0.5] as the reference does) */
+    const double* eta; /* [n_elems] internal viscosity */
+} tf_material;
+
+/* Solver controls.  Zero-initialised fields take the defaults shown. */
+typedef struct tf_options {
+    double newton_tol;    /* 1e-8: |du|_2 threshold, NewtonRaphsonSolver.cpp:17 */
+    int32_t newton_max_iter; /* 20: Simulation.cpp:6451 (the loop allows max_iter+1 solves) */
+    double krylov_rtol;   /* 1e-10: relative residual of each linear solve */
+    int32_t krylov_max_iter; /* 20000 */
+    int32_t krylov_method;   /* 0 auto (CG when every eta is 0, else BiCGStab), 1 CG, 2 BiCGStab */
+    int32_t deterministic;   /* 1: order-fixed assembly (no atomics); 0: atomic scatter */
+    int32_t device;          /* CUDA device ordinal */
+} tf_options;
+
+/* Statistics of one time step (tf_newton_step). */
+typedef struct tf_step_stats {
+    int32_t newton_iters;       /* number of linear solves performed */
+    int32_t krylov_iters_total; /* summed over the step */
+    int32_t krylov_iters_max;
+    int32_t converged;          /* 1 if |du| <= tol before the cap */
+    double dunorm[32];          /* |du|_2 of each Newton iteration (first 32) */
+    double final_relres;        /* relative residual of the last linear solve */
+    float ms_assemble;          /* device time spent in assembly (all iterations) */
+    float ms_solve;             /* device time spent in linear solves */
+    float ms_total;             /* device time of the whole step */
+} tf_step_stats;
+
+TF_API const char* tf_status_string(tf_status s);
+/* Message of the last failure on this thread (never NULL). */
+TF_API const char* tf_last_error(void);
+
+/* Replaces `new NewtonRaphsonSolver(3, nNodes)` (Simulation.cpp:689) plus the
+ * per-element set-up of initiateSystem: reference shape-function derivatives
+ * (Prism::calculateElementShapeFunctionDerivatives, Prism.cpp:705-728),
+ * tissue placement and exposed surfaces (ShapeBase.cpp:705-770,
+ * Prism.cpp:2674-2742).  Builds the block sparsity pattern and the
+ * element-slot -> block map once.  `opts` may be NULL. */
+TF_API tf_status tf_create(const tf_mesh* mesh, const tf_material* mat, const tf_options* opts, tf_handle** out);
+/* Replaces `delete NRSolver` (Simulation.cpp:93). */
+TF_API tf_status tf_destroy(tf_handle* h);
+
+/* Node positions (Node::Position), host <-> device. */
+TF_API tf_status tf_set_positions(tf_handle* h, const double* pos);
+TF_API tf_status tf_get_positions(tf_handle* h, double* pos);
+/* Growth tensors (ShapeBase::setFg, ShapeBase.cpp:858-868): Fg[9*n_elems]. */
+TF_API tf_status tf_set_Fg(tf_handle* h, const double* Fg);
+TF_API tf_status tf_get_Fg(tf_handle* h, double* Fg, double* invFg);
+/* Per-element growth rates in 1/s, [3*n_elems] (x, y, z), applied at each
+ * tf_begin_step as ShapeBase::calculateFgFromRates + growShapeByFg
+ * (ShapeBase.cpp:396-421, :1215-1251).  NULL clears them. */
+TF_API tf_status tf_set_growth_rates(tf_handle* h, const double* rates);
+
+/* --- the NewtonRaphsonSolver call sequence ------------------------------ */
+
+/* Start of a time step: growth update (if rates are set), node viscosity
+ * surfaces (Simulation::updateNodeViscositySurfaces :7563-7581), then
+ * setMatricesToZeroAtTheBeginningOfIteration + constructUnMatrix +
+ * initialteUkMatrix (NewtonRaphsonSolver.cpp:102-146). */
+TF_API tf_status tf_begin_step(tf_handle* h, double dt);
+/* One Newton assembly: calculateDisplacementMatrix, the element loop
+ * calculateForcesAndJacobianMatrixNR, writeForcesTogeAndgvInternal,
+ * writeImplicitElementalKToJacobian, calculateExternalViscousForcesForNR,
+ * addImplicitKViscousExternalToJacobian, calculateSumOfInternalForces,
+ * addExernalForces and calcutateFixedK (NewtonRaphsonSolver.cpp:148-378). */
+TF_API tf_status tf_assemble(tf_handle* h);
+/* Adds host forces to the right-hand side after tf_assemble, at DOFs that are
+ * not fixed -- the gExt hook of addMyosinForces/addPackingForces
+ * (Simulation.cpp:6506-6540). */
+TF_API tf_status tf_add_external_forces(tf_handle* h, const double* gext);
+/* solveForDeltaU (NewtonRaphsonSolver.cpp:382-404): solves K^T du = g, the
+ * transposed system Pardiso is asked for (iparm[11] = 1, :639). */
+TF_API tf_status tf_solve(tf_handle* h, int32_t* iters, double* relres);
+/* checkConvergenceViaDeltaU + updateUkInIteration (:727-761). */
+TF_API tf_status tf_update(tf_handle* h, int32_t* converged, double* dunorm);
+/* updateNodePositionsNR at the end of the step (Simulation.cpp:6576). */
+TF_API tf_status tf_end_step(tf_handle* h);
+/* The whole of updateStepNR, device-resident: tf_begin_step, then
+ * assemble / solve / update until |du| <= tol or the iteration cap, then
+ * tf_end_step.  Returns TF_NOT_CONVERGED when the cap was hit (the state is
+ * still advanced, as in the reference). */
+TF_API tf_status tf_newton_step(tf_handle* h, double dt, tf_step_stats* stats);
+
+/* --- inspection (parity tests) ------------------------------------------ */
+
+/* gSum after the last tf_assemble (fixed DOFs zero), [3*n_nodes]. */
+TF_API tf_status tf_get_residual(tf_handle* h, double* g);
+/* deltaU of the last tf_solve, [3*n_nodes]. */
+TF_API tf_status tf_get_delta_u(tf_handle* h, double* du);
+/* Node::viscositySurface after the last tf_begin_step, [n_nodes]. */
+TF_API tf_status tf_get_viscosity_surfaces(tf_handle* h, double* area);
+TF_API tf_status tf_set_viscosity_surfaces(tf_handle* h, const double* area);
+/* Sets the Newton state directly: uk (current) and un (start of step). */
+TF_API tf_status tf_set_state(tf_handle* h, const double* uk, const double* un, double dt);
+/* The last assembled Jacobian exactly as the reference hands it to Pardiso
+ * (constructiaForPardiso, NewtonRaphsonSolver.cpp:686-707): K (not
+ * transposed), fixed rows/columns applied, entries with |v| <= drop_tol
+ * removed, 0-based CSR.  With ia == NULL only *nnz is written. */
+TF_API tf_status tf_export_csr(tf_handle* h, double drop_tol, int32_t* ia, int32_t* ja, double* a, int64_t* nnz);
+/* Per-element 18x18 elastic and viscous tangents (TriPointKe/TriPointKv,
+ * row-major, reference orientation) and 6x3 element forces
+ * (ElementalElasticSystemForces / ElementalInternalViscousSystemForces) at
+ * the current state, for elements [e0, e0+count).  Any output may be NULL. */
+TF_API tf_status tf_element_eval(tf_handle* h, int32_t e0, int32_t count, double* Ke, double* Kv, double* fe, double* fv);
+/* Sizes: nodes, elements, nonzero 3x3 blocks of the structural pattern. */
+TF_API tf_status tf_get_sizes(tf_handle* h, int64_t* n_nodes, int64_t* n_elems, int64_t* n_blocks);
+/* The CUDA stream all work of this handle runs on (a cudaStream_t). */
+TF_API void* tf_get_stream(tf_handle* h);
+/* Kernel launches issued by this handle since creation (all kernels). */
+TF_API int64_t tf_launch_count(tf_handle* h);
+/* Runs `iters` back-to-back assemblies at the current state and returns the
+ * device time per assembly and per element-kernel launch (CUDA events on the
+ * handle's stream). */
+TF_API tf_status tf_time_assembly(tf_handle* h, int32_t iters, float* ms_per_assembly, float* ms_per_element_kernel);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TF_GPU_H */

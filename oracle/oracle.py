@@ -89,6 +89,8 @@ class Port:
                                            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
             L.tfo_assemble.restype = C.c_long
             L.tfo_assemble.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_int]
+            L.tfo_assemble_sample.restype = C.c_long
+            L.tfo_assemble_sample.argtypes = [C.c_void_p, _dp, _dp, C.c_double, C.c_int, C.c_int]
             L.tfo_structure_nnz.restype = C.c_long
             L.tfo_structure_nnz.argtypes = [C.c_void_p]
             L.tfo_get_structure.argtypes = [C.c_void_p, _ip, _ip]
@@ -190,6 +192,9 @@ class Port:
 
     def assemble(self, uk, un, dt, mode=CLOSED):
         return self.lib().tfo_assemble(self.h, _f64(uk), _f64(un), dt, mode)
+
+    def assemble_sample(self, uk, un, dt, count, mode=LITERAL):
+        return self.lib().tfo_assemble_sample(self.h, _f64(uk), _f64(un), dt, mode, int(count))
 
     def structure(self):
         nnz = self.lib().tfo_structure_nnz(self.h)

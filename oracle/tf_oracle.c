@@ -728,6 +728,47 @@ long tfo_assemble(tfo_model* m, const double* uk, const double* un, double dt, i
     return m->nnz;
 }
 
+/* A bounded sample of one K+f assembly for timing: the element loop over the
+ * first `count` prisms (OpenMP) and their serial scatter into K and g in the
+ * reference's order.  Returns the number of prisms processed. */
+long tfo_assemble_sample(tfo_model* m, const double* uk, const double* un, double dt, int mode, int count) {
+    if (count > m->ne) count = m->ne;
+    const int N3 = 3 * m->nn;
+    double* vel = (double*)malloc(sizeof(double) * (size_t)N3);
+    velocity(m, uk, un, dt, vel);
+    double* Ke = (double*)malloc(sizeof(double) * 324 * (size_t)count);
+    double* Kv = (double*)malloc(sizeof(double) * 324 * (size_t)count);
+    double* fe = (double*)malloc(sizeof(double) * 18 * (size_t)count);
+    double* fv = (double*)malloc(sizeof(double) * 18 * (size_t)count);
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int e = 0; e < count; ++e)
+        element_eval(m, e, uk, vel, dt, mode, 1, &Ke[324L * e], &Kv[324L * e], &fe[18L * e], &fv[18L * e]);
+    memset(m->a, 0, sizeof(double) * (size_t)m->nnz);
+    for (int k = 0; k < N3; ++k) m->g[k] = 0.0;
+    for (int e = 0; e < count; ++e)
+        for (int a = 0; a < 6; ++a)
+            for (int d = 0; d < 3; ++d) {
+                int I = 3 * m->conn[6 * e + a] + d;
+                m->g[I] = m->g[I] + fe[18L * e + 3 * a + d] + fv[18L * e + 3 * a + d];
+            }
+    for (int pass = 0; pass < 2; ++pass)
+        for (int e = 0; e < count; ++e) {
+            if (pass == 0 && m->eta[e] == 0) continue;
+            const double* Kel = pass == 0 ? &Kv[324L * e] : &Ke[324L * e];
+            const int* c = &m->conn[6 * e];
+            for (int a = 0; a < 6; ++a)
+                for (int b = 0; b < 6; ++b) {
+                    long base = entry_index(m, c[a], c[b], 0, 0);
+                    for (int i = 0; i < 3; ++i) {
+                        long row = base + (m->ia[3 * c[a] + i] - m->ia[3 * c[a]]);
+                        for (int j = 0; j < 3; ++j) m->a[row + j] += Kel[(3 * a + i) * 18 + 3 * b + j];
+                    }
+                }
+        }
+    free(vel); free(Ke); free(Kv); free(fe); free(fv);
+    return count;
+}
+
 long tfo_structure_nnz(const tfo_model* m) { return m->nnz; }
 
 void tfo_get_structure(const tfo_model* m, int* ia, int* ja) {

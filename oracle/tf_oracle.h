@@ -64,6 +64,9 @@ void tfo_element_eval(tfo_model* m, const double* uk, const double* un, double d
  * summation order.  Returns the number of structural entries. */
 long tfo_assemble(tfo_model* m, const double* uk, const double* un, double dt, int mode);
 long tfo_structure_nnz(const tfo_model* m);
+/* Element loop over the first `count` prisms plus their serial scatter: a
+ * bounded sample of one K+f assembly, used to time the CPU baseline. */
+long tfo_assemble_sample(tfo_model* m, const double* uk, const double* un, double dt, int mode, int count);
 void tfo_get_structure(const tfo_model* m, int* ia, int* ja);
 void tfo_get_values(const tfo_model* m, double* a, double* g);
 /* The reference's value-filtered CSR of the last assembly (fixed rows and

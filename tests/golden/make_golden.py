@@ -1,0 +1,75 @@
+"""Generates the golden fixtures under tests/golden from the reference itself.
+
+Run where the reference checkout is present (it builds oracle/_ref from the
+reference's own sources with the project-written GSL/uBLAS/Pardiso
+stand-ins):
+
+    python tests/golden/make_golden.py
+
+Every fixture records the seeded inputs that produced it, so tests rebuild
+the same inputs with tissuefolding_paperversion_gb300.mesh and compare.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle.oracle import Ref  # noqa: E402
+from tissuefolding_paperversion_gb300 import mesh  # noqa: E402
+
+
+def element_fixture(name, eta, seed):
+    t = mesh.config_tiny(seed=seed, n=3, n_layers=2, eta=eta)
+    r = Ref(t)
+    assert (r.conn() == t.conn).all()
+    Fg = mesh.growth_Fg(t, seed=seed + 1)
+    r.set_Fg(Fg)
+    uk, un = mesh.perturbed_state(t, seed=seed + 2)
+    ev = r.element_eval(uk, un, t.dt)
+    r.set_positions(uk)
+    area = r.update_viscosity_surfaces()
+    ia, ja, a, g = r.assemble(uk, un, t.dt)
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), seed=seed, eta=eta, Fg=Fg, uk=uk, un=un, dt=t.dt,
+                        Ke=ev["Ke"], Kv=ev["Kv"], fe=ev["fe"], fv=ev["fv"], area=area, ia=ia, ja=ja, a=a, g=g)
+    r.close()
+
+
+def steps_fixture(name, t, n_steps, seed_note):
+    r = Ref(t)
+    assert (r.conn() == t.conn).all()
+    pos, iters, dun = [], [], []
+    t0 = time.time()
+    for s in range(n_steps):
+        out = r.step(t.dt, t.rates)
+        pos.append(r.positions())
+        iters.append(out["iters"])
+        d = np.zeros(21)
+        d[: len(out["dunorm"])] = out["dunorm"]
+        dun.append(d)
+    Fg, invFg = r.get_Fg()
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), positions=np.array(pos), iters=np.array(iters),
+                        dunorm=np.array(dun), Fg=Fg, note=seed_note)
+    r.close()
+    return time.time() - t0
+
+
+def main():
+    element_fixture("elem_tiny_elastic", 0.0, 11)
+    element_fixture("elem_tiny_viscous", 100.0, 12)
+    t = mesh.config_tiny(seed=13, n=4, n_layers=2, eta=0.0)
+    print("tiny elastic steps", steps_fixture("steps_tiny_elastic", t, 5, "config_tiny(seed=13,n=4,n_layers=2,eta=0)"))
+    t = mesh.config_tiny(seed=14, n=4, n_layers=2, eta=100.0)
+    print("tiny viscous steps", steps_fixture("steps_tiny_viscous", t, 5, "config_tiny(seed=14,n=4,n_layers=2,eta=100)"))
+    t = mesh.config_small(seed=0)
+    print("small steps", steps_fixture("steps_small", t, t.n_steps, "config_small(seed=0)"))
+
+
+if __name__ == "__main__":
+    main()

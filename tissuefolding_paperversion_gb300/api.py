@@ -1,0 +1,294 @@
+"""ctypes binding of libtfgpu.so (include/tf_gpu.h).
+
+Python is plumbing here: tests and the benchmark drive the C ABI through this
+module exactly as a C or C++ host would.  Loading fails loudly when the
+library is missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+TF_OK = 0
+TF_NOT_CONVERGED = 1
+TF_KRYLOV_NOT_CONVERGED = 2
+TF_KRYLOV_BREAKDOWN = 3
+TF_NAN_DETECTED = 4
+TF_BAD_INPUT = 5
+TF_CUDA_ERROR = 6
+TF_NO_DEVICE = 7
+TF_OUT_OF_MEMORY = 8
+
+EXPORTED = [
+    "tf_status_string", "tf_last_error", "tf_create", "tf_destroy", "tf_set_positions", "tf_get_positions",
+    "tf_set_Fg", "tf_get_Fg", "tf_set_growth_rates", "tf_begin_step", "tf_assemble", "tf_add_external_forces",
+    "tf_solve", "tf_update", "tf_end_step", "tf_newton_step", "tf_get_residual", "tf_get_delta_u",
+    "tf_get_viscosity_surfaces", "tf_set_viscosity_surfaces", "tf_set_state", "tf_export_csr",
+    "tf_element_eval", "tf_get_sizes", "tf_get_stream", "tf_launch_count", "tf_time_assembly",
+]
+
+
+class TfError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str):
+        super().__init__(f"{where}: status {status} ({msg})")
+        self.status = status
+
+
+class tf_mesh(C.Structure):
+    _fields_ = [("n_nodes", C.c_int32), ("n_elems", C.c_int32), ("node_pos", C.c_void_p), ("conn", C.c_void_p),
+                ("fixed", C.c_void_p), ("ext_visc", C.c_void_p), ("node_placement", C.c_void_p)]
+
+
+class tf_material(C.Structure):
+    _fields_ = [("E", C.c_void_p), ("nu", C.c_void_p), ("eta", C.c_void_p)]
+
+
+class tf_options(C.Structure):
+    _fields_ = [("newton_tol", C.c_double), ("newton_max_iter", C.c_int32), ("krylov_rtol", C.c_double),
+                ("krylov_max_iter", C.c_int32), ("krylov_method", C.c_int32), ("deterministic", C.c_int32),
+                ("device", C.c_int32)]
+
+
+class tf_step_stats(C.Structure):
+    _fields_ = [("newton_iters", C.c_int32), ("krylov_iters_total", C.c_int32), ("krylov_iters_max", C.c_int32),
+                ("converged", C.c_int32), ("dunorm", C.c_double * 32), ("final_relres", C.c_double),
+                ("ms_assemble", C.c_float), ("ms_solve", C.c_float), ("ms_total", C.c_float)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Loads libtfgpu.so (building it first when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing; run tissuefolding_paperversion_gb300.build.build()")
+        _build.build()
+    L = C.CDLL(path)
+    vp, dp, ip, i32, i64 = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32), C.c_int32, C.c_int64
+    L.tf_status_string.restype = C.c_char_p
+    L.tf_status_string.argtypes = [C.c_int]
+    L.tf_last_error.restype = C.c_char_p
+    L.tf_create.argtypes = [C.POINTER(tf_mesh), C.POINTER(tf_material), C.POINTER(tf_options), C.POINTER(vp)]
+    for name in ["tf_destroy", "tf_begin_step", "tf_assemble", "tf_end_step"]:
+        getattr(L, name).argtypes = [vp] if name != "tf_begin_step" else [vp, C.c_double]
+    for name in ["tf_set_positions", "tf_get_positions", "tf_set_Fg", "tf_set_growth_rates",
+                 "tf_add_external_forces", "tf_get_residual", "tf_get_delta_u", "tf_get_viscosity_surfaces",
+                 "tf_set_viscosity_surfaces"]:
+        getattr(L, name).argtypes = [vp, vp]
+    L.tf_get_Fg.argtypes = [vp, vp, vp]
+    L.tf_solve.argtypes = [vp, ip, dp]
+    L.tf_update.argtypes = [vp, ip, dp]
+    L.tf_newton_step.argtypes = [vp, C.c_double, C.POINTER(tf_step_stats)]
+    L.tf_set_state.argtypes = [vp, vp, vp, C.c_double]
+    L.tf_export_csr.argtypes = [vp, C.c_double, vp, vp, vp, C.POINTER(i64)]
+    L.tf_element_eval.argtypes = [vp, i32, i32, vp, vp, vp, vp]
+    L.tf_get_sizes.argtypes = [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]
+    L.tf_get_stream.restype = vp
+    L.tf_get_stream.argtypes = [vp]
+    L.tf_launch_count.restype = i64
+    L.tf_launch_count.argtypes = [vp]
+    L.tf_time_assembly.argtypes = [vp, i32, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    for name in ["tf_create", "tf_destroy", "tf_set_positions", "tf_get_positions", "tf_set_Fg", "tf_get_Fg",
+                 "tf_set_growth_rates", "tf_begin_step", "tf_assemble", "tf_add_external_forces", "tf_solve",
+                 "tf_update", "tf_end_step", "tf_newton_step", "tf_get_residual", "tf_get_delta_u",
+                 "tf_get_viscosity_surfaces", "tf_set_viscosity_surfaces", "tf_set_state", "tf_export_csr",
+                 "tf_element_eval", "tf_get_sizes", "tf_time_assembly"]:
+        getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class Solver:
+    """One GPU Newton solver over one tissue (a ``tf_handle``)."""
+
+    def __init__(self, tissue, newton_tol=1e-8, newton_max_iter=20, krylov_rtol=1e-10, krylov_max_iter=20000,
+                 krylov_method=0, deterministic=False, device=0):
+        self.L = load()
+        t = tissue
+        self.t = t
+        self.nn, self.ne = t.n_nodes, t.n_elems
+        self._arrays = dict(
+            pos=np.ascontiguousarray(t.pos, dtype=np.float64),
+            conn=np.ascontiguousarray(t.conn, dtype=np.int32),
+            fixed=np.ascontiguousarray(t.fixed, dtype=np.uint8),
+            ext_visc=np.ascontiguousarray(t.ext_visc, dtype=np.float64),
+            placement=np.ascontiguousarray(t.node_placement, dtype=np.int32),
+            E=np.ascontiguousarray(t.E, dtype=np.float64),
+            nu=np.ascontiguousarray(t.nu, dtype=np.float64),
+            eta=np.ascontiguousarray(t.eta, dtype=np.float64),
+        )
+        a = self._arrays
+        m = tf_mesh(self.nn, self.ne, _ptr(a["pos"]), _ptr(a["conn"]), _ptr(a["fixed"]), _ptr(a["ext_visc"]),
+                    _ptr(a["placement"]))
+        mat = tf_material(_ptr(a["E"]), _ptr(a["nu"]), _ptr(a["eta"]))
+        opt = tf_options(newton_tol, newton_max_iter, krylov_rtol, krylov_max_iter, krylov_method,
+                         1 if deterministic else 0, device)
+        h = C.c_void_p()
+        self._check(self.L.tf_create(C.byref(m), C.byref(mat), C.byref(opt), C.byref(h)), "tf_create")
+        self.h = h
+
+    # -- plumbing -----------------------------------------------------------
+    def _check(self, s, where, allow=()):
+        if s != TF_OK and s not in allow:
+            msg = self.L.tf_last_error().decode()
+            raise TfError(s, where, msg)
+        return s
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.tf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- state --------------------------------------------------------------
+    def set_positions(self, pos):
+        p = np.ascontiguousarray(pos, dtype=np.float64)
+        self._check(self.L.tf_set_positions(self.h, _ptr(p)), "tf_set_positions")
+
+    def positions(self):
+        p = np.zeros(3 * self.nn)
+        self._check(self.L.tf_get_positions(self.h, _ptr(p)), "tf_get_positions")
+        return p
+
+    def set_Fg(self, Fg):
+        f = np.ascontiguousarray(Fg, dtype=np.float64)
+        self._check(self.L.tf_set_Fg(self.h, _ptr(f)), "tf_set_Fg")
+
+    def get_Fg(self):
+        f = np.zeros(9 * self.ne)
+        i = np.zeros(9 * self.ne)
+        self._check(self.L.tf_get_Fg(self.h, _ptr(f), _ptr(i)), "tf_get_Fg")
+        return f, i
+
+    def set_growth_rates(self, rates):
+        r = None if rates is None else np.ascontiguousarray(rates, dtype=np.float64)
+        self._check(self.L.tf_set_growth_rates(self.h, _ptr(r)), "tf_set_growth_rates")
+
+    def set_state(self, uk, un, dt):
+        a = np.ascontiguousarray(uk, dtype=np.float64)
+        b = np.ascontiguousarray(un, dtype=np.float64)
+        self._check(self.L.tf_set_state(self.h, _ptr(a), _ptr(b), dt), "tf_set_state")
+
+    def set_viscosity_surfaces(self, area):
+        a = np.ascontiguousarray(area, dtype=np.float64)
+        self._check(self.L.tf_set_viscosity_surfaces(self.h, _ptr(a)), "tf_set_viscosity_surfaces")
+
+    def viscosity_surfaces(self):
+        a = np.zeros(self.nn)
+        self._check(self.L.tf_get_viscosity_surfaces(self.h, _ptr(a)), "tf_get_viscosity_surfaces")
+        return a
+
+    # -- the NewtonRaphsonSolver call sequence --------------------------------
+    def begin_step(self, dt):
+        self._check(self.L.tf_begin_step(self.h, dt), "tf_begin_step")
+
+    def assemble(self):
+        self._check(self.L.tf_assemble(self.h), "tf_assemble")
+
+    def add_external_forces(self, gext):
+        g = np.ascontiguousarray(gext, dtype=np.float64)
+        self._check(self.L.tf_add_external_forces(self.h, _ptr(g)), "tf_add_external_forces")
+
+    def solve(self, allow_not_converged=False):
+        it = C.c_int32(0)
+        rr = C.c_double(0.0)
+        allow = (TF_KRYLOV_NOT_CONVERGED,) if allow_not_converged else ()
+        s = self._check(self.L.tf_solve(self.h, C.byref(it), C.byref(rr)), "tf_solve", allow)
+        return {"status": s, "iters": it.value, "relres": rr.value}
+
+    def update(self):
+        conv = C.c_int32(0)
+        dn = C.c_double(0.0)
+        self._check(self.L.tf_update(self.h, C.byref(conv), C.byref(dn)), "tf_update")
+        return bool(conv.value), dn.value
+
+    def end_step(self):
+        self._check(self.L.tf_end_step(self.h), "tf_end_step")
+
+    def newton_step(self, dt, allow_not_converged=True):
+        st = tf_step_stats()
+        allow = (TF_NOT_CONVERGED,) if allow_not_converged else ()
+        s = self._check(self.L.tf_newton_step(self.h, dt, C.byref(st)), "tf_newton_step", allow)
+        n = st.newton_iters
+        return {"status": s, "iters": n, "dunorm": np.array(st.dunorm[: min(n, 32)]),
+                "krylov_total": st.krylov_iters_total, "krylov_max": st.krylov_iters_max,
+                "converged": bool(st.converged), "relres": st.final_relres, "ms_assemble": st.ms_assemble,
+                "ms_solve": st.ms_solve, "ms_total": st.ms_total}
+
+    # -- inspection ---------------------------------------------------------
+    def residual(self):
+        g = np.zeros(3 * self.nn)
+        self._check(self.L.tf_get_residual(self.h, _ptr(g)), "tf_get_residual")
+        return g
+
+    def delta_u(self):
+        d = np.zeros(3 * self.nn)
+        self._check(self.L.tf_get_delta_u(self.h, _ptr(d)), "tf_get_delta_u")
+        return d
+
+    def export_csr(self, drop=1e-13):
+        n = C.c_int64(0)
+        self._check(self.L.tf_export_csr(self.h, drop, None, None, None, C.byref(n)), "tf_export_csr")
+        ia = np.zeros(3 * self.nn + 1, dtype=np.int32)
+        ja = np.zeros(n.value, dtype=np.int32)
+        a = np.zeros(n.value)
+        self._check(self.L.tf_export_csr(self.h, drop, _ptr(ia), _ptr(ja), _ptr(a), C.byref(n)), "tf_export_csr")
+        return ia, ja, a
+
+    def element_eval(self, e0=0, count=None, want_k=True):
+        count = self.ne - e0 if count is None else count
+        Ke = np.zeros(324 * count) if want_k else None
+        Kv = np.zeros(324 * count) if want_k else None
+        fe = np.zeros(18 * count)
+        fv = np.zeros(18 * count)
+        self._check(self.L.tf_element_eval(self.h, e0, count, _ptr(Ke), _ptr(Kv), _ptr(fe), _ptr(fv)),
+                    "tf_element_eval")
+        r = {"fe": fe.reshape(count, 6, 3), "fv": fv.reshape(count, 6, 3)}
+        if want_k:
+            r["Ke"] = Ke.reshape(count, 18, 18)
+            r["Kv"] = Kv.reshape(count, 18, 18)
+        return r
+
+    def sizes(self):
+        a, b, c = C.c_int64(0), C.c_int64(0), C.c_int64(0)
+        self._check(self.L.tf_get_sizes(self.h, C.byref(a), C.byref(b), C.byref(c)), "tf_get_sizes")
+        return a.value, b.value, c.value
+
+    def stream(self):
+        return self.L.tf_get_stream(self.h)
+
+    def launch_count(self):
+        return int(self.L.tf_launch_count(self.h))
+
+    def time_assembly(self, iters):
+        a, b = C.c_float(0), C.c_float(0)
+        self._check(self.L.tf_time_assembly(self.h, iters, C.byref(a), C.byref(b)), "tf_time_assembly")
+        return a.value, b.value

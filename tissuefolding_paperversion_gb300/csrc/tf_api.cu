@@ -1,0 +1,769 @@
+// C ABI of the GB300 implicit prism step (declared in include/tf_gpu.h):
+// set-up of the device-resident mesh, the block-sparse pattern and the
+// element-slot map, and the host side of the NewtonRaphsonSolver call
+// sequence driven by Simulation::updateStepNR
+// (TissueFolding/TissueFolding/SourceCode/Simulation.cpp:6449-6590).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "tf_internal.cuh"
+
+namespace tf {
+
+namespace {
+thread_local std::string g_last_error = "no error";
+
+// Gauss points (eta, nu, zeta), weight 1/6 each: Prism.cpp:123-146.
+// Shape-function derivatives dN (3x6): Prism::setShapeFunctionDerivatives,
+// Prism.cpp:655-680.
+void shape_derivatives(int gp, double dN[3][6]) {
+    const double s = 1.0 / std::sqrt(3.0);
+    const double pts[6][3] = {{1.0 / 6.0, 1.0 / 6.0, s}, {2.0 / 3.0, 1.0 / 6.0, s}, {1.0 / 6.0, 2.0 / 3.0, s},
+                              {1.0 / 6.0, 1.0 / 6.0, -s}, {2.0 / 3.0, 1.0 / 6.0, -s}, {1.0 / 6.0, 2.0 / 3.0, -s}};
+    const double eta = pts[gp][0], nu = pts[gp][1], zeta = pts[gp][2];
+    const double alpha = (1 - zeta) / 2, beta = (1 + zeta) / 2, lambda = 1 - eta - nu;
+    const double d[3][6] = {{-alpha, alpha, 0, -beta, beta, 0},
+                            {-alpha, 0, alpha, -beta, 0, beta},
+                            {-lambda / 2, -eta / 2, -nu / 2, lambda / 2, eta / 2, nu / 2}};
+    std::memcpy(dN, d, sizeof(d));
+}
+
+bool inverse3(const double M[9], double inv[9], double* det_out) {
+    const double c0 = M[4] * M[8] - M[5] * M[7];
+    const double c1 = M[5] * M[6] - M[3] * M[8];
+    const double c2 = M[3] * M[7] - M[4] * M[6];
+    const double det = M[0] * c0 + M[1] * c1 + M[2] * c2;
+    *det_out = det;
+    if (det == 0.0 || !std::isfinite(det)) return false;
+    const double r = 1.0 / det;
+    inv[0] = c0 * r;
+    inv[1] = (M[2] * M[7] - M[1] * M[8]) * r;
+    inv[2] = (M[1] * M[5] - M[2] * M[4]) * r;
+    inv[3] = c1 * r;
+    inv[4] = (M[0] * M[8] - M[2] * M[6]) * r;
+    inv[5] = (M[2] * M[3] - M[0] * M[5]) * r;
+    inv[6] = c2 * r;
+    inv[7] = (M[1] * M[6] - M[0] * M[7]) * r;
+    inv[8] = (M[0] * M[4] - M[1] * M[3]) * r;
+    return true;
+}
+
+template <class T>
+tf_status dev_alloc(T** p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        set_error("device allocation of " + std::to_string(n * sizeof(T)) + " bytes failed");
+        return TF_OUT_OF_MEMORY;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+    return TF_OK;
+}
+
+template <class T>
+tf_status upload(T** p, const std::vector<T>& v) {
+    tf_status s = dev_alloc(p, v.size());
+    if (s != TF_OK) return s;
+    TF_CUDA(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return TF_OK;
+}
+
+void free_all(tf_handle* h) {
+    Device& d = h->d;
+    void* ptrs[] = {d.conn, d.gx, d.wdet, d.detdxde, d.Fg, d.invFg, d.rates, d.lam, d.mu, d.eta, d.exposure,
+                    d.aptr, d.alist, d.farea, d.fixed, d.ext_visc, d.area, d.rowptr, d.colidx, d.diag, d.rowof,
+                    d.slot, d.val, d.eblk, d.ef, d.gptr, d.glist, d.fptr, d.flist, d.uk, d.un, d.vel, d.g,
+                    d.du, d.dinv, d.r, d.p, d.z, d.q, d.rhat, d.s, d.t, d.sh, d.scal, d.part};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (d.host_scal) cudaFreeHost(d.host_scal);
+    for (auto& e : h->ev)
+        if (e) cudaEventDestroy(e);
+    if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+#define TF_TRY(expr)                       \
+    do {                                   \
+        tf_status _s = (expr);             \
+        if (_s != TF_OK) return _s;        \
+    } while (0)
+
+tf_status check_handle(tf_handle* h) {
+    if (!h) {
+        set_error("null handle");
+        return TF_BAD_INPUT;
+    }
+    TF_CUDA(cudaSetDevice(h->device));
+    return TF_OK;
+}
+
+tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat) {
+    Device& d = h->d;
+    const int nn = m->n_nodes, ne = m->n_elems;
+    d.nn = nn;
+    d.ne = ne;
+    // ---- connectivity (SoA) and placement ---------------------------------
+    h->h_conn.assign(m->conn, m->conn + 6 * (size_t)ne);
+    std::vector<int> conn_soa(6 * (size_t)ne);
+    for (int e = 0; e < ne; ++e)
+        for (int a = 0; a < 6; ++a) conn_soa[(size_t)a * ne + e] = m->conn[6 * (size_t)e + a];
+    // ShapeBase::setTissuePlacement (ShapeBase.cpp:705-770) and
+    // Prism::assignExposedSurfaceAreaIndices (Prism.cpp:2674-2742) for
+    // columnar elements: bit0 apical face exposed, bit1 basal face exposed.
+    std::vector<int> exposure(ne);
+    for (int e = 0; e < ne; ++e) {
+        bool hasA = false, hasB = false, hasL = false;
+        for (int a = 0; a < 6; ++a) {
+            int p = m->node_placement[m->conn[6 * (size_t)e + a]];
+            if (p == 1) hasA = true;
+            else if (p == 0) hasB = true;
+            else if (p == 3) hasL = true;
+        }
+        int ex = 0;
+        if (!hasL) {
+            if (hasA && hasB) ex = 3;
+            else if (hasA) ex = 1;
+            else if (hasB) ex = 2;
+        }
+        exposure[e] = ex;
+    }
+    // ---- reference geometry: dN_X per Gauss point --------------------------
+    std::vector<double> gx(18 * 6 * (size_t)ne), wdet(6 * (size_t)ne), detd(6 * (size_t)ne);
+    double dN[6][3][6];
+    for (int gp = 0; gp < 6; ++gp) shape_derivatives(gp, dN[gp]);
+    for (int e = 0; e < ne; ++e) {
+        double X[6][3];
+        for (int a = 0; a < 6; ++a)
+            for (int c = 0; c < 3; ++c) X[a][c] = m->node_pos[3 * (size_t)m->conn[6 * (size_t)e + a] + c];
+        for (int gp = 0; gp < 6; ++gp) {
+            // dX/dxi = (dN X)^T   (Prism.cpp:705-728)
+            double J[9];
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) {
+                    double acc = 0.0;
+                    for (int a = 0; a < 6; ++a) acc += dN[gp][j][a] * X[a][i];
+                    J[3 * i + j] = acc;
+                }
+            double inv[9], det;
+            if (!inverse3(J, inv, &det) || !(det > 0.0)) {
+                set_error("element " + std::to_string(e) + " has a degenerate or inverted reference shape");
+                return TF_BAD_INPUT;
+            }
+            const size_t q = 6 * (size_t)e + gp;
+            detd[q] = det;
+            wdet[q] = (1.0 / 6.0) * det;
+            for (int a = 0; a < 6; ++a)
+                for (int k = 0; k < 3; ++k) {
+                    double acc = 0.0;
+                    for (int j = 0; j < 3; ++j) acc += inv[3 * j + k] * dN[gp][j][a];
+                    gx[(size_t)(3 * a + k) * (6 * (size_t)ne) + q] = acc;
+                }
+        }
+    }
+    // ---- material (Prism::setElasticProperties, Prism.cpp:491-516) ----------
+    std::vector<double> lam(ne), mu(ne), eta(ne);
+    d.any_visc = false;
+    for (int e = 0; e < ne; ++e) {
+        double v = mat->nu[e];
+        if (v > 0.5) v = 0.5;
+        else if (v < 0.0) v = 0.0;
+        const double E = mat->E[e];
+        lam[e] = E * v / (1 + v) / (1 - 2.0 * v);
+        mu[e] = E / 2.0 / (1 + v);
+        eta[e] = mat->eta[e];
+        if (eta[e] != 0.0) d.any_visc = true;
+        if (!std::isfinite(lam[e]) || !std::isfinite(mu[e]) || !std::isfinite(eta[e])) {
+            set_error("element " + std::to_string(e) + " has non-finite material parameters (nu = 0.5 is incompressible)");
+            return TF_BAD_INPUT;
+        }
+    }
+    // ---- node adjacency -> block pattern of A ---------------------------------
+    std::vector<int> cnt(nn + 1, 0);
+    for (int e = 0; e < ne; ++e)
+        for (int a = 0; a < 6; ++a) cnt[m->conn[6 * (size_t)e + a]] += 6;
+    std::vector<int64_t> off(nn + 1, 0);
+    for (int i = 0; i < nn; ++i) off[i + 1] = off[i] + cnt[i];
+    std::vector<int> tmp(off[nn]);
+    std::vector<int64_t> fill(off.begin(), off.end() - 1);
+    for (int e = 0; e < ne; ++e)
+        for (int a = 0; a < 6; ++a) {
+            const int A = m->conn[6 * (size_t)e + a];
+            for (int b = 0; b < 6; ++b) tmp[fill[A]++] = m->conn[6 * (size_t)e + b];
+        }
+    std::vector<int> rowptr(nn + 1, 0);
+    std::vector<int> colidx;
+    colidx.reserve(off[nn] / 2);
+    for (int i = 0; i < nn; ++i) {
+        auto b = tmp.begin() + off[i], en = tmp.begin() + off[i + 1];
+        std::sort(b, en);
+        auto u = std::unique(b, en);
+        colidx.insert(colidx.end(), b, u);
+        rowptr[i + 1] = static_cast<int>(colidx.size());
+        if (colidx.size() > (size_t)INT32_MAX / 9) {
+            set_error("mesh too large for 32-bit block indices");
+            return TF_BAD_INPUT;
+        }
+    }
+    tmp.clear();
+    tmp.shrink_to_fit();
+    const int64_t nnzb = static_cast<int64_t>(colidx.size());
+    d.nnzb = nnzb;
+    std::vector<int> diag(nn), rowof(nnzb);
+    for (int i = 0; i < nn; ++i) {
+        for (int p = rowptr[i]; p < rowptr[i + 1]; ++p) rowof[p] = i;
+        auto it = std::lower_bound(colidx.begin() + rowptr[i], colidx.begin() + rowptr[i + 1], i);
+        diag[i] = static_cast<int>(it - colidx.begin());
+    }
+    auto find_block = [&](int r, int c) {
+        auto it = std::lower_bound(colidx.begin() + rowptr[r], colidx.begin() + rowptr[r + 1], c);
+        return static_cast<int>(it - colidx.begin());
+    };
+    std::vector<int> slot(36 * (size_t)ne);
+    for (int e = 0; e < ne; ++e)
+        for (int a = 0; a < 6; ++a)
+            for (int b = 0; b < 6; ++b)
+                slot[(size_t)(6 * a + b) * ne + e] = find_block(m->conn[6 * (size_t)e + a], m->conn[6 * (size_t)e + b]);
+    // ---- node -> exposed faces (viscosity surfaces) ---------------------------
+    std::vector<int> aptr(nn + 1, 0), alist;
+    {
+        std::vector<std::vector<int>> per(nn);
+        for (int e = 0; e < ne; ++e) {
+            if (exposure[e] & 1)
+                for (int a = 3; a < 6; ++a) per[m->conn[6 * (size_t)e + a]].push_back(0 * ne + e);
+            if (exposure[e] & 2)
+                for (int a = 0; a < 3; ++a) per[m->conn[6 * (size_t)e + a]].push_back(1 * ne + e);
+        }
+        for (int i = 0; i < nn; ++i) {
+            alist.insert(alist.end(), per[i].begin(), per[i].end());
+            aptr[i + 1] = static_cast<int>(alist.size());
+        }
+    }
+    // ---- uploads -----------------------------------------------------------------
+    TF_TRY(upload(&d.conn, conn_soa));
+    TF_TRY(upload(&d.gx, gx));
+    TF_TRY(upload(&d.wdet, wdet));
+    TF_TRY(upload(&d.detdxde, detd));
+    TF_TRY(upload(&d.lam, lam));
+    TF_TRY(upload(&d.mu, mu));
+    TF_TRY(upload(&d.eta, eta));
+    TF_TRY(upload(&d.exposure, exposure));
+    TF_TRY(upload(&d.aptr, aptr));
+    TF_TRY(upload(&d.alist, alist));
+    TF_TRY(dev_alloc(&d.farea, 2 * (size_t)ne));
+    h->h_fixed.assign(m->fixed, m->fixed + 3 * (size_t)nn);
+    TF_TRY(upload(&d.fixed, h->h_fixed));
+    TF_TRY(upload(&d.ext_visc, std::vector<double>(m->ext_visc, m->ext_visc + 3 * (size_t)nn)));
+    TF_TRY(dev_alloc(&d.area, nn));
+    TF_CUDA(cudaMemset(d.area, 0, sizeof(double) * (size_t)nn));
+    TF_TRY(upload(&d.rowptr, rowptr));
+    TF_TRY(upload(&d.colidx, colidx));
+    TF_TRY(upload(&d.diag, diag));
+    TF_TRY(upload(&d.rowof, rowof));
+    TF_TRY(upload(&d.slot, slot));
+    TF_TRY(dev_alloc(&d.val, 9 * (size_t)nnzb));
+    std::vector<double> ident(9 * (size_t)ne, 0.0);
+    for (int k : {0, 4, 8})
+        for (int e = 0; e < ne; ++e) ident[(size_t)k * ne + e] = 1.0;
+    TF_TRY(upload(&d.Fg, ident));
+    TF_TRY(upload(&d.invFg, ident));
+    TF_TRY(upload(&d.rates, std::vector<double>(3 * (size_t)ne, 0.0)));
+    const size_t n3 = 3 * (size_t)nn;
+    std::vector<double> pos(m->node_pos, m->node_pos + n3);
+    TF_TRY(upload(&d.uk, pos));
+    TF_TRY(upload(&d.un, pos));
+    double** vecs[] = {&d.vel, &d.g, &d.du, &d.r, &d.p, &d.z, &d.q, &d.rhat, &d.s, &d.t, &d.sh};
+    for (double** v : vecs) {
+        TF_TRY(dev_alloc(v, n3));
+        TF_CUDA(cudaMemset(*v, 0, n3 * sizeof(double)));
+    }
+    TF_TRY(dev_alloc(&d.dinv, 9 * (size_t)nn));
+    TF_TRY(dev_alloc(&d.scal, (size_t)S_COUNT + 8));
+    TF_CUDA(cudaMemset(d.scal, 0, sizeof(double) * (S_COUNT + 8)));
+    TF_TRY(dev_alloc(&d.part, 3 * (size_t)cdiv(3 * (int64_t)nn, 256) + 64));
+    TF_CUDA(cudaMallocHost(reinterpret_cast<void**>(&d.host_scal), sizeof(double) * (S_COUNT + 8)));
+    // ---- order-fixed assembly lists ----------------------------------------------
+    if (h->opt.deterministic) {
+        std::vector<int> gptr(nnzb + 1, 0), glist(36 * (size_t)ne);
+        for (int e = 0; e < ne; ++e)
+            for (int p = 0; p < 36; ++p) gptr[slot[(size_t)p * ne + e] + 1]++;
+        for (int64_t b = 0; b < nnzb; ++b) gptr[b + 1] += gptr[b];
+        std::vector<int> gf(gptr.begin(), gptr.end() - 1);
+        for (int e = 0; e < ne; ++e)
+            for (int p = 0; p < 36; ++p) glist[gf[slot[(size_t)p * ne + e]]++] = p * ne + e;
+        std::vector<int> fptr(nn + 1, 0), flist(6 * (size_t)ne);
+        for (int e = 0; e < ne; ++e)
+            for (int a = 0; a < 6; ++a) fptr[m->conn[6 * (size_t)e + a] + 1]++;
+        for (int i = 0; i < nn; ++i) fptr[i + 1] += fptr[i];
+        std::vector<int> ff(fptr.begin(), fptr.end() - 1);
+        for (int e = 0; e < ne; ++e)
+            for (int a = 0; a < 6; ++a) flist[ff[m->conn[6 * (size_t)e + a]]++] = a * ne + e;
+        TF_TRY(upload(&d.gptr, gptr));
+        TF_TRY(upload(&d.glist, glist));
+        TF_TRY(upload(&d.fptr, fptr));
+        TF_TRY(upload(&d.flist, flist));
+        TF_TRY(dev_alloc(&d.eblk, 9 * 36 * (size_t)ne));
+        TF_TRY(dev_alloc(&d.ef, 18 * (size_t)ne));
+    }
+    h->h_rowptr = std::move(rowptr);
+    h->h_colidx = std::move(colidx);
+    h->method = h->opt.krylov_method == 0 ? (d.any_visc ? 2 : 1) : h->opt.krylov_method;
+    return TF_OK;
+}
+
+tf_status validate(const tf_mesh* m, const tf_material* mat) {
+    if (!m || !mat) {
+        set_error("mesh and material are required");
+        return TF_BAD_INPUT;
+    }
+    if (m->n_nodes <= 0 || m->n_elems <= 0 || !m->node_pos || !m->conn || !m->fixed || !m->ext_visc ||
+        !m->node_placement || !mat->E || !mat->nu || !mat->eta) {
+        set_error("empty mesh or missing array");
+        return TF_BAD_INPUT;
+    }
+    if ((int64_t)m->n_nodes * 3 > INT32_MAX / 2 || (int64_t)m->n_elems * 36 > INT32_MAX) {
+        set_error("mesh exceeds the 32-bit index range of this build");
+        return TF_BAD_INPUT;
+    }
+    for (int64_t k = 0; k < 6 * (int64_t)m->n_elems; ++k)
+        if (m->conn[k] < 0 || m->conn[k] >= m->n_nodes) {
+            set_error("connectivity entry " + std::to_string(k) + " is out of range");
+            return TF_BAD_INPUT;
+        }
+    for (int64_t k = 0; k < 3 * (int64_t)m->n_nodes; ++k)
+        if (!std::isfinite(m->node_pos[k])) {
+            set_error("non-finite node position");
+            return TF_NAN_DETECTED;
+        }
+    return TF_OK;
+}
+
+tf_status sync(tf_handle* h) {
+    TF_CUDA(cudaStreamSynchronize(h->stream));
+    return TF_OK;
+}
+
+}  // namespace
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+tf_status cuda_fail(cudaError_t e, const char* what) {
+    g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return TF_CUDA_ERROR;
+}
+
+}  // namespace tf
+
+using namespace tf;
+
+extern "C" {
+
+const char* tf_status_string(tf_status s) {
+    switch (s) {
+        case TF_OK: return "ok";
+        case TF_NOT_CONVERGED: return "Newton iteration did not converge";
+        case TF_KRYLOV_NOT_CONVERGED: return "linear solve did not converge";
+        case TF_KRYLOV_BREAKDOWN: return "Krylov breakdown";
+        case TF_NAN_DETECTED: return "non-finite value detected";
+        case TF_BAD_INPUT: return "bad input";
+        case TF_CUDA_ERROR: return "CUDA error";
+        case TF_NO_DEVICE: return "no usable device";
+        case TF_OUT_OF_MEMORY: return "out of device memory";
+    }
+    return "unknown status";
+}
+
+const char* tf_last_error(void) { return g_last_error.c_str(); }
+
+tf_status tf_create(const tf_mesh* mesh, const tf_material* mat, const tf_options* opts, tf_handle** out) {
+    if (!out) {
+        set_error("null output handle");
+        return TF_BAD_INPUT;
+    }
+    *out = nullptr;
+    TF_TRY(validate(mesh, mat));
+    tf_handle* h = new tf_handle;
+    if (opts) h->opt = *opts;
+    if (h->opt.newton_tol <= 0) h->opt.newton_tol = 1e-8;
+    if (h->opt.newton_max_iter <= 0) h->opt.newton_max_iter = 20;
+    if (h->opt.krylov_rtol <= 0) h->opt.krylov_rtol = 1e-10;
+    if (h->opt.krylov_max_iter <= 0) h->opt.krylov_max_iter = 20000;
+    h->device = h->opt.device;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= h->device) {
+        cudaGetLastError();
+        delete h;
+        set_error("no CUDA device available");
+        return TF_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess || prop.major != 10 || prop.minor != 3) {
+        delete h;
+        set_error("this library is built for sm_103 (GB300) only");
+        return TF_NO_DEVICE;
+    }
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    for (auto& ev : h->ev)
+        if (e == cudaSuccess) e = cudaEventCreate(&ev);
+    if (e != cudaSuccess) {
+        tf_status s = cuda_fail(e, "stream/event creation");
+        free_all(h);
+        delete h;
+        return s;
+    }
+    tf_status s = build(h, mesh, mat);
+    if (s != TF_OK) {
+        free_all(h);
+        delete h;
+        return s;
+    }
+    *out = h;
+    return TF_OK;
+}
+
+tf_status tf_destroy(tf_handle* h) {
+    if (!h) return TF_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    free_all(h);
+    delete h;
+    return TF_OK;
+}
+
+tf_status tf_set_positions(tf_handle* h, const double* pos) {
+    TF_TRY(check_handle(h));
+    if (!pos) return set_error("null positions"), TF_BAD_INPUT;
+    TF_CUDA(cudaMemcpyAsync(h->d.uk, pos, sizeof(double) * 3 * (size_t)h->d.nn, cudaMemcpyHostToDevice, h->stream));
+    return sync(h);
+}
+
+tf_status tf_get_positions(tf_handle* h, double* pos) {
+    TF_TRY(check_handle(h));
+    if (!pos) return set_error("null positions"), TF_BAD_INPUT;
+    TF_CUDA(cudaMemcpyAsync(pos, h->d.uk, sizeof(double) * 3 * (size_t)h->d.nn, cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+tf_status tf_set_Fg(tf_handle* h, const double* Fg) {
+    TF_TRY(check_handle(h));
+    if (!Fg) return set_error("null Fg"), TF_BAD_INPUT;
+    const int ne = h->d.ne;
+    std::vector<double> f(9 * (size_t)ne), inv(9 * (size_t)ne);
+    for (int e = 0; e < ne; ++e) {
+        double M[9], I[9], det;
+        for (int k = 0; k < 9; ++k) M[k] = Fg[9 * (size_t)e + k];
+        if (!inverse3(M, I, &det)) {
+            set_error("Fg of element " + std::to_string(e) + " is singular");
+            return TF_BAD_INPUT;
+        }
+        for (int k = 0; k < 9; ++k) {
+            f[(size_t)k * ne + e] = M[k];
+            inv[(size_t)k * ne + e] = I[k];
+        }
+    }
+    TF_CUDA(cudaMemcpyAsync(h->d.Fg, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    TF_CUDA(cudaMemcpyAsync(h->d.invFg, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    return sync(h);
+}
+
+tf_status tf_get_Fg(tf_handle* h, double* Fg, double* invFg) {
+    TF_TRY(check_handle(h));
+    const int ne = h->d.ne;
+    std::vector<double> f(9 * (size_t)ne);
+    for (int which = 0; which < 2; ++which) {
+        double* out = which == 0 ? Fg : invFg;
+        if (!out) continue;
+        TF_CUDA(cudaMemcpyAsync(f.data(), which == 0 ? h->d.Fg : h->d.invFg, f.size() * sizeof(double),
+                                cudaMemcpyDeviceToHost, h->stream));
+        TF_TRY(sync(h));
+        for (int e = 0; e < ne; ++e)
+            for (int k = 0; k < 9; ++k) out[9 * (size_t)e + k] = f[(size_t)k * ne + e];
+    }
+    return TF_OK;
+}
+
+tf_status tf_set_growth_rates(tf_handle* h, const double* rates) {
+    TF_TRY(check_handle(h));
+    const int ne = h->d.ne;
+    std::vector<double> r(3 * (size_t)ne, 0.0);
+    h->have_rates = rates != nullptr;
+    if (rates)
+        for (int e = 0; e < ne; ++e)
+            for (int d = 0; d < 3; ++d) r[(size_t)d * ne + e] = rates[3 * (size_t)e + d];
+    TF_CUDA(cudaMemcpyAsync(h->d.rates, r.data(), r.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    return sync(h);
+}
+
+tf_status tf_begin_step(tf_handle* h, double dt) {
+    TF_TRY(check_handle(h));
+    if (!(dt > 0.0) || !std::isfinite(dt)) return set_error("dt must be positive"), TF_BAD_INPUT;
+    h->dt = dt;
+    if (h->have_rates) TF_TRY(launch_growth(h));
+    TF_TRY(launch_viscosity_surfaces(h));
+    TF_CUDA(cudaMemcpyAsync(h->d.un, h->d.uk, sizeof(double) * 3 * (size_t)h->d.nn, cudaMemcpyDeviceToDevice,
+                            h->stream));
+    h->assembled = false;
+    return TF_OK;
+}
+
+tf_status tf_assemble(tf_handle* h) {
+    TF_TRY(check_handle(h));
+    TF_TRY(launch_prepare(h));
+    TF_TRY(launch_element(h));
+    if (h->opt.deterministic) TF_TRY(launch_deterministic_gather(h));
+    h->assembled = true;
+    return TF_OK;
+}
+
+tf_status tf_add_external_forces(tf_handle* h, const double* gext) {
+    TF_TRY(check_handle(h));
+    if (!gext) return set_error("null forces"), TF_BAD_INPUT;
+    const size_t n3 = 3 * (size_t)h->d.nn;
+    std::vector<double> g(n3);
+    TF_CUDA(cudaMemcpyAsync(g.data(), h->d.g, n3 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TF_TRY(sync(h));
+    for (size_t k = 0; k < n3; ++k)
+        if (!h->h_fixed[k]) g[k] = g[k] + gext[k];
+    TF_CUDA(cudaMemcpyAsync(h->d.g, g.data(), n3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    return sync(h);
+}
+
+tf_status tf_solve(tf_handle* h, int32_t* iters, double* relres) {
+    TF_TRY(check_handle(h));
+    if (!h->assembled) return set_error("tf_solve called before tf_assemble"), TF_BAD_INPUT;
+    int it = 0;
+    double rr = 0.0;
+    tf_status s = krylov_solve(h, &it, &rr);
+    if (iters) *iters = it;
+    if (relres) *relres = rr;
+    return s;
+}
+
+tf_status tf_update(tf_handle* h, int32_t* converged, double* dunorm) {
+    TF_TRY(check_handle(h));
+    TF_TRY(launch_update(h));
+    double du2 = 0.0;
+    TF_CUDA(cudaMemcpyAsync(&du2, h->d.scal + S_DU2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TF_TRY(sync(h));
+    const double dn = std::sqrt(du2);
+    if (dunorm) *dunorm = dn;
+    if (converged) *converged = !(dn > h->opt.newton_tol);
+    if (!std::isfinite(dn)) return set_error("non-finite Newton update"), TF_NAN_DETECTED;
+    return TF_OK;
+}
+
+tf_status tf_end_step(tf_handle* h) {
+    TF_TRY(check_handle(h));
+    return sync(h);
+}
+
+tf_status tf_newton_step(tf_handle* h, double dt, tf_step_stats* stats) {
+    TF_TRY(check_handle(h));
+    tf_step_stats st;
+    std::memset(&st, 0, sizeof(st));
+    TF_CUDA(cudaEventRecord(h->ev[0], h->stream));
+    TF_TRY(tf_begin_step(h, dt));
+    int k = 0;
+    bool converged = false, capped = false;
+    float ms_asm = 0.f;
+    while (!converged) {
+        TF_CUDA(cudaEventRecord(h->ev[2], h->stream));
+        TF_TRY(tf_assemble(h));
+        TF_CUDA(cudaEventRecord(h->ev[3], h->stream));
+        int it = 0;
+        double rr = 0.0;
+        tf_status s = tf_solve(h, &it, &rr);
+        if (s != TF_OK && s != TF_KRYLOV_NOT_CONVERGED) return s;
+        float ms = 0.f;
+        TF_CUDA(cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]));
+        ms_asm += ms;
+        st.krylov_iters_total += it;
+        st.krylov_iters_max = std::max(st.krylov_iters_max, it);
+        st.final_relres = rr;
+        int32_t conv = 0;
+        double dn = 0.0;
+        TF_TRY(tf_update(h, &conv, &dn));
+        if (k < 32) st.dunorm[k] = dn;
+        converged = conv != 0;
+        ++k;
+        if (!converged && k > h->opt.newton_max_iter) {
+            capped = true;
+            converged = true;
+        }
+    }
+    TF_TRY(tf_end_step(h));
+    TF_CUDA(cudaEventRecord(h->ev[1], h->stream));
+    TF_TRY(sync(h));
+    float total = 0.f;
+    TF_CUDA(cudaEventElapsedTime(&total, h->ev[0], h->ev[1]));
+    st.newton_iters = k;
+    st.converged = capped ? 0 : 1;
+    st.ms_assemble = ms_asm;
+    st.ms_total = total;
+    st.ms_solve = total - ms_asm;
+    if (stats) *stats = st;
+    if (capped) {
+        set_error("Newton iteration reached its cap without |du| <= tol");
+        return TF_NOT_CONVERGED;
+    }
+    return TF_OK;
+}
+
+tf_status tf_get_residual(tf_handle* h, double* g) {
+    TF_TRY(check_handle(h));
+    if (!g) return set_error("null output"), TF_BAD_INPUT;
+    TF_CUDA(cudaMemcpyAsync(g, h->d.g, sizeof(double) * 3 * (size_t)h->d.nn, cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+tf_status tf_get_delta_u(tf_handle* h, double* du) {
+    TF_TRY(check_handle(h));
+    if (!du) return set_error("null output"), TF_BAD_INPUT;
+    TF_CUDA(cudaMemcpyAsync(du, h->d.du, sizeof(double) * 3 * (size_t)h->d.nn, cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+tf_status tf_get_viscosity_surfaces(tf_handle* h, double* area) {
+    TF_TRY(check_handle(h));
+    if (!area) return set_error("null output"), TF_BAD_INPUT;
+    TF_CUDA(cudaMemcpyAsync(area, h->d.area, sizeof(double) * (size_t)h->d.nn, cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+tf_status tf_set_viscosity_surfaces(tf_handle* h, const double* area) {
+    TF_TRY(check_handle(h));
+    if (!area) return set_error("null input"), TF_BAD_INPUT;
+    TF_CUDA(cudaMemcpyAsync(h->d.area, area, sizeof(double) * (size_t)h->d.nn, cudaMemcpyHostToDevice, h->stream));
+    return sync(h);
+}
+
+tf_status tf_set_state(tf_handle* h, const double* uk, const double* un, double dt) {
+    TF_TRY(check_handle(h));
+    if (!uk || !un || !(dt > 0.0)) return set_error("bad state"), TF_BAD_INPUT;
+    h->dt = dt;
+    const size_t n3 = 3 * (size_t)h->d.nn;
+    TF_CUDA(cudaMemcpyAsync(h->d.uk, uk, n3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    TF_CUDA(cudaMemcpyAsync(h->d.un, un, n3 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    h->assembled = false;
+    return sync(h);
+}
+
+tf_status tf_export_csr(tf_handle* h, double drop_tol, int32_t* ia, int32_t* ja, double* a, int64_t* nnz) {
+    TF_TRY(check_handle(h));
+    if (!h->assembled) return set_error("tf_export_csr called before tf_assemble"), TF_BAD_INPUT;
+    if (!nnz || (ia && (!ja || !a))) return set_error("bad output arrays"), TF_BAD_INPUT;
+    const Device& d = h->d;
+    std::vector<double> val(9 * (size_t)d.nnzb);
+    TF_CUDA(cudaMemcpyAsync(val.data(), d.val, val.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TF_TRY(sync(h));
+    const std::vector<int>& rp = h->h_rowptr;
+    const std::vector<int>& ci = h->h_colidx;
+    auto find_block = [&](int r, int c) {
+        auto it = std::lower_bound(ci.begin() + rp[r], ci.begin() + rp[r + 1], c);
+        return static_cast<int64_t>(it - ci.begin());
+    };
+    // K(3i+di, 3j+dj) = A(3j+dj, 3i+di): block (j, i) of A, entry (dj, di).
+    int64_t q = 0;
+    if (ia) ia[0] = 0;
+    for (int i = 0; i < d.nn; ++i)
+        for (int di = 0; di < 3; ++di) {
+            const int r = 3 * i + di;
+            for (int p = rp[i]; p < rp[i + 1]; ++p) {
+                const int j = ci[p];
+                const int64_t bt = find_block(j, i);
+                for (int dj = 0; dj < 3; ++dj) {
+                    const int c = 3 * j + dj;
+                    double v;
+                    if (h->h_fixed[r] || h->h_fixed[c]) v = (r == c) ? 1.0 : 0.0;
+                    else v = val[9 * bt + 3 * dj + di];
+                    if (v > drop_tol || v < -drop_tol) {
+                        if (ia) {
+                            ja[q] = c;
+                            a[q] = v;
+                        }
+                        ++q;
+                    }
+                }
+            }
+            if (ia) ia[r + 1] = static_cast<int32_t>(q);
+        }
+    *nnz = q;
+    return TF_OK;
+}
+
+tf_status tf_element_eval(tf_handle* h, int32_t e0, int32_t count, double* Ke, double* Kv, double* fe, double* fv) {
+    TF_TRY(check_handle(h));
+    if (e0 < 0 || count < 0 || (int64_t)e0 + count > h->d.ne) return set_error("element range"), TF_BAD_INPUT;
+    if (count == 0) return TF_OK;
+    // velocity of the current state, as tf_assemble computes it
+    const Device& d = h->d;
+    double *dKe = nullptr, *dKv = nullptr, *dfe = nullptr, *dfv = nullptr;
+    tf_status s = TF_OK;
+    if (Ke) s = dev_alloc(&dKe, 324 * (size_t)count);
+    if (s == TF_OK && Kv) s = dev_alloc(&dKv, 324 * (size_t)count);
+    if (s == TF_OK && fe) s = dev_alloc(&dfe, 18 * (size_t)count);
+    if (s == TF_OK && fv) s = dev_alloc(&dfv, 18 * (size_t)count);
+    if (s == TF_OK) s = launch_prepare(h);
+    if (s == TF_OK) s = launch_element_eval(h, e0, count, dKe, dKv, dfe, dfv);
+    struct Out {
+        double* dev;
+        double* host;
+        size_t n;
+    } outs[] = {{dKe, Ke, 324 * (size_t)count}, {dKv, Kv, 324 * (size_t)count},
+                {dfe, fe, 18 * (size_t)count}, {dfv, fv, 18 * (size_t)count}};
+    for (auto& o : outs)
+        if (s == TF_OK && o.dev) {
+            cudaError_t e = cudaMemcpyAsync(o.host, o.dev, o.n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+            if (e != cudaSuccess) s = cuda_fail(e, "cudaMemcpyAsync");
+        }
+    if (s == TF_OK) s = sync(h);
+    for (auto& o : outs)
+        if (o.dev) cudaFree(o.dev);
+    (void)d;
+    h->assembled = false;  // launch_prepare reset the block values
+    return s;
+}
+
+tf_status tf_get_sizes(tf_handle* h, int64_t* n_nodes, int64_t* n_elems, int64_t* n_blocks) {
+    if (!h) return set_error("null handle"), TF_BAD_INPUT;
+    if (n_nodes) *n_nodes = h->d.nn;
+    if (n_elems) *n_elems = h->d.ne;
+    if (n_blocks) *n_blocks = h->d.nnzb;
+    return TF_OK;
+}
+
+void* tf_get_stream(tf_handle* h) { return h ? reinterpret_cast<void*>(h->stream) : nullptr; }
+
+int64_t tf_launch_count(tf_handle* h) { return h ? h->launches : 0; }
+
+tf_status tf_time_assembly(tf_handle* h, int32_t iters, float* ms_per_assembly, float* ms_per_element_kernel) {
+    TF_TRY(check_handle(h));
+    if (iters <= 0) return set_error("iters must be positive"), TF_BAD_INPUT;
+    float asm_ms = 0.f, elem_ms = 0.f;
+    for (int i = 0; i < iters; ++i) {
+        TF_CUDA(cudaEventRecord(h->ev[4], h->stream));
+        TF_TRY(launch_prepare(h));
+        TF_CUDA(cudaEventRecord(h->ev[5], h->stream));
+        TF_TRY(launch_element(h));
+        TF_CUDA(cudaEventRecord(h->ev[6], h->stream));
+        if (h->opt.deterministic) TF_TRY(launch_deterministic_gather(h));
+        TF_CUDA(cudaEventRecord(h->ev[7], h->stream));
+        TF_TRY(sync(h));
+        float a = 0.f, b = 0.f;
+        TF_CUDA(cudaEventElapsedTime(&a, h->ev[4], h->ev[7]));
+        TF_CUDA(cudaEventElapsedTime(&b, h->ev[5], h->ev[6]));
+        asm_ms += a;
+        elem_ms += b;
+    }
+    h->assembled = true;
+    if (ms_per_assembly) *ms_per_assembly = asm_ms / iters;
+    if (ms_per_element_kernel) *ms_per_element_kernel = elem_ms / iters;
+    return TF_OK;
+}
+
+}  // extern "C"
