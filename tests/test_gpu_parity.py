@@ -155,6 +155,17 @@ def test_deterministic_assembly_is_bitwise_reproducible():
     assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
 
 
+def _force_scale(t):
+    """Force a unit strain produces on one element face: max E times the mean
+    squared in-plane spacing.  Element forces of nearly unstressed elements
+    are tiny, so they are compared at this scale; FP64 evaluation at
+    coordinates ~1000 um carries strain noise ~1e-13 in the reference too."""
+    p = t.pos.reshape(-1, 3)
+    c = t.conn.reshape(-1, 6)
+    h2 = np.mean(np.sum((p[c[:, 1]] - p[c[:, 0]]) ** 2, axis=1))
+    return float(np.max(t.E)) * h2
+
+
 def test_large_mesh_sampled_elements_and_residual():
     """Full-size mesh (320k prisms): size-independent checks against the oracle."""
     t = mesh.config_large(seed=0)
@@ -177,11 +188,13 @@ def test_large_mesh_sampled_elements_and_residual():
     p.set_Fg(Fg)
     p.set_viscosity_surfaces(area)
     g_cpu = p.residual(pos, un, t.dt)
-    # the residual is tiny at convergence, so compare at the scale of the
-    # element forces that cancel in it
-    fscale = np.abs(p.element_eval(pos, un, t.dt, CLOSED, 0, 2000, want_k=False)["fe"]).max()
-    assert np.abs(g_gpu - g_cpu).max() <= 1e-11 * fscale
+    fs = _force_scale(t)
+    assert np.abs(g_gpu - g_cpu).max() <= 1e-11 * fs
+    # the GPU's converged state is an equilibrium of the oracle's physics
+    assert np.abs(g_cpu).max() <= 1e-8 * fs
     for e, r in zip(sample, got):
-        ref = p.element_eval(pos, un, t.dt, CLOSED, int(e), 1)
-        for k in ("Ke", "Kv", "fe", "fv"):
+        ref = p.element_eval(pos, un, t.dt, LITERAL, int(e), 1)
+        for k in ("Ke", "Kv"):
             assert _rel(r[k], ref[k]) <= TOL_K, (e, k)
+        for k in ("fe", "fv"):
+            assert np.abs(r[k] - ref[k]).max() <= 1e-11 * fs, (e, k)

@@ -97,13 +97,17 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
             const int q = 6 * e + gp;
 #pragma unroll
             for (int k = 0; k < 18; ++k) gX[k] = __ldg(&A.gx[(size_t)k * (6 * (size_t)ne) + q]);
-            // F = sum_a x_a (x) dN_X,a
+            // F = sum_a x_a (x) dN_X,a.  The gradients sum to zero, so the
+            // positions are taken relative to node 0: that removes the
+            // cancellation of ~|x| / h between the products at coordinates far
+            // from the origin (the result is unchanged in exact arithmetic).
             double F[9];
 #pragma unroll
             for (int k = 0; k < 9; ++k) F[k] = 0.0;
+            const double o0 = A.uk[3 * nd[0]], o1 = A.uk[3 * nd[0] + 1], o2 = A.uk[3 * nd[0] + 2];
 #pragma unroll
-            for (int a = 0; a < 6; ++a) {
-                const double x0 = A.uk[3 * nd[a]], x1 = A.uk[3 * nd[a] + 1], x2 = A.uk[3 * nd[a] + 2];
+            for (int a = 1; a < 6; ++a) {
+                const double x0 = A.uk[3 * nd[a]] - o0, x1 = A.uk[3 * nd[a] + 1] - o1, x2 = A.uk[3 * nd[a] + 2] - o2;
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
                     F[j] = fma(x0, gX[3 * a + j], F[j]);
@@ -188,9 +192,10 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
                 double L[9];
 #pragma unroll
                 for (int k = 0; k < 9; ++k) L[k] = 0.0;
+                const double w0 = A.vel[3 * nd[0]], w1 = A.vel[3 * nd[0] + 1], w2 = A.vel[3 * nd[0] + 2];
 #pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    const double v0 = A.vel[3 * nd[c]], v1 = A.vel[3 * nd[c] + 1], v2 = A.vel[3 * nd[c] + 2];
+                for (int c = 1; c < 6; ++c) {
+                    const double v0 = A.vel[3 * nd[c]] - w0, v1 = A.vel[3 * nd[c] + 1] - w1, v2 = A.vel[3 * nd[c] + 2] - w2;
 #pragma unroll
                     for (int j = 0; j < 3; ++j) {
                         L[j] = fma(v0, dn[3 * c + j], L[j]);

@@ -403,7 +403,26 @@ Ctx make_ctx(tf_handle* h) {
 
 }  // namespace
 
+namespace {
+tf_status krylov_run(tf_handle* h, int method, int* iters, double* relres);
+}
+
+// Auto mode picks CG when the tangent is symmetric; CG needs a positive
+// definite operator, which large compressive growth can take away (the
+// geometric stiffness term), so a CG breakdown there falls back to
+// BiCGStab, as the reference's direct LU would not care.
 tf_status krylov_solve(tf_handle* h, int* iters, double* relres) {
+    tf_status s = krylov_run(h, h->method, iters, relres);
+    if (s == TF_KRYLOV_BREAKDOWN && h->method == 1 && h->opt.krylov_method == 0) {
+        int it2 = 0;
+        s = krylov_run(h, 2, &it2, relres);
+        *iters += it2;
+    }
+    return s;
+}
+
+namespace {
+tf_status krylov_run(tf_handle* h, int method, int* iters, double* relres) {
     Device& d = h->d;
     Ctx c = make_ctx(h);
     const int nb = cdiv(d.nn, kThreads);
@@ -414,7 +433,7 @@ tf_status krylov_solve(tf_handle* h, int* iters, double* relres) {
     const double tol = h->opt.krylov_rtol;
     const double tol2 = tol * tol;
     TF_CUDA(cudaMemcpyAsync(d.scal + S_TOL2, &tol2, sizeof(double), cudaMemcpyHostToDevice, st));
-    if (h->method == 1) {
+    if (method == 1) {
         k_cg_init<<<nb, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.z, d.p);
     } else {
         k_bi_init<<<nb, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.rhat, d.p, d.q);
@@ -426,7 +445,7 @@ tf_status krylov_solve(tf_handle* h, int* iters, double* relres) {
     while (launched < maxit) {
         const int n = chunk < maxit - launched ? chunk : maxit - launched;
         for (int it = 0; it < n; ++it) {
-            if (h->method == 1) {
+            if (method == 1) {
                 k_cg_spmv<<<nb, kThreads, 0, st>>>(c, d.p, d.q);
                 TF_LAUNCH_CHECK(h);
                 k_cg_update<<<nb, kThreads, 0, st>>>(c, d.du, d.r, d.z, d.p, d.q);
@@ -468,6 +487,7 @@ tf_status krylov_solve(tf_handle* h, int* iters, double* relres) {
     set_error("linear solve reached its iteration cap");
     return TF_KRYLOV_NOT_CONVERGED;
 }
+}  // namespace
 
 tf_status launch_update(tf_handle* h) {
     Device& d = h->d;
