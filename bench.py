@@ -244,19 +244,45 @@ def run_gpu(args, t):
     print(json.dumps(line))
 
 
+def run_assembly_only(args, t):
+    """Back-to-back assemblies at a grown state (for kernel profiling)."""
+    from tissuefolding_paperversion_gb300 import api
+
+    s = api.Solver(t)
+    s.set_growth_rates(t.rates)
+    s.begin_step(t.dt)
+    uk = t.pos + 1e-3 * np.sin(t.pos)
+    s.set_state(uk, t.pos, t.dt)
+    s.time_assembly(args.warmup)
+    per_asm, elem = s.time_assembly(args.steps)
+    print(json.dumps({"mode": "assembly", "workload": t.name, "prisms": t.n_elems, "ms_per_assembly": per_asm,
+                      "ms_element_kernel": elem, "prisms_per_s": t.n_elems / (per_asm / 1e3)}))
+    s.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="large", choices=["large", "small"])
+    ap.add_argument("--config", default="large", choices=["large", "medium", "small"])
+    ap.add_argument("--mode", default="step", choices=["step", "assembly"],
+                    help="step: Newton steps (the bench); assembly: back-to-back K+f assemblies only")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     from tissuefolding_paperversion_gb300 import mesh
 
-    t = mesh.config_large(seed=0) if args.config == "large" else mesh.config_small(seed=0)
+    if args.config == "large":
+        t = mesh.config_large(seed=0)
+    elif args.config == "medium":
+        t = mesh.config_large(seed=0, cells=130)
+    else:
+        t = mesh.config_small(seed=0)
+    if args.mode == "assembly" and args.impl == "ours":
+        run_assembly_only(args, t)
+        return
     if args.impl == "reference":
         run_reference(args, t)
     else:
