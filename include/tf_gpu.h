@@ -172,6 +172,23 @@ TF_API int64_t tf_launch_count(tf_handle* h);
  * handle's stream). */
 TF_API tf_status tf_time_assembly(tf_handle* h, int32_t iters, float* ms_per_assembly, float* ms_per_element_kernel);
 
+/* --- solve without device allocation --------------------------------------
+ * No counterpart in the reference: this is an addition for callers that may
+ * not call cudaMalloc (a host that owns every device allocation, a fixed
+ * memory budget, code that must not allocate between captured launches).
+ * Solves A x = b for a caller-owned 3x3 block-sparse matrix on the current
+ * device with block-Jacobi preconditioned BiCGStab in FP64; every pointer is
+ * a device pointer the caller owns (rowptr[n+1], colidx[nnzb], val[9*nnzb]
+ * row-major blocks, b and x [3n]).  Work space is one static device array of
+ * this library (about 4.3 MB, held by every GPU that loads it until exit),
+ * so n_block_rows is limited to 16384; larger systems return TF_BAD_INPUT.
+ * The first call on a device looks the array up and must come before any
+ * stream capture.  Calls share the array: overlapping calls race, so
+ * serialise them.  `stream` is a cudaStream_t (NULL: the default stream). */
+TF_API tf_status tf_solve_bsr_static(int32_t n_block_rows, const int32_t* rowptr, const int32_t* colidx,
+                                     const double* val, const double* b, double* x, double rtol, int32_t max_iter,
+                                     void* stream, int32_t* iters, double* relres);
+
 #ifdef __cplusplus
 }
 #endif

@@ -29,6 +29,7 @@ EXPORTED = [
     "tf_solve", "tf_update", "tf_end_step", "tf_newton_step", "tf_get_residual", "tf_get_delta_u",
     "tf_get_viscosity_surfaces", "tf_set_viscosity_surfaces", "tf_set_state", "tf_export_csr",
     "tf_element_eval", "tf_get_sizes", "tf_get_stream", "tf_launch_count", "tf_time_assembly",
+    "tf_solve_bsr_static",
 ]
 
 
@@ -101,6 +102,8 @@ def load(build_if_missing: bool = True):
     L.tf_launch_count.restype = i64
     L.tf_launch_count.argtypes = [vp]
     L.tf_time_assembly.argtypes = [vp, i32, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.tf_solve_bsr_static.restype = C.c_int
+    L.tf_solve_bsr_static.argtypes = [i32, vp, vp, vp, vp, vp, C.c_double, i32, vp, ip, dp]
     for name in ["tf_create", "tf_destroy", "tf_set_positions", "tf_get_positions", "tf_set_Fg", "tf_get_Fg",
                  "tf_set_growth_rates", "tf_begin_step", "tf_assemble", "tf_add_external_forces", "tf_solve",
                  "tf_update", "tf_end_step", "tf_newton_step", "tf_get_residual", "tf_get_delta_u",
