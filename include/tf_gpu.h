@@ -65,7 +65,8 @@ typedef struct tf_material {
 typedef struct tf_options {
     double newton_tol;    /* 1e-8: |du|_2 threshold, NewtonRaphsonSolver.cpp:17 */
     int32_t newton_max_iter; /* 20: Simulation.cpp:6451 (the loop allows max_iter+1 solves) */
-    double krylov_rtol;   /* 1e-10: relative residual of each linear solve */
+    double krylov_rtol;   /* 1e-8: relative residual of each linear solve (keeps the Newton
+                             iteration counts of an exact solve on the benchmark sheets) */
     int32_t krylov_max_iter; /* 20000 */
     int32_t krylov_method;   /* 0 auto (CG when every eta is 0, else BiCGStab), 1 CG, 2 BiCGStab */
     int32_t deterministic;   /* 1: order-fixed assembly (no atomics); 0: atomic scatter */

@@ -121,7 +121,7 @@ def _ptr(a):
 class Solver:
     """One GPU Newton solver over one tissue (a ``tf_handle``)."""
 
-    def __init__(self, tissue, newton_tol=1e-8, newton_max_iter=20, krylov_rtol=1e-10, krylov_max_iter=20000,
+    def __init__(self, tissue, newton_tol=1e-8, newton_max_iter=20, krylov_rtol=1e-8, krylov_max_iter=20000,
                  krylov_method=0, deterministic=False, device=0):
         self.L = load()
         t = tissue

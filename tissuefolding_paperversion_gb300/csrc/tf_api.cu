@@ -390,7 +390,7 @@ tf_status tf_create(const tf_mesh* mesh, const tf_material* mat, const tf_option
     if (opts) h->opt = *opts;
     if (h->opt.newton_tol <= 0) h->opt.newton_tol = 1e-8;
     if (h->opt.newton_max_iter <= 0) h->opt.newton_max_iter = 20;
-    if (h->opt.krylov_rtol <= 0) h->opt.krylov_rtol = 1e-10;
+    if (h->opt.krylov_rtol <= 0) h->opt.krylov_rtol = 1e-8;
     if (h->opt.krylov_max_iter <= 0) h->opt.krylov_max_iter = 20000;
     h->device = h->opt.device;
     int ndev = 0;

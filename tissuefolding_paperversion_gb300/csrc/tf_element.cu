@@ -9,27 +9,36 @@
 //   calculateImplicitKElastic            ShapeBase.cpp:2619-2639, :2786-2890
 //   calculateImplicitKViscous            ShapeBase.cpp:2641-2705, :2892-3053
 //   write*ToMainKatrix / ge, gv scatter  ShapeBase.cpp:2148-2180, :2707-2758
-// with two exact identities used to cut FP64 work:
+// with exact identities that cut FP64 work:
 //   * Fe C^-1 Fe^T = I, so sigma = (mu (b - I) + lambda lnJ I) / J with
 //     b = Fe Fe^T, and the 3^6 contraction of integral 1 collapses to
 //     lambda a_i b_k + (mu - lambda lnJ)(delta_ik a.b + a_k b_i);
-//   * dN_x = F^-T dN_X with dN_X = InvdXde^T dN precomputed per element.
+//   * dN_x = F^-T dN_X with dN_X = InvdXde^T dN precomputed per element;
+//   * with a = dN_a, b = dN_b, s = a.b and t = a.(sigma' b) the whole 3x3
+//     block (elastic + both viscous integrals) of one Gauss point is
+//       K_ab = u_a b^T + b w_a^T - v_b a^T + s Q + t I
+//     where per node c:  u_c = c1 dN_c + sigma_v' dN_c,
+//                        w_c = c2 dN_c + P^T dN_c,   v_c = sigma_v' dN_c,
+//     and Q = c2 I + P, P = 0.5 eta w dV (I/dt - grad v) (primes: times
+//     w dV).  That is 45 FP64 FMAs per block and Gauss point instead of 64;
+//     without viscosity K_ab = K_ba^T and only the 21 pairs a <= b are
+//     formed.
 //
-// Layout: one CTA handles kElemPerCta prisms.  Phase A: one thread per
-// (prism, Gauss point) builds the per-point quantities in shared memory.
-// Phase B: each thread owns 3x3 node-pair blocks, sums the six Gauss points
-// and scatters the block.  The matrix assembled is A = K^T, the system the
-// reference solves (Pardiso iparm[11] = 1, NewtonRaphsonSolver.cpp:639); in
-// that orientation every element block (a, b) lands at block
-// (conn[a], conn[b]) without a transpose.  Fixed DOFs are masked here, which
-// is calcutateFixedK (NewtonRaphsonSolver.cpp:237-255) without a second pass.
+// Layout: one CTA handles NE prisms.  Phase A: one thread per (prism, Gauss
+// point) builds the per-point vectors in shared memory.  Phase B: each
+// thread owns 3x3 node-pair blocks, sums the six Gauss points and scatters
+// the block.  The matrix assembled is A = K^T, the system the reference
+// solves (Pardiso iparm[11] = 1, NewtonRaphsonSolver.cpp:639); in that
+// orientation every element block (a, b) lands at block (conn[a], conn[b])
+// without a transpose.  Fixed DOFs are masked here, which is calcutateFixedK
+// (NewtonRaphsonSolver.cpp:237-255) without a second pass.
 #include "tf_internal.cuh"
 
 namespace tf {
 
 namespace {
 
-enum Mode { kAtomic = 0, kEval = 1, kStore = 2 };
+enum Mode { kAtomic = 0, kStore = 2 };
 
 struct ElemArgs {
     int ne;
@@ -44,317 +53,452 @@ struct ElemArgs {
     const int* __restrict__ slot;
     const double* __restrict__ uk;
     const double* __restrict__ vel;
-    double dt;
-    double* __restrict__ val;  // kAtomic: block values
-    double* __restrict__ g;    // kAtomic: right-hand side
-    // kEval outputs (reference orientation), element-relative
+    double idt;                 // 1 / dt
+    double* __restrict__ val;   // kAtomic: block values
+    double* __restrict__ g;     // kAtomic: right-hand side
+    double* __restrict__ eblk;  // kStore: [9][36*ne]
+    double* __restrict__ ef;    // kStore: [18][ne]
+    // parity evaluation (reference orientation), element-relative
     int e0, count;
     double* __restrict__ Ke;
     double* __restrict__ Kv;
     double* __restrict__ fe;
     double* __restrict__ fv;
-    // kStore outputs
-    double* __restrict__ eblk;  // [9][36*ne]
-    double* __restrict__ ef;    // [18][ne]
 };
 
-struct Gp {
-    double dn[18];
-    double c1, c2;
-    double sdn[18];
-    double pv[9];
-    double pdn[18];
-    double svdn[18];
-    double fe[18];
-    double fv[18];
+// Per-Gauss-point values in registers.
+struct GaussPoint {
+    double dn[18];   // current shape gradients dN_c (node-major)
+    double sg[6];    // sigma' = w dV sigma     (00 11 22 01 02 12)
+    double c1, c2;   // w dV lambda / J, w dV (mu - lambda lnJ) / J
+    double sv[6];    // sigma_v' = w dV eta sym(grad v)
+    double pv[9];    // P = 0.5 eta w dV (I/dt - grad v)
 };
 
-template <int NE>
-__device__ __forceinline__ int elem_index(const ElemArgs& A, int el, int mode) {
-    int e = blockIdx.x * NE + el;
-    return mode == kEval ? A.e0 + e : e;
+__device__ __forceinline__ void sym_apply(const double* s, double d0, double d1, double d2, double* o) {
+    o[0] = fma(s[0], d0, fma(s[3], d1, s[4] * d2));
+    o[1] = fma(s[3], d0, fma(s[1], d1, s[5] * d2));
+    o[2] = fma(s[4], d0, fma(s[5], d1, s[2] * d2));
 }
 
-template <int NE, int MODE>
+// Prism::calculateCurrNodalForces (Prism.cpp:749-874) for Gauss point gp of
+// element e, in closed form.
+__device__ __forceinline__ void gauss_point(const ElemArgs& A, int e, int gp, bool visc, GaussPoint& G) {
+    const int ne = A.ne;
+    int nd[6];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) nd[a] = __ldg(&A.conn[a * ne + e]);
+    double gX[18];
+    const size_t q = 6 * (size_t)e + gp;
+#pragma unroll
+    for (int k = 0; k < 18; ++k) gX[k] = __ldg(&A.gx[(size_t)k * (6 * (size_t)ne) + q]);
+    // F = sum_a x_a (x) dN_X,a.  The gradients sum to zero, so positions are
+    // taken relative to node 0, which removes the cancellation of ~|x|/h
+    // between the products far from the origin (exact arithmetic: no change).
+    double F[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) F[k] = 0.0;
+    const double o0 = A.uk[3 * nd[0]], o1 = A.uk[3 * nd[0] + 1], o2 = A.uk[3 * nd[0] + 2];
+#pragma unroll
+    for (int a = 1; a < 6; ++a) {
+        const double x0 = A.uk[3 * nd[a]] - o0, x1 = A.uk[3 * nd[a] + 1] - o1, x2 = A.uk[3 * nd[a] + 2] - o2;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            F[j] = fma(x0, gX[3 * a + j], F[j]);
+            F[3 + j] = fma(x1, gX[3 * a + j], F[3 + j]);
+            F[6 + j] = fma(x2, gX[3 * a + j], F[6 + j]);
+        }
+    }
+    double iFg[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) iFg[k] = __ldg(&A.invFg[k * ne + e]);
+    double Fe[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            Fe[3 * i + j] = fma(F[3 * i], iFg[j], fma(F[3 * i + 1], iFg[3 + j], F[3 * i + 2] * iFg[6 + j]));
+    const double J = Fe[0] * (Fe[4] * Fe[8] - Fe[5] * Fe[7]) - Fe[1] * (Fe[3] * Fe[8] - Fe[5] * Fe[6]) +
+                     Fe[2] * (Fe[3] * Fe[7] - Fe[4] * Fe[6]);
+    const double lnJ = log(J);
+    const double rJ = 1.0 / J;
+    const double lam = __ldg(&A.lam[e]), mu = __ldg(&A.mu[e]);
+    double b[6];
+    b[0] = fma(Fe[0], Fe[0], fma(Fe[1], Fe[1], Fe[2] * Fe[2]));
+    b[1] = fma(Fe[3], Fe[3], fma(Fe[4], Fe[4], Fe[5] * Fe[5]));
+    b[2] = fma(Fe[6], Fe[6], fma(Fe[7], Fe[7], Fe[8] * Fe[8]));
+    b[3] = fma(Fe[0], Fe[3], fma(Fe[1], Fe[4], Fe[2] * Fe[5]));
+    b[4] = fma(Fe[0], Fe[6], fma(Fe[1], Fe[7], Fe[2] * Fe[8]));
+    b[5] = fma(Fe[3], Fe[6], fma(Fe[4], Fe[7], Fe[5] * Fe[8]));
+    double cf[9];  // cofactors: F^-T = cf / det F
+    cf[0] = F[4] * F[8] - F[5] * F[7];
+    cf[1] = F[5] * F[6] - F[3] * F[8];
+    cf[2] = F[3] * F[7] - F[4] * F[6];
+    cf[3] = F[2] * F[7] - F[1] * F[8];
+    cf[4] = F[0] * F[8] - F[2] * F[6];
+    cf[5] = F[1] * F[6] - F[0] * F[7];
+    cf[6] = F[1] * F[5] - F[2] * F[4];
+    cf[7] = F[2] * F[3] - F[0] * F[5];
+    cf[8] = F[0] * F[4] - F[1] * F[3];
+    const double detF = fma(F[0], cf[0], fma(F[1], cf[1], F[2] * cf[2]));
+    const double rdF = 1.0 / detF;
+    const double wdV = __ldg(&A.wdet[q]) * detF;
+    const double sc = wdV * rJ;
+    const double dterm = fma(lam, lnJ, -mu);
+    G.sg[0] = sc * fma(mu, b[0], dterm);
+    G.sg[1] = sc * fma(mu, b[1], dterm);
+    G.sg[2] = sc * fma(mu, b[2], dterm);
+    G.sg[3] = sc * mu * b[3];
+    G.sg[4] = sc * mu * b[4];
+    G.sg[5] = sc * mu * b[5];
+    G.c1 = sc * lam;
+    G.c2 = sc * (mu - lam * lnJ);
+#pragma unroll
+    for (int a = 0; a < 6; ++a) {
+        const double g0 = gX[3 * a], g1 = gX[3 * a + 1], g2 = gX[3 * a + 2];
+        G.dn[3 * a] = rdF * fma(cf[0], g0, fma(cf[1], g1, cf[2] * g2));
+        G.dn[3 * a + 1] = rdF * fma(cf[3], g0, fma(cf[4], g1, cf[5] * g2));
+        G.dn[3 * a + 2] = rdF * fma(cf[6], g0, fma(cf[7], g1, cf[8] * g2));
+    }
+    if (visc) {
+        // grad v = sum_c v_c (x) dN_c (ShapeBase.cpp:2892-2919), velocities
+        // relative to node 0 for the same reason as the positions
+        double L[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) L[k] = 0.0;
+        const double w0 = A.vel[3 * nd[0]], w1 = A.vel[3 * nd[0] + 1], w2 = A.vel[3 * nd[0] + 2];
+#pragma unroll
+        for (int c = 1; c < 6; ++c) {
+            const double v0 = A.vel[3 * nd[c]] - w0, v1 = A.vel[3 * nd[c] + 1] - w1, v2 = A.vel[3 * nd[c] + 2] - w2;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                L[j] = fma(v0, G.dn[3 * c + j], L[j]);
+                L[3 + j] = fma(v1, G.dn[3 * c + j], L[3 + j]);
+                L[6 + j] = fma(v2, G.dn[3 * c + j], L[6 + j]);
+            }
+        }
+        const double eta = __ldg(&A.eta[e]);
+        const double ew = eta * wdV;
+        const double hw = 0.5 * ew;
+        G.sv[0] = ew * L[0];
+        G.sv[1] = ew * L[4];
+        G.sv[2] = ew * L[8];
+        G.sv[3] = hw * (L[1] + L[3]);
+        G.sv[4] = hw * (L[2] + L[6]);
+        G.sv[5] = hw * (L[5] + L[7]);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) G.pv[k] = -hw * L[k];
+        G.pv[0] = fma(hw, A.idt, G.pv[0]);
+        G.pv[4] = fma(hw, A.idt, G.pv[4]);
+        G.pv[8] = fma(hw, A.idt, G.pv[8]);
+    }
+}
+
+// Shared per-Gauss-point vectors of the fast kernel.
+template <bool VISC>
+struct GpFast;
+template <>
+struct GpFast<false> {
+    double dn[18], sdn[18], u[18], w[18];
+    double c2;
+};
+template <>
+struct GpFast<true> {
+    double dn[18], sdn[18], u[18], w[18], v[18];
+    double Q[9];
+};
+
+// Node pairs a <= b of the symmetric (inviscid) case.
+__constant__ int8_t kPairA[21] = {0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 4, 4, 5};
+__constant__ int8_t kPairB[21] = {0, 1, 2, 3, 4, 5, 1, 2, 3, 4, 5, 2, 3, 4, 5, 3, 4, 5, 4, 5, 5};
+
+template <int NE, int MODE, bool VISC>
 __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    using Gp = GpFast<VISC>;
     Gp* sh = reinterpret_cast<Gp*>(smem_raw);  // [NE][6]
     const int tid = threadIdx.x;
-    const int limit = (MODE == kEval) ? A.e0 + A.count : A.ne;
 
-    // ---------------- phase A: one thread per (prism, Gauss point) -------
+    // ---------------- phase A ----------------------------------------------
     {
         const int el = tid / kGauss;
         const int gp = tid - el * kGauss;
-        const int e = elem_index<NE>(A, el, MODE);
-        Gp& S = sh[el * kGauss + gp];
-        if (e < limit) {
-            const int ne = A.ne;
-            int nd[6];
-#pragma unroll
-            for (int a = 0; a < 6; ++a) nd[a] = __ldg(&A.conn[a * ne + e]);
-            double gX[18];
-            const int q = 6 * e + gp;
-#pragma unroll
-            for (int k = 0; k < 18; ++k) gX[k] = __ldg(&A.gx[(size_t)k * (6 * (size_t)ne) + q]);
-            // F = sum_a x_a (x) dN_X,a.  The gradients sum to zero, so the
-            // positions are taken relative to node 0: that removes the
-            // cancellation of ~|x| / h between the products at coordinates far
-            // from the origin (the result is unchanged in exact arithmetic).
-            double F[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) F[k] = 0.0;
-            const double o0 = A.uk[3 * nd[0]], o1 = A.uk[3 * nd[0] + 1], o2 = A.uk[3 * nd[0] + 2];
-#pragma unroll
-            for (int a = 1; a < 6; ++a) {
-                const double x0 = A.uk[3 * nd[a]] - o0, x1 = A.uk[3 * nd[a] + 1] - o1, x2 = A.uk[3 * nd[a] + 2] - o2;
-#pragma unroll
-                for (int j = 0; j < 3; ++j) {
-                    F[j] = fma(x0, gX[3 * a + j], F[j]);
-                    F[3 + j] = fma(x1, gX[3 * a + j], F[3 + j]);
-                    F[6 + j] = fma(x2, gX[3 * a + j], F[6 + j]);
-                }
-            }
-            double iFg[9];
-#pragma unroll
-            for (int k = 0; k < 9; ++k) iFg[k] = __ldg(&A.invFg[k * ne + e]);
-            double Fe[9];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-                for (int j = 0; j < 3; ++j)
-                    Fe[3 * i + j] = fma(F[3 * i], iFg[j], fma(F[3 * i + 1], iFg[3 + j], F[3 * i + 2] * iFg[6 + j]));
-            // J = det Fe, b = Fe Fe^T
-            const double J = Fe[0] * (Fe[4] * Fe[8] - Fe[5] * Fe[7]) - Fe[1] * (Fe[3] * Fe[8] - Fe[5] * Fe[6]) +
-                             Fe[2] * (Fe[3] * Fe[7] - Fe[4] * Fe[6]);
-            const double lnJ = log(J);
-            const double rJ = 1.0 / J;
-            const double lam = __ldg(&A.lam[e]), mu = __ldg(&A.mu[e]);
-            double b[6];  // 00 11 22 01 02 12
-            b[0] = fma(Fe[0], Fe[0], fma(Fe[1], Fe[1], Fe[2] * Fe[2]));
-            b[1] = fma(Fe[3], Fe[3], fma(Fe[4], Fe[4], Fe[5] * Fe[5]));
-            b[2] = fma(Fe[6], Fe[6], fma(Fe[7], Fe[7], Fe[8] * Fe[8]));
-            b[3] = fma(Fe[0], Fe[3], fma(Fe[1], Fe[4], Fe[2] * Fe[5]));
-            b[4] = fma(Fe[0], Fe[6], fma(Fe[1], Fe[7], Fe[2] * Fe[8]));
-            b[5] = fma(Fe[3], Fe[6], fma(Fe[4], Fe[7], Fe[5] * Fe[8]));
-            // cofactors of F: F^-T = cof / detF
-            double cf[9];
-            cf[0] = F[4] * F[8] - F[5] * F[7];
-            cf[1] = F[5] * F[6] - F[3] * F[8];
-            cf[2] = F[3] * F[7] - F[4] * F[6];
-            cf[3] = F[2] * F[7] - F[1] * F[8];
-            cf[4] = F[0] * F[8] - F[2] * F[6];
-            cf[5] = F[1] * F[6] - F[0] * F[7];
-            cf[6] = F[1] * F[5] - F[2] * F[4];
-            cf[7] = F[2] * F[3] - F[0] * F[5];
-            cf[8] = F[0] * F[4] - F[1] * F[3];
-            const double detF = fma(F[0], cf[0], fma(F[1], cf[1], F[2] * cf[2]));
-            const double rdF = 1.0 / detF;
-            const double wdV = __ldg(&A.wdet[q]) * detF;
-            // sigma' = w dV sigma = (w dV / J) (mu (b - I) + lambda lnJ I)
-            const double sc = wdV * rJ;
-            const double dterm = fma(lam, lnJ, -mu);
-            double sg[6];
-            sg[0] = sc * fma(mu, b[0], dterm);
-            sg[1] = sc * fma(mu, b[1], dterm);
-            sg[2] = sc * fma(mu, b[2], dterm);
-            sg[3] = sc * mu * b[3];
-            sg[4] = sc * mu * b[4];
-            sg[5] = sc * mu * b[5];
-            S.c1 = sc * lam;
-            S.c2 = sc * (mu - lam * lnJ);
-            double dn[18];
+        const int e = blockIdx.x * NE + el;
+        if (e < A.ne) {
+            const bool visc = VISC && (__ldg(&A.eta[e]) != 0.0);
+            GaussPoint G;
+            gauss_point(A, e, gp, visc, G);
+            Gp& S = sh[el * kGauss + gp];
 #pragma unroll
             for (int a = 0; a < 6; ++a) {
-                const double g0 = gX[3 * a], g1 = gX[3 * a + 1], g2 = gX[3 * a + 2];
-                dn[3 * a] = rdF * fma(cf[0], g0, fma(cf[1], g1, cf[2] * g2));
-                dn[3 * a + 1] = rdF * fma(cf[3], g0, fma(cf[4], g1, cf[5] * g2));
-                dn[3 * a + 2] = rdF * fma(cf[6], g0, fma(cf[7], g1, cf[8] * g2));
-            }
-#pragma unroll
-            for (int k = 0; k < 18; ++k) S.dn[k] = dn[k];
-#pragma unroll
-            for (int a = 0; a < 6; ++a) {
-                const double d0 = dn[3 * a], d1 = dn[3 * a + 1], d2 = dn[3 * a + 2];
-                const double s0 = fma(sg[0], d0, fma(sg[3], d1, sg[4] * d2));
-                const double s1 = fma(sg[3], d0, fma(sg[1], d1, sg[5] * d2));
-                const double s2 = fma(sg[4], d0, fma(sg[5], d1, sg[2] * d2));
-                S.sdn[3 * a] = s0;
-                S.sdn[3 * a + 1] = s1;
-                S.sdn[3 * a + 2] = s2;
-                S.fe[3 * a] = -s0;
-                S.fe[3 * a + 1] = -s1;
-                S.fe[3 * a + 2] = -s2;
-            }
-            const double eta = __ldg(&A.eta[e]);
-            if (eta != 0.0) {
-                // grad v = sum_c v_c (x) dn_c  (ShapeBase.cpp:2892-2919)
-                double L[9];
-#pragma unroll
-                for (int k = 0; k < 9; ++k) L[k] = 0.0;
-                const double w0 = A.vel[3 * nd[0]], w1 = A.vel[3 * nd[0] + 1], w2 = A.vel[3 * nd[0] + 2];
-#pragma unroll
-                for (int c = 1; c < 6; ++c) {
-                    const double v0 = A.vel[3 * nd[c]] - w0, v1 = A.vel[3 * nd[c] + 1] - w1, v2 = A.vel[3 * nd[c] + 2] - w2;
-#pragma unroll
-                    for (int j = 0; j < 3; ++j) {
-                        L[j] = fma(v0, dn[3 * c + j], L[j]);
-                        L[3 + j] = fma(v1, dn[3 * c + j], L[3 + j]);
-                        L[6 + j] = fma(v2, dn[3 * c + j], L[6 + j]);
+                const double d0 = G.dn[3 * a], d1 = G.dn[3 * a + 1], d2 = G.dn[3 * a + 2];
+                double s3[3];
+                sym_apply(G.sg, d0, d1, d2, s3);
+                S.dn[3 * a] = d0;
+                S.dn[3 * a + 1] = d1;
+                S.dn[3 * a + 2] = d2;
+                S.sdn[3 * a] = s3[0];
+                S.sdn[3 * a + 1] = s3[1];
+                S.sdn[3 * a + 2] = s3[2];
+                if constexpr (VISC) {
+                    double v3[3] = {0.0, 0.0, 0.0}, p3[3] = {0.0, 0.0, 0.0};
+                    if (visc) {
+                        sym_apply(G.sv, d0, d1, d2, v3);
+                        p3[0] = fma(G.pv[0], d0, fma(G.pv[3], d1, G.pv[6] * d2));
+                        p3[1] = fma(G.pv[1], d0, fma(G.pv[4], d1, G.pv[7] * d2));
+                        p3[2] = fma(G.pv[2], d0, fma(G.pv[5], d1, G.pv[8] * d2));
                     }
+                    S.u[3 * a] = fma(G.c1, d0, v3[0]);
+                    S.u[3 * a + 1] = fma(G.c1, d1, v3[1]);
+                    S.u[3 * a + 2] = fma(G.c1, d2, v3[2]);
+                    S.w[3 * a] = fma(G.c2, d0, p3[0]);
+                    S.w[3 * a + 1] = fma(G.c2, d1, p3[1]);
+                    S.w[3 * a + 2] = fma(G.c2, d2, p3[2]);
+                    S.v[3 * a] = v3[0];
+                    S.v[3 * a + 1] = v3[1];
+                    S.v[3 * a + 2] = v3[2];
+                } else {
+                    S.u[3 * a] = G.c1 * d0;
+                    S.u[3 * a + 1] = G.c1 * d1;
+                    S.u[3 * a + 2] = G.c1 * d2;
+                    S.w[3 * a] = G.c2 * d0;
+                    S.w[3 * a + 1] = G.c2 * d1;
+                    S.w[3 * a + 2] = G.c2 * d2;
                 }
-                // sigma_v' = w dV eta sym(L);  pv = 0.5 eta w dV (I/dt - L)
-                const double ew = eta * wdV;
-                const double hw = 0.5 * ew;
-                double sv[6];
-                sv[0] = ew * L[0];
-                sv[1] = ew * L[4];
-                sv[2] = ew * L[8];
-                sv[3] = hw * (L[1] + L[3]);
-                sv[4] = hw * (L[2] + L[6]);
-                sv[5] = hw * (L[5] + L[7]);
-                const double idt = 1.0 / A.dt;
-                double pv[9];
+            }
+            if constexpr (VISC) {
 #pragma unroll
-                for (int k = 0; k < 9; ++k) pv[k] = -hw * L[k];
-                pv[0] = fma(hw, idt, pv[0]);
-                pv[4] = fma(hw, idt, pv[4]);
-                pv[8] = fma(hw, idt, pv[8]);
-#pragma unroll
-                for (int k = 0; k < 9; ++k) S.pv[k] = pv[k];
-#pragma unroll
-                for (int a = 0; a < 6; ++a) {
-                    const double d0 = dn[3 * a], d1 = dn[3 * a + 1], d2 = dn[3 * a + 2];
-                    S.pdn[3 * a] = fma(pv[0], d0, fma(pv[3], d1, pv[6] * d2));
-                    S.pdn[3 * a + 1] = fma(pv[1], d0, fma(pv[4], d1, pv[7] * d2));
-                    S.pdn[3 * a + 2] = fma(pv[2], d0, fma(pv[5], d1, pv[8] * d2));
-                    const double s0 = fma(sv[0], d0, fma(sv[3], d1, sv[4] * d2));
-                    const double s1 = fma(sv[3], d0, fma(sv[1], d1, sv[5] * d2));
-                    const double s2 = fma(sv[4], d0, fma(sv[5], d1, sv[2] * d2));
-                    S.svdn[3 * a] = s0;
-                    S.svdn[3 * a + 1] = s1;
-                    S.svdn[3 * a + 2] = s2;
-                    S.fv[3 * a] = -s0;
-                    S.fv[3 * a + 1] = -s1;
-                    S.fv[3 * a + 2] = -s2;
-                }
+                for (int k = 0; k < 9; ++k) S.Q[k] = visc ? G.pv[k] : 0.0;
+                S.Q[0] += G.c2;
+                S.Q[4] += G.c2;
+                S.Q[8] += G.c2;
+            } else {
+                S.c2 = G.c2;
             }
         }
     }
     __syncthreads();
 
     // ---------------- element forces: Gauss sum, fixed mask, scatter ------
+    // f_a = - sum_g (sigma' + sigma_v') dN_a  (ShapeBase.cpp:2203-2227)
     for (int task = tid; task < NE * 18; task += NE * kGauss) {
         const int el = task / 18;
         const int k = task - el * 18;
-        const int e = elem_index<NE>(A, el, MODE);
-        if (e >= limit) continue;
-        const bool visc = __ldg(&A.eta[e]) != 0.0;
-        double se = 0.0, sv = 0.0;
+        const int e = blockIdx.x * NE + el;
+        if (e >= A.ne) continue;
+        double f = 0.0;
 #pragma unroll
         for (int gp = 0; gp < kGauss; ++gp) {
-            se += sh[el * kGauss + gp].fe[k];
-            if (visc) sv += sh[el * kGauss + gp].fv[k];
+            f -= sh[el * kGauss + gp].sdn[k];
+            if constexpr (VISC) f -= sh[el * kGauss + gp].v[k];
         }
         const int a = k / 3, d = k - 3 * (k / 3);
         const int node = __ldg(&A.conn[a * A.ne + e]);
         const bool fx = A.fixed[3 * node + d] != 0;
-        if (MODE == kEval) {
-            const int r = e - A.e0;
-            if (A.fe) A.fe[18 * (size_t)r + k] = fx ? 0.0 : se;
-            if (A.fv) A.fv[18 * (size_t)r + k] = fx ? 0.0 : sv;
-        } else if (MODE == kStore) {
-            A.ef[(size_t)k * A.ne + e] = fx ? 0.0 : se + sv;
-        } else {
-            if (!fx) atomicAdd(&A.g[3 * node + d], se + sv);
-        }
+        if (MODE == kStore) A.ef[(size_t)k * A.ne + e] = fx ? 0.0 : f;
+        else if (!fx) atomicAdd(&A.g[3 * node + d], f);
     }
 
     // ---------------- phase B: 3x3 node-pair blocks ------------------------
+    constexpr int kPairs = VISC ? 36 : 21;
+    for (int task = tid; task < NE * kPairs; task += NE * kGauss) {
+        const int el = task / kPairs;
+        const int pr = task - el * kPairs;
+        const int e = blockIdx.x * NE + el;
+        if (e >= A.ne) continue;
+        const int a = VISC ? pr / 6 : kPairA[pr];
+        const int bq = VISC ? pr - 6 * (pr / 6) : kPairB[pr];
+        double acc[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+#pragma unroll
+        for (int gp = 0; gp < kGauss; ++gp) {
+            const Gp& S = sh[el * kGauss + gp];
+            const double a3[3] = {S.dn[3 * a], S.dn[3 * a + 1], S.dn[3 * a + 2]};
+            const double b3[3] = {S.dn[3 * bq], S.dn[3 * bq + 1], S.dn[3 * bq + 2]};
+            const double s = fma(a3[0], b3[0], fma(a3[1], b3[1], a3[2] * b3[2]));
+            const double t = fma(a3[0], S.sdn[3 * bq], fma(a3[1], S.sdn[3 * bq + 1], a3[2] * S.sdn[3 * bq + 2]));
+            const double ua[3] = {S.u[3 * a], S.u[3 * a + 1], S.u[3 * a + 2]};
+            const double wa[3] = {S.w[3 * a], S.w[3 * a + 1], S.w[3 * a + 2]};
+            if constexpr (VISC) {
+                const double vb[3] = {S.v[3 * bq], S.v[3 * bq + 1], S.v[3 * bq + 2]};
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        double x = fma(ua[i], b3[k], acc[3 * i + k]);
+                        x = fma(b3[i], wa[k], x);
+                        x = fma(-vb[i], a3[k], x);
+                        x = fma(s, S.Q[3 * i + k], x);
+                        if (i == k) x += t;
+                        acc[3 * i + k] = x;
+                    }
+            } else {
+                const double dg = fma(S.c2, s, t);
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        double x = fma(ua[i], b3[k], acc[3 * i + k]);
+                        x = fma(b3[i], wa[k], x);
+                        if (i == k) x += dg;
+                        acc[3 * i + k] = x;
+                    }
+            }
+        }
+        const int na = __ldg(&A.conn[a * A.ne + e]);
+        const int nb = __ldg(&A.conn[bq * A.ne + e]);
+        bool fr[3], fc[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            fr[i] = A.fixed[3 * na + i] != 0;
+            fc[i] = A.fixed[3 * nb + i] != 0;
+        }
+        const bool mirror = !VISC && (a != bq);
+        if (MODE == kStore) {
+            const size_t stride = (size_t)36 * A.ne;
+            const size_t base = (size_t)(6 * a + bq) * A.ne + e;
+            const size_t baseT = (size_t)(6 * bq + a) * A.ne + e;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const double v = (fr[i] || fc[k]) ? 0.0 : acc[3 * i + k];
+                    A.eblk[(3 * i + k) * stride + base] = v;
+                    if (mirror) A.eblk[(3 * k + i) * stride + baseT] = v;
+                }
+        } else {
+            double* dst = A.val + 9 * (size_t)__ldg(&A.slot[(6 * a + bq) * A.ne + e]);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+                    if (!fr[i] && !fc[k]) atomicAdd(dst + 3 * i + k, acc[3 * i + k]);
+            if (mirror) {
+                double* dt = A.val + 9 * (size_t)__ldg(&A.slot[(6 * bq + a) * A.ne + e]);
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        if (!fr[i] && !fc[k]) atomicAdd(dt + 3 * k + i, acc[3 * i + k]);
+            }
+        }
+    }
+}
+
+// ---- parity evaluation: separate elastic / viscous outputs ----------------
+
+struct GpEval {
+    double dn[18];
+    double c1, c2;
+    double sdn[18];
+    double pv[9];
+    double pdn[18];
+    double svdn[18];
+};
+
+template <int NE>
+__global__ void __launch_bounds__(NE * kGauss) k_element_eval(ElemArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    GpEval* sh = reinterpret_cast<GpEval*>(smem_raw);
+    const int tid = threadIdx.x;
+    const int limit = A.e0 + A.count;
+    {
+        const int el = tid / kGauss;
+        const int gp = tid - el * kGauss;
+        const int e = A.e0 + blockIdx.x * NE + el;
+        if (e < limit) {
+            const bool visc = __ldg(&A.eta[e]) != 0.0;
+            GaussPoint G;
+            gauss_point(A, e, gp, visc, G);
+            GpEval& S = sh[el * kGauss + gp];
+            S.c1 = G.c1;
+            S.c2 = G.c2;
+#pragma unroll
+            for (int a = 0; a < 6; ++a) {
+                const double d0 = G.dn[3 * a], d1 = G.dn[3 * a + 1], d2 = G.dn[3 * a + 2];
+                S.dn[3 * a] = d0;
+                S.dn[3 * a + 1] = d1;
+                S.dn[3 * a + 2] = d2;
+                sym_apply(G.sg, d0, d1, d2, &S.sdn[3 * a]);
+                if (visc) {
+                    sym_apply(G.sv, d0, d1, d2, &S.svdn[3 * a]);
+                    S.pdn[3 * a] = fma(G.pv[0], d0, fma(G.pv[3], d1, G.pv[6] * d2));
+                    S.pdn[3 * a + 1] = fma(G.pv[1], d0, fma(G.pv[4], d1, G.pv[7] * d2));
+                    S.pdn[3 * a + 2] = fma(G.pv[2], d0, fma(G.pv[5], d1, G.pv[8] * d2));
+                } else {
+                    S.svdn[3 * a] = S.svdn[3 * a + 1] = S.svdn[3 * a + 2] = 0.0;
+                    S.pdn[3 * a] = S.pdn[3 * a + 1] = S.pdn[3 * a + 2] = 0.0;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 9; ++k) S.pv[k] = visc ? G.pv[k] : 0.0;
+        }
+    }
+    __syncthreads();
+    for (int task = tid; task < NE * 18; task += NE * kGauss) {
+        const int el = task / 18;
+        const int k = task - el * 18;
+        const int e = A.e0 + blockIdx.x * NE + el;
+        if (e >= limit) continue;
+        double se = 0.0, sv = 0.0;
+#pragma unroll
+        for (int gp = 0; gp < kGauss; ++gp) {
+            se -= sh[el * kGauss + gp].sdn[k];
+            sv -= sh[el * kGauss + gp].svdn[k];
+        }
+        const int a = k / 3, d = k - 3 * (k / 3);
+        const bool fx = A.fixed[3 * __ldg(&A.conn[a * A.ne + e]) + d] != 0;
+        const size_t r = (size_t)(e - A.e0);
+        if (A.fe) A.fe[18 * r + k] = fx ? 0.0 : se;
+        if (A.fv) A.fv[18 * r + k] = fx ? 0.0 : sv;
+    }
     for (int task = tid; task < NE * 36; task += NE * kGauss) {
         const int el = task / 36;
         const int pr = task - el * 36;
-        const int e = elem_index<NE>(A, el, MODE);
+        const int e = A.e0 + blockIdx.x * NE + el;
         if (e >= limit) continue;
         const int a = pr / 6, bq = pr - 6 * (pr / 6);
         const bool visc = __ldg(&A.eta[e]) != 0.0;
         double ke[9], kv[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            ke[k] = 0.0;
-            kv[k] = 0.0;
-        }
+        for (int k = 0; k < 9; ++k) ke[k] = kv[k] = 0.0;
 #pragma unroll
         for (int gp = 0; gp < kGauss; ++gp) {
-            const Gp& S = sh[el * kGauss + gp];
-            const double a0 = S.dn[3 * a], a1 = S.dn[3 * a + 1], a2 = S.dn[3 * a + 2];
-            const double b0 = S.dn[3 * bq], b1 = S.dn[3 * bq + 1], b2 = S.dn[3 * bq + 2];
-            const double c1 = S.c1, c2 = S.c2;
-            const double s = fma(a0, b0, fma(a1, b1, a2 * b2));
-            const double t = fma(a0, S.sdn[3 * bq], fma(a1, S.sdn[3 * bq + 1], a2 * S.sdn[3 * bq + 2]));
-            const double dg = fma(c2, s, t);
-            const double ca[3] = {c1 * a0, c1 * a1, c1 * a2};
-            const double da[3] = {c2 * a0, c2 * a1, c2 * a2};
-            const double bb[3] = {b0, b1, b2};
+            const GpEval& S = sh[el * kGauss + gp];
+            const double aa[3] = {S.dn[3 * a], S.dn[3 * a + 1], S.dn[3 * a + 2]};
+            const double bb[3] = {S.dn[3 * bq], S.dn[3 * bq + 1], S.dn[3 * bq + 2]};
+            const double s = fma(aa[0], bb[0], fma(aa[1], bb[1], aa[2] * bb[2]));
+            const double t = fma(aa[0], S.sdn[3 * bq], fma(aa[1], S.sdn[3 * bq + 1], aa[2] * S.sdn[3 * bq + 2]));
+            const double dg = fma(S.c2, s, t);
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
-                    double v = fma(ca[i], bb[k], fma(da[k], bb[i], ke[3 * i + k]));
+                    double v = fma(S.c1 * aa[i], bb[k], fma(S.c2 * aa[k], bb[i], ke[3 * i + k]));
                     if (i == k) v += dg;
                     ke[3 * i + k] = v;
                 }
             if (visc) {
-                const double pa[3] = {S.pdn[3 * a], S.pdn[3 * a + 1], S.pdn[3 * a + 2]};
-                const double sva[3] = {S.svdn[3 * a], S.svdn[3 * a + 1], S.svdn[3 * a + 2]};
-                const double svb[3] = {S.svdn[3 * bq], S.svdn[3 * bq + 1], S.svdn[3 * bq + 2]};
-                const double aa[3] = {a0, a1, a2};
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
                     for (int k = 0; k < 3; ++k)
                         kv[3 * i + k] = fma(s, S.pv[3 * i + k],
-                                            fma(bb[i], pa[k], fma(sva[i], bb[k], fma(-svb[i], aa[k], kv[3 * i + k]))));
+                                            fma(bb[i], S.pdn[3 * a + k],
+                                                fma(S.svdn[3 * a + i], bb[k], fma(-S.svdn[3 * bq + i], aa[k], kv[3 * i + k]))));
             }
         }
-        if (MODE == kEval) {
-            // reference orientation: TriPointKe[3a+i][3b+k] = ke(i,k);
-            // TriPointKv[3b+k][3a+i] = kv(i,k)  (ShapeBase.cpp:2968-2975)
-            const size_t r = (size_t)(e - A.e0);
+        // reference orientation: TriPointKe[3a+i][3b+k] = ke(i,k);
+        // TriPointKv[3b+k][3a+i] = kv(i,k)  (ShapeBase.cpp:2968-2975)
+        const size_t r = (size_t)(e - A.e0);
 #pragma unroll
-            for (int i = 0; i < 3; ++i)
+        for (int i = 0; i < 3; ++i)
 #pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    if (A.Ke) A.Ke[324 * r + (3 * a + i) * 18 + 3 * bq + k] = ke[3 * i + k];
-                    if (A.Kv) A.Kv[324 * r + (3 * bq + k) * 18 + 3 * a + i] = visc ? kv[3 * i + k] : 0.0;
-                }
-        } else {
-            const int na = __ldg(&A.conn[a * A.ne + e]);
-            const int nb = __ldg(&A.conn[bq * A.ne + e]);
-            bool fr[3], fc[3];
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                fr[i] = A.fixed[3 * na + i] != 0;
-                fc[i] = A.fixed[3 * nb + i] != 0;
+            for (int k = 0; k < 3; ++k) {
+                if (A.Ke) A.Ke[324 * r + (3 * a + i) * 18 + 3 * bq + k] = ke[3 * i + k];
+                if (A.Kv) A.Kv[324 * r + (3 * bq + k) * 18 + 3 * a + i] = visc ? kv[3 * i + k] : 0.0;
             }
-            if (MODE == kStore) {
-                const size_t base = (size_t)pr * A.ne + e;
-                const size_t stride = (size_t)36 * A.ne;
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                    for (int k = 0; k < 3; ++k)
-                        A.eblk[(3 * i + k) * stride + base] = (fr[i] || fc[k]) ? 0.0 : ke[3 * i + k] + kv[3 * i + k];
-            } else {
-                const int blk = __ldg(&A.slot[pr * A.ne + e]);
-                double* dst = A.val + 9 * (size_t)blk;
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                    for (int k = 0; k < 3; ++k)
-                        if (!fr[i] && !fc[k]) atomicAdd(dst + 3 * i + k, ke[3 * i + k] + kv[3 * i + k]);
-            }
-        }
     }
 }
 
@@ -373,7 +517,7 @@ ElemArgs make_args(tf_handle* h) {
     A.slot = d.slot;
     A.uk = d.uk;
     A.vel = d.vel;
-    A.dt = h->dt;
+    A.idt = 1.0 / h->dt;
     A.val = d.val;
     A.g = d.g;
     A.eblk = d.eblk;
@@ -381,16 +525,15 @@ ElemArgs make_args(tf_handle* h) {
     return A;
 }
 
-template <int NE, int MODE>
-tf_status launch_mode(tf_handle* h, ElemArgs A, int n) {
-    if (n <= 0) return TF_OK;
-    const size_t smem = sizeof(Gp) * NE * kGauss;
+template <int NE, int MODE, bool VISC>
+tf_status launch_fast(tf_handle* h, const ElemArgs& A) {
+    const size_t smem = sizeof(GpFast<VISC>) * NE * kGauss;
     static bool configured = false;
     if (!configured) {
-        TF_CUDA(cudaFuncSetAttribute(k_element<NE, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        TF_CUDA(cudaFuncSetAttribute(k_element<NE, MODE, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured = true;
     }
-    k_element<NE, MODE><<<cdiv(n, NE), NE * kGauss, smem, h->stream>>>(A);
+    k_element<NE, MODE, VISC><<<cdiv(A.ne, NE), NE * kGauss, smem, h->stream>>>(A);
     TF_LAUNCH_CHECK(h);
     return TF_OK;
 }
@@ -398,9 +541,12 @@ tf_status launch_mode(tf_handle* h, ElemArgs A, int n) {
 }  // namespace
 
 tf_status launch_element(tf_handle* h) {
-    ElemArgs A = make_args(h);
-    if (h->opt.deterministic) return launch_mode<kElemPerCta, kStore>(h, A, h->d.ne);
-    return launch_mode<kElemPerCta, kAtomic>(h, A, h->d.ne);
+    const ElemArgs A = make_args(h);
+    if (A.ne <= 0) return TF_OK;
+    const bool visc = h->d.any_visc;
+    if (h->opt.deterministic)
+        return visc ? launch_fast<kElemPerCta, kStore, true>(h, A) : launch_fast<kElemPerCta, kStore, false>(h, A);
+    return visc ? launch_fast<kElemPerCta, kAtomic, true>(h, A) : launch_fast<kElemPerCta, kAtomic, false>(h, A);
 }
 
 tf_status launch_element_eval(tf_handle* h, int e0, int count, double* Ke, double* Kv, double* fe, double* fv) {
@@ -411,7 +557,17 @@ tf_status launch_element_eval(tf_handle* h, int e0, int count, double* Ke, doubl
     A.Kv = Kv;
     A.fe = fe;
     A.fv = fv;
-    return launch_mode<8, kEval>(h, A, count);
+    if (count <= 0) return TF_OK;
+    constexpr int NE = 8;
+    const size_t smem = sizeof(GpEval) * NE * kGauss;
+    static bool configured = false;
+    if (!configured) {
+        TF_CUDA(cudaFuncSetAttribute(k_element_eval<NE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        configured = true;
+    }
+    k_element_eval<NE><<<cdiv(count, NE), NE * kGauss, smem, h->stream>>>(A);
+    TF_LAUNCH_CHECK(h);
+    return TF_OK;
 }
 
 }  // namespace tf
