@@ -260,6 +260,60 @@ def run_assembly_only(args, t):
     s.close()
 
 
+def run_batch(args):
+    """Batched sweep: 256 tissues of 1k-50k prisms in one handle vs the plain
+    GPU step looped over the instances (one handle each).  Metric: instance
+    time steps (implicit solves) per second."""
+    from tissuefolding_paperversion_gb300 import api, mesh
+
+    n = args.instances
+    ts = [mesh.config_batch_instance(s) for s in range(n)]
+    prisms = sum(t.n_elems for t in ts)
+    b = api.Batch(ts)
+    b.set_growth_rates()
+    for _ in range(args.warmup):
+        b.step(ts[0].dt)
+    l0 = b.launch_count()
+    w0 = time.perf_counter()
+    outs = [b.step(ts[0].dt) for _ in range(args.steps)]
+    wall_b = time.perf_counter() - w0
+    launches = b.launch_count() - l0
+    ms_b = sum(o["ms_total"] for o in outs)
+    ept = b.elements_per_cta()
+    b.close()
+    solvers = []
+    for t in ts:
+        s = api.Solver(t)
+        s.set_growth_rates(t.rates)
+        solvers.append(s)
+    for s, t in zip(solvers, ts):
+        for _ in range(max(1, args.warmup)):
+            s.newton_step(t.dt)
+    loop_steps = max(1, min(args.steps, 2))
+    w0 = time.perf_counter()
+    ms_l = 0.0
+    for _ in range(loop_steps):
+        for s, t in zip(solvers, ts):
+            ms_l += s.newton_step(t.dt)["ms_total"]
+    wall_l = time.perf_counter() - w0
+    for s in solvers:
+        s.close()
+    rate_b = n * args.steps / wall_b
+    rate_l = n * loop_steps / wall_l
+    print(json.dumps({
+        "metric": "batched implicit solves/s", "value": rate_b, "unit": "instance steps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall_b / args.steps * 1e3, "higher_is_better": True,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"batch-{n}", "instances": n, "prisms": prisms, "elements_per_cta": ept},
+        "looped_plain": {"value": rate_l, "unit": "instance steps/s", "steps": loop_steps,
+                         "device_ms_per_step": ms_l / loop_steps},
+        "speedup_vs_looped": rate_b / rate_l,
+        "batched_device_ms_per_step": ms_b / args.steps,
+        "newton_iters_max": int(max(o["iters"].max() for o in outs)),
+        "gpu_launches": launches,
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -267,6 +321,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="large", choices=["large", "medium", "small"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch"],
+                    help="plain: the 320k-prism Newton step; batch: the 256-instance sweep")
+    ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--mode", default="step", choices=["step", "assembly"],
                     help="step: Newton steps (the bench); assembly: back-to-back K+f assemblies only")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
@@ -274,6 +331,9 @@ def main():
     args = ap.parse_args()
     from tissuefolding_paperversion_gb300 import mesh
 
+    if args.workload == "batch":
+        run_batch(args)
+        return
     if args.config == "large":
         t = mesh.config_large(seed=0)
     elif args.config == "medium":

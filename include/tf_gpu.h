@@ -71,6 +71,7 @@ typedef struct tf_options {
     int32_t krylov_method;   /* 0 auto (CG when every eta is 0, else BiCGStab), 1 CG, 2 BiCGStab */
     int32_t deterministic;   /* 1: order-fixed assembly (no atomics); 0: atomic scatter */
     int32_t device;          /* CUDA device ordinal */
+    int32_t autotune_off;    /* 1: keep 16 prisms per CTA instead of timing 8/16/32 on the mesh */
 } tf_options;
 
 /* Statistics of one time step (tf_newton_step). */
@@ -140,6 +141,27 @@ TF_API tf_status tf_end_step(tf_handle* h);
  * tf_end_step.  Returns TF_NOT_CONVERGED when the cap was hit (the state is
  * still advanced, as in the reference). */
 TF_API tf_status tf_newton_step(tf_handle* h, double dt, tf_step_stats* stats);
+
+/* --- batches of independent tissues ---------------------------------------
+ * No counterpart in the reference (it simulates one tissue per process).
+ * n_instances meshes are held by one handle as one block-diagonal system:
+ * one element-kernel launch and one Krylov launch sequence cover every
+ * instance (ragged node / element offsets), with separate Krylov scalars,
+ * convergence flags and Newton iteration counts per instance; an instance
+ * that has converged is masked out of later assemblies and solves.  All other
+ * calls act on the concatenation (positions, Fg and rates of instance i
+ * start at its node / element offset, see tf_get_instances). */
+TF_API tf_status tf_batch_create(const tf_mesh* meshes, const tf_material* mats, int32_t n_instances,
+                                 const tf_options* opts, tf_handle** out);
+/* One implicit time step of every instance.  newton_iters and converged
+ * ([n_instances], may be NULL) receive the per-instance counts.  Returns
+ * TF_NOT_CONVERGED when any instance hit the iteration cap. */
+TF_API tf_status tf_batch_step(tf_handle* h, double dt, int32_t* newton_iters, int32_t* converged,
+                               tf_step_stats* stats);
+/* Instance count and offsets ([n+1] each, may be NULL). */
+TF_API tf_status tf_get_instances(tf_handle* h, int32_t* n_instances, int32_t* node_offsets, int32_t* elem_offsets);
+/* Prisms per CTA of the element kernel chosen by the autotuner (8, 16, 32). */
+TF_API int32_t tf_elements_per_cta(tf_handle* h);
 
 /* --- inspection (parity tests) ------------------------------------------ */
 

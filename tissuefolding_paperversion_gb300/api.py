@@ -29,7 +29,7 @@ EXPORTED = [
     "tf_solve", "tf_update", "tf_end_step", "tf_newton_step", "tf_get_residual", "tf_get_delta_u",
     "tf_get_viscosity_surfaces", "tf_set_viscosity_surfaces", "tf_set_state", "tf_export_csr",
     "tf_element_eval", "tf_get_sizes", "tf_get_stream", "tf_launch_count", "tf_time_assembly",
-    "tf_solve_bsr_static",
+    "tf_solve_bsr_static", "tf_batch_create", "tf_batch_step", "tf_get_instances", "tf_elements_per_cta",
 ]
 
 
@@ -51,7 +51,7 @@ class tf_material(C.Structure):
 class tf_options(C.Structure):
     _fields_ = [("newton_tol", C.c_double), ("newton_max_iter", C.c_int32), ("krylov_rtol", C.c_double),
                 ("krylov_max_iter", C.c_int32), ("krylov_method", C.c_int32), ("deterministic", C.c_int32),
-                ("device", C.c_int32)]
+                ("device", C.c_int32), ("autotune_off", C.c_int32)]
 
 
 class tf_step_stats(C.Structure):
@@ -102,6 +102,14 @@ def load(build_if_missing: bool = True):
     L.tf_launch_count.restype = i64
     L.tf_launch_count.argtypes = [vp]
     L.tf_time_assembly.argtypes = [vp, i32, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.tf_batch_create.restype = C.c_int
+    L.tf_batch_create.argtypes = [C.POINTER(tf_mesh), C.POINTER(tf_material), i32, C.POINTER(tf_options), C.POINTER(vp)]
+    L.tf_batch_step.restype = C.c_int
+    L.tf_batch_step.argtypes = [vp, C.c_double, vp, vp, C.POINTER(tf_step_stats)]
+    L.tf_get_instances.restype = C.c_int
+    L.tf_get_instances.argtypes = [vp, ip, vp, vp]
+    L.tf_elements_per_cta.restype = i32
+    L.tf_elements_per_cta.argtypes = [vp]
     L.tf_solve_bsr_static.restype = C.c_int
     L.tf_solve_bsr_static.argtypes = [i32, vp, vp, vp, vp, vp, C.c_double, i32, vp, ip, dp]
     for name in ["tf_create", "tf_destroy", "tf_set_positions", "tf_get_positions", "tf_set_Fg", "tf_get_Fg",
@@ -118,31 +126,35 @@ def _ptr(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
 
 
+def _mesh_structs(t):
+    a = dict(
+        pos=np.ascontiguousarray(t.pos, dtype=np.float64),
+        conn=np.ascontiguousarray(t.conn, dtype=np.int32),
+        fixed=np.ascontiguousarray(t.fixed, dtype=np.uint8),
+        ext_visc=np.ascontiguousarray(t.ext_visc, dtype=np.float64),
+        placement=np.ascontiguousarray(t.node_placement, dtype=np.int32),
+        E=np.ascontiguousarray(t.E, dtype=np.float64),
+        nu=np.ascontiguousarray(t.nu, dtype=np.float64),
+        eta=np.ascontiguousarray(t.eta, dtype=np.float64),
+    )
+    m = tf_mesh(t.n_nodes, t.n_elems, _ptr(a["pos"]), _ptr(a["conn"]), _ptr(a["fixed"]), _ptr(a["ext_visc"]),
+                _ptr(a["placement"]))
+    mat = tf_material(_ptr(a["E"]), _ptr(a["nu"]), _ptr(a["eta"]))
+    return a, m, mat
+
+
 class Solver:
     """One GPU Newton solver over one tissue (a ``tf_handle``)."""
 
     def __init__(self, tissue, newton_tol=1e-8, newton_max_iter=20, krylov_rtol=1e-8, krylov_max_iter=20000,
-                 krylov_method=0, deterministic=False, device=0):
+                 krylov_method=0, deterministic=False, device=0, autotune=True):
         self.L = load()
         t = tissue
         self.t = t
         self.nn, self.ne = t.n_nodes, t.n_elems
-        self._arrays = dict(
-            pos=np.ascontiguousarray(t.pos, dtype=np.float64),
-            conn=np.ascontiguousarray(t.conn, dtype=np.int32),
-            fixed=np.ascontiguousarray(t.fixed, dtype=np.uint8),
-            ext_visc=np.ascontiguousarray(t.ext_visc, dtype=np.float64),
-            placement=np.ascontiguousarray(t.node_placement, dtype=np.int32),
-            E=np.ascontiguousarray(t.E, dtype=np.float64),
-            nu=np.ascontiguousarray(t.nu, dtype=np.float64),
-            eta=np.ascontiguousarray(t.eta, dtype=np.float64),
-        )
-        a = self._arrays
-        m = tf_mesh(self.nn, self.ne, _ptr(a["pos"]), _ptr(a["conn"]), _ptr(a["fixed"]), _ptr(a["ext_visc"]),
-                    _ptr(a["placement"]))
-        mat = tf_material(_ptr(a["E"]), _ptr(a["nu"]), _ptr(a["eta"]))
+        self._arrays, m, mat = _mesh_structs(t)
         opt = tf_options(newton_tol, newton_max_iter, krylov_rtol, krylov_max_iter, krylov_method,
-                         1 if deterministic else 0, device)
+                         1 if deterministic else 0, device, 0 if autotune else 1)
         h = C.c_void_p()
         self._check(self.L.tf_create(C.byref(m), C.byref(mat), C.byref(opt), C.byref(h)), "tf_create")
         self.h = h
@@ -295,3 +307,54 @@ class Solver:
         a, b = C.c_float(0), C.c_float(0)
         self._check(self.L.tf_time_assembly(self.h, iters, C.byref(a), C.byref(b)), "tf_time_assembly")
         return a.value, b.value
+
+
+class Batch(Solver):
+    """Many independent tissues in one handle (tf_batch_create)."""
+
+    def __init__(self, tissues, newton_tol=1e-8, newton_max_iter=20, krylov_rtol=1e-8, krylov_max_iter=20000,
+                 krylov_method=0, deterministic=False, device=0, autotune=True):
+        self.L = load()
+        self.tissues = list(tissues)
+        n = len(self.tissues)
+        keep, meshes, mats = [], (tf_mesh * n)(), (tf_material * n)()
+        for i, t in enumerate(self.tissues):
+            a, m, mat = _mesh_structs(t)
+            keep.append(a)
+            meshes[i] = m
+            mats[i] = mat
+        self._arrays = keep
+        opt = tf_options(newton_tol, newton_max_iter, krylov_rtol, krylov_max_iter, krylov_method,
+                         1 if deterministic else 0, device, 0 if autotune else 1)
+        h = C.c_void_p()
+        self._check(self.L.tf_batch_create(meshes, mats, n, C.byref(opt), C.byref(h)), "tf_batch_create")
+        self.h = h
+        cnt = C.c_int32(0)
+        self.node_off = np.zeros(n + 1, dtype=np.int32)
+        self.elem_off = np.zeros(n + 1, dtype=np.int32)
+        self._check(self.L.tf_get_instances(self.h, C.byref(cnt), _ptr(self.node_off), _ptr(self.elem_off)),
+                    "tf_get_instances")
+        self.n_instances = cnt.value
+        self.nn, self.ne = int(self.node_off[-1]), int(self.elem_off[-1])
+
+    def set_growth_rates(self, rates=None):
+        if rates is None:
+            rates = np.concatenate([t.rates for t in self.tissues])
+        super().set_growth_rates(rates)
+
+    def step(self, dt, allow_not_converged=True):
+        n = self.n_instances
+        iters = np.zeros(n, dtype=np.int32)
+        conv = np.zeros(n, dtype=np.int32)
+        st = tf_step_stats()
+        allow = (TF_NOT_CONVERGED,) if allow_not_converged else ()
+        s = self._check(self.L.tf_batch_step(self.h, dt, _ptr(iters), _ptr(conv), C.byref(st)), "tf_batch_step", allow)
+        return {"status": s, "iters": iters, "converged": conv.astype(bool), "krylov_total": st.krylov_iters_total,
+                "ms_total": st.ms_total, "ms_assemble": st.ms_assemble, "newton_rounds": st.newton_iters}
+
+    def instance_positions(self, i):
+        p = self.positions()
+        return p[3 * self.node_off[i]:3 * self.node_off[i + 1]]
+
+    def elements_per_cta(self):
+        return int(self.L.tf_elements_per_cta(self.h))

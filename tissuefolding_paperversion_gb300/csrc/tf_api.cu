@@ -78,7 +78,9 @@ void free_all(tf_handle* h) {
     void* ptrs[] = {d.conn, d.gx, d.wdet, d.detdxde, d.Fg, d.invFg, d.rates, d.lam, d.mu, d.eta, d.exposure,
                     d.aptr, d.alist, d.farea, d.fixed, d.ext_visc, d.area, d.rowptr, d.colidx, d.diag, d.rowof,
                     d.slot, d.val, d.eblk, d.ef, d.gptr, d.glist, d.fptr, d.flist, d.uk, d.un, d.vel, d.g,
-                    d.du, d.dinv, d.r, d.p, d.z, d.q, d.rhat, d.s, d.t, d.sh, d.scal, d.part};
+                    d.du, d.dinv, d.r, d.p, d.z, d.q, d.rhat, d.s, d.t, d.sh, d.scal, d.part, d.tickets,
+                    d.seg_node0, d.elem_seg, d.cta_seg, d.cta_node0, d.cta_node1, d.seg_cta0, d.seg_active, d.seg_solve};
+    destroy_graphs(h);
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (d.host_scal) cudaFreeHost(d.host_scal);
@@ -102,7 +104,46 @@ tf_status check_handle(tf_handle* h) {
     return TF_OK;
 }
 
-tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat) {
+// CTA tables of the node-parallel kernels: every CTA covers up to
+// kNodeThreads consecutive nodes of one instance.
+tf_status setup_instances(tf_handle* h, const std::vector<int>& seg_node0, const std::vector<int>& seg_elem0) {
+    Device& d = h->d;
+    const int nseg = static_cast<int>(seg_node0.size()) - 1;
+    d.nseg = nseg;
+    std::vector<int> cta_seg, cta0, cta1, seg_cta0(nseg + 1, 0), elem_seg(d.ne);
+    for (int g = 0; g < nseg; ++g) {
+        seg_cta0[g] = static_cast<int>(cta_seg.size());
+        for (int n0 = seg_node0[g]; n0 < seg_node0[g + 1]; n0 += kNodeThreads) {
+            cta_seg.push_back(g);
+            cta0.push_back(n0);
+            cta1.push_back(std::min(n0 + kNodeThreads, seg_node0[g + 1]));
+        }
+        for (int e = seg_elem0[g]; e < seg_elem0[g + 1]; ++e) elem_seg[e] = g;
+    }
+    seg_cta0[nseg] = static_cast<int>(cta_seg.size());
+    d.ncta = static_cast<int>(cta_seg.size());
+    TF_TRY(upload(&d.seg_node0, seg_node0));
+    TF_TRY(upload(&d.elem_seg, elem_seg));
+    TF_TRY(upload(&d.cta_seg, cta_seg));
+    TF_TRY(upload(&d.cta_node0, cta0));
+    TF_TRY(upload(&d.cta_node1, cta1));
+    TF_TRY(upload(&d.seg_cta0, seg_cta0));
+    h->h_active.assign(nseg, 1);
+    TF_TRY(upload(&d.seg_active, h->h_active));
+    TF_TRY(upload(&d.seg_solve, h->h_active));
+    TF_TRY(dev_alloc(&d.tickets, nseg));
+    TF_CUDA(cudaMemset(d.tickets, 0, sizeof(unsigned) * (size_t)nseg));
+    TF_TRY(dev_alloc(&d.scal, (size_t)nseg * S_COUNT));
+    TF_CUDA(cudaMemset(d.scal, 0, sizeof(double) * (size_t)nseg * S_COUNT));
+    TF_TRY(dev_alloc(&d.part, 3 * (size_t)d.ncta));
+    TF_CUDA(cudaMallocHost(reinterpret_cast<void**>(&d.host_scal), sizeof(double) * (size_t)nseg * S_COUNT));
+    h->h_seg_node0 = seg_node0;
+    h->h_seg_elem0 = seg_elem0;
+    return TF_OK;
+}
+
+tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat, const std::vector<int>& seg_node0,
+                const std::vector<int>& seg_elem0) {
     Device& d = h->d;
     const int nn = m->n_nodes, ne = m->n_elems;
     d.nn = nn;
@@ -282,10 +323,7 @@ tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat) {
         TF_CUDA(cudaMemset(*v, 0, n3 * sizeof(double)));
     }
     TF_TRY(dev_alloc(&d.dinv, 9 * (size_t)nn));
-    TF_TRY(dev_alloc(&d.scal, (size_t)S_COUNT + 8));
-    TF_CUDA(cudaMemset(d.scal, 0, sizeof(double) * (S_COUNT + 8)));
-    TF_TRY(dev_alloc(&d.part, 3 * (size_t)cdiv(3 * (int64_t)nn, 256) + 64));
-    TF_CUDA(cudaMallocHost(reinterpret_cast<void**>(&d.host_scal), sizeof(double) * (S_COUNT + 8)));
+    TF_TRY(setup_instances(h, seg_node0, seg_elem0));
     // ---- order-fixed assembly lists ----------------------------------------------
     if (h->opt.deterministic) {
         std::vector<int> gptr(nnzb + 1, 0), glist(36 * (size_t)ne);
@@ -356,36 +394,9 @@ tf_status cuda_fail(cudaError_t e, const char* what) {
     return TF_CUDA_ERROR;
 }
 
-}  // namespace tf
 
-using namespace tf;
-
-extern "C" {
-
-const char* tf_status_string(tf_status s) {
-    switch (s) {
-        case TF_OK: return "ok";
-        case TF_NOT_CONVERGED: return "Newton iteration did not converge";
-        case TF_KRYLOV_NOT_CONVERGED: return "linear solve did not converge";
-        case TF_KRYLOV_BREAKDOWN: return "Krylov breakdown";
-        case TF_NAN_DETECTED: return "non-finite value detected";
-        case TF_BAD_INPUT: return "bad input";
-        case TF_CUDA_ERROR: return "CUDA error";
-        case TF_NO_DEVICE: return "no usable device";
-        case TF_OUT_OF_MEMORY: return "out of device memory";
-    }
-    return "unknown status";
-}
-
-const char* tf_last_error(void) { return g_last_error.c_str(); }
-
-tf_status tf_create(const tf_mesh* mesh, const tf_material* mat, const tf_options* opts, tf_handle** out) {
-    if (!out) {
-        set_error("null output handle");
-        return TF_BAD_INPUT;
-    }
-    *out = nullptr;
-    TF_TRY(validate(mesh, mat));
+tf_status create_handle(const tf_mesh* mesh, const tf_material* mat, const tf_options* opts,
+                        const std::vector<int>& seg_node0, const std::vector<int>& seg_elem0, tf_handle** out) {
     tf_handle* h = new tf_handle;
     if (opts) h->opt = *opts;
     if (h->opt.newton_tol <= 0) h->opt.newton_tol = 1e-8;
@@ -416,7 +427,7 @@ tf_status tf_create(const tf_mesh* mesh, const tf_material* mat, const tf_option
         delete h;
         return s;
     }
-    tf_status s = build(h, mesh, mat);
+    tf_status s = build(h, mesh, mat, seg_node0, seg_elem0);
     if (s != TF_OK) {
         free_all(h);
         delete h;
@@ -425,6 +436,186 @@ tf_status tf_create(const tf_mesh* mesh, const tf_material* mat, const tf_option
     *out = h;
     return TF_OK;
 }
+
+// Newton loop of updateStepNR (Simulation.cpp:6449-6590) over every
+// instance of the handle: an instance leaves the loop once |du| <= tol or
+// after max_iter+1 solves; the others continue.  Per-instance iteration
+// counts and convergence go to iters / conv (may be NULL).
+tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* iters, int32_t* conv) {
+    Device& d = h->d;
+    tf_step_stats st;
+    std::memset(&st, 0, sizeof(st));
+    TF_CUDA(cudaEventRecord(h->ev[0], h->stream));
+    TF_TRY(tf_begin_step(h, dt));
+    std::vector<int> it(d.nseg, 0), cv(d.nseg, 0), capped(d.nseg, 0);
+    std::vector<double> du2(d.nseg);
+    float ms_asm = 0.f;
+    int k = 0;
+    while (true) {
+        TF_CUDA(cudaEventRecord(h->ev[2], h->stream));
+        TF_TRY(tf_assemble(h));
+        TF_CUDA(cudaEventRecord(h->ev[3], h->stream));
+        int kit = 0;
+        double rr = 0.0;
+        tf_status s = tf_solve(h, &kit, &rr);
+        if (s != TF_OK && s != TF_KRYLOV_NOT_CONVERGED) return s;
+        float ms = 0.f;
+        TF_CUDA(cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]));
+        ms_asm += ms;
+        st.krylov_iters_total += kit;
+        st.krylov_iters_max = std::max(st.krylov_iters_max, kit);
+        st.final_relres = rr;
+        TF_TRY(launch_update(h));
+        TF_CUDA(cudaMemcpy2DAsync(du2.data(), sizeof(double), d.scal + S_DU2, sizeof(double) * S_COUNT,
+                                  sizeof(double), d.nseg, cudaMemcpyDeviceToHost, h->stream));
+        TF_TRY(sync(h));
+        double dmax = 0.0;
+        bool any_active = false;
+        for (int g = 0; g < d.nseg; ++g) {
+            if (!h->h_active[g]) continue;
+            const double dn = std::sqrt(du2[g]);
+            if (!std::isfinite(dn)) return set_error("non-finite Newton update"), TF_NAN_DETECTED;
+            dmax = std::max(dmax, dn);
+            ++it[g];
+            if (!(dn > h->opt.newton_tol)) {
+                cv[g] = 1;
+                h->h_active[g] = 0;
+            } else if (it[g] > h->opt.newton_max_iter) {
+                capped[g] = 1;
+                h->h_active[g] = 0;
+            } else {
+                any_active = true;
+            }
+        }
+        if (k < 32) st.dunorm[k] = dmax;
+        ++k;
+        if (!any_active) break;
+        TF_CUDA(cudaMemcpyAsync(d.seg_active, h->h_active.data(), sizeof(int) * (size_t)d.nseg,
+                                cudaMemcpyHostToDevice, h->stream));
+    }
+    std::fill(h->h_active.begin(), h->h_active.end(), 1);
+    TF_CUDA(cudaMemcpyAsync(d.seg_active, h->h_active.data(), sizeof(int) * (size_t)d.nseg, cudaMemcpyHostToDevice,
+                            h->stream));
+    TF_TRY(tf_end_step(h));
+    TF_CUDA(cudaEventRecord(h->ev[1], h->stream));
+    TF_TRY(sync(h));
+    float total = 0.f;
+    TF_CUDA(cudaEventElapsedTime(&total, h->ev[0], h->ev[1]));
+    int ncap = 0;
+    for (int g = 0; g < d.nseg; ++g) {
+        ncap += capped[g];
+        if (iters) iters[g] = it[g];
+        if (conv) conv[g] = cv[g];
+    }
+    st.newton_iters = k;
+    st.converged = ncap == 0 ? 1 : 0;
+    st.ms_assemble = ms_asm;
+    st.ms_total = total;
+    st.ms_solve = total - ms_asm;
+    if (stats) *stats = st;
+    if (ncap) {
+        set_error("Newton iteration reached its cap without |du| <= tol in " + std::to_string(ncap) + " instance(s)");
+        return TF_NOT_CONVERGED;
+    }
+    return TF_OK;
+}
+
+}  // namespace tf
+
+using namespace tf;
+
+extern "C" {
+
+const char* tf_status_string(tf_status s) {
+    switch (s) {
+        case TF_OK: return "ok";
+        case TF_NOT_CONVERGED: return "Newton iteration did not converge";
+        case TF_KRYLOV_NOT_CONVERGED: return "linear solve did not converge";
+        case TF_KRYLOV_BREAKDOWN: return "Krylov breakdown";
+        case TF_NAN_DETECTED: return "non-finite value detected";
+        case TF_BAD_INPUT: return "bad input";
+        case TF_CUDA_ERROR: return "CUDA error";
+        case TF_NO_DEVICE: return "no usable device";
+        case TF_OUT_OF_MEMORY: return "out of device memory";
+    }
+    return "unknown status";
+}
+
+const char* tf_last_error(void) { return g_last_error.c_str(); }
+
+tf_status tf_create(const tf_mesh* mesh, const tf_material* mat, const tf_options* opts, tf_handle** out) {
+    if (!out) {
+        set_error("null output handle");
+        return TF_BAD_INPUT;
+    }
+    *out = nullptr;
+    TF_TRY(validate(mesh, mat));
+    return create_handle(mesh, mat, opts, {0, mesh->n_nodes}, {0, mesh->n_elems}, out);
+}
+
+tf_status tf_batch_create(const tf_mesh* meshes, const tf_material* mats, int32_t n, const tf_options* opts,
+                          tf_handle** out) {
+    if (!out || !meshes || !mats || n <= 0) {
+        set_error("tf_batch_create: bad arguments");
+        return TF_BAD_INPUT;
+    }
+    *out = nullptr;
+    int64_t nn = 0, ne = 0;
+    for (int i = 0; i < n; ++i) {
+        const tf_status s = validate(&meshes[i], &mats[i]);
+        if (s != TF_OK) {
+            set_error("instance " + std::to_string(i) + ": " + g_last_error);
+            return s;
+        }
+        nn += meshes[i].n_nodes;
+        ne += meshes[i].n_elems;
+    }
+    if (nn * 3 > INT32_MAX / 2 || ne * 36 > INT32_MAX) {
+        set_error("tf_batch_create: the batch exceeds the 32-bit index range of this build");
+        return TF_BAD_INPUT;
+    }
+    std::vector<double> pos, ev, E, nu, eta;
+    std::vector<int32_t> conn, placement;
+    std::vector<uint8_t> fixed;
+    std::vector<int> node0{0}, elem0{0};
+    pos.reserve(3 * nn);
+    conn.reserve(6 * ne);
+    for (int i = 0; i < n; ++i) {
+        const tf_mesh& m = meshes[i];
+        const int off = node0.back();
+        pos.insert(pos.end(), m.node_pos, m.node_pos + 3 * (size_t)m.n_nodes);
+        ev.insert(ev.end(), m.ext_visc, m.ext_visc + 3 * (size_t)m.n_nodes);
+        fixed.insert(fixed.end(), m.fixed, m.fixed + 3 * (size_t)m.n_nodes);
+        placement.insert(placement.end(), m.node_placement, m.node_placement + m.n_nodes);
+        for (int64_t k = 0; k < 6 * (int64_t)m.n_elems; ++k) conn.push_back(m.conn[k] + off);
+        E.insert(E.end(), mats[i].E, mats[i].E + m.n_elems);
+        nu.insert(nu.end(), mats[i].nu, mats[i].nu + m.n_elems);
+        eta.insert(eta.end(), mats[i].eta, mats[i].eta + m.n_elems);
+        node0.push_back(off + m.n_nodes);
+        elem0.push_back(elem0.back() + m.n_elems);
+    }
+    tf_mesh all{static_cast<int32_t>(nn), static_cast<int32_t>(ne), pos.data(), conn.data(), fixed.data(), ev.data(),
+                placement.data()};
+    tf_material mat{E.data(), nu.data(), eta.data()};
+    return create_handle(&all, &mat, opts, node0, elem0, out);
+}
+
+tf_status tf_batch_step(tf_handle* h, double dt, int32_t* newton_iters, int32_t* converged, tf_step_stats* stats) {
+    TF_TRY(check_handle(h));
+    return newton_run(h, dt, stats, newton_iters, converged);
+}
+
+tf_status tf_get_instances(tf_handle* h, int32_t* n_instances, int32_t* node_offsets, int32_t* elem_offsets) {
+    if (!h) return set_error("null handle"), TF_BAD_INPUT;
+    if (n_instances) *n_instances = h->d.nseg;
+    for (int i = 0; i <= h->d.nseg; ++i) {
+        if (node_offsets) node_offsets[i] = h->h_seg_node0[i];
+        if (elem_offsets) elem_offsets[i] = h->h_seg_elem0[i];
+    }
+    return TF_OK;
+}
+
+int32_t tf_elements_per_cta(tf_handle* h) { return h ? h->elem_cta : 0; }
 
 tf_status tf_destroy(tf_handle* h) {
     if (!h) return TF_OK;
@@ -513,6 +704,7 @@ tf_status tf_begin_step(tf_handle* h, double dt) {
 
 tf_status tf_assemble(tf_handle* h) {
     TF_TRY(check_handle(h));
+    TF_TRY(autotune_element(h));
     TF_TRY(launch_prepare(h));
     TF_TRY(launch_element(h));
     if (h->opt.deterministic) TF_TRY(launch_deterministic_gather(h));
@@ -547,10 +739,13 @@ tf_status tf_solve(tf_handle* h, int32_t* iters, double* relres) {
 tf_status tf_update(tf_handle* h, int32_t* converged, double* dunorm) {
     TF_TRY(check_handle(h));
     TF_TRY(launch_update(h));
-    double du2 = 0.0;
-    TF_CUDA(cudaMemcpyAsync(&du2, h->d.scal + S_DU2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    Device& d = h->d;
+    std::vector<double> du2(d.nseg);
+    TF_CUDA(cudaMemcpy2DAsync(du2.data(), sizeof(double), d.scal + S_DU2, sizeof(double) * S_COUNT, sizeof(double),
+                              d.nseg, cudaMemcpyDeviceToHost, h->stream));
     TF_TRY(sync(h));
-    const double dn = std::sqrt(du2);
+    double dn = 0.0;
+    for (double v : du2) dn = std::max(dn, std::sqrt(v));
     if (dunorm) *dunorm = dn;
     if (converged) *converged = !(dn > h->opt.newton_tol);
     if (!std::isfinite(dn)) return set_error("non-finite Newton update"), TF_NAN_DETECTED;
@@ -564,54 +759,7 @@ tf_status tf_end_step(tf_handle* h) {
 
 tf_status tf_newton_step(tf_handle* h, double dt, tf_step_stats* stats) {
     TF_TRY(check_handle(h));
-    tf_step_stats st;
-    std::memset(&st, 0, sizeof(st));
-    TF_CUDA(cudaEventRecord(h->ev[0], h->stream));
-    TF_TRY(tf_begin_step(h, dt));
-    int k = 0;
-    bool converged = false, capped = false;
-    float ms_asm = 0.f;
-    while (!converged) {
-        TF_CUDA(cudaEventRecord(h->ev[2], h->stream));
-        TF_TRY(tf_assemble(h));
-        TF_CUDA(cudaEventRecord(h->ev[3], h->stream));
-        int it = 0;
-        double rr = 0.0;
-        tf_status s = tf_solve(h, &it, &rr);
-        if (s != TF_OK && s != TF_KRYLOV_NOT_CONVERGED) return s;
-        float ms = 0.f;
-        TF_CUDA(cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]));
-        ms_asm += ms;
-        st.krylov_iters_total += it;
-        st.krylov_iters_max = std::max(st.krylov_iters_max, it);
-        st.final_relres = rr;
-        int32_t conv = 0;
-        double dn = 0.0;
-        TF_TRY(tf_update(h, &conv, &dn));
-        if (k < 32) st.dunorm[k] = dn;
-        converged = conv != 0;
-        ++k;
-        if (!converged && k > h->opt.newton_max_iter) {
-            capped = true;
-            converged = true;
-        }
-    }
-    TF_TRY(tf_end_step(h));
-    TF_CUDA(cudaEventRecord(h->ev[1], h->stream));
-    TF_TRY(sync(h));
-    float total = 0.f;
-    TF_CUDA(cudaEventElapsedTime(&total, h->ev[0], h->ev[1]));
-    st.newton_iters = k;
-    st.converged = capped ? 0 : 1;
-    st.ms_assemble = ms_asm;
-    st.ms_total = total;
-    st.ms_solve = total - ms_asm;
-    if (stats) *stats = st;
-    if (capped) {
-        set_error("Newton iteration reached its cap without |du| <= tol");
-        return TF_NOT_CONVERGED;
-    }
-    return TF_OK;
+    return newton_run(h, dt, stats, nullptr, nullptr);
 }
 
 tf_status tf_get_residual(tf_handle* h, double* g) {

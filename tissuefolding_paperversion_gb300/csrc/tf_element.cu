@@ -58,6 +58,10 @@ struct ElemArgs {
     double* __restrict__ g;     // kAtomic: right-hand side
     double* __restrict__ eblk;  // kStore: [9][36*ne]
     double* __restrict__ ef;    // kStore: [18][ne]
+    // batches: elements of instances whose Newton loop has stopped are skipped
+    const int* __restrict__ elem_seg;
+    const int* __restrict__ seg_active;
+    int masked;
     // parity evaluation (reference orientation), element-relative
     int e0, count;
     double* __restrict__ Ke;
@@ -73,6 +77,9 @@ struct GaussPoint {
     double c1, c2;   // w dV lambda / J, w dV (mu - lambda lnJ) / J
     double sv[6];    // sigma_v' = w dV eta sym(grad v)
     double pv[9];    // P = 0.5 eta w dV (I/dt - grad v)
+    double fe[9];    // Fe (row-major), kept for the adjoint
+    double wdv;      // w dV
+    double sc;       // w dV / J
 };
 
 __device__ __forceinline__ void sym_apply(const double* s, double d0, double d1, double d2, double* o) {
@@ -118,8 +125,12 @@ __device__ __forceinline__ void gauss_point(const ElemArgs& A, int e, int gp, bo
 #pragma unroll
         for (int j = 0; j < 3; ++j)
             Fe[3 * i + j] = fma(F[3 * i], iFg[j], fma(F[3 * i + 1], iFg[3 + j], F[3 * i + 2] * iFg[6 + j]));
-    const double J = Fe[0] * (Fe[4] * Fe[8] - Fe[5] * Fe[7]) - Fe[1] * (Fe[3] * Fe[8] - Fe[5] * Fe[6]) +
-                     Fe[2] * (Fe[3] * Fe[7] - Fe[4] * Fe[6]);
+    // Every multiply-add below is an explicit fma, so the rounding does not
+    // depend on how the compiler contracts expressions in each instantiation
+    // of the kernel (the order-fixed assembly stays bitwise reproducible
+    // whatever tile the autotuner picks).
+    const double J = fma(Fe[0], fma(Fe[4], Fe[8], -(Fe[5] * Fe[7])),
+                         fma(-Fe[1], fma(Fe[3], Fe[8], -(Fe[5] * Fe[6])), Fe[2] * fma(Fe[3], Fe[7], -(Fe[4] * Fe[6]))));
     const double lnJ = log(J);
     const double rJ = 1.0 / J;
     const double lam = __ldg(&A.lam[e]), mu = __ldg(&A.mu[e]);
@@ -131,19 +142,23 @@ __device__ __forceinline__ void gauss_point(const ElemArgs& A, int e, int gp, bo
     b[4] = fma(Fe[0], Fe[6], fma(Fe[1], Fe[7], Fe[2] * Fe[8]));
     b[5] = fma(Fe[3], Fe[6], fma(Fe[4], Fe[7], Fe[5] * Fe[8]));
     double cf[9];  // cofactors: F^-T = cf / det F
-    cf[0] = F[4] * F[8] - F[5] * F[7];
-    cf[1] = F[5] * F[6] - F[3] * F[8];
-    cf[2] = F[3] * F[7] - F[4] * F[6];
-    cf[3] = F[2] * F[7] - F[1] * F[8];
-    cf[4] = F[0] * F[8] - F[2] * F[6];
-    cf[5] = F[1] * F[6] - F[0] * F[7];
-    cf[6] = F[1] * F[5] - F[2] * F[4];
-    cf[7] = F[2] * F[3] - F[0] * F[5];
-    cf[8] = F[0] * F[4] - F[1] * F[3];
+    cf[0] = fma(F[4], F[8], -(F[5] * F[7]));
+    cf[1] = fma(F[5], F[6], -(F[3] * F[8]));
+    cf[2] = fma(F[3], F[7], -(F[4] * F[6]));
+    cf[3] = fma(F[2], F[7], -(F[1] * F[8]));
+    cf[4] = fma(F[0], F[8], -(F[2] * F[6]));
+    cf[5] = fma(F[1], F[6], -(F[0] * F[7]));
+    cf[6] = fma(F[1], F[5], -(F[2] * F[4]));
+    cf[7] = fma(F[2], F[3], -(F[0] * F[5]));
+    cf[8] = fma(F[0], F[4], -(F[1] * F[3]));
     const double detF = fma(F[0], cf[0], fma(F[1], cf[1], F[2] * cf[2]));
     const double rdF = 1.0 / detF;
     const double wdV = __ldg(&A.wdet[q]) * detF;
+    G.wdv = wdV;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) G.fe[k] = Fe[k];
     const double sc = wdV * rJ;
+    G.sc = sc;
     const double dterm = fma(lam, lnJ, -mu);
     G.sg[0] = sc * fma(mu, b[0], dterm);
     G.sg[1] = sc * fma(mu, b[1], dterm);
@@ -152,7 +167,7 @@ __device__ __forceinline__ void gauss_point(const ElemArgs& A, int e, int gp, bo
     G.sg[4] = sc * mu * b[4];
     G.sg[5] = sc * mu * b[5];
     G.c1 = sc * lam;
-    G.c2 = sc * (mu - lam * lnJ);
+    G.c2 = sc * fma(-lam, lnJ, mu);
 #pragma unroll
     for (int a = 0; a < 6; ++a) {
         const double g0 = gX[3 * a], g1 = gX[3 * a + 1], g2 = gX[3 * a + 2];
@@ -212,6 +227,10 @@ struct GpFast<true> {
 __constant__ int8_t kPairA[21] = {0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 4, 4, 5};
 __constant__ int8_t kPairB[21] = {0, 1, 2, 3, 4, 5, 1, 2, 3, 4, 5, 2, 3, 4, 5, 3, 4, 5, 4, 5, 5};
 
+__device__ __forceinline__ bool element_live(const ElemArgs& A, int e) {
+    return e < A.ne && (!A.masked || A.seg_active[A.elem_seg[e]] != 0);
+}
+
 template <int NE, int MODE, bool VISC>
 __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -224,7 +243,7 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
         const int el = tid / kGauss;
         const int gp = tid - el * kGauss;
         const int e = blockIdx.x * NE + el;
-        if (e < A.ne) {
+        if (element_live(A, e)) {
             const bool visc = VISC && (__ldg(&A.eta[e]) != 0.0);
             GaussPoint G;
             gauss_point(A, e, gp, visc, G);
@@ -285,7 +304,7 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
         const int el = task / 18;
         const int k = task - el * 18;
         const int e = blockIdx.x * NE + el;
-        if (e >= A.ne) continue;
+        if (!element_live(A, e)) continue;
         double f = 0.0;
 #pragma unroll
         for (int gp = 0; gp < kGauss; ++gp) {
@@ -305,7 +324,7 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
         const int el = task / kPairs;
         const int pr = task - el * kPairs;
         const int e = blockIdx.x * NE + el;
-        if (e >= A.ne) continue;
+        if (!element_live(A, e)) continue;
         const int a = VISC ? pr / 6 : kPairA[pr];
         const int bq = VISC ? pr - 6 * (pr / 6) : kPairB[pr];
         double acc[9];
@@ -502,6 +521,118 @@ __global__ void __launch_bounds__(NE * kGauss) k_element_eval(ElemArgs A) {
     }
 }
 
+// ---- adjoint contractions of one converged step --------------------------
+//
+// With lambda the adjoint of step n (A^T lambda = rhs) and
+// Lam = sum_a lambda_a (x) dN_a per Gauss point:
+//   dL/dlogE_e += sum_gp w dV <sigma, Lam>                 (forces are linear in E)
+//   dL/dr_e    += n dt sum_{j=x,y} sum_gp w dV [<sigma,Lam> - (2 mu c_j.Lam c_j
+//                  + lambda tr Lam) / J]                   (c_j = column j of Fe,
+//                  d Fe / d ln Fg_jj = -Fe e_j e_j^T, ln Fg_jj = n r dt)
+//   carry to step n-1 (velocity terms, d v / d u_{n-1} = -1/dt):
+//     w_b += sum_gp 0.5 eta w dV / dt (Lam + Lam^T) dN_b
+// Element-relative outputs: gr[e], ge[e] (no atomics), carry via atomics.
+struct AdjArgs {
+    const double* __restrict__ lamv;  // adjoint vector lambda [3N]
+    double* __restrict__ carry;       // [3N] accumulates the carry to step n-1
+    double* __restrict__ gr;          // [E] growth-rate gradient (accumulated)
+    double* __restrict__ ge;          // [E] log E gradient (accumulated)
+    double ndt;                       // n * dt
+    double idt;
+};
+
+template <int NE>
+__global__ void __launch_bounds__(NE * kGauss) k_adjoint_element(ElemArgs A, AdjArgs D) {
+    __shared__ double s_gr[NE][kGauss], s_ge[NE][kGauss];
+    __shared__ double s_w[NE][kGauss][18];
+    const int el = threadIdx.x / kGauss, gp = threadIdx.x - (threadIdx.x / kGauss) * kGauss;
+    const int e = blockIdx.x * NE + el;
+    double tr = 0.0, te = 0.0;
+    double w18[18];
+#pragma unroll
+    for (int k = 0; k < 18; ++k) w18[k] = 0.0;
+    if (e < A.ne) {
+        const bool visc = __ldg(&A.eta[e]) != 0.0;
+        GaussPoint G;
+        gauss_point(A, e, gp, visc, G);
+        double Lm[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) Lm[k] = 0.0;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) {
+            const int nd = __ldg(&A.conn[a * A.ne + e]);
+            const double l0 = D.lamv[3 * nd], l1 = D.lamv[3 * nd + 1], l2 = D.lamv[3 * nd + 2];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                Lm[j] = fma(l0, G.dn[3 * a + j], Lm[j]);
+                Lm[3 + j] = fma(l1, G.dn[3 * a + j], Lm[3 + j]);
+                Lm[6 + j] = fma(l2, G.dn[3 * a + j], Lm[6 + j]);
+            }
+        }
+        // <sigma', Lam> with sigma' symmetric (00 11 22 01 02 12)
+        const double sl = fma(G.sg[0], Lm[0], fma(G.sg[1], Lm[4], fma(G.sg[2], Lm[8],
+                          fma(G.sg[3], Lm[1] + Lm[3], fma(G.sg[4], Lm[2] + Lm[6], G.sg[5] * (Lm[5] + Lm[7]))))));
+        te = sl;
+        // Fe columns, 1/J and the material, recomputed as in gauss_point
+        const double lam = __ldg(&A.lam[e]), mu = __ldg(&A.mu[e]);
+        const double trL = Lm[0] + Lm[4] + Lm[8];
+        // w dV (2 mu c.Lam c + lambda tr Lam) / J = 2 mu sc c.Lam c + c1 tr Lam
+        const double sc = G.sc;
+        (void)lam;
+        double t = 0.0;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const double c0 = G.fe[j], c1v = G.fe[3 + j], c2v = G.fe[6 + j];
+            const double Lc0 = fma(Lm[0], c0, fma(Lm[1], c1v, Lm[2] * c2v));
+            const double Lc1 = fma(Lm[3], c0, fma(Lm[4], c1v, Lm[5] * c2v));
+            const double Lc2 = fma(Lm[6], c0, fma(Lm[7], c1v, Lm[8] * c2v));
+            const double cLc = fma(c0, Lc0, fma(c1v, Lc1, c2v * Lc2));
+            t += sl - fma(2.0 * mu * sc, cLc, G.c1 * trL);
+        }
+        tr = D.ndt * t;
+        if (visc) {
+            const double hw = 0.5 * __ldg(&A.eta[e]) * G.wdv * D.idt;
+            double S[9];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) S[3 * i + k] = hw * (Lm[3 * i + k] + Lm[3 * k + i]);
+#pragma unroll
+            for (int b = 0; b < 6; ++b) {
+                const double d0 = G.dn[3 * b], d1 = G.dn[3 * b + 1], d2 = G.dn[3 * b + 2];
+                w18[3 * b] = fma(S[0], d0, fma(S[1], d1, S[2] * d2));
+                w18[3 * b + 1] = fma(S[3], d0, fma(S[4], d1, S[5] * d2));
+                w18[3 * b + 2] = fma(S[6], d0, fma(S[7], d1, S[8] * d2));
+            }
+        }
+    }
+    s_gr[el][gp] = tr;
+    s_ge[el][gp] = te;
+#pragma unroll
+    for (int k = 0; k < 18; ++k) s_w[el][gp][k] = w18[k];
+    __syncthreads();
+    if (e < A.ne && gp == 0) {
+        double a = 0.0, b = 0.0;
+#pragma unroll
+        for (int q = 0; q < kGauss; ++q) {
+            a += s_gr[el][q];
+            b += s_ge[el][q];
+        }
+        D.gr[e] += a;
+        D.ge[e] += b;
+    }
+    for (int task = threadIdx.x; task < NE * 18; task += NE * kGauss) {
+        const int l = task / 18, k = task - 18 * (task / 18);
+        const int ee = blockIdx.x * NE + l;
+        if (ee >= A.ne || __ldg(&A.eta[ee]) == 0.0) continue;
+        double v = 0.0;
+#pragma unroll
+        for (int q = 0; q < kGauss; ++q) v += s_w[l][q][k];
+        const int nd = __ldg(&A.conn[(k / 3) * A.ne + ee]);
+        atomicAdd(&D.carry[3 * nd + (k % 3)], v);
+    }
+}
+
 ElemArgs make_args(tf_handle* h) {
     const Device& d = h->d;
     ElemArgs A{};
@@ -522,20 +653,38 @@ ElemArgs make_args(tf_handle* h) {
     A.g = d.g;
     A.eblk = d.eblk;
     A.ef = d.ef;
+    A.elem_seg = d.elem_seg;
+    A.seg_active = d.seg_active;
+    A.masked = d.nseg > 1 ? 1 : 0;
     return A;
 }
 
 template <int NE, int MODE, bool VISC>
 tf_status launch_fast(tf_handle* h, const ElemArgs& A) {
     const size_t smem = sizeof(GpFast<VISC>) * NE * kGauss;
-    static bool configured = false;
-    if (!configured) {
+    static int configured_device = -1;
+    if (configured_device != h->device) {
         TF_CUDA(cudaFuncSetAttribute(k_element<NE, MODE, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
+        configured_device = h->device;
     }
     k_element<NE, MODE, VISC><<<cdiv(A.ne, NE), NE * kGauss, smem, h->stream>>>(A);
     TF_LAUNCH_CHECK(h);
     return TF_OK;
+}
+
+template <int NE>
+tf_status launch_ne(tf_handle* h, const ElemArgs& A) {
+    const bool visc = h->d.any_visc;
+    if (h->opt.deterministic) return visc ? launch_fast<NE, kStore, true>(h, A) : launch_fast<NE, kStore, false>(h, A);
+    return visc ? launch_fast<NE, kAtomic, true>(h, A) : launch_fast<NE, kAtomic, false>(h, A);
+}
+
+tf_status launch_with(tf_handle* h, const ElemArgs& A, int ne_per_cta) {
+    switch (ne_per_cta) {
+        case 8: return launch_ne<8>(h, A);
+        case 32: return launch_ne<32>(h, A);
+        default: return launch_ne<16>(h, A);
+    }
 }
 
 }  // namespace
@@ -543,10 +692,47 @@ tf_status launch_fast(tf_handle* h, const ElemArgs& A) {
 tf_status launch_element(tf_handle* h) {
     const ElemArgs A = make_args(h);
     if (A.ne <= 0) return TF_OK;
-    const bool visc = h->d.any_visc;
-    if (h->opt.deterministic)
-        return visc ? launch_fast<kElemPerCta, kStore, true>(h, A) : launch_fast<kElemPerCta, kStore, false>(h, A);
-    return visc ? launch_fast<kElemPerCta, kAtomic, true>(h, A) : launch_fast<kElemPerCta, kAtomic, false>(h, A);
+    return launch_with(h, A, h->elem_cta);
+}
+
+// Picks the prisms-per-CTA tile (8, 16 or 32 prisms x 6 Gauss points) by
+// timing each candidate on the handle's own mesh; run once per handle before
+// the first assembly.  Results do not depend on the choice.
+tf_status autotune_element(tf_handle* h) {
+    if (h->tuned || h->d.ne <= 0) return TF_OK;
+    h->tuned = true;
+    if (h->opt.autotune_off) return TF_OK;
+    const ElemArgs A = make_args(h);
+    const int cand[3] = {8, 16, 32};
+    float best = 1e30f;
+    for (int c : cand) {
+        if (launch_with(h, A, c) != TF_OK) continue;  // warm-up (and smem attribute)
+        TF_CUDA(cudaEventRecord(h->ev[4], h->stream));
+        for (int r = 0; r < 2; ++r) {
+            const tf_status s = launch_with(h, A, c);
+            if (s != TF_OK) return s;
+        }
+        TF_CUDA(cudaEventRecord(h->ev[5], h->stream));
+        TF_CUDA(cudaEventSynchronize(h->ev[5]));
+        float ms = 0.f;
+        TF_CUDA(cudaEventElapsedTime(&ms, h->ev[4], h->ev[5]));
+        if (ms < best) {
+            best = ms;
+            h->elem_cta = c;
+        }
+    }
+    return TF_OK;
+}
+
+tf_status launch_adjoint_element(tf_handle* h, const double* lamv, double* carry, double* gr, double* ge,
+                                 double ndt) {
+    ElemArgs A = make_args(h);
+    if (A.ne <= 0) return TF_OK;
+    AdjArgs D{lamv, carry, gr, ge, ndt, 1.0 / h->dt};
+    constexpr int NE = 16;
+    k_adjoint_element<NE><<<cdiv(A.ne, NE), NE * kGauss, 0, h->stream>>>(A, D);
+    TF_LAUNCH_CHECK(h);
+    return TF_OK;
 }
 
 tf_status launch_element_eval(tf_handle* h, int e0, int count, double* Ke, double* Kv, double* fe, double* fv) {

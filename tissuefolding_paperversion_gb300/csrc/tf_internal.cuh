@@ -62,20 +62,31 @@ struct Device {
     double* dinv = nullptr;     // [9nn] inverse diagonal blocks
     // Krylov work vectors
     double *r = nullptr, *p = nullptr, *z = nullptr, *q = nullptr, *rhat = nullptr, *s = nullptr, *t = nullptr, *sh = nullptr;
-    double* scal = nullptr;     // device scalars
-    double* part = nullptr;     // per-CTA partial sums
-    double* host_scal = nullptr; // pinned mirror
+    double* scal = nullptr;     // device scalars, S_COUNT per instance
+    double* part = nullptr;     // per-CTA partial sums [3][ncta]
+    double* host_scal = nullptr; // pinned mirror of scal
+    unsigned* tickets = nullptr; // per-instance reduction tickets
+    // instances (a batch is one block-diagonal system; a single mesh is a
+    // batch of one)
+    int nseg = 1;
+    int ncta = 0;               // CTAs of the node-parallel kernels
+    int* seg_node0 = nullptr;   // [nseg+1] node offsets
+    int* elem_seg = nullptr;    // [ne] instance of each element
+    int* cta_seg = nullptr;     // [ncta] instance of each CTA
+    int* cta_node0 = nullptr;   // [ncta] first node of each CTA
+    int* cta_node1 = nullptr;   // [ncta] end node of each CTA
+    int* seg_cta0 = nullptr;    // [nseg+1] CTA ranges per instance
+    int* seg_active = nullptr;  // [nseg] 1 while the instance's Newton loop runs
+    int* seg_solve = nullptr;   // [nseg] instances a linear solve works on
 };
 
 // Indices into Device::scal (device-resident Krylov scalars).
 enum Scal {
     S_RZ = 0, S_RZ_OLD, S_PQ, S_ALPHA, S_BETA, S_OMEGA, S_RHO, S_RHO_OLD,
-    S_TS, S_TT, S_RR, S_BB, S_RR0, S_DU2, S_FLAG, S_COUNT = 32
+    S_TS, S_TT, S_RR, S_BB, S_RR0, S_DU2, S_FLAG, S_ITER, S_TOL2, S_COUNT = 32
 };
 
-constexpr int kRedBlocks = 608;      // 4 x 152 SMs: CTAs of the reduction-bearing vector kernels
-constexpr int kRedThreads = 256;
-constexpr int kPartStride = 1024;    // doubles between partial-sum groups
+constexpr int kNodeThreads = 256;    // nodes per CTA of the node-parallel kernels
 
 }  // namespace tf
 
@@ -93,6 +104,12 @@ struct tf_handle {
     std::vector<int> h_conn;
     std::vector<int> h_rowptr, h_colidx;
     std::vector<uint8_t> h_fixed;
+    std::vector<int> h_seg_node0, h_seg_elem0;  // host copies of the instance offsets
+    std::vector<int> h_active;                  // host mirror of seg_active
+    int elem_cta = 16;                          // prisms per CTA of the element kernel (autotuned)
+    bool tuned = false;
+    cudaGraphExec_t graph[2][4] = {};           // Krylov chunks [method-1][log2(chunk/8)]
+    int64_t graph_kernels[2][4] = {};
 };
 
 namespace tf {
@@ -123,6 +140,8 @@ tf_status launch_viscosity_surfaces(tf_handle* h);
 tf_status launch_block_inverse(tf_handle* h);
 tf_status krylov_solve(tf_handle* h, int* iters, double* relres);
 tf_status launch_update(tf_handle* h);
+tf_status autotune_element(tf_handle* h);
+void destroy_graphs(tf_handle* h);
 
 inline int cdiv(int64_t a, int64_t b) { return static_cast<int>((a + b - 1) / b); }
 

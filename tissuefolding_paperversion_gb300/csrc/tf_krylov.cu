@@ -5,32 +5,62 @@
 //   * block-Jacobi preconditioner on the 3x3 diagonal blocks;
 //   * CG when every element has zero internal viscosity (A symmetric),
 //     BiCGStab otherwise (the viscous tangent is not symmetric);
+//   * a batch of independent instances is one block-diagonal system, solved
+//     with separate Krylov scalars, tolerance and stop flag per instance:
+//     every CTA of the node-parallel kernels covers nodes of one instance,
+//     reductions are per instance, and an instance whose flag is set is
+//     skipped by all later kernels (a single mesh is a batch of one);
 //   * all scalars stay on the device: each reduction kernel writes per-CTA
-//     partial sums and the last CTA to finish (atomic ticket, no waiting)
-//     folds them in a fixed order, so results are bitwise reproducible;
-//   * the host checks convergence once per chunk of iterations; kernels of
-//     a chunk that run after convergence or breakdown return immediately.
+//     partial sums and the last CTA of the instance to finish (atomic ticket,
+//     no waiting) folds them in a fixed order, so results are bitwise
+//     reproducible;
+//   * iterations run in chunks of 8-64 replayed from CUDA graphs; the host
+//     reads the flags once per chunk.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "tf_internal.cuh"
 
 namespace tf {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = kNodeThreads;
 
 enum Flag { F_RUNNING = 0, F_CONVERGED = 1, F_BREAKDOWN = 2, F_NAN = 3 };
-enum Extra { S_ITER = 20, S_TOL2 = 21, S_RHAT_V = 22 };
 
 struct Ctx {
-    int nn;
     const int* __restrict__ rowptr;
     const int* __restrict__ colidx;
     const double* __restrict__ val;
     const double* __restrict__ dinv;
-    double* scal;
-    double* part;         // [3][gridDim.x]
-    unsigned* counter;
+    double* scal;               // [nseg][S_COUNT]
+    double* part;               // [3][ncta]
+    unsigned* tickets;          // [nseg]
+    int ncta;
+    const int* __restrict__ cta_seg;
+    const int* __restrict__ cta_node0;
+    const int* __restrict__ cta_node1;
+    const int* __restrict__ seg_cta0;
+    const int* __restrict__ seg_solve;
 };
+
+struct Where {
+    int node;    // node of this thread
+    bool valid;  // node inside this CTA's range
+    int seg;     // instance of this CTA
+    double* s;   // its scalars
+};
+
+__device__ __forceinline__ Where where(const Ctx& c) {
+    Where w;
+    w.seg = c.cta_seg[blockIdx.x];
+    w.node = c.cta_node0[blockIdx.x] + threadIdx.x;
+    w.valid = w.node < c.cta_node1[blockIdx.x];
+    w.s = c.scal + (size_t)w.seg * S_COUNT;
+    return w;
+}
 
 template <int NV>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double (*sm)[kThreads / 32]) {
@@ -52,21 +82,23 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double (*sm)[kThreads
             v[k] = x;  // valid in thread 0
         }
     }
+    __syncthreads();
 }
 
-// Writes this CTA's partial sums and returns true in the CTA that arrives
-// last; that CTA then holds the fixed-order totals in `tot` (thread 0).
+// Writes this CTA's partial sums; returns true in the CTA of the instance
+// that arrives last, whose thread 0 then holds the fixed-order totals.
 template <int NV>
-__device__ bool reduce_grid(const Ctx& c, double (&v)[NV], double (&tot)[NV]) {
+__device__ bool reduce_seg(const Ctx& c, int seg, double (&v)[NV], double (&tot)[NV]) {
     __shared__ double sm[NV][kThreads / 32];
     __shared__ bool last;
     block_sum<NV>(v, sm);
+    const int b0 = c.seg_cta0[seg], b1 = c.seg_cta0[seg + 1];
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) c.part[k * gridDim.x + blockIdx.x] = v[k];
+        for (int k = 0; k < NV; ++k) c.part[(size_t)k * c.ncta + blockIdx.x] = v[k];
         __threadfence();
-        const unsigned ticket = atomicAdd(c.counter, 1u);
-        last = (ticket == gridDim.x - 1);
+        const unsigned ticket = atomicAdd(&c.tickets[seg], 1u);
+        last = (ticket == (unsigned)(b1 - b0 - 1));
     }
     __syncthreads();
     if (!last) return false;
@@ -75,17 +107,16 @@ __device__ bool reduce_grid(const Ctx& c, double (&v)[NV], double (&tot)[NV]) {
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
         acc[k] = 0.0;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += kThreads) acc[k] += __ldcg(&c.part[k * gridDim.x + b]);
+        for (int b = b0 + threadIdx.x; b < b1; b += kThreads) acc[k] += __ldcg(&c.part[(size_t)k * c.ncta + b]);
     }
-    __syncthreads();
     block_sum<NV>(acc, sm);
 #pragma unroll
     for (int k = 0; k < NV; ++k) tot[k] = acc[k];
-    if (threadIdx.x == 0) *c.counter = 0u;
+    if (threadIdx.x == 0) c.tickets[seg] = 0u;
     return true;
 }
 
-__device__ __forceinline__ bool stopped(const Ctx& c) { return __ldcg(&c.scal[S_FLAG]) != 0.0; }
+__device__ __forceinline__ bool stopped(const Where& w) { return __ldcg(&w.s[S_FLAG]) != 0.0; }
 
 __device__ __forceinline__ void apply_dinv(const double* __restrict__ D, const double r[3], double z[3]) {
     z[0] = fma(D[0], r[0], fma(D[1], r[1], D[2] * r[2]));
@@ -109,24 +140,44 @@ __device__ __forceinline__ void bsr_row(const Ctx& c, int i, const double* __res
     y[2] = y2;
 }
 
+// Sets an instance's stop flag from its first scalars (bb = |b|^2).
+__device__ __forceinline__ void start_flags(double* s, double bb, double tol2) {
+    s[S_BB] = bb;
+    s[S_RR] = bb;
+    s[S_RR0] = bb;
+    s[S_ITER] = 0.0;
+    s[S_TOL2] = tol2;
+    s[S_FLAG] = (bb == 0.0) ? F_CONVERGED : (isfinite(bb) ? F_RUNNING : F_NAN);
+}
+
 // ---- CG -------------------------------------------------------------------
 
-// r = b, z = M^-1 r, p = z, x = 0;  rz = (r,z), bb = (b,b)
+// r = b, z = M^-1 r, p = z, x = 0;  rz = (r,z), bb = (b,b).  Instances left
+// out of this solve (seg_solve = 0) either keep their x (keep != 0, a retry of
+// other instances) or solve with b = 0, which sets x = 0 (an instance whose
+// Newton loop has stopped); both are flagged done at once.
 __global__ void k_cg_init(Ctx c, const double* __restrict__ b, double* __restrict__ x, double* __restrict__ r,
-                          double* __restrict__ z, double* __restrict__ p) {
-    const int i = blockIdx.x * kThreads + threadIdx.x;
+                          double* __restrict__ z, double* __restrict__ p, double tol2, int keep) {
+    const Where w = where(c);
+    const bool active = c.seg_solve[w.seg] != 0;
+    if (!active && keep) {
+        if (threadIdx.x == 0) w.s[S_FLAG] = F_CONVERGED;
+        return;
+    }
     double v[2] = {0.0, 0.0};
-    if (i < c.nn) {
+    if (w.valid) {
+        const int i = w.node;
         double rr[3], zz[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            rr[d] = b[3 * i + d];
+            rr[d] = active ? b[3 * i + d] : 0.0;
             r[3 * i + d] = rr[d];
             x[3 * i + d] = 0.0;
         }
         apply_dinv(c.dinv + 9 * (size_t)i, rr, zz);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
+            if (!active) zz[d] = 0.0;
             z[3 * i + d] = zz[d];
             p[3 * i + d] = zz[d];
             v[0] = fma(rr[d], zz[d], v[0]);
@@ -134,38 +185,34 @@ __global__ void k_cg_init(Ctx c, const double* __restrict__ b, double* __restric
         }
     }
     double tot[2];
-    if (reduce_grid<2>(c, v, tot) && threadIdx.x == 0) {
-        c.scal[S_RZ] = tot[0];
-        c.scal[S_BB] = tot[1];
-        c.scal[S_RR] = tot[1];
-        c.scal[S_RR0] = tot[1];
-        c.scal[S_ITER] = 0.0;
-        c.scal[S_FLAG] = (tot[1] == 0.0) ? F_CONVERGED : (isfinite(tot[1]) ? F_RUNNING : F_NAN);
+    if (reduce_seg<2>(c, w.seg, v, tot) && threadIdx.x == 0) {
+        w.s[S_RZ] = tot[0];
+        start_flags(w.s, tot[1], tol2);
     }
 }
 
 // q = A p; alpha = rz / (p, q)
 __global__ void k_cg_spmv(Ctx c, const double* __restrict__ p, double* __restrict__ q) {
-    if (stopped(c)) return;
-    const int i = blockIdx.x * kThreads + threadIdx.x;
+    const Where w = where(c);
+    if (stopped(w)) return;
     double v[1] = {0.0};
-    if (i < c.nn) {
+    if (w.valid) {
         double y[3];
-        bsr_row(c, i, p, y);
+        bsr_row(c, w.node, p, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            q[3 * i + d] = y[d];
-            v[0] = fma(p[3 * i + d], y[d], v[0]);
+            q[3 * w.node + d] = y[d];
+            v[0] = fma(p[3 * w.node + d], y[d], v[0]);
         }
     }
     double tot[1];
-    if (reduce_grid<1>(c, v, tot) && threadIdx.x == 0) {
+    if (reduce_seg<1>(c, w.seg, v, tot) && threadIdx.x == 0) {
         const double pq = tot[0];
         if (!(pq > 0.0) || !isfinite(pq)) {
-            c.scal[S_FLAG] = isfinite(pq) ? F_BREAKDOWN : F_NAN;
+            w.s[S_FLAG] = isfinite(pq) ? F_BREAKDOWN : F_NAN;
         } else {
-            c.scal[S_PQ] = pq;
-            c.scal[S_ALPHA] = c.scal[S_RZ] / pq;
+            w.s[S_PQ] = pq;
+            w.s[S_ALPHA] = w.s[S_RZ] / pq;
         }
     }
 }
@@ -173,11 +220,12 @@ __global__ void k_cg_spmv(Ctx c, const double* __restrict__ p, double* __restric
 // x += alpha p; r -= alpha q; z = M^-1 r;  beta = (r,z)_new / (r,z)
 __global__ void k_cg_update(Ctx c, double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
                             const double* __restrict__ p, const double* __restrict__ q) {
-    if (stopped(c)) return;
-    const double alpha = __ldcg(&c.scal[S_ALPHA]);
-    const int i = blockIdx.x * kThreads + threadIdx.x;
+    const Where w = where(c);
+    if (stopped(w)) return;
+    const double alpha = __ldcg(&w.s[S_ALPHA]);
     double v[2] = {0.0, 0.0};
-    if (i < c.nn) {
+    if (w.valid) {
+        const int i = w.node;
         double rr[3], zz[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
@@ -195,38 +243,49 @@ __global__ void k_cg_update(Ctx c, double* __restrict__ x, double* __restrict__ 
         }
     }
     double tot[2];
-    if (reduce_grid<2>(c, v, tot) && threadIdx.x == 0) {
+    if (reduce_seg<2>(c, w.seg, v, tot) && threadIdx.x == 0) {
+        double* s = w.s;
         const double rz = tot[0], rr = tot[1];
-        c.scal[S_BETA] = rz / c.scal[S_RZ];
-        c.scal[S_RZ] = rz;
-        c.scal[S_RR] = rr;
-        c.scal[S_ITER] += 1.0;
-        if (!isfinite(rr)) c.scal[S_FLAG] = F_NAN;
-        else if (rr <= c.scal[S_TOL2] * c.scal[S_BB]) c.scal[S_FLAG] = F_CONVERGED;
-        else if (!(rz > 0.0)) c.scal[S_FLAG] = F_BREAKDOWN;
+        s[S_BETA] = rz / s[S_RZ];
+        s[S_RZ] = rz;
+        s[S_RR] = rr;
+        s[S_ITER] += 1.0;
+        if (!isfinite(rr)) s[S_FLAG] = F_NAN;
+        else if (rr <= s[S_TOL2] * s[S_BB]) s[S_FLAG] = F_CONVERGED;
+        else if (!(rz > 0.0)) s[S_FLAG] = F_BREAKDOWN;
     }
 }
 
 // p = z + beta p
 __global__ void k_cg_direction(Ctx c, const double* __restrict__ z, double* __restrict__ p) {
-    if (stopped(c)) return;
-    const double beta = __ldcg(&c.scal[S_BETA]);
-    const int k = blockIdx.x * kThreads + threadIdx.x;
-    if (k < 3 * c.nn) p[k] = fma(beta, p[k], z[k]);
+    const Where w = where(c);
+    if (stopped(w) || !w.valid) return;
+    const double beta = __ldcg(&w.s[S_BETA]);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int k = 3 * w.node + d;
+        p[k] = fma(beta, p[k], z[k]);
+    }
 }
 
 // ---- BiCGStab ---------------------------------------------------------------
 
 // r = rhat = b, p = v = 0, x = 0; rho = (rhat, r)
 __global__ void k_bi_init(Ctx c, const double* __restrict__ b, double* __restrict__ x, double* __restrict__ r,
-                          double* __restrict__ rhat, double* __restrict__ p, double* __restrict__ v) {
-    const int i = blockIdx.x * kThreads + threadIdx.x;
+                          double* __restrict__ rhat, double* __restrict__ p, double* __restrict__ v, double tol2,
+                          int keep) {
+    const Where w = where(c);
+    const bool active = c.seg_solve[w.seg] != 0;
+    if (!active && keep) {
+        if (threadIdx.x == 0) w.s[S_FLAG] = F_CONVERGED;
+        return;
+    }
     double s[1] = {0.0};
-    if (i < c.nn) {
+    if (w.valid) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const int k = 3 * i + d;
-            const double bk = b[k];
+            const int k = 3 * w.node + d;
+            const double bk = active ? b[k] : 0.0;
             r[k] = bk;
             rhat[k] = bk;
             p[k] = 0.0;
@@ -236,26 +295,22 @@ __global__ void k_bi_init(Ctx c, const double* __restrict__ b, double* __restric
         }
     }
     double tot[1];
-    if (reduce_grid<1>(c, s, tot) && threadIdx.x == 0) {
-        c.scal[S_RHO] = tot[0];
-        c.scal[S_BB] = tot[0];
-        c.scal[S_RR] = tot[0];
-        c.scal[S_RR0] = tot[0];
-        c.scal[S_ALPHA] = 1.0;
-        c.scal[S_OMEGA] = 1.0;
-        c.scal[S_BETA] = 0.0;
-        c.scal[S_ITER] = 0.0;
-        c.scal[S_FLAG] = (tot[0] == 0.0) ? F_CONVERGED : (isfinite(tot[0]) ? F_RUNNING : F_NAN);
+    if (reduce_seg<1>(c, w.seg, s, tot) && threadIdx.x == 0) {
+        w.s[S_RHO] = tot[0];
+        w.s[S_ALPHA] = 1.0;
+        w.s[S_OMEGA] = 1.0;
+        w.s[S_BETA] = 0.0;
+        start_flags(w.s, tot[0], tol2);
     }
 }
 
 // p = r + beta (p - omega v); phat = M^-1 p
 __global__ void k_bi_dir(Ctx c, const double* __restrict__ r, const double* __restrict__ v, double* __restrict__ p,
                          double* __restrict__ phat) {
-    if (stopped(c)) return;
-    const double beta = __ldcg(&c.scal[S_BETA]), omega = __ldcg(&c.scal[S_OMEGA]);
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    if (i >= c.nn) return;
+    const Where w = where(c);
+    if (stopped(w) || !w.valid) return;
+    const double beta = __ldcg(&w.s[S_BETA]), omega = __ldcg(&w.s[S_OMEGA]);
+    const int i = w.node;
     double pp[3], z[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -271,66 +326,97 @@ __global__ void k_bi_dir(Ctx c, const double* __restrict__ r, const double* __re
 // v = A phat; alpha = rho / (rhat, v)
 __global__ void k_bi_spmv1(Ctx c, const double* __restrict__ phat, const double* __restrict__ rhat,
                            double* __restrict__ v) {
-    if (stopped(c)) return;
-    const int i = blockIdx.x * kThreads + threadIdx.x;
+    const Where w = where(c);
+    if (stopped(w)) return;
     double s[1] = {0.0};
-    if (i < c.nn) {
+    if (w.valid) {
         double y[3];
-        bsr_row(c, i, phat, y);
+        bsr_row(c, w.node, phat, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            v[3 * i + d] = y[d];
-            s[0] = fma(rhat[3 * i + d], y[d], s[0]);
+            v[3 * w.node + d] = y[d];
+            s[0] = fma(rhat[3 * w.node + d], y[d], s[0]);
         }
     }
     double tot[1];
-    if (reduce_grid<1>(c, s, tot) && threadIdx.x == 0) {
+    if (reduce_seg<1>(c, w.seg, s, tot) && threadIdx.x == 0) {
         const double rv = tot[0];
-        if (rv == 0.0 || !isfinite(rv)) c.scal[S_FLAG] = isfinite(rv) ? F_BREAKDOWN : F_NAN;
-        else c.scal[S_ALPHA] = c.scal[S_RHO] / rv;
+        if (rv == 0.0 || !isfinite(rv)) w.s[S_FLAG] = isfinite(rv) ? F_BREAKDOWN : F_NAN;
+        else w.s[S_ALPHA] = w.s[S_RHO] / rv;
     }
 }
 
-// s = r - alpha v; shat = M^-1 s
+// s = r - alpha v; shat = M^-1 s; |s|^2.  When |s| already meets the
+// tolerance the half step is the solution: x += alpha phat and stop (t and
+// omega would otherwise be formed from a vanishing s).
 __global__ void k_bi_s(Ctx c, const double* __restrict__ r, const double* __restrict__ v, double* __restrict__ s,
-                       double* __restrict__ shat) {
-    if (stopped(c)) return;
-    const double alpha = __ldcg(&c.scal[S_ALPHA]);
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    if (i >= c.nn) return;
-    double ss[3], z[3];
+                       double* __restrict__ shat, double* __restrict__ x, const double* __restrict__ phat) {
+    const Where w = where(c);
+    if (stopped(w)) return;
+    const double alpha = __ldcg(&w.s[S_ALPHA]);
+    double acc[1] = {0.0};
+    if (w.valid) {
+        const int i = w.node;
+        double ss[3], z[3];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const int k = 3 * i + d;
-        ss[d] = fma(-alpha, v[k], r[k]);
-        s[k] = ss[d];
+        for (int d = 0; d < 3; ++d) {
+            const int k = 3 * i + d;
+            ss[d] = fma(-alpha, v[k], r[k]);
+            s[k] = ss[d];
+            acc[0] = fma(ss[d], ss[d], acc[0]);
+        }
+        apply_dinv(c.dinv + 9 * (size_t)i, ss, z);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) shat[3 * i + d] = z[d];
     }
-    apply_dinv(c.dinv + 9 * (size_t)i, ss, z);
+    double tot[1];
+    if (reduce_seg<1>(c, w.seg, acc, tot) && threadIdx.x == 0) {
+        if (!isfinite(tot[0])) w.s[S_FLAG] = F_NAN;
+        else if (tot[0] <= w.s[S_TOL2] * w.s[S_BB]) w.s[S_FLAG] = -1.0;  // half step converged
+    }
+}
+
+// Applies the half step x += alpha phat of instances flagged -1 by k_bi_s
+// and marks them converged.
+__global__ void k_bi_half(Ctx c, double* __restrict__ x, const double* __restrict__ phat) {
+    const Where w = where(c);
+    if (__ldcg(&w.s[S_FLAG]) != -1.0) return;
+    const double alpha = __ldcg(&w.s[S_ALPHA]);
+    if (w.valid)
 #pragma unroll
-    for (int d = 0; d < 3; ++d) shat[3 * i + d] = z[d];
+        for (int d = 0; d < 3; ++d) {
+            const int k = 3 * w.node + d;
+            x[k] = fma(alpha, phat[k], x[k]);
+        }
+    double tot[1] = {0.0}, v[1] = {0.0};
+    if (reduce_seg<1>(c, w.seg, v, tot) && threadIdx.x == 0) {
+        w.s[S_RR] = 0.0;
+        w.s[S_ITER] += 1.0;
+        w.s[S_FLAG] = F_CONVERGED;
+    }
 }
 
 // t = A shat; omega = (t, s) / (t, t)
 __global__ void k_bi_spmv2(Ctx c, const double* __restrict__ shat, const double* __restrict__ s,
                            double* __restrict__ t) {
-    if (stopped(c)) return;
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    double w[2] = {0.0, 0.0};
-    if (i < c.nn) {
+    const Where w = where(c);
+    if (stopped(w)) return;
+    double acc[2] = {0.0, 0.0};
+    if (w.valid) {
         double y[3];
-        bsr_row(c, i, shat, y);
+        bsr_row(c, w.node, shat, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            t[3 * i + d] = y[d];
-            w[0] = fma(y[d], s[3 * i + d], w[0]);
-            w[1] = fma(y[d], y[d], w[1]);
+            t[3 * w.node + d] = y[d];
+            acc[0] = fma(y[d], s[3 * w.node + d], acc[0]);
+            acc[1] = fma(y[d], y[d], acc[1]);
         }
     }
     double tot[2];
-    if (reduce_grid<2>(c, w, tot) && threadIdx.x == 0) {
+    if (reduce_seg<2>(c, w.seg, acc, tot) && threadIdx.x == 0) {
         const double ts = tot[0], tt = tot[1];
-        if (!isfinite(ts) || !isfinite(tt)) c.scal[S_FLAG] = F_NAN;
-        else c.scal[S_OMEGA] = (tt > 0.0) ? ts / tt : 0.0;
+        if (!isfinite(ts) || !isfinite(tt)) w.s[S_FLAG] = F_NAN;
+        else w.s[S_OMEGA] = (tt > 0.0) ? ts / tt : 0.0;
     }
 }
 
@@ -338,163 +424,227 @@ __global__ void k_bi_spmv2(Ctx c, const double* __restrict__ shat, const double*
 __global__ void k_bi_x(Ctx c, double* __restrict__ x, double* __restrict__ r, const double* __restrict__ rhat,
                        const double* __restrict__ phat, const double* __restrict__ shat, const double* __restrict__ s,
                        const double* __restrict__ t) {
-    if (stopped(c)) return;
-    const double alpha = __ldcg(&c.scal[S_ALPHA]), omega = __ldcg(&c.scal[S_OMEGA]);
-    const int i = blockIdx.x * kThreads + threadIdx.x;
-    double w[2] = {0.0, 0.0};
-    if (i < c.nn) {
+    const Where w = where(c);
+    if (stopped(w)) return;
+    const double alpha = __ldcg(&w.s[S_ALPHA]), omega = __ldcg(&w.s[S_OMEGA]);
+    double acc[2] = {0.0, 0.0};
+    if (w.valid) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const int k = 3 * i + d;
+            const int k = 3 * w.node + d;
             x[k] = fma(omega, shat[k], fma(alpha, phat[k], x[k]));
             const double rk = fma(-omega, t[k], s[k]);
             r[k] = rk;
-            w[0] = fma(rhat[k], rk, w[0]);
-            w[1] = fma(rk, rk, w[1]);
+            acc[0] = fma(rhat[k], rk, acc[0]);
+            acc[1] = fma(rk, rk, acc[1]);
         }
     }
     double tot[2];
-    if (reduce_grid<2>(c, w, tot) && threadIdx.x == 0) {
+    if (reduce_seg<2>(c, w.seg, acc, tot) && threadIdx.x == 0) {
+        double* q = w.s;
         const double rho = tot[0], rr = tot[1];
-        const double omega_ = c.scal[S_OMEGA];
-        c.scal[S_BETA] = (rho / c.scal[S_RHO]) * (c.scal[S_ALPHA] / omega_);
-        c.scal[S_RHO] = rho;
-        c.scal[S_RR] = rr;
-        c.scal[S_ITER] += 1.0;
-        if (!isfinite(rr)) c.scal[S_FLAG] = F_NAN;
-        else if (rr <= c.scal[S_TOL2] * c.scal[S_BB]) c.scal[S_FLAG] = F_CONVERGED;
-        else if (omega_ == 0.0 || rho == 0.0) c.scal[S_FLAG] = F_BREAKDOWN;
+        const double om = q[S_OMEGA];
+        q[S_BETA] = (rho / q[S_RHO]) * (q[S_ALPHA] / om);
+        q[S_RHO] = rho;
+        q[S_RR] = rr;
+        q[S_ITER] += 1.0;
+        if (!isfinite(rr)) q[S_FLAG] = F_NAN;
+        else if (rr <= q[S_TOL2] * q[S_BB]) q[S_FLAG] = F_CONVERGED;
+        else if (om == 0.0 || rho == 0.0) q[S_FLAG] = F_BREAKDOWN;
     }
 }
 
 // ---- Newton update ------------------------------------------------------------
 
-// uk += du; |du|^2  (NewtonRaphsonSolver::updateUkInIteration :755-761,
-// checkConvergenceViaDeltaU :727-740)
+// uk += du; |du|^2 per instance  (NewtonRaphsonSolver::updateUkInIteration
+// :755-761, checkConvergenceViaDeltaU :727-740)
 __global__ void k_update(Ctx c, double* __restrict__ uk, const double* __restrict__ du) {
-    const int i = blockIdx.x * kThreads + threadIdx.x;
+    const Where w = where(c);
     double v[1] = {0.0};
-    if (i < c.nn) {
+    if (w.valid) {
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-            const int k = 3 * i + d;
+            const int k = 3 * w.node + d;
             const double dk = du[k];
             uk[k] = uk[k] + dk;
             v[0] = fma(dk, dk, v[0]);
         }
     }
     double tot[1];
-    if (reduce_grid<1>(c, v, tot) && threadIdx.x == 0) c.scal[S_DU2] = tot[0];
+    if (reduce_seg<1>(c, w.seg, v, tot) && threadIdx.x == 0) w.s[S_DU2] = tot[0];
 }
 
 Ctx make_ctx(tf_handle* h) {
     Device& d = h->d;
     Ctx c;
-    c.nn = d.nn;
     c.rowptr = d.rowptr;
     c.colidx = d.colidx;
     c.val = d.val;
     c.dinv = d.dinv;
     c.scal = d.scal;
     c.part = d.part;
-    c.counter = reinterpret_cast<unsigned*>(d.scal + S_COUNT);
+    c.tickets = d.tickets;
+    c.ncta = d.ncta;
+    c.cta_seg = d.cta_seg;
+    c.cta_node0 = d.cta_node0;
+    c.cta_node1 = d.cta_node1;
+    c.seg_cta0 = d.seg_cta0;
+    c.seg_solve = d.seg_solve;
     return c;
 }
 
-}  // namespace
-
-namespace {
-tf_status krylov_run(tf_handle* h, int method, int* iters, double* relres);
-}
-
-// Auto mode picks CG when the tangent is symmetric; CG needs a positive
-// definite operator, which large compressive growth can take away (the
-// geometric stiffness term), so a CG breakdown there falls back to
-// BiCGStab, as the reference's direct LU would not care.
-tf_status krylov_solve(tf_handle* h, int* iters, double* relres) {
-    tf_status s = krylov_run(h, h->method, iters, relres);
-    if (s == TF_KRYLOV_BREAKDOWN && h->method == 1 && h->opt.krylov_method == 0) {
-        int it2 = 0;
-        s = krylov_run(h, 2, &it2, relres);
-        *iters += it2;
-    }
-    return s;
-}
-
-namespace {
-tf_status krylov_run(tf_handle* h, int method, int* iters, double* relres) {
+// Issues n iterations of `method` on the stream (no host interaction).
+void issue_iterations(tf_handle* h, const Ctx& c, int method, int n) {
     Device& d = h->d;
-    Ctx c = make_ctx(h);
-    const int nb = cdiv(d.nn, kThreads);
-    const int nbv = cdiv(3 * (int64_t)d.nn, kThreads);
+    cudaStream_t st = h->stream;
+    const int nb = d.ncta;
+    for (int it = 0; it < n; ++it) {
+        if (method == 1) {
+            k_cg_spmv<<<nb, kThreads, 0, st>>>(c, d.p, d.q);
+            k_cg_update<<<nb, kThreads, 0, st>>>(c, d.du, d.r, d.z, d.p, d.q);
+            k_cg_direction<<<nb, kThreads, 0, st>>>(c, d.z, d.p);
+        } else {
+            k_bi_dir<<<nb, kThreads, 0, st>>>(c, d.r, d.q, d.p, d.z);
+            k_bi_spmv1<<<nb, kThreads, 0, st>>>(c, d.z, d.rhat, d.q);
+            k_bi_s<<<nb, kThreads, 0, st>>>(c, d.r, d.q, d.s, d.sh, d.du, d.z);
+            k_bi_half<<<nb, kThreads, 0, st>>>(c, d.du, d.z);
+            k_bi_spmv2<<<nb, kThreads, 0, st>>>(c, d.sh, d.s, d.t);
+            k_bi_x<<<nb, kThreads, 0, st>>>(c, d.du, d.r, d.rhat, d.z, d.sh, d.s, d.t);
+        }
+    }
+}
+
+int kernels_per_iteration(int method) { return method == 1 ? 3 : 6; }
+
+// A chunk of `8 << ci` iterations, captured once into a CUDA graph.
+tf_status run_chunk(tf_handle* h, const Ctx& c, int method, int ci) {
+    const int n = 8 << ci;
+    cudaGraphExec_t& ex = h->graph[method - 1][ci];
+    if (!ex) {
+        cudaGraph_t g = nullptr;
+        TF_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        issue_iterations(h, c, method, n);
+        const cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+        const cudaError_t e2 = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        if (e2 != cudaSuccess) {
+            ex = nullptr;
+            return cuda_fail(e2, "cudaGraphInstantiate");
+        }
+        h->graph_kernels[method - 1][ci] = (int64_t)n * kernels_per_iteration(method);
+    }
+    TF_CUDA(cudaGraphLaunch(ex, h->stream));
+    h->launches += h->graph_kernels[method - 1][ci];
+    return TF_OK;
+}
+
+tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* relres) {
+    Device& d = h->d;
+    const Ctx c = make_ctx(h);
     cudaStream_t st = h->stream;
     const tf_status sb = launch_block_inverse(h);
     if (sb != TF_OK) return sb;
-    const double tol = h->opt.krylov_rtol;
-    const double tol2 = tol * tol;
-    TF_CUDA(cudaMemcpyAsync(d.scal + S_TOL2, &tol2, sizeof(double), cudaMemcpyHostToDevice, st));
-    if (method == 1) {
-        k_cg_init<<<nb, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.z, d.p);
-    } else {
-        k_bi_init<<<nb, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.rhat, d.p, d.q);
-    }
+    const double tol2 = h->opt.krylov_rtol * h->opt.krylov_rtol;
+    if (method == 1) k_cg_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.z, d.p, tol2, keep);
+    else k_bi_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.rhat, d.p, d.q, tol2, keep);
     TF_LAUNCH_CHECK(h);
     const int maxit = h->opt.krylov_max_iter;
-    int launched = 0, chunk = 8;
-    double flag = 0.0;
-    while (launched < maxit) {
-        const int n = chunk < maxit - launched ? chunk : maxit - launched;
-        for (int it = 0; it < n; ++it) {
-            if (method == 1) {
-                k_cg_spmv<<<nb, kThreads, 0, st>>>(c, d.p, d.q);
-                TF_LAUNCH_CHECK(h);
-                k_cg_update<<<nb, kThreads, 0, st>>>(c, d.du, d.r, d.z, d.p, d.q);
-                TF_LAUNCH_CHECK(h);
-                k_cg_direction<<<nbv, kThreads, 0, st>>>(c, d.z, d.p);
-                TF_LAUNCH_CHECK(h);
-            } else {
-                k_bi_dir<<<nb, kThreads, 0, st>>>(c, d.r, d.q, d.p, d.z);
-                TF_LAUNCH_CHECK(h);
-                k_bi_spmv1<<<nb, kThreads, 0, st>>>(c, d.z, d.rhat, d.q);
-                TF_LAUNCH_CHECK(h);
-                k_bi_s<<<nb, kThreads, 0, st>>>(c, d.r, d.q, d.s, d.sh);
-                TF_LAUNCH_CHECK(h);
-                k_bi_spmv2<<<nb, kThreads, 0, st>>>(c, d.sh, d.s, d.t);
-                TF_LAUNCH_CHECK(h);
-                k_bi_x<<<nb, kThreads, 0, st>>>(c, d.du, d.r, d.rhat, d.z, d.sh, d.s, d.t);
-                TF_LAUNCH_CHECK(h);
-            }
+    const size_t nscal = (size_t)d.nseg * S_COUNT;
+    int launched = 0, ci = 0;
+    bool done = false;
+    while (launched < maxit && !done) {
+        const int n = 8 << ci;
+        if (n <= maxit - launched) {
+            const tf_status s = run_chunk(h, c, method, ci);
+            if (s != TF_OK) return s;
+            launched += n;
+        } else {
+            const int rest = maxit - launched;
+            issue_iterations(h, c, method, rest);
+            TF_LAUNCH_CHECK(h);
+            h->launches += (int64_t)rest * kernels_per_iteration(method) - 1;
+            launched = maxit;
         }
-        launched += n;
-        TF_CUDA(cudaMemcpyAsync(d.host_scal, d.scal, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, st));
+        TF_CUDA(cudaMemcpyAsync(d.host_scal, d.scal, sizeof(double) * nscal, cudaMemcpyDeviceToHost, st));
         TF_CUDA(cudaStreamSynchronize(st));
-        flag = d.host_scal[S_FLAG];
-        if (flag != 0.0) break;
-        if (chunk < 64) chunk *= 2;
+        done = true;
+        for (int g = 0; g < d.nseg && done; ++g)
+            if (d.host_scal[(size_t)g * S_COUNT + S_FLAG] == F_RUNNING) done = false;
+        if (ci < 3) ++ci;
     }
-    const double bb = d.host_scal[S_BB], rr = d.host_scal[S_RR];
-    *iters = static_cast<int>(d.host_scal[S_ITER]);
-    *relres = bb > 0.0 ? sqrt(rr / bb) : 0.0;
-    if (flag == F_CONVERGED) return TF_OK;
-    if (flag == F_NAN) {
-        set_error("non-finite value in the linear solve");
+    int worst = F_CONVERGED, itmax = 0, bad = -1, bad_it = 0;
+    double rmax = 0.0;
+    for (int g = 0; g < d.nseg; ++g) {
+        const double* s = d.host_scal + (size_t)g * S_COUNT;
+        const int f = static_cast<int>(s[S_FLAG]);
+        if ((f == F_BREAKDOWN || f == F_NAN) && bad < 0) {
+            bad = g;
+            bad_it = static_cast<int>(s[S_ITER]);
+        }
+        itmax = std::max(itmax, static_cast<int>(s[S_ITER]));
+        if (s[S_BB] > 0.0) rmax = std::max(rmax, std::sqrt(s[S_RR] / s[S_BB]));
+        if (f == F_NAN) worst = F_NAN;
+        else if (f == F_BREAKDOWN && worst != F_NAN) worst = F_BREAKDOWN;
+        else if (f == F_RUNNING && worst == F_CONVERGED) worst = F_RUNNING;
+    }
+    *iters = itmax;
+    *relres = rmax;
+    if (worst == F_CONVERGED) return TF_OK;
+    const std::string where = " (instance " + std::to_string(bad) + ", iteration " + std::to_string(bad_it) +
+                              (method == 1 ? ", CG)" : ", BiCGStab)");
+    if (worst == F_NAN) {
+        set_error("non-finite value in the linear solve" + where);
         return TF_NAN_DETECTED;
     }
-    if (flag == F_BREAKDOWN) {
-        set_error("Krylov breakdown");
+    if (worst == F_BREAKDOWN) {
+        set_error("Krylov breakdown" + where);
         return TF_KRYLOV_BREAKDOWN;
     }
     set_error("linear solve reached its iteration cap");
     return TF_KRYLOV_NOT_CONVERGED;
 }
+
 }  // namespace
+
+// Auto mode picks CG when the tangent is symmetric; CG needs a positive
+// definite operator, which large compressive growth can take away (the
+// geometric stiffness term), so the instances whose CG breaks down are solved
+// again with BiCGStab -- the others keep their CG result -- as the
+// reference's direct LU would not care.
+tf_status krylov_solve(tf_handle* h, int* iters, double* relres) {
+    Device& d = h->d;
+    TF_CUDA(cudaMemcpyAsync(d.seg_solve, d.seg_active, sizeof(int) * (size_t)d.nseg, cudaMemcpyDeviceToDevice,
+                            h->stream));
+    tf_status s = krylov_run(h, h->method, 0, iters, relres);
+    if (s == TF_KRYLOV_BREAKDOWN && h->method == 1 && h->opt.krylov_method == 0) {
+        std::vector<int> redo(d.nseg, 0);
+        for (int g = 0; g < d.nseg; ++g)
+            redo[g] = d.host_scal[(size_t)g * S_COUNT + S_FLAG] == F_BREAKDOWN ? 1 : 0;
+        TF_CUDA(cudaMemcpyAsync(d.seg_solve, redo.data(), sizeof(int) * (size_t)d.nseg, cudaMemcpyHostToDevice,
+                                h->stream));
+        int it2 = 0;
+        s = krylov_run(h, 2, 1, &it2, relres);
+        *iters += it2;
+    }
+    return s;
+}
 
 tf_status launch_update(tf_handle* h) {
     Device& d = h->d;
-    Ctx c = make_ctx(h);
-    k_update<<<cdiv(d.nn, kThreads), kThreads, 0, h->stream>>>(c, d.uk, d.du);
+    const Ctx c = make_ctx(h);
+    k_update<<<d.ncta, kThreads, 0, h->stream>>>(c, d.uk, d.du);
     TF_LAUNCH_CHECK(h);
     return TF_OK;
+}
+
+void destroy_graphs(tf_handle* h) {
+    for (auto& row : h->graph)
+        for (auto& g : row)
+            if (g) {
+                cudaGraphExecDestroy(g);
+                g = nullptr;
+            }
 }
 
 }  // namespace tf

@@ -278,7 +278,9 @@ def config_batch_instance(seed: int, min_prisms: int = 1000, max_prisms: int = 5
     tris = target / n_layers
     elliptic = bool(rng.integers(0, 2))
     if elliptic:
-        a = 5.0 * math.sqrt(tris / 2.0 / math.pi * 1.3) * 1.2
+        # a structured grid of spacing h puts 2 triangles in each h^2 of the
+        # ellipse's area pi a b, b = a / 1.3
+        a = math.sqrt(tris * 1.3 * 25.0 / (2.0 * math.pi))
         b = a / 1.3
         pos, conn, pl = ellipse_sheet(a, b, 5.0, n_layers, 5.0 * n_layers, 0.5, rng)
     else:
