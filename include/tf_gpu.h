@@ -212,6 +212,24 @@ TF_API tf_status tf_solve_bsr_static(int32_t n_block_rows, const int32_t* rowptr
                                      const double* val, const double* b, double* x, double rtol, int32_t max_iter,
                                      void* stream, int32_t* iters, double* relres);
 
+/* ---- discrete adjoint (no counterpart in the reference) ------------------
+ * Gradients of a shape loss after n implicit steps with respect to per-element
+ * in-plane growth rates r_e (rates (r_e, r_e, 0), Fg starting at I) and log
+ * Young's moduli.  loss_params = {cx, cy, amp, w}:
+ *   L = sum over apical nodes (z - amp exp(-((x-cx)^2 + (y-cy)^2) / (2 w^2)))^2.
+ * tf_adj_forward overwrites the handle's Fg, growth rates and elastic
+ * moduli (E_e = exp(logE_e), Poisson ratios kept), runs n_steps Newton steps
+ * of length dt from the current positions and keeps the state every `every`
+ * steps in *saved.  tf_adj_backward recomputes each span of `every` steps
+ * from its saved state and solves A^T lambda = rhs per step, scaling dL by
+ * dloss; it leaves the handle at the final state.  Single-mesh handles only. */
+typedef struct tf_adjoint tf_adjoint;
+TF_API tf_status tf_adj_forward(tf_handle* h, const double* rate, const double* logE, int32_t n_steps, double dt,
+                                int32_t every, const double* loss_params, double* loss, tf_adjoint** saved);
+TF_API tf_status tf_adj_backward(tf_handle* h, tf_adjoint* saved, double dloss, double* grad_rate,
+                                 double* grad_logE);
+TF_API tf_status tf_adj_free(tf_adjoint* saved);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,115 @@
+"""Discrete adjoint of n implicit steps (tf_adj_forward / tf_adj_backward).
+
+The gradients of the apical shape loss with respect to per-element growth
+rates and log Young's moduli are checked against central finite differences
+of the GPU forward run (directional derivatives along seeded directions),
+to 1e-6 relative.  The forward run itself is checked against the oracle's
+Newton steps (node positions to 1e-8 relative).
+"""
+import numpy as np
+import pytest
+
+from oracle.oracle import Port
+from tissuefolding_paperversion_gb300 import api, mesh
+
+pytestmark = pytest.mark.gpu
+TOL_GRAD = 1e-6
+
+
+def _tissue(eta, seed=5):
+    t = mesh.config_tiny(seed=seed, n=5, n_layers=2, eta=eta)
+    rng = np.random.default_rng(seed + 100)
+    rate = 1e-4 * (1.0 + 0.5 * rng.uniform(-1, 1, t.n_elems))   # 1/s, about 0.6 % per 60 s step
+    logE = np.log(t.E)
+    xy = t.pos.reshape(-1, 3)
+    z_top = xy[t.node_placement == 1, 2].mean()
+    c = xy[:, :2].mean(axis=0)
+    params = np.array([c[0], c[1], 1.2 * z_top, 8.0])
+    return t, rate, logE, params
+
+
+def _solver(t):
+    return api.Solver(t, newton_tol=1e-10, krylov_rtol=1e-12, krylov_max_iter=5000, deterministic=True)
+
+
+def _loss(s, t, rate, logE, n, every, params):
+    s.set_positions(t.pos)
+    loss, saved = s.adjoint_forward(rate, logE, n, t.dt, every, params)
+    return loss, saved
+
+
+@pytest.mark.parametrize("eta,n,every", [(0.0, 4, 2), (100.0, 4, 2), (100.0, 5, 3), (100.0, 3, 1)])
+def test_adjoint_matches_central_differences(eta, n, every):
+    t, rate, logE, params = _tissue(eta)
+    rng = np.random.default_rng(7)
+    with _solver(t) as s:
+        loss0, saved = _loss(s, t, rate, logE, n, every, params)
+        gr, ge = s.adjoint_backward(saved)
+        saved.free()
+        assert np.all(np.isfinite(gr)) and np.all(np.isfinite(ge))
+        assert np.abs(gr).max() > 0 and np.abs(ge).max() > 0
+        for which in ("rate", "logE"):
+            for _ in range(2):
+                d = rng.standard_normal(t.n_elems)
+                if which == "rate":
+                    h = 1e-3 * np.abs(rate).mean()
+                    lp, sp = _loss(s, t, rate + h * d, logE, n, every, params)
+                    lm, sm = _loss(s, t, rate - h * d, logE, n, every, params)
+                    adj = gr @ d
+                else:
+                    h = 1e-4
+                    lp, sp = _loss(s, t, rate, logE + h * d, n, every, params)
+                    lm, sm = _loss(s, t, rate, logE - h * d, n, every, params)
+                    adj = ge @ d
+                sp.free()
+                sm.free()
+                fd = (lp - lm) / (2 * h)
+                assert abs(adj - fd) <= TOL_GRAD * abs(fd), (which, adj, fd)
+
+
+def test_adjoint_gradient_is_independent_of_checkpoint_spacing():
+    t, rate, logE, params = _tissue(100.0, seed=9)
+    out = []
+    with _solver(t) as s:
+        for every in (1, 2, 5):
+            _, saved = _loss(s, t, rate, logE, 5, every, params)
+            out.append(s.adjoint_backward(saved))
+            saved.free()
+    for gr, ge in out[1:]:
+        np.testing.assert_allclose(gr, out[0][0], rtol=1e-9, atol=1e-9 * np.abs(out[0][0]).max())
+        np.testing.assert_allclose(ge, out[0][1], rtol=1e-9, atol=1e-9 * np.abs(out[0][1]).max())
+
+
+def test_adjoint_forward_matches_oracle_steps():
+    t, rate, logE, params = _tissue(100.0, seed=11)
+    n = 3
+    t.E = np.exp(logE)
+    rates3 = np.zeros((t.n_elems, 3))
+    rates3[:, 0] = rate
+    rates3[:, 1] = rate
+    p = Port(t)
+    for _ in range(n):
+        p.step(t.dt, rates3.reshape(-1))
+    ref = p.positions()
+    with _solver(t) as s:
+        loss, saved = _loss(s, t, rate, logE, n, 2, params)
+        got = s.positions()
+        saved.free()
+    scale = np.abs(ref).max()
+    assert np.abs(got - ref).max() / scale <= 1e-8
+    x = ref.reshape(-1, 3)[t.node_placement == 1]
+    f = params[2] * np.exp(-((x[:, 0] - params[0]) ** 2 + (x[:, 1] - params[1]) ** 2) / (2 * params[3] ** 2))
+    assert abs(loss - np.sum((x[:, 2] - f) ** 2)) <= 1e-7 * max(1.0, loss)
+
+
+def test_adjoint_rejects_bad_arguments():
+    t, rate, logE, params = _tissue(0.0)
+    with _solver(t) as s:
+        with pytest.raises(api.TfError):
+            s.adjoint_forward(rate, logE, 0, t.dt, 1, params)
+        with pytest.raises(api.TfError):
+            s.adjoint_forward(rate, logE, 2, t.dt, 0, params)
+        bad = params.copy()
+        bad[3] = 0.0
+        with pytest.raises(api.TfError):
+            s.adjoint_forward(rate, logE, 2, t.dt, 1, bad)

@@ -30,6 +30,7 @@ EXPORTED = [
     "tf_get_viscosity_surfaces", "tf_set_viscosity_surfaces", "tf_set_state", "tf_export_csr",
     "tf_element_eval", "tf_get_sizes", "tf_get_stream", "tf_launch_count", "tf_time_assembly",
     "tf_solve_bsr_static", "tf_batch_create", "tf_batch_step", "tf_get_instances", "tf_elements_per_cta",
+    "tf_adj_forward", "tf_adj_backward", "tf_adj_free",
 ]
 
 
@@ -112,6 +113,12 @@ def load(build_if_missing: bool = True):
     L.tf_elements_per_cta.argtypes = [vp]
     L.tf_solve_bsr_static.restype = C.c_int
     L.tf_solve_bsr_static.argtypes = [i32, vp, vp, vp, vp, vp, C.c_double, i32, vp, ip, dp]
+    L.tf_adj_forward.restype = C.c_int
+    L.tf_adj_forward.argtypes = [vp, vp, vp, i32, C.c_double, i32, vp, dp, C.POINTER(vp)]
+    L.tf_adj_backward.restype = C.c_int
+    L.tf_adj_backward.argtypes = [vp, vp, C.c_double, vp, vp]
+    L.tf_adj_free.restype = C.c_int
+    L.tf_adj_free.argtypes = [vp]
     for name in ["tf_create", "tf_destroy", "tf_set_positions", "tf_get_positions", "tf_set_Fg", "tf_get_Fg",
                  "tf_set_growth_rates", "tf_begin_step", "tf_assemble", "tf_add_external_forces", "tf_solve",
                  "tf_update", "tf_end_step", "tf_newton_step", "tf_get_residual", "tf_get_delta_u",
@@ -307,6 +314,47 @@ class Solver:
         a, b = C.c_float(0), C.c_float(0)
         self._check(self.L.tf_time_assembly(self.h, iters, C.byref(a), C.byref(b)), "tf_time_assembly")
         return a.value, b.value
+
+    # -- adjoint --------------------------------------------------------------
+    def adjoint_forward(self, rate, logE, n_steps, dt, every, loss_params):
+        """Run ``n_steps`` steps from the current positions with Fg = I, growth
+        rates (r_e, r_e, 0) and E_e = exp(logE_e); returns (loss, saved)."""
+        r = np.ascontiguousarray(rate, dtype=np.float64)
+        e = np.ascontiguousarray(logE, dtype=np.float64)
+        lp = np.ascontiguousarray(loss_params, dtype=np.float64)
+        if r.shape != (self.ne,) or e.shape != (self.ne,) or lp.shape != (4,):
+            raise ValueError("rate and logE need one value per element, loss_params four values")
+        loss = C.c_double(0.0)
+        saved = C.c_void_p()
+        self._check(self.L.tf_adj_forward(self.h, _ptr(r), _ptr(e), n_steps, dt, every, _ptr(lp), C.byref(loss),
+                                          C.byref(saved)), "tf_adj_forward", (TF_NOT_CONVERGED,))
+        return loss.value, AdjointState(self.L, saved)
+
+    def adjoint_backward(self, saved, dloss=1.0):
+        """Gradients (dL/d rate, dL/d logE) for the run held by ``saved``."""
+        gr = np.zeros(self.ne)
+        ge = np.zeros(self.ne)
+        self._check(self.L.tf_adj_backward(self.h, saved.p, dloss, _ptr(gr), _ptr(ge)), "tf_adj_backward")
+        return gr, ge
+
+
+class AdjointState:
+    """Saved states of one adjoint forward run (``tf_adjoint``)."""
+
+    def __init__(self, L, p):
+        self.L = L
+        self.p = p
+
+    def free(self):
+        if self.p:
+            self.L.tf_adj_free(self.p)
+            self.p = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 class Batch(Solver):

@@ -79,7 +79,8 @@ void free_all(tf_handle* h) {
                     d.aptr, d.alist, d.farea, d.fixed, d.ext_visc, d.area, d.rowptr, d.colidx, d.diag, d.rowof,
                     d.slot, d.val, d.eblk, d.ef, d.gptr, d.glist, d.fptr, d.flist, d.uk, d.un, d.vel, d.g,
                     d.du, d.dinv, d.r, d.p, d.z, d.q, d.rhat, d.s, d.t, d.sh, d.scal, d.part, d.tickets,
-                    d.seg_node0, d.elem_seg, d.cta_seg, d.cta_node0, d.cta_node1, d.seg_cta0, d.seg_active, d.seg_solve};
+                    d.seg_node0, d.elem_seg, d.cta_seg, d.cta_node0, d.cta_node1, d.seg_cta0, d.seg_active, d.seg_solve,
+                    d.tblk, d.valT, d.lamv, d.carry, d.dldu, d.gr, d.ge, d.nu, d.apical};
     destroy_graphs(h);
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -209,10 +210,14 @@ tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat, const st
     // ---- material (Prism::setElasticProperties, Prism.cpp:491-516) ----------
     std::vector<double> lam(ne), mu(ne), eta(ne);
     d.any_visc = false;
+    h->h_nu.resize(ne);
+    h->h_apical.resize(nn);
+    for (int i = 0; i < nn; ++i) h->h_apical[i] = m->node_placement[i] == 1 ? 1 : 0;
     for (int e = 0; e < ne; ++e) {
         double v = mat->nu[e];
         if (v > 0.5) v = 0.5;
         else if (v < 0.0) v = 0.0;
+        h->h_nu[e] = v;
         const double E = mat->E[e];
         lam[e] = E * v / (1 + v) / (1 - 2.0 * v);
         mu[e] = E / 2.0 / (1 + v);

@@ -78,12 +78,22 @@ struct Device {
     int* seg_cta0 = nullptr;    // [nseg+1] CTA ranges per instance
     int* seg_active = nullptr;  // [nseg] 1 while the instance's Newton loop runs
     int* seg_solve = nullptr;   // [nseg] instances a linear solve works on
+    // adjoint (allocated by the first tf_adj_forward)
+    int* tblk = nullptr;        // [nnzb] block index of the transposed block
+    double* valT = nullptr;     // [9*nnzb] transposed block values
+    double* lamv = nullptr;     // [3nn] adjoint of the current step
+    double* carry = nullptr;    // [3nn] carry to the previous step
+    double* dldu = nullptr;     // [3nn] dL/du at the final state
+    double* gr = nullptr;       // [ne] dL/d growth rate
+    double* ge = nullptr;       // [ne] dL/d log E
+    double* nu = nullptr;       // [ne] Poisson ratios (clamped to [0, 0.5])
+    int* apical = nullptr;      // [nn] 1 for apical nodes
 };
 
 // Indices into Device::scal (device-resident Krylov scalars).
 enum Scal {
     S_RZ = 0, S_RZ_OLD, S_PQ, S_ALPHA, S_BETA, S_OMEGA, S_RHO, S_RHO_OLD,
-    S_TS, S_TT, S_RR, S_BB, S_RR0, S_DU2, S_FLAG, S_ITER, S_TOL2, S_COUNT = 32
+    S_TS, S_TT, S_RR, S_BB, S_RR0, S_DU2, S_FLAG, S_ITER, S_TOL2, S_WHY, S_COUNT = 32
 };
 
 constexpr int kNodeThreads = 256;    // nodes per CTA of the node-parallel kernels
@@ -104,6 +114,8 @@ struct tf_handle {
     std::vector<int> h_conn;
     std::vector<int> h_rowptr, h_colidx;
     std::vector<uint8_t> h_fixed;
+    std::vector<double> h_nu;                   // Poisson ratios, clamped as the material setup does
+    std::vector<int> h_apical;                  // 1 for apical nodes (tissue placement 1)
     std::vector<int> h_seg_node0, h_seg_elem0;  // host copies of the instance offsets
     std::vector<int> h_active;                  // host mirror of seg_active
     int elem_cta = 16;                          // prisms per CTA of the element kernel (autotuned)
@@ -141,6 +153,7 @@ tf_status launch_block_inverse(tf_handle* h);
 tf_status krylov_solve(tf_handle* h, int* iters, double* relres);
 tf_status launch_update(tf_handle* h);
 tf_status autotune_element(tf_handle* h);
+tf_status launch_adjoint_element(tf_handle* h, const double* lamv, double* carry, double* gr, double* ge, double ndt);
 void destroy_graphs(tf_handle* h);
 
 inline int cdiv(int64_t a, int64_t b) { return static_cast<int>((a + b - 1) / b); }

@@ -18,6 +18,7 @@
 //     reads the flags once per chunk.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <vector>
 
 #include "tf_internal.cuh"
@@ -29,6 +30,10 @@ namespace {
 constexpr int kThreads = kNodeThreads;
 
 enum Flag { F_RUNNING = 0, F_CONVERGED = 1, F_BREAKDOWN = 2, F_NAN = 3 };
+// Cause of a breakdown (S_WHY): which denominator vanished.
+enum Why { W_NONE = 0, W_CG_PAP = 1, W_CG_RZ = 2, W_BI_RV = 3, W_BI_OMEGA = 4, W_BI_RHO = 5 };
+const char* const kWhy[] = {"", "(p, Ap) <= 0", "(r, M^-1 r) <= 0", "(rhat, A phat) = 0", "omega = 0",
+                            "(rhat, r) = 0"};
 
 struct Ctx {
     const int* __restrict__ rowptr;
@@ -147,6 +152,7 @@ __device__ __forceinline__ void start_flags(double* s, double bb, double tol2) {
     s[S_RR0] = bb;
     s[S_ITER] = 0.0;
     s[S_TOL2] = tol2;
+    s[S_WHY] = W_NONE;
     s[S_FLAG] = (bb == 0.0) ? F_CONVERGED : (isfinite(bb) ? F_RUNNING : F_NAN);
 }
 
@@ -210,6 +216,7 @@ __global__ void k_cg_spmv(Ctx c, const double* __restrict__ p, double* __restric
         const double pq = tot[0];
         if (!(pq > 0.0) || !isfinite(pq)) {
             w.s[S_FLAG] = isfinite(pq) ? F_BREAKDOWN : F_NAN;
+            w.s[S_WHY] = W_CG_PAP;
         } else {
             w.s[S_PQ] = pq;
             w.s[S_ALPHA] = w.s[S_RZ] / pq;
@@ -252,7 +259,10 @@ __global__ void k_cg_update(Ctx c, double* __restrict__ x, double* __restrict__ 
         s[S_ITER] += 1.0;
         if (!isfinite(rr)) s[S_FLAG] = F_NAN;
         else if (rr <= s[S_TOL2] * s[S_BB]) s[S_FLAG] = F_CONVERGED;
-        else if (!(rz > 0.0)) s[S_FLAG] = F_BREAKDOWN;
+        else if (!(rz > 0.0)) {
+            s[S_FLAG] = F_BREAKDOWN;
+            s[S_WHY] = W_CG_RZ;
+        }
     }
 }
 
@@ -341,8 +351,12 @@ __global__ void k_bi_spmv1(Ctx c, const double* __restrict__ phat, const double*
     double tot[1];
     if (reduce_seg<1>(c, w.seg, s, tot) && threadIdx.x == 0) {
         const double rv = tot[0];
-        if (rv == 0.0 || !isfinite(rv)) w.s[S_FLAG] = isfinite(rv) ? F_BREAKDOWN : F_NAN;
-        else w.s[S_ALPHA] = w.s[S_RHO] / rv;
+        if (rv == 0.0 || !isfinite(rv)) {
+            w.s[S_FLAG] = isfinite(rv) ? F_BREAKDOWN : F_NAN;
+            w.s[S_WHY] = W_BI_RV;
+        } else {
+            w.s[S_ALPHA] = w.s[S_RHO] / rv;
+        }
     }
 }
 
@@ -450,7 +464,48 @@ __global__ void k_bi_x(Ctx c, double* __restrict__ x, double* __restrict__ r, co
         q[S_ITER] += 1.0;
         if (!isfinite(rr)) q[S_FLAG] = F_NAN;
         else if (rr <= q[S_TOL2] * q[S_BB]) q[S_FLAG] = F_CONVERGED;
-        else if (om == 0.0 || rho == 0.0) q[S_FLAG] = F_BREAKDOWN;
+        else if (om == 0.0 || rho == 0.0) {
+            q[S_FLAG] = F_BREAKDOWN;
+            q[S_WHY] = om == 0.0 ? W_BI_OMEGA : W_BI_RHO;
+        }
+    }
+}
+
+// Restart of BiCGStab from the current iterate after a breakdown: x and its
+// residual r are kept, the shadow residual becomes rhat = r and the search
+// directions start again.  |b|, the tolerance and the iteration count carry
+// over.  Instances outside seg_solve keep their result and are flagged done.
+__global__ void k_bi_restart(Ctx c, const double* __restrict__ r, double* __restrict__ rhat, double* __restrict__ p,
+                             double* __restrict__ v) {
+    const Where w = where(c);
+    const bool active = c.seg_solve[w.seg] != 0;
+    if (!active) {
+        if (threadIdx.x == 0) w.s[S_FLAG] = F_CONVERGED;
+        return;
+    }
+    double s[1] = {0.0};
+    if (w.valid) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int k = 3 * w.node + d;
+            const double rk = r[k];
+            rhat[k] = rk;
+            p[k] = 0.0;
+            v[k] = 0.0;
+            s[0] = fma(rk, rk, s[0]);
+        }
+    }
+    double tot[1];
+    if (reduce_seg<1>(c, w.seg, s, tot) && threadIdx.x == 0) {
+        double* q = w.s;
+        q[S_RHO] = tot[0];
+        q[S_RR] = tot[0];
+        q[S_ALPHA] = 1.0;
+        q[S_OMEGA] = 1.0;
+        q[S_BETA] = 0.0;
+        q[S_WHY] = W_NONE;
+        if (!isfinite(tot[0])) q[S_FLAG] = F_NAN;
+        else q[S_FLAG] = (tot[0] <= q[S_TOL2] * q[S_BB]) ? F_CONVERGED : F_RUNNING;
     }
 }
 
@@ -543,11 +598,15 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
     Device& d = h->d;
     const Ctx c = make_ctx(h);
     cudaStream_t st = h->stream;
-    const tf_status sb = launch_block_inverse(h);
-    if (sb != TF_OK) return sb;
     const double tol2 = h->opt.krylov_rtol * h->opt.krylov_rtol;
-    if (method == 1) k_cg_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.z, d.p, tol2, keep);
-    else k_bi_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.rhat, d.p, d.q, tol2, keep);
+    if (keep == 2) {  // BiCGStab restart: block inverse and x are kept
+        k_bi_restart<<<d.ncta, kThreads, 0, st>>>(c, d.r, d.rhat, d.p, d.q);
+    } else {
+        const tf_status sb = launch_block_inverse(h);
+        if (sb != TF_OK) return sb;
+        if (method == 1) k_cg_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.z, d.p, tol2, keep);
+        else k_bi_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.rhat, d.p, d.q, tol2, keep);
+    }
     TF_LAUNCH_CHECK(h);
     const int maxit = h->opt.krylov_max_iter;
     const size_t nscal = (size_t)d.nseg * S_COUNT;
@@ -573,14 +632,16 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
             if (d.host_scal[(size_t)g * S_COUNT + S_FLAG] == F_RUNNING) done = false;
         if (ci < 3) ++ci;
     }
-    int worst = F_CONVERGED, itmax = 0, bad = -1, bad_it = 0;
-    double rmax = 0.0;
+    int worst = F_CONVERGED, itmax = 0, bad = -1, bad_it = 0, why = 0;
+    double rmax = 0.0, bad_rel = 0.0;
     for (int g = 0; g < d.nseg; ++g) {
         const double* s = d.host_scal + (size_t)g * S_COUNT;
         const int f = static_cast<int>(s[S_FLAG]);
         if ((f == F_BREAKDOWN || f == F_NAN) && bad < 0) {
             bad = g;
             bad_it = static_cast<int>(s[S_ITER]);
+            why = static_cast<int>(s[S_WHY]);
+            bad_rel = s[S_BB] > 0.0 ? std::sqrt(s[S_RR] / s[S_BB]) : 0.0;
         }
         itmax = std::max(itmax, static_cast<int>(s[S_ITER]));
         if (s[S_BB] > 0.0) rmax = std::max(rmax, std::sqrt(s[S_RR] / s[S_BB]));
@@ -591,8 +652,11 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
     *iters = itmax;
     *relres = rmax;
     if (worst == F_CONVERGED) return TF_OK;
+    char rel[32];
+    std::snprintf(rel, sizeof(rel), "%.3g", bad_rel);
     const std::string where = " (instance " + std::to_string(bad) + ", iteration " + std::to_string(bad_it) +
-                              (method == 1 ? ", CG)" : ", BiCGStab)");
+                              (method == 1 ? ", CG, " : ", BiCGStab, ") + kWhy[why < 0 || why > 5 ? 0 : why] +
+                              ", relative residual " + rel + ")";
     if (worst == F_NAN) {
         set_error("non-finite value in the linear solve" + where);
         return TF_NAN_DETECTED;
@@ -625,6 +689,19 @@ tf_status krylov_solve(tf_handle* h, int* iters, double* relres) {
                                 h->stream));
         int it2 = 0;
         s = krylov_run(h, 2, 1, &it2, relres);
+        *iters += it2;
+    }
+    // BiCGStab breakdowns: restart the instances concerned from their
+    // current iterate with a fresh shadow residual
+    const bool bicg = h->method == 2 || h->opt.krylov_method == 0;
+    for (int restart = 0; restart < 3 && s == TF_KRYLOV_BREAKDOWN && bicg; ++restart) {
+        std::vector<int> redo(d.nseg, 0);
+        for (int g = 0; g < d.nseg; ++g)
+            redo[g] = d.host_scal[(size_t)g * S_COUNT + S_FLAG] == F_BREAKDOWN ? 1 : 0;
+        TF_CUDA(cudaMemcpyAsync(d.seg_solve, redo.data(), sizeof(int) * (size_t)d.nseg, cudaMemcpyHostToDevice,
+                                h->stream));
+        int it2 = 0;
+        s = krylov_run(h, 2, 2, &it2, relres);
         *iters += it2;
     }
     return s;
