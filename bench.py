@@ -163,9 +163,10 @@ def run_gpu(args, t):
         import torch.distributed as dist  # noqa: F811
 
         dist.init_process_group("gloo")
-    s = api.Solver(t, device=local if world > 1 else 0)
+    s = api.Solver(t, device=local if world > 1 else 0, precond=args.precond)
     s.set_growth_rates(t.rates)
     nn, ne, nnzb = s.sizes()
+    mg_nodes, _ = s.multigrid_info()
 
     def barrier():
         if dist is not None:
@@ -226,6 +227,7 @@ def run_gpu(args, t):
         "config": {"workload": t.name, "prisms": ne, "nodes": nn, "dof": 3 * nn, "block_nonzeros": nnzb,
                    "dt_s": t.dt, "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single"},
         "newton": {"ms_per_step": step_ms, "assemblies_per_step": n_asm / len(stats),
+                   "preconditioner": "multigrid " + "/".join(map(str, mg_nodes)) if mg_nodes else "block-Jacobi",
                    "krylov_iters_per_step": sum(x["krylov_total"] for x in stats) / len(stats),
                    "ms_assembly": ms_asm / n_asm, "wall_s": wall},
         "e2e": {"value": ne / e2e_s, "unit": "prisms/s", "h2d_bytes_per_step": 2 * 8 * 3 * nn,
@@ -314,19 +316,83 @@ def run_batch(args):
     }))
 
 
+def run_adjoint(args, t):
+    """Adjoint of n implicit steps on the 320k-prism sheet: loss = squared
+    distance of the final apical surface to z = 5 exp(-r^2 / (2 40^2)) µm
+    (r from the sheet centre), gradient with respect to the per-element
+    growth rates and log E; states saved every `every` steps and recomputed
+    in between.  Reports forward and backward device-synchronised wall time
+    and their ratio."""
+    from tissuefolding_paperversion_gb300 import api
+
+    s = api.Solver(t)
+    xy = t.pos.reshape(-1, 3)[:, :2]
+    c = 0.5 * (xy.min(axis=0) + xy.max(axis=0))
+    params = np.array([c[0], c[1], 5.0, 40.0])
+    rate = t.rates.reshape(-1, 3)[:, 0].copy()
+    logE = np.log(t.E)
+    n, every = args.adj_steps, args.adj_every
+    # warm-up: one short forward/backward (graphs, autotuner)
+    s.set_positions(t.pos)
+    _, sv = s.adjoint_forward(rate, logE, 1, t.dt, 1, params)
+    s.adjoint_backward(sv)
+    sv.free()
+    s.set_positions(t.pos)
+    l0 = s.launch_count()
+    w0 = time.perf_counter()
+    loss, sv = s.adjoint_forward(rate, logE, n, t.dt, every, params)
+    fwd = time.perf_counter() - w0
+    w0 = time.perf_counter()
+    gr, ge = s.adjoint_backward(sv)
+    bwd = time.perf_counter() - w0
+    launches = s.launch_count() - l0
+    sv.free()
+    fd = []
+    rng = np.random.default_rng(1234)
+    for _ in range(args.adj_fd):
+        d = rng.standard_normal(t.n_elems)
+        h = 1e-3 * np.abs(rate).mean()
+        out = []
+        for sgn in (1.0, -1.0):
+            s.set_positions(t.pos)
+            lv, sp = s.adjoint_forward(rate + sgn * h * d, logE, n, t.dt, every, params)
+            sp.free()
+            out.append(lv)
+        f = (out[0] - out[1]) / (2 * h)
+        fd.append({"adjoint": float(gr @ d), "fd": f, "rel": abs(float(gr @ d) - f) / max(abs(f), 1e-300)})
+    s.close()
+    print(json.dumps({
+        "metric": "adjoint backward / forward cost", "value": bwd / fwd, "unit": "ratio", "n_gpus": 1,
+        "steps": n, "warmup": 1, "ms_per_step": (fwd + bwd) / n * 1e3, "higher_is_better": False,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"adjoint-{t.name}", "prisms": t.n_elems, "steps": n, "checkpoint_every": every,
+                   "loss": "sum over apical nodes (z - 5 exp(-r^2/(2 40^2)))^2", "parameters": 2 * t.n_elems},
+        "forward_s": fwd, "backward_s": bwd, "loss": loss,
+        "grad_norm": {"rate": float(np.linalg.norm(gr)), "logE": float(np.linalg.norm(ge))},
+        "fd_checks": fd,
+        "gpu_launches": launches,
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="large", choices=["large", "medium", "small"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch"],
-                    help="plain: the 320k-prism Newton step; batch: the 256-instance sweep")
+    ap.add_argument("--config", default="large", choices=["large", "medium", "small", "wing"])
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint"],
+                    help="plain: the 320k-prism Newton step; batch: the 256-instance sweep; "
+                         "adjoint: gradient of an apical shape loss through n steps")
+    ap.add_argument("--adj-steps", type=int, default=50)
+    ap.add_argument("--adj-every", type=int, default=10)
+    ap.add_argument("--adj-fd", type=int, default=0, help="central-difference checks along random directions")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--mode", default="step", choices=["step", "assembly"],
                     help="step: Newton steps (the bench); assembly: back-to-back K+f assemblies only")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
+    ap.add_argument("--precond", type=int, default=0,
+                    help="0 auto (multigrid from 20,000 nodes), 1 block-Jacobi, 2 multigrid")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     from tissuefolding_paperversion_gb300 import mesh
@@ -336,12 +402,17 @@ def main():
         return
     if args.config == "large":
         t = mesh.config_large(seed=0)
+    elif args.config == "wing":
+        t = mesh.config_wing(seed=0)
     elif args.config == "medium":
         t = mesh.config_large(seed=0, cells=130)
     else:
         t = mesh.config_small(seed=0)
     if args.mode == "assembly" and args.impl == "ours":
         run_assembly_only(args, t)
+        return
+    if args.workload == "adjoint":
+        run_adjoint(args, t)
         return
     if args.impl == "reference":
         run_reference(args, t)

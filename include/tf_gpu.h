@@ -72,6 +72,8 @@ typedef struct tf_options {
     int32_t deterministic;   /* 1: order-fixed assembly (no atomics); 0: atomic scatter */
     int32_t device;          /* CUDA device ordinal */
     int32_t autotune_off;    /* 1: keep 16 prisms per CTA instead of timing 8/16/32 on the mesh */
+    int32_t precond;         /* 0 auto (multigrid from 20,000 nodes on), 1 block-Jacobi,
+                                2 aggregation multigrid (no reference counterpart) */
 } tf_options;
 
 /* Statistics of one time step (tf_newton_step). */
@@ -223,6 +225,12 @@ TF_API tf_status tf_solve_bsr_static(int32_t n_block_rows, const int32_t* rowptr
  * steps in *saved.  tf_adj_backward recomputes each span of `every` steps
  * from its saved state and solves A^T lambda = rhs per step, scaling dL by
  * dloss; it leaves the handle at the final state.  Single-mesh handles only. */
+/* Multigrid hierarchy of the handle (tf_options.precond): number of levels
+ * (0 when block-Jacobi is used), nodes per level and the smoother weights
+ * of the last numeric set-up (4 / (3 lambda_max(D^-1 A)) per level; arrays of
+ * at least 10 entries, either may be NULL).  No reference counterpart. */
+TF_API tf_status tf_multigrid_info(tf_handle* h, int32_t* levels, int32_t* nodes, double* weights);
+
 typedef struct tf_adjoint tf_adjoint;
 TF_API tf_status tf_adj_forward(tf_handle* h, const double* rate, const double* logE, int32_t n_steps, double dt,
                                 int32_t every, const double* loss_params, double* loss, tf_adjoint** saved);

@@ -30,7 +30,7 @@ EXPORTED = [
     "tf_get_viscosity_surfaces", "tf_set_viscosity_surfaces", "tf_set_state", "tf_export_csr",
     "tf_element_eval", "tf_get_sizes", "tf_get_stream", "tf_launch_count", "tf_time_assembly",
     "tf_solve_bsr_static", "tf_batch_create", "tf_batch_step", "tf_get_instances", "tf_elements_per_cta",
-    "tf_adj_forward", "tf_adj_backward", "tf_adj_free",
+    "tf_adj_forward", "tf_adj_backward", "tf_adj_free", "tf_multigrid_info",
 ]
 
 
@@ -52,7 +52,7 @@ class tf_material(C.Structure):
 class tf_options(C.Structure):
     _fields_ = [("newton_tol", C.c_double), ("newton_max_iter", C.c_int32), ("krylov_rtol", C.c_double),
                 ("krylov_max_iter", C.c_int32), ("krylov_method", C.c_int32), ("deterministic", C.c_int32),
-                ("device", C.c_int32), ("autotune_off", C.c_int32)]
+                ("device", C.c_int32), ("autotune_off", C.c_int32), ("precond", C.c_int32)]
 
 
 class tf_step_stats(C.Structure):
@@ -119,6 +119,8 @@ def load(build_if_missing: bool = True):
     L.tf_adj_backward.argtypes = [vp, vp, C.c_double, vp, vp]
     L.tf_adj_free.restype = C.c_int
     L.tf_adj_free.argtypes = [vp]
+    L.tf_multigrid_info.restype = C.c_int
+    L.tf_multigrid_info.argtypes = [vp, ip, vp, vp]
     for name in ["tf_create", "tf_destroy", "tf_set_positions", "tf_get_positions", "tf_set_Fg", "tf_get_Fg",
                  "tf_set_growth_rates", "tf_begin_step", "tf_assemble", "tf_add_external_forces", "tf_solve",
                  "tf_update", "tf_end_step", "tf_newton_step", "tf_get_residual", "tf_get_delta_u",
@@ -154,14 +156,14 @@ class Solver:
     """One GPU Newton solver over one tissue (a ``tf_handle``)."""
 
     def __init__(self, tissue, newton_tol=1e-8, newton_max_iter=20, krylov_rtol=1e-8, krylov_max_iter=20000,
-                 krylov_method=0, deterministic=False, device=0, autotune=True):
+                 krylov_method=0, deterministic=False, device=0, autotune=True, precond=0):
         self.L = load()
         t = tissue
         self.t = t
         self.nn, self.ne = t.n_nodes, t.n_elems
         self._arrays, m, mat = _mesh_structs(t)
         opt = tf_options(newton_tol, newton_max_iter, krylov_rtol, krylov_max_iter, krylov_method,
-                         1 if deterministic else 0, device, 0 if autotune else 1)
+                         1 if deterministic else 0, device, 0 if autotune else 1, precond)
         h = C.c_void_p()
         self._check(self.L.tf_create(C.byref(m), C.byref(mat), C.byref(opt), C.byref(h)), "tf_create")
         self.h = h
@@ -315,6 +317,15 @@ class Solver:
         self._check(self.L.tf_time_assembly(self.h, iters, C.byref(a), C.byref(b)), "tf_time_assembly")
         return a.value, b.value
 
+    def multigrid_info(self):
+        """(nodes per level, smoother weights) of the multigrid hierarchy; empty
+        lists when block-Jacobi is used."""
+        lv = C.c_int32(0)
+        nodes = np.zeros(10, dtype=np.int32)
+        w = np.zeros(10)
+        self._check(self.L.tf_multigrid_info(self.h, C.byref(lv), _ptr(nodes), _ptr(w)), "tf_multigrid_info")
+        return nodes[: lv.value].tolist(), w[: lv.value].tolist()
+
     # -- adjoint --------------------------------------------------------------
     def adjoint_forward(self, rate, logE, n_steps, dt, every, loss_params):
         """Run ``n_steps`` steps from the current positions with Fg = I, growth
@@ -361,7 +372,7 @@ class Batch(Solver):
     """Many independent tissues in one handle (tf_batch_create)."""
 
     def __init__(self, tissues, newton_tol=1e-8, newton_max_iter=20, krylov_rtol=1e-8, krylov_max_iter=20000,
-                 krylov_method=0, deterministic=False, device=0, autotune=True):
+                 krylov_method=0, deterministic=False, device=0, autotune=True, precond=0):
         self.L = load()
         self.tissues = list(tissues)
         n = len(self.tissues)
@@ -373,7 +384,7 @@ class Batch(Solver):
             mats[i] = mat
         self._arrays = keep
         opt = tf_options(newton_tol, newton_max_iter, krylov_rtol, krylov_max_iter, krylov_method,
-                         1 if deterministic else 0, device, 0 if autotune else 1)
+                         1 if deterministic else 0, device, 0 if autotune else 1, precond)
         h = C.c_void_p()
         self._check(self.L.tf_batch_create(meshes, mats, n, C.byref(opt), C.byref(h)), "tf_batch_create")
         self.h = h

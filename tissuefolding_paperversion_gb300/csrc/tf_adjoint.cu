@@ -92,16 +92,16 @@ __global__ void k_rhs(int n3, const double* __restrict__ src, double scale, cons
 }
 
 // transposed copy of the block values: blocks (i,j) <- (j,i)^T
-__global__ void k_transpose_blocks(int64_t nnzb, const int* __restrict__ tblk, const double* __restrict__ val,
-                                   double* __restrict__ valT) {
+__global__ void k_transpose_blocks(int64_t nnzb, const int* __restrict__ tblk, const int* __restrict__ bofs,
+                                   const double* __restrict__ val, double* __restrict__ valT) {
     const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nnzb) return;
-    const double* src = val + 9 * (size_t)tblk[b];
-    double* dst = valT + 9 * (size_t)b;
+    const double* src = val + bofs[tblk[b]];
+    double* dst = valT + bofs[b];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) dst[3 * i + k] = src[3 * k + i];
+        for (int k = 0; k < 3; ++k) dst[kSlice * (3 * i + k)] = src[kSlice * (3 * k + i)];
 }
 
 // node terms of the carry to step n-1: external viscosity
@@ -233,7 +233,8 @@ tf_status ensure_adjoint_buffers(tf_handle* h) {
     const size_t n3 = 3 * (size_t)d.nn;
     TFA_TRY(ialloc(&d.tblk, d.nnzb));
     TFA_TRY(ialloc(&d.apical, d.nn));
-    TFA_TRY(dalloc(&d.valT, 9 * (size_t)d.nnzb));
+    TFA_TRY(dalloc(&d.valT, (size_t)d.nval));
+    TF_CUDA(cudaMemset(d.valT, 0, sizeof(double) * (size_t)d.nval));  // padding stays zero
     TFA_TRY(dalloc(&d.lamv, n3));
     TFA_TRY(dalloc(&d.carry, n3));
     TFA_TRY(dalloc(&d.dldu, n3));
@@ -267,10 +268,11 @@ tf_status loss_value(tf_handle* h, const double* params, double* loss) {
 // Krylov graphs (which hold the value pointer) stay valid.
 tf_status solve_transposed(tf_handle* h, int* iters) {
     Device& d = h->d;
-    k_transpose_blocks<<<cdiv(d.nnzb, kT), kT, 0, h->stream>>>(d.nnzb, d.tblk, d.val, d.valT);
+    k_transpose_blocks<<<cdiv(d.nnzb, kT), kT, 0, h->stream>>>(d.nnzb, d.tblk, d.bofs, d.val, d.valT);
     TF_LAUNCH_CHECK(h);
-    TF_CUDA(cudaMemcpyAsync(d.val, d.valT, sizeof(double) * 9 * (size_t)d.nnzb, cudaMemcpyDeviceToDevice,
+    TF_CUDA(cudaMemcpyAsync(d.val, d.valT, sizeof(double) * (size_t)d.nval, cudaMemcpyDeviceToDevice,
                             h->stream));
+    amg_mark_stale(h, 2);  // the multigrid hierarchy follows the transposed matrix
     double rr = 0.0;
     const tf_status s = krylov_solve(h, iters, &rr);
     return s == TF_KRYLOV_NOT_CONVERGED ? TF_OK : s;

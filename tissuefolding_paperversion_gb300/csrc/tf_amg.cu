@@ -1,0 +1,1102 @@
+// Aggregation algebraic multigrid: the preconditioner of the Krylov solve of
+// A du = g (A = K^T) on large meshes, in place of the block-Jacobi one.  No
+// counterpart in the reference, which factorises the system with Pardiso
+// (NewtonRaphsonSolver.cpp:418-683); the solution it converges to is the
+// same (the Krylov tolerance is unchanged).
+//
+// Set-up, once per handle, on the host from the block pattern and the
+// reference node positions:
+//   * greedy aggregation of the node graph: a node whose neighbours are all
+//     free becomes an aggregate with them; left-over nodes join the
+//     neighbouring aggregate they touch most.  Aggregates never cross
+//     instances (the graph of a batch is disconnected);
+//   * near-null space: the six rigid-body modes at level 0 (translations and
+//     rotations about the aggregate centroid), zero on fixed DOFs; at coarser
+//     levels the R factors of the level below;
+//   * tentative prolongator per aggregate from a modified Gram-Schmidt QR of
+//     its near-null-space rows (6 coarse DOFs per aggregate; a dependent
+//     column is dropped and its coarse DOF gets a unit diagonal);
+//   * coarse block patterns and, per coarse block, the ordered list of fine
+//     blocks contributing to it (Galerkin product without atomics).
+// Numeric phase, once per assembled matrix (all on the device):
+//   A_{l+1} = P_l^T A_l P_l block by block; 6x6 block inverses; lambda_max of
+//   D^-1 A per level by power iteration (smoother weight 4 / (3.15 lambda));
+//   Gauss-Jordan inverse of the coarsest level per instance (<= 16 nodes).
+// Application (one V-cycle per preconditioner call, all kernels, capturable
+// in a CUDA graph): damped block-Jacobi pre- and post-smoothing, residual,
+// restriction, coarse correction.  Kernels of an instance whose Krylov
+// solve has stopped return at once.
+// Precision: the preconditioner is any fixed linear operator as far as the
+// Krylov method is concerned, so the matrices it reads (a copy of the
+// level-0 values, the coarse operators, the level-0 block inverses) are
+// stored in FP32 -- half the bytes of its bandwidth-bound SpMVs -- while
+// every product, sum and vector stays FP64.  The Krylov recurrences, their
+// SpMVs with A and the convergence test are untouched FP64.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "tf_internal.cuh"
+
+namespace tf {
+
+namespace {
+
+constexpr int kT = 256;
+constexpr int kCoarseNodes = 16;  // nodes per instance at the coarsest level (96 DOFs)
+constexpr int kCoarseDofs = 6 * kCoarseNodes;
+constexpr int kPowerIters = 16;
+
+// ---- host set-up -----------------------------------------------------------------
+
+struct HostLevel {
+    int n = 0, bs = 3;
+    std::vector<int> rowptr, colidx;   // block pattern of this level
+    std::vector<int> seg0;             // [nseg+1] node offsets per instance
+    std::vector<double> B;             // [n * bs * 6] near-null space rows
+};
+
+// Greedy aggregation; returns the aggregate of each node and their count.
+int aggregate(const std::vector<int>& rowptr, const std::vector<int>& colidx, int n, std::vector<int>& agg) {
+    agg.assign(n, -1);
+    int na = 0;
+    for (int i = 0; i < n; ++i) {
+        if (agg[i] >= 0) continue;
+        bool free = true;
+        for (int p = rowptr[i]; p < rowptr[i + 1] && free; ++p) free = agg[colidx[p]] < 0;
+        if (!free) continue;
+        for (int p = rowptr[i]; p < rowptr[i + 1]; ++p) agg[colidx[p]] = na;
+        agg[i] = na++;
+    }
+    std::vector<int> cnt;
+    for (int i = 0; i < n; ++i) {
+        if (agg[i] >= 0) continue;
+        // join the neighbouring aggregate with most connections (smallest id on ties)
+        int best = -1, bestc = 0;
+        for (int p = rowptr[i]; p < rowptr[i + 1]; ++p) {
+            const int a = agg[colidx[p]];
+            if (a < 0) continue;
+            int c = 0;
+            for (int q = rowptr[i]; q < rowptr[i + 1]; ++q) c += agg[colidx[q]] == a;
+            if (c > bestc || (c == bestc && a < best)) {
+                best = a;
+                bestc = c;
+            }
+        }
+        agg[i] = best >= 0 ? best : na++;
+    }
+    return na;
+}
+
+// Modified Gram-Schmidt of the m x 6 matrix M (row-major) in place: Q in M,
+// R (6 x 6, row-major).  Returns the mask of dropped (dependent) columns.
+int mgs(std::vector<double>& M, int m, double* R) {
+    int dead = 0;
+    std::fill(R, R + 36, 0.0);
+    double ref[6];
+    for (int c = 0; c < 6; ++c) {
+        double s = 0.0;
+        for (int r = 0; r < m; ++r) s += M[6 * r + c] * M[6 * r + c];
+        ref[c] = std::sqrt(s);
+    }
+    for (int c = 0; c < 6; ++c) {
+        for (int q = 0; q < c; ++q) {
+            if (dead & (1 << q)) continue;
+            double s = 0.0;
+            for (int r = 0; r < m; ++r) s += M[6 * r + q] * M[6 * r + c];
+            R[6 * q + c] = s;
+            for (int r = 0; r < m; ++r) M[6 * r + c] -= s * M[6 * r + q];
+        }
+        double s = 0.0;
+        for (int r = 0; r < m; ++r) s += M[6 * r + c] * M[6 * r + c];
+        const double nv = std::sqrt(s);
+        if (!(nv > 1e-10 * ref[c]) || !(ref[c] > 0.0)) {
+            dead |= 1 << c;
+            for (int r = 0; r < m; ++r) M[6 * r + c] = 0.0;
+            for (int q = 0; q < 6; ++q) R[6 * q + c] = 0.0;
+            continue;
+        }
+        R[6 * c + c] = nv;
+        for (int r = 0; r < m; ++r) M[6 * r + c] /= nv;
+    }
+    return dead;
+}
+
+template <class T>
+tf_status up(T** dst, const std::vector<T>& v) {
+    const size_t n = std::max<size_t>(v.size(), 1);
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(dst), n * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("device allocation failed in the multigrid set-up");
+        return TF_OUT_OF_MEMORY;
+    }
+    if (!v.empty()) TF_CUDA(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return TF_OK;
+}
+
+template <class T>
+tf_status zeros(T** dst, size_t n) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(dst), std::max<size_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error("device allocation failed in the multigrid set-up");
+        return TF_OUT_OF_MEMORY;
+    }
+    TF_CUDA(cudaMemset(*dst, 0, std::max<size_t>(n, 1) * sizeof(T)));
+    return TF_OK;
+}
+
+#define AMG_TRY(expr)               \
+    do {                            \
+        tf_status _s = (expr);      \
+        if (_s != TF_OK) return _s; \
+    } while (0)
+
+}  // namespace
+
+// Device view of one level.  Everything the V-cycle reads or writes is
+// FP32 (see the precision note above); the smoother weights are FP64 scalars.
+struct AmgLevel {
+    int n = 0, bs = 3;
+    // matrix of levels >= 1: CSR of 6x6 row-major blocks
+    int* rowptr = nullptr;
+    int* colidx = nullptr;
+    int* rowof = nullptr;
+    int* diag = nullptr;  // block index of (i, i)
+    float* val = nullptr;
+    int64_t nnzb = 0;
+    float* dinv = nullptr;   // [n][36] block inverses (levels >= 1)
+    int* seg = nullptr;      // [n] instance of each node (levels >= 1)
+    // transfer to level + 1 (absent at the coarsest level)
+    int* agg = nullptr;      // [n]
+    float* P = nullptr;      // [n][bs*6]
+    int* mptr = nullptr;     // [n_{l+1}+1] members of each next-level node
+    int* mlist = nullptr;
+    int* gptr = nullptr;     // [nnzb_{l+1}+1] fine blocks of each next-level block
+    int* glist = nullptr;
+    uint8_t* dead = nullptr; // [n * bs] (levels >= 1) DOFs with a zero prolongator column
+    // vectors (levels >= 1: r input, e output; all levels: x, t work)
+    float *r = nullptr, *x = nullptr, *t = nullptr, *e = nullptr;
+};
+
+struct Amg {
+    int nlev = 0;
+    AmgLevel L[kAmgMaxLevels];
+    double* omega = nullptr;   // [nlev] smoother weights
+    double* pscal = nullptr;   // [nlev][2] power-iteration scalars (scale, lambda)
+    float* pv = nullptr;       // power-iteration vectors (max n*bs each)
+    float* pw = nullptr;
+    double* part = nullptr;    // per-CTA partial sums
+    unsigned* ticket = nullptr;
+    float* val32 = nullptr;    // FP32 copy of the level-0 values (sliced layout)
+    float* dinv32 = nullptr;   // FP32 copy of the level-0 block inverses
+    int nseg = 1;
+    int* cnode0 = nullptr;     // [nseg+1] coarsest-level node offsets per instance
+    int* cinv0 = nullptr;      // [nseg+1] offsets of the dense inverses
+    float* cinv = nullptr;     // coarsest inverses, m_g x m_g row-major
+    bool coarse_exact = true;
+    int max_cm = 0;
+    std::vector<int> h_n;      // nodes per level (host)
+    // what the next solve has to redo: 0 nothing, 1 the FP32 copies of the
+    // level-0 matrix (new assembly, same time step), 2 the whole hierarchy
+    int stale = 2;
+    bool reused = false;       // the last numeric phase kept the coarse levels
+};
+
+void amg_free(Amg* a) {
+    if (!a) return;
+    for (int l = 0; l < a->nlev; ++l) {
+        AmgLevel& L = a->L[l];
+        void* ptrs[] = {L.rowptr, L.colidx, L.rowof, L.diag, L.val, L.seg, L.agg, L.P, L.mptr, L.mlist, L.gptr,
+                        L.glist, L.dead, L.r, L.x, L.t, L.e};
+        for (void* p : ptrs)
+            if (p) cudaFree(p);
+        if (l > 0 && L.dinv) cudaFree(L.dinv);
+    }
+    void* ptrs[] = {a->omega, a->pscal, a->pv, a->pw, a->part, a->ticket, a->cnode0, a->cinv0, a->cinv,
+                    a->val32, a->dinv32};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete a;
+}
+
+// Symbolic set-up from the level-0 pattern, the reference positions and the
+// fixed DOFs.  Level 0 uses the handle's own matrix, block inverses and
+// sliced storage.
+tf_status amg_build(tf_handle* h, const double* pos) {
+    Device& d = h->d;
+    Amg* a = new Amg;
+    h->amg = a;
+    a->nseg = d.nseg;
+    std::vector<HostLevel> H(1);
+    H[0].n = d.nn;
+    H[0].bs = 3;
+    H[0].rowptr = h->h_rowptr;
+    H[0].colidx = h->h_colidx;
+    H[0].seg0 = h->h_seg_node0;
+    int lev = 0;
+    while (true) {
+        HostLevel& F = H[lev];
+        int maxn = 0;
+        for (int g = 0; g < d.nseg; ++g) maxn = std::max(maxn, F.seg0[g + 1] - F.seg0[g]);
+        if (maxn <= kCoarseNodes || lev + 1 >= kAmgMaxLevels) break;
+        std::vector<int> agg;
+        const int na = aggregate(F.rowptr, F.colidx, F.n, agg);
+        if (na >= F.n) break;  // no coarsening possible
+        // members per aggregate (node order)
+        std::vector<int> mptr(na + 1, 0), mlist(F.n);
+        for (int i = 0; i < F.n; ++i) mptr[agg[i] + 1]++;
+        for (int c = 0; c < na; ++c) mptr[c + 1] += mptr[c];
+        {
+            std::vector<int> fill(mptr.begin(), mptr.end() - 1);
+            for (int i = 0; i < F.n; ++i) mlist[fill[agg[i]]++] = i;
+        }
+        // tentative prolongator and the next near-null space
+        const int bs = F.bs;
+        std::vector<double> P((size_t)F.n * bs * 6, 0.0), Bc((size_t)na * 36, 0.0);
+        std::vector<uint8_t> dead((size_t)na * 6, 0);
+        std::vector<double> M;
+        for (int c = 0; c < na; ++c) {
+            const int m0 = mptr[c], m1 = mptr[c + 1];
+            const int rows = (m1 - m0) * bs;
+            M.assign((size_t)rows * 6, 0.0);
+            if (lev == 0) {
+                double cen[3] = {0, 0, 0};
+                for (int q = m0; q < m1; ++q)
+                    for (int k = 0; k < 3; ++k) cen[k] += pos[3 * (size_t)mlist[q] + k];
+                for (int k = 0; k < 3; ++k) cen[k] /= (m1 - m0);
+                for (int q = m0; q < m1; ++q) {
+                    const int i = mlist[q];
+                    const double rx = pos[3 * (size_t)i] - cen[0], ry = pos[3 * (size_t)i + 1] - cen[1],
+                                 rz = pos[3 * (size_t)i + 2] - cen[2];
+                    // rows x, y, z of [I | e_x x r, e_y x r, e_z x r]
+                    const double rowsv[3][6] = {{1, 0, 0, 0, rz, -ry}, {0, 1, 0, -rz, 0, rx}, {0, 0, 1, ry, -rx, 0}};
+                    for (int k = 0; k < 3; ++k) {
+                        const bool fx = h->h_fixed[3 * (size_t)i + k] != 0;
+                        for (int col = 0; col < 6; ++col)
+                            M[(size_t)(bs * (q - m0) + k) * 6 + col] = fx ? 0.0 : rowsv[k][col];
+                    }
+                }
+            } else {
+                for (int q = m0; q < m1; ++q) {
+                    const int i = mlist[q];
+                    for (int k = 0; k < 6; ++k)
+                        for (int col = 0; col < 6; ++col)
+                            M[(size_t)(6 * (q - m0) + k) * 6 + col] = F.B[(size_t)i * 36 + 6 * k + col];
+                }
+            }
+            double R[36];
+            const int dm = mgs(M, rows, R);
+            for (int k = 0; k < 6; ++k) dead[(size_t)c * 6 + k] = (dm >> k) & 1;
+            std::copy(R, R + 36, Bc.begin() + (size_t)c * 36);
+            for (int q = m0; q < m1; ++q) {
+                const int i = mlist[q];
+                for (int k = 0; k < bs; ++k)
+                    for (int col = 0; col < 6; ++col)
+                        P[((size_t)i * bs + k) * 6 + col] = M[(size_t)(bs * (q - m0) + k) * 6 + col];
+            }
+        }
+        // coarse pattern
+        HostLevel C;
+        C.n = na;
+        C.bs = 6;
+        C.B = std::move(Bc);
+        C.seg0.assign(d.nseg + 1, 0);
+        // aggregates of an instance are contiguous and its first node is a
+        // root: roots are created in node order, left-over nodes only join
+        // aggregates of their own instance
+        for (int g = 0; g <= d.nseg; ++g) C.seg0[g] = g < d.nseg ? (F.seg0[g] < F.n ? agg[F.seg0[g]] : na) : na;
+        C.rowptr.assign(na + 1, 0);
+        {
+            std::vector<int> mark(na, -1), cols;
+            for (int c = 0; c < na; ++c) {
+                cols.clear();
+                for (int q = mptr[c]; q < mptr[c + 1]; ++q) {
+                    const int i = mlist[q];
+                    for (int p = F.rowptr[i]; p < F.rowptr[i + 1]; ++p) {
+                        const int J = agg[F.colidx[p]];
+                        if (mark[J] != c) {
+                            mark[J] = c;
+                            cols.push_back(J);
+                        }
+                    }
+                }
+                std::sort(cols.begin(), cols.end());
+                C.colidx.insert(C.colidx.end(), cols.begin(), cols.end());
+                C.rowptr[c + 1] = static_cast<int>(C.colidx.size());
+            }
+        }
+        const int64_t cnnzb = (int64_t)C.colidx.size();
+        // Galerkin lists: fine block b -> coarse block, grouped per coarse block
+        const int64_t fnnzb = (int64_t)F.colidx.size();
+        std::vector<int> cb(fnnzb);
+        for (int i = 0; i < F.n; ++i)
+            for (int p = F.rowptr[i]; p < F.rowptr[i + 1]; ++p) {
+                const int I = agg[i], J = agg[F.colidx[p]];
+                auto b = C.colidx.begin() + C.rowptr[I], e = C.colidx.begin() + C.rowptr[I + 1];
+                cb[p] = static_cast<int>(std::lower_bound(b, e, J) - C.colidx.begin());
+            }
+        std::vector<int> gptr(cnnzb + 1, 0), glist(fnnzb);
+        for (int64_t b = 0; b < fnnzb; ++b) gptr[cb[b] + 1]++;
+        for (int64_t c = 0; c < cnnzb; ++c) gptr[c + 1] += gptr[c];
+        {
+            std::vector<int> fill(gptr.begin(), gptr.end() - 1);
+            for (int64_t b = 0; b < fnnzb; ++b) glist[fill[cb[b]]++] = static_cast<int>(b);
+        }
+        // device arrays of the fine level's transfer
+        AmgLevel& DL = a->L[lev];
+        AMG_TRY(up(&DL.agg, agg));
+        AMG_TRY(up(&DL.P, std::vector<float>(P.begin(), P.end())));
+        AMG_TRY(up(&DL.mptr, mptr));
+        AMG_TRY(up(&DL.mlist, mlist));
+        AMG_TRY(up(&DL.gptr, gptr));
+        AMG_TRY(up(&DL.glist, glist));
+        // the coarse level's own arrays
+        AmgLevel& CL = a->L[lev + 1];
+        CL.n = na;
+        CL.bs = 6;
+        CL.nnzb = cnnzb;
+        std::vector<int> rowof(cnnzb), diag(na);
+        std::vector<int> seg(na);
+        for (int c = 0; c < na; ++c) {
+            for (int p = C.rowptr[c]; p < C.rowptr[c + 1]; ++p) {
+                rowof[p] = c;
+                if (C.colidx[p] == c) diag[c] = p;
+            }
+        }
+        for (int g = 0; g < d.nseg; ++g)
+            for (int c = C.seg0[g]; c < C.seg0[g + 1]; ++c) seg[c] = g;
+        AMG_TRY(up(&CL.rowptr, C.rowptr));
+        AMG_TRY(up(&CL.colidx, C.colidx));
+        AMG_TRY(up(&CL.rowof, rowof));
+        AMG_TRY(up(&CL.diag, diag));
+        AMG_TRY(up(&CL.seg, seg));
+        AMG_TRY(up(&CL.dead, dead));
+        AMG_TRY(zeros(&CL.val, (size_t)cnnzb * 36));  // float
+        AMG_TRY(zeros(&CL.dinv, (size_t)na * 36));
+        H.push_back(std::move(C));
+        ++lev;
+    }
+    a->nlev = lev + 1;
+    if (a->nlev < 2) {  // nothing to coarsen: block-Jacobi is used instead
+        amg_free(a);
+        h->amg = nullptr;
+        return TF_OK;
+    }
+    // level 0 device view: the handle's own arrays
+    AmgLevel& L0 = a->L[0];
+    L0.n = d.nn;
+    L0.bs = 3;
+    L0.nnzb = d.nnzb;
+    size_t maxv = 0;
+    for (int l = 0; l < a->nlev; ++l) {
+        AmgLevel& L = a->L[l];
+        const size_t nv = (size_t)L.n * L.bs;
+        maxv = std::max(maxv, nv);
+        AMG_TRY(zeros(&L.x, nv));
+        AMG_TRY(zeros(&L.t, nv));
+        if (l > 0) {
+            AMG_TRY(zeros(&L.r, nv));
+            AMG_TRY(zeros(&L.e, nv));
+        }
+        a->h_n.push_back(L.n);
+    }
+    AMG_TRY(zeros(&a->omega, (size_t)a->nlev));
+    AMG_TRY(zeros(&a->val32, (size_t)d.nval));
+    AMG_TRY(zeros(&a->dinv32, 9 * (size_t)d.nn));
+    AMG_TRY(zeros(&a->pscal, 2 * (size_t)a->nlev));
+    AMG_TRY(zeros(&a->pv, maxv));
+    AMG_TRY(zeros(&a->pw, maxv));
+    int64_t maxc = 0;  // CTAs of the warp-per-row power iteration on the coarse levels
+    for (int l = 1; l < a->nlev; ++l) maxc = std::max<int64_t>(maxc, cdiv(32 * (int64_t)a->L[l].n, kT));
+    AMG_TRY(zeros(&a->part, (size_t)std::max<int64_t>({(int64_t)cdiv((int64_t)maxv, kT), (int64_t)d.ncta, maxc}) + 1));
+    AMG_TRY(zeros(&a->ticket, 1));
+    // coarsest level: dense inverse per instance
+    const HostLevel& CH = H.back();
+    std::vector<int> cinv0(d.nseg + 1, 0);
+    a->max_cm = 0;
+    for (int g = 0; g < d.nseg; ++g) {
+        const int m = CH.bs * (CH.seg0[g + 1] - CH.seg0[g]);
+        a->max_cm = std::max(a->max_cm, m);
+        cinv0[g + 1] = cinv0[g] + m * m;
+    }
+    a->coarse_exact = a->max_cm <= kCoarseDofs;
+    AMG_TRY(up(&a->cnode0, CH.seg0));
+    AMG_TRY(up(&a->cinv0, cinv0));
+    AMG_TRY(zeros(&a->cinv, (size_t)std::max(cinv0[d.nseg], 1)));
+    return TF_OK;
+}
+
+
+namespace {
+
+__device__ __forceinline__ bool seg_stopped(const double* scal, int seg) {
+    return __ldcg(&scal[(size_t)seg * S_COUNT + S_FLAG]) != 0.0;
+}
+
+// Sum of one value over the grid: partials per CTA, the last CTA to arrive
+// adds them in CTA order (no waiting).  True in thread 0 of that CTA.
+__device__ bool grid_sum(double v, double* part, unsigned* ticket, double* total) {
+    __shared__ double sm[kT / 32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sm[warp] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += sm[w];
+        part[blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return false;
+    __threadfence();
+    double t = 0.0;
+    for (unsigned b = 0; b < gridDim.x; ++b) t += __ldcg(&part[b]);
+    *total = t;
+    *ticket = 0u;
+    return true;
+}
+
+// Level-0 node of this thread (CTA tables of the node-parallel kernels).
+struct Node0 {
+    int i, seg;
+    bool valid;
+};
+__device__ __forceinline__ Node0 node0(const Device& d) {
+    Node0 q;
+    q.seg = d.cta_seg[blockIdx.x];
+    q.i = d.cta_node0[blockIdx.x] + threadIdx.x;
+    q.valid = q.i < d.cta_node1[blockIdx.x];
+    return q;
+}
+
+__device__ __forceinline__ void mul3(const float* __restrict__ D, const float r[3], float z[3]) {
+    z[0] = fmaf(D[0], r[0], fmaf(D[1], r[1], D[2] * r[2]));
+    z[1] = fmaf(D[3], r[0], fmaf(D[4], r[1], D[5] * r[2]));
+    z[2] = fmaf(D[6], r[0], fmaf(D[7], r[1], D[8] * r[2]));
+}
+
+// Row of the FP32 copy of the sliced level-0 matrix times x (FP32 vectors).
+__device__ __forceinline__ void sliced_row32(const int* __restrict__ wslot0, const int* __restrict__ scol,
+                                             const float* __restrict__ val, const float* __restrict__ x,
+                                             float y[3]) {
+    const int lane = threadIdx.x & 31;
+    const int wg = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const int s0 = __ldg(&wslot0[wg]), s1 = __ldg(&wslot0[wg + 1]);
+    float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+    const int* __restrict__ col = scol + lane;
+    const float* __restrict__ a = val + lane;
+#pragma unroll 4
+    for (int s = s0; s < s1; ++s) {
+        const int j = __ldg(&col[(size_t)s * kSlice]);
+        const float* __restrict__ v = a + (size_t)s * kSlotDoubles;
+        const float x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+        y0 = fmaf(__ldg(&v[0]), x0, fmaf(__ldg(&v[32]), x1, fmaf(__ldg(&v[64]), x2, y0)));
+        y1 = fmaf(__ldg(&v[96]), x0, fmaf(__ldg(&v[128]), x1, fmaf(__ldg(&v[160]), x2, y1)));
+        y2 = fmaf(__ldg(&v[192]), x0, fmaf(__ldg(&v[224]), x1, fmaf(__ldg(&v[256]), x2, y2)));
+    }
+    y[0] = y0;
+    y[1] = y1;
+    y[2] = y2;
+}
+
+// Warp-cooperative product of row i of a 6x6-block CSR matrix with x.
+// Lane 6 k + a (< 30) takes row a of blocks k, k + 5, k + 10, ... of the
+// row: six FMAs per block row, every value used once (lane groups read
+// 5 consecutive blocks); the five partial sums of each row a are then
+// gathered by shuffles.  Every lane returns y.
+__device__ __forceinline__ void row6_warp(const AmgLevel& L, int i, const float* __restrict__ x, float y[6]) {
+    const int lane = threadIdx.x & 31;
+    const int kb = lane / 6, a = lane - 6 * kb;
+    float acc = 0.f;
+    const int p0 = L.rowptr[i], p1 = L.rowptr[i + 1];
+    if (lane < 30) {
+#pragma unroll 2
+        for (int p = p0 + kb; p < p1; p += 5) {
+            const int j = __ldg(&L.colidx[p]);
+            const float* __restrict__ v = L.val + 36 * (size_t)p + 6 * a;
+            const float* __restrict__ xj = x + 6 * (size_t)j;
+#pragma unroll
+            for (int b2 = 0; b2 < 6; ++b2) acc = fmaf(__ldg(&v[b2]), xj[b2], acc);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        float s2 = 0.f;
+#pragma unroll
+        for (int g = 0; g < 5; ++g) s2 += __shfl_sync(0xffffffffu, acc, 6 * g + k);
+        y[k] = s2;
+    }
+}
+
+// r[a] without dynamic register indexing (which would go to local memory).
+__device__ __forceinline__ float pick6(const float r[6], int a) {
+    float v = 0.f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) v = (k == a) ? r[k] : v;
+    return v;
+}
+
+// Lane a < 6 of the warp: (D r)_a for the 6x6 block D (r known to all lanes).
+__device__ __forceinline__ float lane_mul6(const float* __restrict__ D, const float r[6], int a) {
+    float s = 0.f;
+#pragma unroll
+    for (int b = 0; b < 6; ++b) s = fmaf(__ldg(&D[6 * a + b]), r[b], s);
+    return s;
+}
+
+// ---- numeric phase -----------------------------------------------------------
+
+__global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        b[k] = (float)a[k];
+}
+
+// Coarse block c, row p: sum over its fine blocks b = (i, j) of
+// (P_i^T A_b P_j)(p, :).  Level 0 reads the FP32 copy of the sliced storage.
+template <int BS, bool L0>
+__global__ void k_galerkin(AmgLevel F, AmgLevel C, const int* __restrict__ rowof0, const int* __restrict__ colidx0,
+                           const int* __restrict__ bofs0, const float* __restrict__ val0) {
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= C.nnzb * 6) return;
+    const int64_t c = gid / 6;
+    const int p = static_cast<int>(gid - 6 * c);
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int q = F.gptr[c]; q < F.gptr[c + 1]; ++q) {
+        const int b = __ldg(&F.glist[q]);
+        const int i = L0 ? __ldg(&rowof0[b]) : __ldg(&F.rowof[b]);
+        const int j = L0 ? __ldg(&colidx0[b]) : __ldg(&F.colidx[b]);
+        const float* __restrict__ Pi = F.P + (size_t)i * BS * 6;
+        const float* __restrict__ Pj = F.P + (size_t)j * BS * 6;
+        const int base = L0 ? __ldg(&bofs0[b]) : 0;
+        float t[BS];
+#pragma unroll
+        for (int s2 = 0; s2 < BS; ++s2) t[s2] = 0.f;
+#pragma unroll
+        for (int r = 0; r < BS; ++r) {
+            const float pr = __ldg(&Pi[6 * r + p]);
+#pragma unroll
+            for (int s2 = 0; s2 < BS; ++s2) {
+                const float av = L0 ? __ldg(&val0[base + kSlice * (3 * r + s2)])
+                                    : __ldg(&F.val[36 * (size_t)b + 6 * r + s2]);
+                t[s2] = fmaf(pr, av, t[s2]);
+            }
+        }
+#pragma unroll
+        for (int s2 = 0; s2 < BS; ++s2)
+#pragma unroll
+            for (int q2 = 0; q2 < 6; ++q2) acc[q2] = fmaf(t[s2], __ldg(&Pj[6 * s2 + q2]), acc[q2]);
+    }
+    const int I = C.rowof[c];
+    if (C.colidx[c] == I && C.dead[6 * I + p]) acc[p] = 1.f;  // dropped coarse DOF: unit diagonal
+    float* out = C.val + 36 * (size_t)c + 6 * p;
+#pragma unroll
+    for (int q2 = 0; q2 < 6; ++q2) out[q2] = acc[q2];
+}
+
+// Inverse of a 6x6 block by Gauss-Jordan with partial pivoting (FP64 work).
+__device__ void inv6(const float* __restrict__ A, float* __restrict__ out) {
+    double M[6][12];
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+#pragma unroll
+        for (int b = 0; b < 6; ++b) {
+            M[a][b] = A[6 * a + b];
+            M[a][6 + b] = a == b ? 1.0 : 0.0;
+        }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        int piv = k;
+        double best = fabs(M[k][k]);
+#pragma unroll
+        for (int r = k + 1; r < 6; ++r)
+            if (fabs(M[r][k]) > best) {
+                best = fabs(M[r][k]);
+                piv = r;
+            }
+        if (piv != k)
+#pragma unroll
+            for (int c = 0; c < 12; ++c) {
+                const double tmp = M[k][c];
+                M[k][c] = M[piv][c];
+                M[piv][c] = tmp;
+            }
+        const double dk = M[k][k];
+        const double rinv = dk != 0.0 ? 1.0 / dk : 1.0;
+#pragma unroll
+        for (int c = 0; c < 12; ++c) M[k][c] *= rinv;
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            if (r == k) continue;
+            const double f = M[r][k];
+#pragma unroll
+            for (int c = 0; c < 12; ++c) M[r][c] = fma(-f, M[k][c], M[r][c]);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+#pragma unroll
+        for (int b = 0; b < 6; ++b) out[6 * a + b] = (float)M[a][6 + b];
+}
+
+__global__ void k_inv6(AmgLevel L) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= L.n) return;
+    inv6(L.val + 36 * (size_t)L.diag[i], L.dinv + 36 * (size_t)i);
+}
+
+// power iteration for lambda_max(D^-1 A): v0 deterministic, scale = 1/|v0|
+__global__ void k_pw_init(int64_t m, float* __restrict__ v, double* part, unsigned* ticket, double* scal) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double s = 0.0;
+    if (k < m) {
+        unsigned h = static_cast<unsigned>(k) * 2654435761u + 12345u;
+        h ^= h >> 13;
+        h *= 0x5bd1e995u;
+        h ^= h >> 15;
+        // zero-mean pseudo-random values: every mode, the rough ones included,
+        // is present from the start (a positive vector barely excites the
+        // largest eigenvalues, which would be underestimated)
+        const float x = (h & 0xffffu) / 65536.0f - 0.5f;
+        v[k] = x;
+        s = (double)x * x;
+    }
+    double tot;
+    if (grid_sum(s, part, ticket, &tot)) scal[0] = 1.0 / sqrt(tot);
+}
+
+__device__ __forceinline__ void pw_finish(double tot, double* scal, double* omega) {
+    const double lam = sqrt(tot);
+    scal[0] = lam > 0.0 ? 1.0 / lam : 1.0;
+    scal[1] = lam;
+    // 5 % margin: the power iteration approaches lambda_max from below
+    *omega = lam > 0.0 ? (4.0 / 3.0) / (1.05 * lam) : 1.0;
+}
+
+__global__ void k_pw_step0(Device d, const float* __restrict__ val32, const float* __restrict__ dinv32,
+                           const float* __restrict__ v, float* __restrict__ w, double* part, unsigned* ticket,
+                           double* scal, double* omega) {
+    const Node0 q = node0(d);
+    double s = 0.0;
+    float y[3] = {0.f, 0.f, 0.f};
+    if (q.valid) sliced_row32(d.wslot0, d.scol, val32, v, y);
+    if (q.valid) {
+        const float sc = (float)__ldcg(&scal[0]);
+        float yy[3] = {sc * y[0], sc * y[1], sc * y[2]}, z[3];
+        mul3(dinv32 + 9 * (size_t)q.i, yy, z);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            w[3 * q.i + k] = z[k];
+            s += (double)z[k] * z[k];
+        }
+    }
+    double tot;
+    if (grid_sum(s, part, ticket, &tot)) pw_finish(tot, scal, omega);
+}
+
+__global__ void k_pw_step6(AmgLevel L, const float* __restrict__ v, float* __restrict__ w, double* part,
+                           unsigned* ticket, double* scal, double* omega) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // one warp per row
+    const int lane = threadIdx.x & 31;
+    double s = 0.0;
+    if (i < L.n) {
+        float y[6];
+        row6_warp(L, i, v, y);
+        const float sc = (float)__ldcg(&scal[0]);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) y[k] *= sc;
+        if (lane < 6) {
+            const float z = lane_mul6(L.dinv + 36 * (size_t)i, y, lane);
+            w[6 * i + lane] = z;
+            s = (double)z * z;
+        }
+    }
+    double tot;
+    if (grid_sum(s, part, ticket, &tot)) pw_finish(tot, scal, omega);
+}
+
+// Gauss-Jordan inverse of the coarsest matrix of each instance (one CTA
+// each, FP64 work, FP32 result)
+__global__ void k_coarse_invert(AmgLevel L, const int* __restrict__ cnode0, const int* __restrict__ cinv0,
+                                float* __restrict__ cinv) {
+    extern __shared__ double M[];  // m x 2m
+    __shared__ double f[kCoarseDofs];
+    __shared__ int piv;
+    __shared__ double tiny;
+    const int g = blockIdx.x;
+    const int n0 = cnode0[g], n1 = cnode0[g + 1];
+    const int m = 6 * (n1 - n0), w = 2 * m;
+    if (m == 0) return;
+    for (int k = threadIdx.x; k < m * w; k += blockDim.x) {
+        const int r = k / w, c = k - r * w;
+        M[k] = (c - m == r) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    for (int I = n0 + threadIdx.x; I < n1; I += blockDim.x)
+        for (int p = L.rowptr[I]; p < L.rowptr[I + 1]; ++p) {
+            const int J = L.colidx[p] - n0;
+            const float* v = L.val + 36 * (size_t)p;
+            for (int a = 0; a < 6; ++a)
+                for (int b = 0; b < 6; ++b) M[(6 * (I - n0) + a) * w + 6 * J + b] = (double)v[6 * a + b];
+        }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double dmax = 0.0;
+        for (int r = 0; r < m; ++r) dmax = fmax(dmax, fabs(M[r * w + r]));
+        tiny = 1e-12 * dmax;
+    }
+    __syncthreads();
+    for (int k = 0; k < m; ++k) {
+        if (threadIdx.x == 0) {
+            int best = k;
+            double bv = fabs(M[k * w + k]);
+            for (int r = k + 1; r < m; ++r)
+                if (fabs(M[r * w + k]) > bv) {
+                    bv = fabs(M[r * w + k]);
+                    best = r;
+                }
+            piv = bv > tiny ? best : -1;
+        }
+        __syncthreads();
+        if (piv < 0) {
+            // (numerically) singular direction, e.g. a free rigid mode of an
+            // unconstrained sheet: no coarse correction along it
+            for (int c = threadIdx.x; c < w; c += blockDim.x) M[k * w + c] = 0.0;
+            for (int r = threadIdx.x; r < m; r += blockDim.x) M[r * w + k] = 0.0;
+            __syncthreads();
+            continue;
+        }
+        const int pr = piv;
+        if (pr != k)
+            for (int c = threadIdx.x; c < w; c += blockDim.x) {
+                const double tmp = M[k * w + c];
+                M[k * w + c] = M[pr * w + c];
+                M[pr * w + c] = tmp;
+            }
+        __syncthreads();
+        const double dk = M[k * w + k];
+        const double rinv = 1.0 / dk;
+        __syncthreads();
+        for (int c = threadIdx.x; c < w; c += blockDim.x) M[k * w + c] *= rinv;
+        for (int r = threadIdx.x; r < m; r += blockDim.x) f[r] = M[r * w + k];
+        __syncthreads();
+        for (int q = threadIdx.x; q < m * w; q += blockDim.x) {
+            const int r = q / w, c = q - r * w;
+            if (r != k) M[q] = fma(-f[r], M[k * w + c], M[q]);
+        }
+        __syncthreads();
+    }
+    float* out = cinv + cinv0[g];
+    for (int q = threadIdx.x; q < m * m; q += blockDim.x) {
+        const int r = q / m, c = q - r * m;
+        out[q] = (float)M[r * w + m + c];
+    }
+}
+
+// ---- V-cycle (FP32) -------------------------------------------------------------
+
+struct V0 {  // level-0 operands
+    Device d;
+    const double* omega;
+    const float* val32;   // FP32 copy of the values
+    const float* dinv32;  // FP32 copy of the block inverses
+};
+
+// x = omega D^-1 r  (r is the Krylov method's FP64 vector)
+__global__ void k_v0_pre(V0 a, const double* __restrict__ r, float* __restrict__ x) {
+    const Node0 q = node0(a.d);
+    if (!q.valid || seg_stopped(a.d.scal, q.seg)) return;
+    const float om = (float)__ldg(a.omega);
+    float rr[3] = {(float)r[3 * q.i], (float)r[3 * q.i + 1], (float)r[3 * q.i + 2]}, z[3];
+    mul3(a.dinv32 + 9 * (size_t)q.i, rr, z);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) x[3 * q.i + k] = om * z[k];
+}
+
+// t = r - A x
+__global__ void k_v0_resid(V0 a, const double* __restrict__ r, const float* __restrict__ x, float* __restrict__ t) {
+    const Node0 q = node0(a.d);
+    if (seg_stopped(a.d.scal, q.seg)) return;
+    float y[3];
+    if (q.valid) sliced_row32(a.d.wslot0, a.d.scol, a.val32, x, y);
+    if (!q.valid) return;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) t[3 * q.i + k] = (float)r[3 * q.i + k] - y[k];
+}
+
+// out = x + omega D^-1 (r - A x), written back as the FP64 preconditioned vector
+__global__ void k_v0_post(V0 a, const double* __restrict__ r, const float* __restrict__ x, double* __restrict__ out) {
+    const Node0 q = node0(a.d);
+    if (seg_stopped(a.d.scal, q.seg)) return;
+    float y[3];
+    if (q.valid) sliced_row32(a.d.wslot0, a.d.scol, a.val32, x, y);
+    if (!q.valid) return;
+    const float om = (float)__ldg(a.omega);
+    float rr[3], z[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) rr[k] = (float)r[3 * q.i + k] - y[k];
+    mul3(a.dinv32 + 9 * (size_t)q.i, rr, z);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) out[3 * q.i + k] = (double)fmaf(om, z[k], x[3 * q.i + k]);
+}
+
+// x_i += P_i e_agg(i)
+__global__ void k_v0_prolong(V0 a, AmgLevel F, const float* __restrict__ e, float* __restrict__ x) {
+    const Node0 q = node0(a.d);
+    if (!q.valid || seg_stopped(a.d.scal, q.seg)) return;
+    const int I = F.agg[q.i];
+    const float* __restrict__ P = F.P + 18 * (size_t)q.i;
+    float ec[6];
+#pragma unroll
+    for (int b = 0; b < 6; ++b) ec[b] = e[6 * I + b];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float s = x[3 * q.i + k];
+#pragma unroll
+        for (int b = 0; b < 6; ++b) s = fmaf(__ldg(&P[6 * k + b]), ec[b], s);
+        x[3 * q.i + k] = s;
+    }
+}
+
+// r_C(I) = sum over members i of P_i^T t_i; x_C = omega_C D_C^-1 r_C
+// (pre-smoothing).  One warp per coarse node: the lanes stride over the
+// (member, DOF) pairs.
+template <int BS>
+__global__ void k_restrict(AmgLevel F, AmgLevel C, const float* __restrict__ t, const double* __restrict__ scal,
+                           const double* __restrict__ omegaC, int presmooth) {
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (I >= C.n || seg_stopped(scal, C.seg[I])) return;
+    float rc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const int q0 = F.mptr[I], np = BS * (F.mptr[I + 1] - q0);
+    for (int qa = lane; qa < np; qa += 64) {
+        // two (member, DOF) pairs per lane and pass: their loads overlap
+        float tk[2] = {0.f, 0.f};
+        const float* __restrict__ P[2] = {F.P, F.P};
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int q = qa + 32 * u;
+            if (q < np) {
+                const int m = q / BS, k = q - BS * m;
+                const int i = __ldg(&F.mlist[q0 + m]);
+                tk[u] = t[BS * (size_t)i + k];
+                P[u] = F.P + ((size_t)i * BS + k) * 6;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int b = 0; b < 6; ++b) rc[b] = fmaf(__ldg(&P[u][b]), tk[u], rc[b]);
+    }
+#pragma unroll
+    for (int b = 0; b < 6; ++b)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) rc[b] += __shfl_xor_sync(0xffffffffu, rc[b], o);
+    if (lane < 6) {
+        C.r[6 * I + lane] = pick6(rc, lane);
+        if (presmooth) C.x[6 * I + lane] = (float)__ldg(omegaC) * lane_mul6(C.dinv + 36 * (size_t)I, rc, lane);
+    }
+}
+
+// t = r - A x  (one warp per row)
+__global__ void k_v6_resid(AmgLevel L, const double* __restrict__ scal) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= L.n || seg_stopped(scal, L.seg[i])) return;
+    float y[6];
+    row6_warp(L, i, L.x, y);
+    if (lane < 6) L.t[6 * i + lane] = L.r[6 * i + lane] - pick6(y, lane);
+}
+
+// out = x + omega D^-1 (r - A x)  (one warp per row)
+__global__ void k_v6_post(AmgLevel L, const double* __restrict__ scal, const double* __restrict__ omega,
+                          const float* __restrict__ x, float* __restrict__ out) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= L.n || seg_stopped(scal, L.seg[i])) return;
+    float y[6], rr[6];
+    row6_warp(L, i, x, y);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) rr[k] = L.r[6 * i + k] - y[k];
+    if (lane < 6)
+        out[6 * i + lane] = fmaf((float)__ldg(omega), lane_mul6(L.dinv + 36 * (size_t)i, rr, lane), x[6 * i + lane]);
+}
+
+// x_i += P_i e_agg(i)  (6-DOF fine level)
+__global__ void k_v6_prolong(AmgLevel F, const double* __restrict__ scal, const float* __restrict__ e) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= F.n || seg_stopped(scal, F.seg[i])) return;
+    const int I = F.agg[i];
+    const float* __restrict__ P = F.P + 36 * (size_t)i;
+    float ec[6];
+#pragma unroll
+    for (int b = 0; b < 6; ++b) ec[b] = e[6 * I + b];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        float s = F.x[6 * i + k];
+#pragma unroll
+        for (int b = 0; b < 6; ++b) s = fmaf(__ldg(&P[6 * k + b]), ec[b], s);
+        F.x[6 * i + k] = s;
+    }
+}
+
+// e = C^-1 r on the coarsest level, one CTA per instance
+__global__ void k_coarse_solve(AmgLevel L, const double* __restrict__ scal, const int* __restrict__ cnode0,
+                               const int* __restrict__ cinv0, const float* __restrict__ cinv) {
+    const int g = blockIdx.x;
+    if (seg_stopped(scal, g)) return;
+    const int n0 = cnode0[g], m = 6 * (cnode0[g + 1] - n0);
+    const float* __restrict__ Mi = cinv + cinv0[g];
+    const float* __restrict__ r = L.r + 6 * (size_t)n0;
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        float s = 0.f;
+        for (int j = 0; j < m; ++j) s = fmaf(__ldg(&Mi[(size_t)k * m + j]), r[j], s);
+        L.e[6 * (size_t)n0 + k] = s;
+    }
+}
+
+}  // namespace
+
+void amg_mark_stale(tf_handle* h, int level) {
+    if (h->amg) h->amg->stale = std::max(h->amg->stale, level);
+}
+
+bool amg_reused(const tf_handle* h) { return h->amg && h->amg->reused; }
+
+// Numeric phase for the current matrix.  Within a time step the matrix of
+// a later Newton iteration differs little from the first one's, so a new
+// assembly only refreshes the FP32 copies the level-0 smoother reads; the
+// coarse operators, block inverses and smoother weights are rebuilt at the
+// first solve of each time step (and whenever a solve with reused coarse
+// levels fails, see krylov_solve).
+tf_status amg_numeric(tf_handle* h) {
+    Amg* a = h->amg;
+    if (a->stale == 0) return TF_OK;
+    Device& d = h->d;
+    cudaStream_t st = h->stream;
+    // FP32 copies of the level-0 values and block inverses for the smoother
+    k_to_f32<<<4 * 152, kT, 0, st>>>(d.nval, d.val, a->val32);
+    TF_LAUNCH_CHECK(h);
+    k_to_f32<<<4 * 152, kT, 0, st>>>(9 * (int64_t)d.nn, d.dinv, a->dinv32);
+    TF_LAUNCH_CHECK(h);
+    a->reused = a->stale == 1;
+    if (a->reused) {
+        a->stale = 0;
+        return TF_OK;
+    }
+    // Galerkin products and block inverses, level by level
+    for (int l = 0; l + 1 < a->nlev; ++l) {
+        AmgLevel& F = a->L[l];
+        AmgLevel& C = a->L[l + 1];
+        const int nb = cdiv(C.nnzb * 6, kT);
+        if (l == 0) k_galerkin<3, true><<<nb, kT, 0, st>>>(F, C, d.rowof, d.colidx, d.bofs, a->val32);
+        else k_galerkin<6, false><<<nb, kT, 0, st>>>(F, C, nullptr, nullptr, nullptr, nullptr);
+        TF_LAUNCH_CHECK(h);
+        k_inv6<<<cdiv(C.n, kT), kT, 0, st>>>(C);
+        TF_LAUNCH_CHECK(h);
+    }
+    // smoother weights from lambda_max(D^-1 A) per level
+    const int last = a->coarse_exact ? a->nlev - 1 : a->nlev;
+    for (int l = 0; l < last; ++l) {
+        AmgLevel& L = a->L[l];
+        const int64_t m = (int64_t)L.n * L.bs;
+        double* scal = a->pscal + 2 * l;
+        float *v = a->pv, *w = a->pw;
+        k_pw_init<<<cdiv(m, kT), kT, 0, st>>>(m, v, a->part, a->ticket, scal);
+        TF_LAUNCH_CHECK(h);
+        for (int it = 0; it < kPowerIters; ++it) {
+            if (l == 0)
+                k_pw_step0<<<d.ncta, kNodeThreads, 0, st>>>(d, a->val32, a->dinv32, v, w, a->part, a->ticket, scal,
+                                                            a->omega);
+            else
+                k_pw_step6<<<cdiv(32 * (int64_t)L.n, kT), kT, 0, st>>>(L, v, w, a->part, a->ticket, scal,
+                                                                        a->omega + l);
+            TF_LAUNCH_CHECK(h);
+            std::swap(v, w);
+        }
+    }
+    if (a->coarse_exact) {
+        AmgLevel& L = a->L[a->nlev - 1];
+        const size_t smem = sizeof(double) * (size_t)a->max_cm * 2 * a->max_cm;
+        static bool configured = false;
+        if (!configured) {
+            TF_CUDA(cudaFuncSetAttribute(k_coarse_invert, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(double) * 2 * kCoarseDofs * kCoarseDofs)));
+            configured = true;
+        }
+        k_coarse_invert<<<a->nseg, kT, smem, st>>>(L, a->cnode0, a->cinv0, a->cinv);
+        TF_LAUNCH_CHECK(h);
+    }
+    a->stale = 0;
+    return TF_OK;
+}
+
+int amg_vcycle_kernels(const tf_handle* h) {
+    const Amg* a = h->amg;
+    return 4 * (a->nlev - 2) + 6 + (a->coarse_exact ? 0 : 2);
+}
+
+// out = M^-1 r: one V-cycle (all launches on h->stream, no host work)
+void amg_vcycle(tf_handle* h, const double* r, double* out) {
+    Amg* a = h->amg;
+    Device& d = h->d;
+    cudaStream_t st = h->stream;
+    const int nl = a->nlev;
+    V0 v0{d, a->omega, a->val32, a->dinv32};
+    AmgLevel& L0 = a->L[0];
+    k_v0_pre<<<d.ncta, kNodeThreads, 0, st>>>(v0, r, L0.x);
+    k_v0_resid<<<d.ncta, kNodeThreads, 0, st>>>(v0, r, L0.x, L0.t);
+    k_restrict<3><<<cdiv(32 * (int64_t)a->L[1].n, kT), kT, 0, st>>>(L0, a->L[1], L0.t, d.scal, a->omega + 1,
+                                                                    (1 < nl - 1 || !a->coarse_exact) ? 1 : 0);
+    for (int l = 1; l + 1 < nl; ++l) {
+        AmgLevel& L = a->L[l];
+        k_v6_resid<<<cdiv(32 * (int64_t)L.n, kT), kT, 0, st>>>(L, d.scal);
+        k_restrict<6><<<cdiv(32 * (int64_t)a->L[l + 1].n, kT), kT, 0, st>>>(L, a->L[l + 1], L.t, d.scal,
+                                                                              a->omega + l + 1,
+                                                                              (l + 1 < nl - 1 || !a->coarse_exact) ? 1 : 0);
+    }
+    AmgLevel& LC = a->L[nl - 1];
+    if (a->coarse_exact) {
+        k_coarse_solve<<<a->nseg, 128, 0, st>>>(LC, d.scal, a->cnode0, a->cinv0, a->cinv);
+    } else {
+        // x from the restriction's pre-smoothing; three more sweeps into e
+        const int nbc = cdiv(32 * (int64_t)LC.n, kT);
+        k_v6_post<<<nbc, kT, 0, st>>>(LC, d.scal, a->omega + nl - 1, LC.x, LC.e);
+        k_v6_post<<<nbc, kT, 0, st>>>(LC, d.scal, a->omega + nl - 1, LC.e, LC.t);
+        k_v6_post<<<nbc, kT, 0, st>>>(LC, d.scal, a->omega + nl - 1, LC.t, LC.e);
+    }
+    for (int l = nl - 2; l >= 1; --l) {
+        AmgLevel& L = a->L[l];
+        k_v6_prolong<<<cdiv(L.n, kT), kT, 0, st>>>(L, d.scal, a->L[l + 1].e);
+        k_v6_post<<<cdiv(32 * (int64_t)L.n, kT), kT, 0, st>>>(L, d.scal, a->omega + l, L.x, L.e);
+    }
+    k_v0_prolong<<<d.ncta, kNodeThreads, 0, st>>>(v0, L0, a->L[1].e, L0.x);
+    k_v0_post<<<d.ncta, kNodeThreads, 0, st>>>(v0, r, L0.x, out);
+}
+
+}  // namespace tf
+
+extern "C" TF_API tf_status tf_multigrid_info(tf_handle* h, int32_t* levels, int32_t* nodes, double* weights) {
+    if (!h || !levels) {
+        tf::set_error("tf_multigrid_info: bad arguments");
+        return TF_BAD_INPUT;
+    }
+    tf::Amg* a = h->amg;
+    *levels = a ? a->nlev : 0;
+    if (!a) return TF_OK;
+    if (nodes)
+        for (int l = 0; l < a->nlev; ++l) nodes[l] = a->h_n[l];
+    if (weights) {
+        TF_CUDA(cudaSetDevice(h->device));
+        TF_CUDA(cudaStreamSynchronize(h->stream));
+        TF_CUDA(cudaMemcpy(weights, a->omega, sizeof(double) * a->nlev, cudaMemcpyDeviceToHost));
+    }
+    return TF_OK;
+}

@@ -77,11 +77,15 @@ void free_all(tf_handle* h) {
     Device& d = h->d;
     void* ptrs[] = {d.conn, d.gx, d.wdet, d.detdxde, d.Fg, d.invFg, d.rates, d.lam, d.mu, d.eta, d.exposure,
                     d.aptr, d.alist, d.farea, d.fixed, d.ext_visc, d.area, d.rowptr, d.colidx, d.diag, d.rowof,
-                    d.slot, d.val, d.eblk, d.ef, d.gptr, d.glist, d.fptr, d.flist, d.uk, d.un, d.vel, d.g,
+                    d.slot, d.bofs, d.wslot0, d.scol, d.val, d.eblk, d.ef, d.gptr, d.glist, d.fptr, d.flist, d.uk, d.un, d.vel, d.g,
                     d.du, d.dinv, d.r, d.p, d.z, d.q, d.rhat, d.s, d.t, d.sh, d.scal, d.part, d.tickets,
                     d.seg_node0, d.elem_seg, d.cta_seg, d.cta_node0, d.cta_node1, d.seg_cta0, d.seg_active, d.seg_solve,
                     d.tblk, d.valT, d.lamv, d.carry, d.dldu, d.gr, d.ge, d.nu, d.apical};
     destroy_graphs(h);
+    if (h->amg) {
+        amg_free(h->amg);
+        h->amg = nullptr;
+    }
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (d.host_scal) cudaFreeHost(d.host_scal);
@@ -308,10 +312,7 @@ tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat, const st
     TF_CUDA(cudaMemset(d.area, 0, sizeof(double) * (size_t)nn));
     TF_TRY(upload(&d.rowptr, rowptr));
     TF_TRY(upload(&d.colidx, colidx));
-    TF_TRY(upload(&d.diag, diag));
     TF_TRY(upload(&d.rowof, rowof));
-    TF_TRY(upload(&d.slot, slot));
-    TF_TRY(dev_alloc(&d.val, 9 * (size_t)nnzb));
     std::vector<double> ident(9 * (size_t)ne, 0.0);
     for (int k : {0, 4, 8})
         for (int e = 0; e < ne; ++e) ident[(size_t)k * ne + e] = 1.0;
@@ -329,6 +330,64 @@ tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat, const st
     }
     TF_TRY(dev_alloc(&d.dinv, 9 * (size_t)nn));
     TF_TRY(setup_instances(h, seg_node0, seg_elem0));
+    // ---- sliced value storage ----------------------------------------------------
+    // Warp w of CTA c covers rows cta0[c] + 32 w ... (as in the node-parallel
+    // kernels); its slots are as many as its longest row.
+    std::vector<int> bofs(nnzb), scol, wslot0;
+    {
+        std::vector<int> cta0;
+        std::vector<int> cta1;
+        for (size_t g = 0; g + 1 < seg_node0.size(); ++g)
+            for (int n0 = seg_node0[g]; n0 < seg_node0[g + 1]; n0 += kNodeThreads) {
+                cta0.push_back(n0);
+                cta1.push_back(std::min(n0 + kNodeThreads, seg_node0[g + 1]));
+            }
+        const size_t nwarp = cta0.size() * kWarps;
+        wslot0.assign(nwarp + 1, 0);
+        int64_t nslots = 0;
+        for (size_t c = 0; c < cta0.size(); ++c)
+            for (int w = 0; w < kWarps; ++w) {
+                const int r0 = cta0[c] + 32 * w, r1 = std::min(r0 + 32, cta1[c]);
+                int W = 0;
+                for (int i = r0; i < r1; ++i) W = std::max(W, rowptr[i + 1] - rowptr[i]);
+                wslot0[c * kWarps + w] = static_cast<int>(nslots);
+                nslots += W;
+                if (nslots * kSlotDoubles > (int64_t)INT32_MAX) {
+                    set_error("mesh too large for 32-bit value offsets");
+                    return TF_BAD_INPUT;
+                }
+                for (int i = r0; i < r1; ++i)
+                    for (int p = rowptr[i]; p < rowptr[i + 1]; ++p)
+                        bofs[p] = (wslot0[c * kWarps + w] + (p - rowptr[i])) * kSlotDoubles + (i - r0);
+            }
+        wslot0[nwarp] = static_cast<int>(nslots);
+        scol.assign(nslots * kSlice, 0);
+        for (size_t c = 0; c < cta0.size(); ++c)
+            for (int w = 0; w < kWarps; ++w) {
+                const int r0 = cta0[c] + 32 * w, r1 = std::min(r0 + 32, cta1[c]);
+                const int s0 = wslot0[c * kWarps + w], s1 = wslot0[c * kWarps + w + 1];
+                for (int l = 0; l < 32; ++l) {
+                    const int i = r0 + l;
+                    const int len = i < r1 ? rowptr[i + 1] - rowptr[i] : 0;
+                    for (int sl = s0; sl < s1; ++sl) {
+                        const int k = sl - s0;
+                        // padding: own row (or the warp's first row), value 0
+                        scol[(size_t)sl * kSlice + l] = k < len ? colidx[rowptr[i] + k] : (i < r1 ? i : r0);
+                    }
+                }
+            }
+        d.nval = nslots * kSlotDoubles;
+    }
+    std::vector<int> slot_ofs(slot.size()), diag_ofs(nn);
+    for (size_t q = 0; q < slot.size(); ++q) slot_ofs[q] = bofs[slot[q]];
+    for (int i = 0; i < nn; ++i) diag_ofs[i] = bofs[diag[i]];
+    TF_TRY(upload(&d.diag, diag_ofs));
+    TF_TRY(upload(&d.slot, slot_ofs));
+    TF_TRY(upload(&d.bofs, bofs));
+    TF_TRY(upload(&d.wslot0, wslot0));
+    TF_TRY(upload(&d.scol, scol));
+    TF_TRY(dev_alloc(&d.val, d.nval));
+    TF_CUDA(cudaMemset(d.val, 0, sizeof(double) * (size_t)d.nval));
     // ---- order-fixed assembly lists ----------------------------------------------
     if (h->opt.deterministic) {
         std::vector<int> gptr(nnzb + 1, 0), glist(36 * (size_t)ne);
@@ -354,6 +413,7 @@ tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat, const st
     }
     h->h_rowptr = std::move(rowptr);
     h->h_colidx = std::move(colidx);
+    h->h_bofs = std::move(bofs);
     h->method = h->opt.krylov_method == 0 ? (d.any_visc ? 2 : 1) : h->opt.krylov_method;
     return TF_OK;
 }
@@ -400,6 +460,9 @@ tf_status cuda_fail(cudaError_t e, const char* what) {
 }
 
 
+// Meshes from this many nodes on use the multigrid preconditioner by default.
+constexpr int kAutoMultigridNodes = 20000;
+
 tf_status create_handle(const tf_mesh* mesh, const tf_material* mat, const tf_options* opts,
                         const std::vector<int>& seg_node0, const std::vector<int>& seg_elem0, tf_handle** out) {
     tf_handle* h = new tf_handle;
@@ -433,6 +496,8 @@ tf_status create_handle(const tf_mesh* mesh, const tf_material* mat, const tf_op
         return s;
     }
     tf_status s = build(h, mesh, mat, seg_node0, seg_elem0);
+    const bool amg = h->opt.precond == 2 || (h->opt.precond == 0 && mesh->n_nodes >= kAutoMultigridNodes);
+    if (s == TF_OK && amg) s = amg_build(h, mesh->node_pos);
     if (s != TF_OK) {
         free_all(h);
         delete h;
@@ -699,6 +764,7 @@ tf_status tf_begin_step(tf_handle* h, double dt) {
     TF_TRY(check_handle(h));
     if (!(dt > 0.0) || !std::isfinite(dt)) return set_error("dt must be positive"), TF_BAD_INPUT;
     h->dt = dt;
+    amg_mark_stale(h, 2);  // a new time step: rebuild the multigrid hierarchy at its first solve
     if (h->have_rates) TF_TRY(launch_growth(h));
     TF_TRY(launch_viscosity_surfaces(h));
     TF_CUDA(cudaMemcpyAsync(h->d.un, h->d.uk, sizeof(double) * 3 * (size_t)h->d.nn, cudaMemcpyDeviceToDevice,
@@ -709,6 +775,7 @@ tf_status tf_begin_step(tf_handle* h, double dt) {
 
 tf_status tf_assemble(tf_handle* h) {
     TF_TRY(check_handle(h));
+    amg_mark_stale(h, 1);
     TF_TRY(autotune_element(h));
     TF_TRY(launch_prepare(h));
     TF_TRY(launch_element(h));
@@ -811,7 +878,7 @@ tf_status tf_export_csr(tf_handle* h, double drop_tol, int32_t* ia, int32_t* ja,
     if (!h->assembled) return set_error("tf_export_csr called before tf_assemble"), TF_BAD_INPUT;
     if (!nnz || (ia && (!ja || !a))) return set_error("bad output arrays"), TF_BAD_INPUT;
     const Device& d = h->d;
-    std::vector<double> val(9 * (size_t)d.nnzb);
+    std::vector<double> val((size_t)d.nval);
     TF_CUDA(cudaMemcpyAsync(val.data(), d.val, val.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     TF_TRY(sync(h));
     const std::vector<int>& rp = h->h_rowptr;
@@ -833,7 +900,7 @@ tf_status tf_export_csr(tf_handle* h, double drop_tol, int32_t* ia, int32_t* ja,
                     const int c = 3 * j + dj;
                     double v;
                     if (h->h_fixed[r] || h->h_fixed[c]) v = (r == c) ? 1.0 : 0.0;
-                    else v = val[9 * bt + 3 * dj + di];
+                    else v = val[(size_t)h->h_bofs[bt] + kSlice * (3 * dj + di)];
                     if (v > drop_tol || v < -drop_tol) {
                         if (ia) {
                             ja[q] = c;

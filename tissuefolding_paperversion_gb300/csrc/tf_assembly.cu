@@ -29,7 +29,7 @@ __global__ void k_prepare(int nn, const double* __restrict__ uk, const double* _
     const double idt = 1.0 / dt;
     const double A = area[i];
     const double Adt = A / dt;
-    double* D = val + 9 * (size_t)diag[i];
+    double* D = val + diag[i];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const int k = 3 * i + d;
@@ -37,7 +37,7 @@ __global__ void k_prepare(int nn, const double* __restrict__ uk, const double* _
         vel[k] = v;
         const bool fx = fixed[k] != 0;
         g[k] = fx ? 0.0 : (A * ext_visc[k] * v) * -1.0;
-        if (write_diag) D[4 * d] = fx ? 1.0 : Adt * ext_visc[k];
+        if (write_diag) D[kSlice * 4 * d] = fx ? 1.0 : Adt * ext_visc[k];
     }
 }
 
@@ -46,7 +46,8 @@ __global__ void k_prepare(int nn, const double* __restrict__ uk, const double* _
 // element order.
 __global__ void k_gather_blocks(int64_t nnzb, int ne, const int* __restrict__ gptr, const int* __restrict__ glist,
                                 const double* __restrict__ eblk, const int* __restrict__ rowof,
-                                const int* __restrict__ diag, const double* __restrict__ area,
+                                const int* __restrict__ colidx, const int* __restrict__ bofs,
+                                const double* __restrict__ area,
                                 const double* __restrict__ ext_visc, const uint8_t* __restrict__ fixed, double dt,
                                 double* __restrict__ val) {
     const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -61,7 +62,7 @@ __global__ void k_gather_blocks(int64_t nnzb, int ne, const int* __restrict__ gp
         for (int k = 0; k < 9; ++k) acc[k] += eblk[k * stride + id];
     }
     const int row = rowof[b];
-    if (diag[row] == b) {
+    if (colidx[b] == row) {
         const double Adt = area[row] / dt;
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
@@ -69,9 +70,9 @@ __global__ void k_gather_blocks(int64_t nnzb, int ne, const int* __restrict__ gp
             acc[4 * d] = fixed[k] ? 1.0 : Adt * ext_visc[k] + acc[4 * d];
         }
     }
-    double* dst = val + 9 * (size_t)b;
+    double* dst = val + bofs[b];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) dst[k] = acc[k];
+    for (int k = 0; k < 9; ++k) dst[kSlice * k] = acc[k];
 }
 
 // Deterministic assembly: forces.  flist holds (a * ne + e) sorted by
@@ -185,9 +186,9 @@ __global__ void k_block_inverse(int nn, const int* __restrict__ diag, const doub
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
     double M[9], inv[9];
-    const double* D = val + 9 * (size_t)diag[i];
+    const double* D = val + diag[i];
 #pragma unroll
-    for (int k = 0; k < 9; ++k) M[k] = D[k];
+    for (int k = 0; k < 9; ++k) M[k] = D[kSlice * k];
     inv3_cof(M, inv);
 #pragma unroll
     for (int k = 0; k < 9; ++k) dinv[9 * (size_t)i + k] = inv[k];
@@ -197,7 +198,7 @@ __global__ void k_block_inverse(int nn, const int* __restrict__ diag, const doub
 
 tf_status launch_prepare(tf_handle* h) {
     Device& d = h->d;
-    if (!h->opt.deterministic) TF_CUDA(cudaMemsetAsync(d.val, 0, sizeof(double) * 9 * (size_t)d.nnzb, h->stream));
+    if (!h->opt.deterministic) TF_CUDA(cudaMemsetAsync(d.val, 0, sizeof(double) * (size_t)d.nval, h->stream));
     k_prepare<<<cdiv(d.nn, 256), 256, 0, h->stream>>>(d.nn, d.uk, d.un, h->dt, d.area, d.ext_visc, d.fixed, d.diag,
                                                        d.vel, d.g, d.val, h->opt.deterministic ? 0 : 1);
     TF_LAUNCH_CHECK(h);
@@ -206,7 +207,7 @@ tf_status launch_prepare(tf_handle* h) {
 
 tf_status launch_deterministic_gather(tf_handle* h) {
     Device& d = h->d;
-    k_gather_blocks<<<cdiv(d.nnzb, 256), 256, 0, h->stream>>>(d.nnzb, d.ne, d.gptr, d.glist, d.eblk, d.rowof, d.diag,
+    k_gather_blocks<<<cdiv(d.nnzb, 256), 256, 0, h->stream>>>(d.nnzb, d.ne, d.gptr, d.glist, d.eblk, d.rowof, d.colidx, d.bofs,
                                                               d.area, d.ext_visc, d.fixed, h->dt, d.val);
     TF_LAUNCH_CHECK(h);
     k_gather_forces<<<cdiv(d.nn, 256), 256, 0, h->stream>>>(d.nn, d.ne, d.fptr, d.flist, d.ef, d.fixed, d.g);

@@ -387,19 +387,19 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
                     if (mirror) A.eblk[(3 * k + i) * stride + baseT] = v;
                 }
         } else {
-            double* dst = A.val + 9 * (size_t)__ldg(&A.slot[(6 * a + bq) * A.ne + e]);
+            double* dst = A.val + __ldg(&A.slot[(6 * a + bq) * A.ne + e]);
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int k = 0; k < 3; ++k)
-                    if (!fr[i] && !fc[k]) atomicAdd(dst + 3 * i + k, acc[3 * i + k]);
+                    if (!fr[i] && !fc[k]) atomicAdd(dst + kSlice * (3 * i + k), acc[3 * i + k]);
             if (mirror) {
-                double* dt = A.val + 9 * (size_t)__ldg(&A.slot[(6 * bq + a) * A.ne + e]);
+                double* dt = A.val + __ldg(&A.slot[(6 * bq + a) * A.ne + e]);
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
                     for (int k = 0; k < 3; ++k)
-                        if (!fr[i] && !fc[k]) atomicAdd(dt + 3 * k + i, acc[3 * i + k]);
+                        if (!fr[i] && !fc[k]) atomicAdd(dt + kSlice * (3 * k + i), acc[3 * i + k]);
             }
         }
     }

@@ -11,6 +11,10 @@
 
 namespace tf {
 
+// Sliced block storage: a slot holds one 3x3 block for each of 32 rows.
+constexpr int kSlice = 32;
+constexpr int kSlotDoubles = 9 * kSlice;
+
 // Element-kernel tiling: NE prisms per CTA, one thread per Gauss point.
 constexpr int kGauss = 6;
 constexpr int kElemPerCta = 16;
@@ -39,13 +43,22 @@ struct Device {
     uint8_t* fixed = nullptr;   // [3nn]
     double* ext_visc = nullptr; // [3nn]
     double* area = nullptr;     // [nn]
-    // block sparse A = K^T (3x3 blocks, row-major inside a block)
+    // block sparse A = K^T, 3x3 blocks.  Logical pattern: CSR over block rows
+    // (rowptr, colidx; block index b).  Values are stored sliced: the 32 rows
+    // of one warp of the node-parallel kernels share slots, slot s holding the
+    // k-th block of each of the 32 rows; entry (r, c) of the block of lane l
+    // is val[s * 288 + 32 * (3 r + c) + l].  A block's base offset is
+    // s * 288 + l; padding slots hold zeros and a valid column.
     int* rowptr = nullptr;      // [nn+1]
     int* colidx = nullptr;      // [nnzb]
-    int* diag = nullptr;        // [nn] block index of (i,i)
+    int* diag = nullptr;        // [nn] base offset of block (i,i)
     int* rowof = nullptr;       // [nnzb] block row of each block
-    int* slot = nullptr;        // [36][ne] block index of pair (a,b)
-    double* val = nullptr;      // [9*nnzb]
+    int* bofs = nullptr;        // [nnzb] base offset of block b
+    int* slot = nullptr;        // [36][ne] base offset of the block of pair (a,b)
+    int* wslot0 = nullptr;      // [ncta * kWarps + 1] first slot of each warp's rows
+    int* scol = nullptr;        // [nslots * 32] column of each slot and lane
+    int64_t nval = 0;           // doubles in val (nslots * 288)
+    double* val = nullptr;      // [nval]
     // deterministic assembly: per-element blocks and the gather lists
     double* eblk = nullptr;     // [9][36*ne] element blocks (A orientation)
     double* ef = nullptr;       // [18][ne] element forces
@@ -97,6 +110,40 @@ enum Scal {
 };
 
 constexpr int kNodeThreads = 256;    // nodes per CTA of the node-parallel kernels
+constexpr int kWarps = kNodeThreads / 32;
+constexpr int kAmgMaxLevels = 10;
+
+struct Amg;  // multigrid hierarchy (tf_amg.cu)
+
+// y = this thread's row of the sliced block matrix times x.  T is the
+// storage type of the values (double for the Krylov operator, float for the
+// copy the multigrid smoother reads); products and sums are FP64.  The thread is
+// node cta_node0[blockIdx.x] + threadIdx.x of a node-parallel kernel (CTAs
+// of kNodeThreads); the warp walks its slots together, each lane reading
+// its own row's block, so every load of a block entry or column is one
+// coalesced access.
+template <class T>
+__device__ __forceinline__ void sliced_row(const int* __restrict__ wslot0, const int* __restrict__ scol,
+                                           const T* __restrict__ val, const double* __restrict__ x, double y[3]) {
+    const int lane = threadIdx.x & 31;
+    const int wg = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const int s0 = __ldg(&wslot0[wg]), s1 = __ldg(&wslot0[wg + 1]);
+    double y0 = 0.0, y1 = 0.0, y2 = 0.0;
+    const int* __restrict__ col = scol + lane;
+    const T* __restrict__ a = val + lane;
+#pragma unroll 2
+    for (int s = s0; s < s1; ++s) {
+        const int j = __ldg(&col[(size_t)s * kSlice]);
+        const T* __restrict__ v = a + (size_t)s * kSlotDoubles;
+        const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+        y0 = fma((double)__ldg(&v[0]), x0, fma((double)__ldg(&v[32]), x1, fma((double)__ldg(&v[64]), x2, y0)));
+        y1 = fma((double)__ldg(&v[96]), x0, fma((double)__ldg(&v[128]), x1, fma((double)__ldg(&v[160]), x2, y1)));
+        y2 = fma((double)__ldg(&v[192]), x0, fma((double)__ldg(&v[224]), x1, fma((double)__ldg(&v[256]), x2, y2)));
+    }
+    y[0] = y0;
+    y[1] = y1;
+    y[2] = y2;
+}
 
 }  // namespace tf
 
@@ -112,7 +159,7 @@ struct tf_handle {
     int64_t launches = 0;
     int method = 1;  // 1 CG, 2 BiCGStab
     std::vector<int> h_conn;
-    std::vector<int> h_rowptr, h_colidx;
+    std::vector<int> h_rowptr, h_colidx, h_bofs;
     std::vector<uint8_t> h_fixed;
     std::vector<double> h_nu;                   // Poisson ratios, clamped as the material setup does
     std::vector<int> h_apical;                  // 1 for apical nodes (tissue placement 1)
@@ -122,6 +169,7 @@ struct tf_handle {
     bool tuned = false;
     cudaGraphExec_t graph[2][4] = {};           // Krylov chunks [method-1][log2(chunk/8)]
     int64_t graph_kernels[2][4] = {};
+    tf::Amg* amg = nullptr;                     // multigrid preconditioner (null: block-Jacobi)
 };
 
 namespace tf {
@@ -153,6 +201,13 @@ tf_status launch_block_inverse(tf_handle* h);
 tf_status krylov_solve(tf_handle* h, int* iters, double* relres);
 tf_status launch_update(tf_handle* h);
 tf_status autotune_element(tf_handle* h);
+tf_status amg_build(tf_handle* h, const double* ref_pos);
+tf_status amg_numeric(tf_handle* h);
+void amg_vcycle(tf_handle* h, const double* r, double* out);
+int amg_vcycle_kernels(const tf_handle* h);
+void amg_free(Amg* a);
+void amg_mark_stale(tf_handle* h, int level);  // 1: new assembly, 2: rebuild the hierarchy
+bool amg_reused(const tf_handle* h);
 tf_status launch_adjoint_element(tf_handle* h, const double* lamv, double* carry, double* gr, double* ge, double ndt);
 void destroy_graphs(tf_handle* h);
 

@@ -36,8 +36,8 @@ const char* const kWhy[] = {"", "(p, Ap) <= 0", "(r, M^-1 r) <= 0", "(rhat, A ph
                             "(rhat, r) = 0"};
 
 struct Ctx {
-    const int* __restrict__ rowptr;
-    const int* __restrict__ colidx;
+    const int* __restrict__ wslot0;
+    const int* __restrict__ scol;
     const double* __restrict__ val;
     const double* __restrict__ dinv;
     double* scal;               // [nseg][S_COUNT]
@@ -129,20 +129,8 @@ __device__ __forceinline__ void apply_dinv(const double* __restrict__ D, const d
     z[2] = fma(D[6], r[0], fma(D[7], r[1], D[8] * r[2]));
 }
 
-__device__ __forceinline__ void bsr_row(const Ctx& c, int i, const double* __restrict__ x, double y[3]) {
-    double y0 = 0.0, y1 = 0.0, y2 = 0.0;
-    const int b0 = c.rowptr[i], b1 = c.rowptr[i + 1];
-    for (int b = b0; b < b1; ++b) {
-        const int j = __ldg(&c.colidx[b]);
-        const double* __restrict__ a = c.val + 9 * (size_t)b;
-        const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
-        y0 = fma(a[0], x0, fma(a[1], x1, fma(a[2], x2, y0)));
-        y1 = fma(a[3], x0, fma(a[4], x1, fma(a[5], x2, y1)));
-        y2 = fma(a[6], x0, fma(a[7], x1, fma(a[8], x2, y2)));
-    }
-    y[0] = y0;
-    y[1] = y1;
-    y[2] = y2;
+__device__ __forceinline__ void bsr_row(const Ctx& c, const double* __restrict__ x, double y[3]) {
+    sliced_row(c.wslot0, c.scol, c.val, x, y);
 }
 
 // Sets an instance's stop flag from its first scalars (bb = |b|^2).
@@ -163,7 +151,7 @@ __device__ __forceinline__ void start_flags(double* s, double bb, double tol2) {
 // other instances) or solve with b = 0, which sets x = 0 (an instance whose
 // Newton loop has stopped); both are flagged done at once.
 __global__ void k_cg_init(Ctx c, const double* __restrict__ b, double* __restrict__ x, double* __restrict__ r,
-                          double* __restrict__ z, double* __restrict__ p, double tol2, int keep) {
+                          double* __restrict__ z, double* __restrict__ p, double tol2, int keep, int jac) {
     const Where w = where(c);
     const bool active = c.seg_solve[w.seg] != 0;
     if (!active && keep) {
@@ -180,19 +168,22 @@ __global__ void k_cg_init(Ctx c, const double* __restrict__ b, double* __restric
             r[3 * i + d] = rr[d];
             x[3 * i + d] = 0.0;
         }
-        apply_dinv(c.dinv + 9 * (size_t)i, rr, zz);
+        if (jac) {
+            apply_dinv(c.dinv + 9 * (size_t)i, rr, zz);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            if (!active) zz[d] = 0.0;
-            z[3 * i + d] = zz[d];
-            p[3 * i + d] = zz[d];
-            v[0] = fma(rr[d], zz[d], v[0]);
-            v[1] = fma(rr[d], rr[d], v[1]);
+            for (int d = 0; d < 3; ++d) {
+                if (!active) zz[d] = 0.0;
+                z[3 * i + d] = zz[d];
+                p[3 * i + d] = zz[d];
+                v[0] = fma(rr[d], zz[d], v[0]);
+            }
         }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) v[1] = fma(rr[d], rr[d], v[1]);
     }
     double tot[2];
     if (reduce_seg<2>(c, w.seg, v, tot) && threadIdx.x == 0) {
-        w.s[S_RZ] = tot[0];
+        if (jac) w.s[S_RZ] = tot[0];
         start_flags(w.s, tot[1], tol2);
     }
 }
@@ -204,7 +195,7 @@ __global__ void k_cg_spmv(Ctx c, const double* __restrict__ p, double* __restric
     double v[1] = {0.0};
     if (w.valid) {
         double y[3];
-        bsr_row(c, w.node, p, y);
+        bsr_row(c, p, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             q[3 * w.node + d] = y[d];
@@ -226,7 +217,7 @@ __global__ void k_cg_spmv(Ctx c, const double* __restrict__ p, double* __restric
 
 // x += alpha p; r -= alpha q; z = M^-1 r;  beta = (r,z)_new / (r,z)
 __global__ void k_cg_update(Ctx c, double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
-                            const double* __restrict__ p, const double* __restrict__ q) {
+                            const double* __restrict__ p, const double* __restrict__ q, int jac) {
     const Where w = where(c);
     if (stopped(w)) return;
     const double alpha = __ldcg(&w.s[S_ALPHA]);
@@ -241,25 +232,59 @@ __global__ void k_cg_update(Ctx c, double* __restrict__ x, double* __restrict__ 
             rr[d] = fma(-alpha, q[k], r[k]);
             r[k] = rr[d];
         }
-        apply_dinv(c.dinv + 9 * (size_t)i, rr, zz);
+        if (jac) {
+            apply_dinv(c.dinv + 9 * (size_t)i, rr, zz);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            z[3 * i + d] = zz[d];
-            v[0] = fma(rr[d], zz[d], v[0]);
-            v[1] = fma(rr[d], rr[d], v[1]);
+            for (int d = 0; d < 3; ++d) {
+                z[3 * i + d] = zz[d];
+                v[0] = fma(rr[d], zz[d], v[0]);
+            }
         }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) v[1] = fma(rr[d], rr[d], v[1]);
     }
     double tot[2];
     if (reduce_seg<2>(c, w.seg, v, tot) && threadIdx.x == 0) {
         double* s = w.s;
         const double rz = tot[0], rr = tot[1];
-        s[S_BETA] = rz / s[S_RZ];
-        s[S_RZ] = rz;
+        if (jac) {
+            s[S_BETA] = rz / s[S_RZ];
+            s[S_RZ] = rz;
+        }
         s[S_RR] = rr;
         s[S_ITER] += 1.0;
         if (!isfinite(rr)) s[S_FLAG] = F_NAN;
         else if (rr <= s[S_TOL2] * s[S_BB]) s[S_FLAG] = F_CONVERGED;
-        else if (!(rz > 0.0)) {
+        else if (jac && !(rz > 0.0)) {
+            s[S_FLAG] = F_BREAKDOWN;
+            s[S_WHY] = W_CG_RZ;
+        }
+    }
+}
+
+// With the multigrid preconditioner (z = M^-1 r computed between kernels):
+// rz = (r, z), beta = rz / rz_old; start != 0 also sets p = z (first step).
+__global__ void k_cg_rz(Ctx c, const double* __restrict__ r, const double* __restrict__ z, double* __restrict__ p,
+                        int start) {
+    const Where w = where(c);
+    if (stopped(w)) return;
+    double v[1] = {0.0};
+    if (w.valid)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int k = 3 * w.node + d;
+            v[0] = fma(r[k], z[k], v[0]);
+            if (start) p[k] = z[k];
+        }
+    double tot[1];
+    if (reduce_seg<1>(c, w.seg, v, tot) && threadIdx.x == 0) {
+        double* s = w.s;
+        const double rz = tot[0];
+        if (!start) s[S_BETA] = rz / s[S_RZ];
+        s[S_RZ] = rz;
+        if (!isfinite(rz)) {
+            s[S_FLAG] = F_NAN;
+        } else if (!(rz > 0.0)) {
             s[S_FLAG] = F_BREAKDOWN;
             s[S_WHY] = W_CG_RZ;
         }
@@ -316,7 +341,7 @@ __global__ void k_bi_init(Ctx c, const double* __restrict__ b, double* __restric
 
 // p = r + beta (p - omega v); phat = M^-1 p
 __global__ void k_bi_dir(Ctx c, const double* __restrict__ r, const double* __restrict__ v, double* __restrict__ p,
-                         double* __restrict__ phat) {
+                         double* __restrict__ phat, int jac) {
     const Where w = where(c);
     if (stopped(w) || !w.valid) return;
     const double beta = __ldcg(&w.s[S_BETA]), omega = __ldcg(&w.s[S_OMEGA]);
@@ -328,6 +353,7 @@ __global__ void k_bi_dir(Ctx c, const double* __restrict__ r, const double* __re
         pp[d] = fma(beta, fma(-omega, v[k], p[k]), r[k]);
         p[k] = pp[d];
     }
+    if (!jac) return;
     apply_dinv(c.dinv + 9 * (size_t)i, pp, z);
 #pragma unroll
     for (int d = 0; d < 3; ++d) phat[3 * i + d] = z[d];
@@ -341,7 +367,7 @@ __global__ void k_bi_spmv1(Ctx c, const double* __restrict__ phat, const double*
     double s[1] = {0.0};
     if (w.valid) {
         double y[3];
-        bsr_row(c, w.node, phat, y);
+        bsr_row(c, phat, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             v[3 * w.node + d] = y[d];
@@ -364,7 +390,7 @@ __global__ void k_bi_spmv1(Ctx c, const double* __restrict__ phat, const double*
 // tolerance the half step is the solution: x += alpha phat and stop (t and
 // omega would otherwise be formed from a vanishing s).
 __global__ void k_bi_s(Ctx c, const double* __restrict__ r, const double* __restrict__ v, double* __restrict__ s,
-                       double* __restrict__ shat, double* __restrict__ x, const double* __restrict__ phat) {
+                       double* __restrict__ shat, double* __restrict__ x, const double* __restrict__ phat, int jac) {
     const Where w = where(c);
     if (stopped(w)) return;
     const double alpha = __ldcg(&w.s[S_ALPHA]);
@@ -379,14 +405,19 @@ __global__ void k_bi_s(Ctx c, const double* __restrict__ r, const double* __rest
             s[k] = ss[d];
             acc[0] = fma(ss[d], ss[d], acc[0]);
         }
-        apply_dinv(c.dinv + 9 * (size_t)i, ss, z);
+        if (jac) {
+            apply_dinv(c.dinv + 9 * (size_t)i, ss, z);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) shat[3 * i + d] = z[d];
+            for (int d = 0; d < 3; ++d) shat[3 * i + d] = z[d];
+        }
     }
     double tot[1];
     if (reduce_seg<1>(c, w.seg, acc, tot) && threadIdx.x == 0) {
         if (!isfinite(tot[0])) w.s[S_FLAG] = F_NAN;
-        else if (tot[0] <= w.s[S_TOL2] * w.s[S_BB]) w.s[S_FLAG] = -1.0;  // half step converged
+        else if (tot[0] <= w.s[S_TOL2] * w.s[S_BB]) {
+            w.s[S_RR] = tot[0];  // the residual of x + alpha phat is s
+            w.s[S_FLAG] = -1.0;  // half step converged
+        }
     }
 }
 
@@ -404,7 +435,6 @@ __global__ void k_bi_half(Ctx c, double* __restrict__ x, const double* __restric
         }
     double tot[1] = {0.0}, v[1] = {0.0};
     if (reduce_seg<1>(c, w.seg, v, tot) && threadIdx.x == 0) {
-        w.s[S_RR] = 0.0;
         w.s[S_ITER] += 1.0;
         w.s[S_FLAG] = F_CONVERGED;
     }
@@ -418,7 +448,7 @@ __global__ void k_bi_spmv2(Ctx c, const double* __restrict__ shat, const double*
     double acc[2] = {0.0, 0.0};
     if (w.valid) {
         double y[3];
-        bsr_row(c, w.node, shat, y);
+        bsr_row(c, shat, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             t[3 * w.node + d] = y[d];
@@ -532,8 +562,8 @@ __global__ void k_update(Ctx c, double* __restrict__ uk, const double* __restric
 Ctx make_ctx(tf_handle* h) {
     Device& d = h->d;
     Ctx c;
-    c.rowptr = d.rowptr;
-    c.colidx = d.colidx;
+    c.wslot0 = d.wslot0;
+    c.scol = d.scol;
     c.val = d.val;
     c.dinv = d.dinv;
     c.scal = d.scal;
@@ -553,15 +583,22 @@ void issue_iterations(tf_handle* h, const Ctx& c, int method, int n) {
     Device& d = h->d;
     cudaStream_t st = h->stream;
     const int nb = d.ncta;
+    const int jac = h->amg ? 0 : 1;
     for (int it = 0; it < n; ++it) {
         if (method == 1) {
             k_cg_spmv<<<nb, kThreads, 0, st>>>(c, d.p, d.q);
-            k_cg_update<<<nb, kThreads, 0, st>>>(c, d.du, d.r, d.z, d.p, d.q);
+            k_cg_update<<<nb, kThreads, 0, st>>>(c, d.du, d.r, d.z, d.p, d.q, jac);
+            if (!jac) {
+                amg_vcycle(h, d.r, d.z);
+                k_cg_rz<<<nb, kThreads, 0, st>>>(c, d.r, d.z, d.p, 0);
+            }
             k_cg_direction<<<nb, kThreads, 0, st>>>(c, d.z, d.p);
         } else {
-            k_bi_dir<<<nb, kThreads, 0, st>>>(c, d.r, d.q, d.p, d.z);
+            k_bi_dir<<<nb, kThreads, 0, st>>>(c, d.r, d.q, d.p, d.z, jac);
+            if (!jac) amg_vcycle(h, d.p, d.z);
             k_bi_spmv1<<<nb, kThreads, 0, st>>>(c, d.z, d.rhat, d.q);
-            k_bi_s<<<nb, kThreads, 0, st>>>(c, d.r, d.q, d.s, d.sh, d.du, d.z);
+            k_bi_s<<<nb, kThreads, 0, st>>>(c, d.r, d.q, d.s, d.sh, d.du, d.z, jac);
+            if (!jac) amg_vcycle(h, d.s, d.sh);
             k_bi_half<<<nb, kThreads, 0, st>>>(c, d.du, d.z);
             k_bi_spmv2<<<nb, kThreads, 0, st>>>(c, d.sh, d.s, d.t);
             k_bi_x<<<nb, kThreads, 0, st>>>(c, d.du, d.r, d.rhat, d.z, d.sh, d.s, d.t);
@@ -569,7 +606,11 @@ void issue_iterations(tf_handle* h, const Ctx& c, int method, int n) {
     }
 }
 
-int kernels_per_iteration(int method) { return method == 1 ? 3 : 6; }
+int kernels_per_iteration(const tf_handle* h, int method) {
+    if (!h->amg) return method == 1 ? 3 : 6;
+    const int v = amg_vcycle_kernels(h);
+    return method == 1 ? 4 + v : 6 + 2 * v;
+}
 
 // A chunk of `8 << ci` iterations, captured once into a CUDA graph.
 tf_status run_chunk(tf_handle* h, const Ctx& c, int method, int ci) {
@@ -587,7 +628,7 @@ tf_status run_chunk(tf_handle* h, const Ctx& c, int method, int ci) {
             ex = nullptr;
             return cuda_fail(e2, "cudaGraphInstantiate");
         }
-        h->graph_kernels[method - 1][ci] = (int64_t)n * kernels_per_iteration(method);
+        h->graph_kernels[method - 1][ci] = (int64_t)n * kernels_per_iteration(h, method);
     }
     TF_CUDA(cudaGraphLaunch(ex, h->stream));
     h->launches += h->graph_kernels[method - 1][ci];
@@ -599,13 +640,27 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
     const Ctx c = make_ctx(h);
     cudaStream_t st = h->stream;
     const double tol2 = h->opt.krylov_rtol * h->opt.krylov_rtol;
+    const int jac = h->amg ? 0 : 1;
     if (keep == 2) {  // BiCGStab restart: block inverse and x are kept
         k_bi_restart<<<d.ncta, kThreads, 0, st>>>(c, d.r, d.rhat, d.p, d.q);
     } else {
         const tf_status sb = launch_block_inverse(h);
         if (sb != TF_OK) return sb;
-        if (method == 1) k_cg_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.z, d.p, tol2, keep);
-        else k_bi_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.rhat, d.p, d.q, tol2, keep);
+        if (h->amg) {
+            const tf_status sa = amg_numeric(h);
+            if (sa != TF_OK) return sa;
+        }
+        if (method == 1) {
+            k_cg_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.z, d.p, tol2, keep, jac);
+            if (!jac) {
+                TF_LAUNCH_CHECK(h);
+                amg_vcycle(h, d.r, d.z);
+                h->launches += amg_vcycle_kernels(h);
+                k_cg_rz<<<d.ncta, kThreads, 0, st>>>(c, d.r, d.z, d.p, 1);
+            }
+        } else {
+            k_bi_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.rhat, d.p, d.q, tol2, keep);
+        }
     }
     TF_LAUNCH_CHECK(h);
     const int maxit = h->opt.krylov_max_iter;
@@ -622,7 +677,7 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
             const int rest = maxit - launched;
             issue_iterations(h, c, method, rest);
             TF_LAUNCH_CHECK(h);
-            h->launches += (int64_t)rest * kernels_per_iteration(method) - 1;
+            h->launches += (int64_t)rest * kernels_per_iteration(h, method) - 1;
             launched = maxit;
         }
         TF_CUDA(cudaMemcpyAsync(d.host_scal, d.scal, sizeof(double) * nscal, cudaMemcpyDeviceToHost, st));
@@ -681,6 +736,16 @@ tf_status krylov_solve(tf_handle* h, int* iters, double* relres) {
     TF_CUDA(cudaMemcpyAsync(d.seg_solve, d.seg_active, sizeof(int) * (size_t)d.nseg, cudaMemcpyDeviceToDevice,
                             h->stream));
     tf_status s = krylov_run(h, h->method, 0, iters, relres);
+    if (s != TF_OK && amg_reused(h)) {
+        // the coarse levels came from an earlier Newton iteration: rebuild
+        // them for this matrix and solve again
+        amg_mark_stale(h, 2);
+        TF_CUDA(cudaMemcpyAsync(d.seg_solve, d.seg_active, sizeof(int) * (size_t)d.nseg, cudaMemcpyDeviceToDevice,
+                                h->stream));
+        int it2 = 0;
+        s = krylov_run(h, h->method, 0, &it2, relres);
+        *iters += it2;
+    }
     if (s == TF_KRYLOV_BREAKDOWN && h->method == 1 && h->opt.krylov_method == 0) {
         std::vector<int> redo(d.nseg, 0);
         for (int g = 0; g < d.nseg; ++g)
