@@ -12,6 +12,8 @@ Reported (one JSON line on rank 0):
   e2e          the same metric through the C ABI from host buffers: per step
                tf_set_state (H2D of uk, un), tf_assemble, tf_get_residual (D2H)
   roofline     element kernel: algorithmic bytes / kernel time vs measured HBM
+  fp64         element kernel: FP64 flops / kernel time vs GB300's FP64 peak
+               (the kernel's binding roofline)
   cpu_baseline the reference's algorithm (oracle port, literal 3^6 tangent),
                all host threads, on a bounded sample of prisms
 
@@ -97,6 +99,20 @@ def algorithmic_bytes(nn, ne, nnz):
     int32 slot offsets (408 B); per node uk and un (48 B) and g (24 B); K
     written once (8 B per nonzero)."""
     return 408 * ne + 48 * nn + 24 * nn + 8 * nnz
+
+
+# FP64 flops per prism of one element-kernel launch, counted with ncu
+# (2 x DFMA + DADD + DMUL thread instructions / prisms) on the 135,200-prism
+# sheet with internal viscosity; the elastic-only count applies when every
+# eta is 0.
+FP64_FLOPS_PER_PRISM = {"viscous": 23968, "elastic": None}
+# DRAM bytes (read + write) per prism of one element-kernel launch, from the
+# same ncu capture (331.4 MB at 135,200 prisms); the kernel's traffic grows
+# with the number of prisms, so a full launch is scaled from it.
+DRAM_BYTES_PER_PRISM = {"viscous": 331.4e6 / 135200, "elastic": None}
+# FP64 peak of GB300: 304 DFMA per cycle (ncu's peak_sustained for the whole
+# GPU) x 2 flop x 2.07 GHz
+FP64_PEAK_TFLOPS = 304 * 2 * 2.07e9 / 1e12
 
 
 def cpu_sample(t, seconds_target=15.0, literal=True):
@@ -202,6 +218,16 @@ def run_gpu(args, t):
     alg = algorithmic_bytes(nn, ne, nnz)
     hbm, how = peaks()
     achieved = alg / (elem_ms / 1e3) / 1e9
+    # the kernel's binding roofline: FP64 issue (see profiles/)
+    kind = "viscous" if np.any(t.eta != 0) else "elastic"
+    fpp = FP64_FLOPS_PER_PRISM[kind]
+    traffic = DRAM_BYTES_PER_PRISM[kind] * ne if DRAM_BYTES_PER_PRISM[kind] else None
+    fp64 = None
+    if fpp:
+        tf = fpp * ne / (elem_ms / 1e3) / 1e12
+        fp64 = {"kernel": "k_element", "achieved": tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
+                "frac": tf / FP64_PEAK_TFLOPS, "flops_per_prism": fpp,
+                "peak_source": "ncu peak_sustained DFMA rate x max SM clock"}
 
     # e2e through the C ABI with host buffers
     uk = s.positions()
@@ -233,8 +259,10 @@ def run_gpu(args, t):
         "e2e": {"value": ne / e2e_s, "unit": "prisms/s", "h2d_bytes_per_step": 2 * 8 * 3 * nn,
                 "d2h_bytes_per_step": 8 * 3 * nn},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_source": how, "kernel": "k_element", "ms_per_launch": elem_ms,
-                     "algorithmic_bytes": alg},
+                     "traffic": traffic, "peak_source": how, "kernel": "k_element", "ms_per_launch": elem_ms,
+                     "algorithmic_bytes": alg,
+                     "traffic_source": "ncu dram bytes per prism at 135,200 prisms x prisms" if traffic else None},
+        "fp64": fp64,
         "gpu_launches": launches,
         "clocks": clk,
     }
