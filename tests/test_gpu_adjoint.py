@@ -113,3 +113,41 @@ def test_adjoint_rejects_bad_arguments():
         bad[3] = 0.0
         with pytest.raises(api.TfError):
             s.adjoint_forward(rate, logE, 2, t.dt, 1, bad)
+
+
+def _oracle_loss(t, rate, logE, n, params):
+    """Loss after n steps of the oracle's Newton solver (direct solves)."""
+    t2 = mesh.Tissue(**{**t.__dict__, "E": np.exp(logE)})
+    rates3 = np.zeros((t.n_elems, 3))
+    rates3[:, 0] = rate
+    rates3[:, 1] = rate
+    p = Port(t2)
+    for _ in range(n):
+        p.step(t.dt, rates3.reshape(-1))
+    x = p.positions().reshape(-1, 3)[t.node_placement == 1]
+    f = params[2] * np.exp(-((x[:, 0] - params[0]) ** 2 + (x[:, 1] - params[1]) ** 2) / (2 * params[3] ** 2))
+    return float(np.sum((x[:, 2] - f) ** 2))
+
+
+@pytest.mark.parametrize("eta", [0.0, 100.0])
+def test_adjoint_matches_differences_of_the_oracle_solver(eta):
+    """The GPU adjoint against central differences of the CPU oracle's own
+    Newton steps (the reference's algorithm with direct solves)."""
+    t, rate, logE, params = _tissue(eta, seed=21)
+    n = 3
+    with _solver(t) as s:
+        _, saved = _loss(s, t, rate, logE, n, 1, params)
+        gr, ge = s.adjoint_backward(saved)
+        saved.free()
+    rng = np.random.default_rng(23)
+    for which in ("rate", "logE"):
+        d = rng.standard_normal(t.n_elems)
+        if which == "rate":
+            h = 1e-3 * np.abs(rate).mean()
+            fd = (_oracle_loss(t, rate + h * d, logE, n, params) - _oracle_loss(t, rate - h * d, logE, n, params)) / (2 * h)
+            adj = gr @ d
+        else:
+            h = 1e-4
+            fd = (_oracle_loss(t, rate, logE + h * d, n, params) - _oracle_loss(t, rate, logE - h * d, n, params)) / (2 * h)
+            adj = ge @ d
+        assert abs(adj - fd) <= TOL_GRAD * abs(fd), (which, adj, fd)
