@@ -51,6 +51,9 @@ typedef struct tf_mesh {
     const uint8_t* fixed;          /* [3*n_nodes] Node::FixedPos */
     const double* ext_visc;        /* [3*n_nodes] Node::externalViscosity */
     const int32_t* node_placement; /* [n_nodes] Node::tissuePlacement (0 basal, 1 apical, 2 mid) */
+    const double* ref_pos;         /* [18*n_elems] reference (stress-free) prism shapes, 6 x 3 per prism
+                                      (ShapeBase::ReferenceShape->Positions as read from a mesh file,
+                                      ShapeBase.cpp:935-944); NULL: the node positions */
 } tf_mesh;
 
 /* Per-element material, Prism::setElasticProperties (Prism.cpp:491-516) and
@@ -225,6 +228,22 @@ TF_API tf_status tf_solve_bsr_static(int32_t n_block_rows, const int32_t* rowptr
  * steps in *saved.  tf_adj_backward recomputes each span of `every` steps
  * from its saved state and solves A^T lambda = rhs per step, scaling dL by
  * dloss; it leaves the handle at the final state.  Single-mesh handles only. */
+/* The reference's mesh input file (.mesh; Simulation.cpp:2074-2239): node
+ * positions, tissue placement / type / circumference flags, prism node ids
+ * (after Prism::checkRotationConsistency3D, Prism.cpp:364-410) and the 6 x 3
+ * reference positions per prism.  Call with NULL arrays to get the sizes,
+ * then again with arrays of those sizes.  Host only (no device work). */
+TF_API tf_status tf_read_mesh_file(const char* path, int32_t* n_nodes, int32_t* n_elems, double* pos, int32_t* conn,
+                                   int32_t* placement, int32_t* tissue_type, int32_t* at_circumference,
+                                   double* ref_pos);
+/* One save frame in the reference's format (Simulation::saveStep header,
+ * writeNodes, writeElements, footer; Simulation.cpp:9265-9356), written to
+ * `path` (appended when `append` != 0).  Host only. */
+TF_API tf_status tf_write_frame(const char* path, int32_t append, double time_sec, int32_t n_nodes, const double* pos,
+                                const int32_t* placement, const int32_t* tissue_type,
+                                const int32_t* at_circumference, int32_t n_elems, const int32_t* conn,
+                                const double* ref_pos);
+
 /* Multigrid hierarchy of the handle (tf_options.precond): number of levels
  * (0 when block-Jacobi is used), nodes per level and the smoother weights
  * of the last numeric set-up (4 / (3 lambda_max(D^-1 A)) per level; arrays of

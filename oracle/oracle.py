@@ -102,6 +102,8 @@ class Port:
             L.tfo_solve.argtypes = [C.c_void_p, _dp]
             L.tfo_step.restype = C.c_int
             L.tfo_step.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.c_int, C.POINTER(C.c_int), _dp, C.c_int]
+            L.tfo_set_reference_shapes.restype = None
+            L.tfo_set_reference_shapes.argtypes = [C.c_void_p, _dp]
             cls._lib = L
         return cls._lib
 
@@ -112,6 +114,9 @@ class Port:
         self._keep = [_f64(t.pos), _i32(t.conn), np.ascontiguousarray(t.fixed, dtype=np.uint8),
                       _f64(t.ext_visc), _i32(t.node_placement), _f64(t.E), _f64(t.nu), _f64(t.eta)]
         self.h = L.tfo_create(self.nn, self.ne, *self._keep)
+        if getattr(t, "ref_pos", None) is not None:
+            self._ref = _f64(t.ref_pos)
+            L.tfo_set_reference_shapes(self.h, self._ref)
 
     def close(self):
         if self.h:

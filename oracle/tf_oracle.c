@@ -197,6 +197,31 @@ static long entry_index(const tfo_model* m, int A, int B, int i, int j) {
     return (long)m->ia[3 * A + i] + 3L * k + j;
 }
 
+/* Prism::calculateElementShapeFunctionDerivatives, Prism.cpp:705-728: per
+ * Gauss point dX/dxi of the reference shape X (6 x 3), its determinant and
+ * inverse. */
+static void reference_geometry(tfo_model* m, int e, const double* X) {
+    for (int p = 0; p < 6; ++p) {
+        double Jt[9], J[9];
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                double acc = 0.0;
+                for (int a = 0; a < 6; ++a) acc += DNREF[p][r][a] * X[3 * a + c];
+                Jt[3 * r + c] = acc;
+            }
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) J[3 * r + c] = Jt[3 * c + r];
+        m->detdXde[6 * e + p] = det3(J);
+        inv3(J, &m->invdXde[54L * e + 9 * p]);
+    }
+}
+
+void tfo_set_reference_shapes(tfo_model* m, const double* ref_pos) {
+    /* ReferenceShape->Positions read from a mesh file
+     * (ShapeBase::updateReferencePositionMatrixFromSave, ShapeBase.cpp:935-944) */
+    for (int e = 0; e < m->ne; ++e) reference_geometry(m, e, &ref_pos[18L * e]);
+}
+
 tfo_model* tfo_create(int n_nodes, int n_elems, const double* pos0, const int* conn,
                       const unsigned char* fixed, const double* ext_visc, const int* node_placement,
                       const double* E, const double* nu, const double* eta) {
@@ -241,20 +266,10 @@ tfo_model* tfo_create(int n_nodes, int n_elems, const double* pos0, const int* c
         m->lam[e] = E[e] * v / (1 + v) / (1 - 2.0 * v);
         m->mu[e] = E[e] / 2.0 / (1 + v);
         m->eta[e] = eta[e];
-        /* Prism::calculateElementShapeFunctionDerivatives, Prism.cpp:705-728 */
-        for (int p = 0; p < 6; ++p) {
-            double Jt[9], J[9];
-            for (int r = 0; r < 3; ++r)
-                for (int c = 0; c < 3; ++c) {
-                    double acc = 0.0;
-                    for (int a = 0; a < 6; ++a) acc += DNREF[p][r][a] * pos0[3 * conn[6 * e + a] + c];
-                    Jt[3 * r + c] = acc;
-                }
-            for (int r = 0; r < 3; ++r)
-                for (int c = 0; c < 3; ++c) J[3 * r + c] = Jt[3 * c + r];
-            m->detdXde[6 * e + p] = det3(J);
-            inv3(J, &m->invdXde[54L * e + 9 * p]);
-        }
+        double X[18];
+        for (int a = 0; a < 6; ++a)
+            for (int c = 0; c < 3; ++c) X[3 * a + c] = pos0[3 * conn[6 * e + a] + c];
+        reference_geometry(m, e, X);
         for (int k = 0; k < 9; ++k) {
             m->Fg[9L * e + k] = (k % 4 == 0) ? 1.0 : 0.0;
             m->invFg[9L * e + k] = (k % 4 == 0) ? 1.0 : 0.0;

@@ -39,6 +39,9 @@ tfo_model* tfo_create(int n_nodes, int n_elems, const double* pos0, const int* c
                       const unsigned char* fixed, const double* ext_visc, const int* node_placement,
                       const double* E, const double* nu, const double* eta);
 void tfo_destroy(tfo_model* m);
+/* Reference (stress-free) prism shapes different from the node positions the
+ * model was created with: ref_pos[18*n_elems], 6 x 3 per prism. */
+void tfo_set_reference_shapes(tfo_model* m, const double* ref_pos);
 void tfo_set_threads(int n);
 int tfo_get_threads(void);
 

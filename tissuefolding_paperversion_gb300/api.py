@@ -30,7 +30,8 @@ EXPORTED = [
     "tf_get_viscosity_surfaces", "tf_set_viscosity_surfaces", "tf_set_state", "tf_export_csr",
     "tf_element_eval", "tf_get_sizes", "tf_get_stream", "tf_launch_count", "tf_time_assembly",
     "tf_solve_bsr_static", "tf_batch_create", "tf_batch_step", "tf_get_instances", "tf_elements_per_cta",
-    "tf_adj_forward", "tf_adj_backward", "tf_adj_free", "tf_multigrid_info",
+    "tf_adj_forward", "tf_adj_backward", "tf_adj_free", "tf_multigrid_info", "tf_read_mesh_file",
+    "tf_write_frame",
 ]
 
 
@@ -42,7 +43,8 @@ class TfError(RuntimeError):
 
 class tf_mesh(C.Structure):
     _fields_ = [("n_nodes", C.c_int32), ("n_elems", C.c_int32), ("node_pos", C.c_void_p), ("conn", C.c_void_p),
-                ("fixed", C.c_void_p), ("ext_visc", C.c_void_p), ("node_placement", C.c_void_p)]
+                ("fixed", C.c_void_p), ("ext_visc", C.c_void_p), ("node_placement", C.c_void_p),
+                ("ref_pos", C.c_void_p)]
 
 
 class tf_material(C.Structure):
@@ -121,6 +123,10 @@ def load(build_if_missing: bool = True):
     L.tf_adj_free.argtypes = [vp]
     L.tf_multigrid_info.restype = C.c_int
     L.tf_multigrid_info.argtypes = [vp, ip, vp, vp]
+    L.tf_read_mesh_file.restype = C.c_int
+    L.tf_read_mesh_file.argtypes = [C.c_char_p, ip, ip, vp, vp, vp, vp, vp, vp]
+    L.tf_write_frame.restype = C.c_int
+    L.tf_write_frame.argtypes = [C.c_char_p, i32, C.c_double, i32, vp, vp, vp, vp, i32, vp, vp]
     for name in ["tf_create", "tf_destroy", "tf_set_positions", "tf_get_positions", "tf_set_Fg", "tf_get_Fg",
                  "tf_set_growth_rates", "tf_begin_step", "tf_assemble", "tf_add_external_forces", "tf_solve",
                  "tf_update", "tf_end_step", "tf_newton_step", "tf_get_residual", "tf_get_delta_u",
@@ -146,8 +152,10 @@ def _mesh_structs(t):
         nu=np.ascontiguousarray(t.nu, dtype=np.float64),
         eta=np.ascontiguousarray(t.eta, dtype=np.float64),
     )
+    ref = getattr(t, "ref_pos", None)
+    a["ref"] = None if ref is None else np.ascontiguousarray(ref, dtype=np.float64)
     m = tf_mesh(t.n_nodes, t.n_elems, _ptr(a["pos"]), _ptr(a["conn"]), _ptr(a["fixed"]), _ptr(a["ext_visc"]),
-                _ptr(a["placement"]))
+                _ptr(a["placement"]), _ptr(a["ref"]))
     mat = tf_material(_ptr(a["E"]), _ptr(a["nu"]), _ptr(a["eta"]))
     return a, m, mat
 
@@ -417,3 +425,45 @@ class Batch(Solver):
 
     def elements_per_cta(self):
         return int(self.L.tf_elements_per_cta(self.h))
+
+
+def _raise(L, s, where):
+    if s != TF_OK:
+        raise TfError(s, where, L.tf_last_error().decode())
+
+
+def read_mesh_file(path):
+    """The reference's .mesh input file: dict with pos (3N), conn (6E, after the
+    reference's orientation check), placement, tissue_type, at_circumference
+    (N) and ref_pos (18E)."""
+    L = load()
+    nn, ne = C.c_int32(0), C.c_int32(0)
+    b = os.fsencode(path)
+    _raise(L, L.tf_read_mesh_file(b, C.byref(nn), C.byref(ne), None, None, None, None, None, None),
+           "tf_read_mesh_file")
+    n, e = nn.value, ne.value
+    out = {"pos": np.zeros(3 * n), "conn": np.zeros(6 * e, dtype=np.int32), "placement": np.zeros(n, dtype=np.int32),
+           "tissue_type": np.zeros(n, dtype=np.int32), "at_circumference": np.zeros(n, dtype=np.int32),
+           "ref_pos": np.zeros(18 * e)}
+    _raise(L, L.tf_read_mesh_file(b, C.byref(nn), C.byref(ne), _ptr(out["pos"]), _ptr(out["conn"]),
+                                  _ptr(out["placement"]), _ptr(out["tissue_type"]), _ptr(out["at_circumference"]),
+                                  _ptr(out["ref_pos"])), "tf_read_mesh_file")
+    return out
+
+
+def write_frame(path, time_sec, pos, conn, placement, tissue_type=None, at_circumference=None, ref_pos=None,
+                append=True):
+    """Append one save frame in the reference's format (its viewer's input)."""
+    L = load()
+    p = np.ascontiguousarray(pos, dtype=np.float64)
+    c = np.ascontiguousarray(conn, dtype=np.int32)
+    n, e = p.size // 3, c.size // 6
+    pl = np.ascontiguousarray(placement, dtype=np.int32)
+    ty = np.zeros(n, dtype=np.int32) if tissue_type is None else np.ascontiguousarray(tissue_type, dtype=np.int32)
+    ci = np.zeros(n, dtype=np.int32) if at_circumference is None else np.ascontiguousarray(at_circumference,
+                                                                                         dtype=np.int32)
+    rp = (p.reshape(-1, 3)[c.reshape(-1, 6)].reshape(-1) if ref_pos is None
+          else np.ascontiguousarray(ref_pos, dtype=np.float64))
+    _raise(L, L.tf_write_frame(os.fsencode(path), 1 if append else 0, float(time_sec), n, _ptr(p), _ptr(pl),
+                               _ptr(ty), _ptr(ci), e, _ptr(c), _ptr(rp)), "tf_write_frame")
+

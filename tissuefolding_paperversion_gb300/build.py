@@ -16,7 +16,8 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libtfgpu.so")
-SOURCES = ["tf_api.cu", "tf_element.cu", "tf_assembly.cu", "tf_krylov.cu", "tf_static_solve.cu", "tf_adjoint.cu", "tf_amg.cu"]
+SOURCES = ["tf_api.cu", "tf_element.cu", "tf_assembly.cu", "tf_krylov.cu", "tf_static_solve.cu", "tf_adjoint.cu", "tf_amg.cu",
+           "tf_meshio.cpp"]
 HEADERS = ["tf_internal.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
@@ -45,7 +46,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     objs = []
     for s in SOURCES:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(OBJ, s.replace(".cu", ".o"))
+        obj = os.path.join(OBJ, os.path.splitext(s)[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src, *hdrs]):
             jobs.append([nvcc(), *ARCH, *FLAGS, "-c", src, "-o", obj])

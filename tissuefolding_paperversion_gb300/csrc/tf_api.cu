@@ -183,9 +183,11 @@ tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat, const st
     double dN[6][3][6];
     for (int gp = 0; gp < 6; ++gp) shape_derivatives(gp, dN[gp]);
     for (int e = 0; e < ne; ++e) {
-        double X[6][3];
+        double X[6][3];  // the reference shape (ReferenceShape->Positions)
         for (int a = 0; a < 6; ++a)
-            for (int c = 0; c < 3; ++c) X[a][c] = m->node_pos[3 * (size_t)m->conn[6 * (size_t)e + a] + c];
+            for (int c = 0; c < 3; ++c)
+                X[a][c] = m->ref_pos ? m->ref_pos[18 * (size_t)e + 3 * a + c]
+                                     : m->node_pos[3 * (size_t)m->conn[6 * (size_t)e + a] + c];
         for (int gp = 0; gp < 6; ++gp) {
             // dX/dxi = (dN X)^T   (Prism.cpp:705-728)
             double J[9];
@@ -644,15 +646,24 @@ tf_status tf_batch_create(const tf_mesh* meshes, const tf_material* mats, int32_
         set_error("tf_batch_create: the batch exceeds the 32-bit index range of this build");
         return TF_BAD_INPUT;
     }
-    std::vector<double> pos, ev, E, nu, eta;
+    std::vector<double> pos, ev, E, nu, eta, ref;
     std::vector<int32_t> conn, placement;
     std::vector<uint8_t> fixed;
     std::vector<int> node0{0}, elem0{0};
     pos.reserve(3 * nn);
     conn.reserve(6 * ne);
+    bool any_ref = false;
+    for (int i = 0; i < n; ++i) any_ref |= meshes[i].ref_pos != nullptr;
     for (int i = 0; i < n; ++i) {
         const tf_mesh& m = meshes[i];
         const int off = node0.back();
+        if (any_ref) {
+            for (int64_t e = 0; e < m.n_elems; ++e)
+                for (int a = 0; a < 6; ++a)
+                    for (int c = 0; c < 3; ++c)
+                        ref.push_back(m.ref_pos ? m.ref_pos[18 * e + 3 * a + c]
+                                                : m.node_pos[3 * (size_t)m.conn[6 * e + a] + c]);
+        }
         pos.insert(pos.end(), m.node_pos, m.node_pos + 3 * (size_t)m.n_nodes);
         ev.insert(ev.end(), m.ext_visc, m.ext_visc + 3 * (size_t)m.n_nodes);
         fixed.insert(fixed.end(), m.fixed, m.fixed + 3 * (size_t)m.n_nodes);
@@ -665,7 +676,7 @@ tf_status tf_batch_create(const tf_mesh* meshes, const tf_material* mats, int32_
         elem0.push_back(elem0.back() + m.n_elems);
     }
     tf_mesh all{static_cast<int32_t>(nn), static_cast<int32_t>(ne), pos.data(), conn.data(), fixed.data(), ev.data(),
-                placement.data()};
+                placement.data(), any_ref ? ref.data() : nullptr};
     tf_material mat{E.data(), nu.data(), eta.data()};
     return create_handle(&all, &mat, opts, node0, elem0, out);
 }

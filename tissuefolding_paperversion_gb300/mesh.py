@@ -45,6 +45,7 @@ class Tissue:
     dt: float = 60.0           # time step (s)
     n_steps: int = 20
     name: str = "tissue"
+    ref_pos: np.ndarray = None  # (18E,) reference (stress-free) prism shapes; None: the node positions
 
     @property
     def n_nodes(self) -> int:
