@@ -169,6 +169,7 @@ struct tf_handle {
     bool tuned = false;
     cudaGraphExec_t graph[2][4] = {};           // Krylov chunks [method-1][log2(chunk/8)]
     int64_t graph_kernels[2][4] = {};
+    int last_iters[2] = {0, 0};                 // iterations of the last solve per method (chunk planning)
     tf::Amg* amg = nullptr;                     // multigrid preconditioner (null: block-Jacobi)
 };
 

@@ -665,21 +665,34 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
     TF_LAUNCH_CHECK(h);
     const int maxit = h->opt.krylov_max_iter;
     const size_t nscal = (size_t)d.nseg * S_COUNT;
+    // Iterations run in graph chunks of 8/16/32/64 with a flag check after
+    // each batch.  Consecutive solves of a handle need similar counts, so the
+    // first batch covers 7/8 of the previous solve's iterations (largest
+    // chunks first, no check in between) and the rest goes in chunks of 8:
+    // at most 8 iterations run past convergence.  Without a previous count
+    // the chunks double from 8.
     int launched = 0, ci = 0;
-    bool done = false;
+    int planned = (keep == 0) ? (h->last_iters[method - 1] * 7) / 8 : 0;
+    bool done = false, fixed8 = planned > 0;
     while (launched < maxit && !done) {
-        const int n = 8 << ci;
-        if (n <= maxit - launched) {
-            const tf_status s = run_chunk(h, c, method, ci);
-            if (s != TF_OK) return s;
-            launched += n;
-        } else {
-            const int rest = maxit - launched;
+        int target = planned > 0 ? planned : (fixed8 ? 8 : (8 << ci));
+        planned = 0;
+        target = std::min(target, maxit - launched);
+        int issued = 0;
+        for (int cj = 3; cj >= 0 && issued < target; --cj)
+            while (target - issued >= (8 << cj)) {
+                const tf_status s = run_chunk(h, c, method, cj);
+                if (s != TF_OK) return s;
+                issued += 8 << cj;
+            }
+        if (issued < target) {  // fewer than 8 left before maxit
+            const int rest = target - issued;
             issue_iterations(h, c, method, rest);
             TF_LAUNCH_CHECK(h);
             h->launches += (int64_t)rest * kernels_per_iteration(h, method) - 1;
-            launched = maxit;
+            issued = target;
         }
+        launched += issued;
         TF_CUDA(cudaMemcpyAsync(d.host_scal, d.scal, sizeof(double) * nscal, cudaMemcpyDeviceToHost, st));
         TF_CUDA(cudaStreamSynchronize(st));
         done = true;
@@ -706,6 +719,7 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
     }
     *iters = itmax;
     *relres = rmax;
+    if (keep == 0) h->last_iters[method - 1] = itmax;
     if (worst == F_CONVERGED) return TF_OK;
     char rel[32];
     std::snprintf(rel, sizeof(rel), "%.3g", bad_rel);
