@@ -811,6 +811,7 @@ struct V0 {  // level-0 operands
 
 // x = omega D^-1 r  (r is the Krylov method's FP64 vector)
 __global__ void k_v0_pre(V0 a, const double* __restrict__ r, float* __restrict__ x) {
+    pdl_enter();
     const Node0 q = node0(a.d);
     if (!q.valid || seg_stopped(a.d.scal, q.seg)) return;
     const float om = (float)__ldg(a.omega);
@@ -822,6 +823,7 @@ __global__ void k_v0_pre(V0 a, const double* __restrict__ r, float* __restrict__
 
 // t = r - A x
 __global__ void k_v0_resid(V0 a, const double* __restrict__ r, const float* __restrict__ x, float* __restrict__ t) {
+    pdl_enter();
     const Node0 q = node0(a.d);
     if (seg_stopped(a.d.scal, q.seg)) return;
     float y[3];
@@ -833,6 +835,7 @@ __global__ void k_v0_resid(V0 a, const double* __restrict__ r, const float* __re
 
 // out = x + omega D^-1 (r - A x), written back as the FP64 preconditioned vector
 __global__ void k_v0_post(V0 a, const double* __restrict__ r, const float* __restrict__ x, double* __restrict__ out) {
+    pdl_enter();
     const Node0 q = node0(a.d);
     if (seg_stopped(a.d.scal, q.seg)) return;
     float y[3];
@@ -849,6 +852,7 @@ __global__ void k_v0_post(V0 a, const double* __restrict__ r, const float* __res
 
 // x_i += P_i e_agg(i)
 __global__ void k_v0_prolong(V0 a, AmgLevel F, const float* __restrict__ e, float* __restrict__ x) {
+    pdl_enter();
     const Node0 q = node0(a.d);
     if (!q.valid || seg_stopped(a.d.scal, q.seg)) return;
     const int I = F.agg[q.i];
@@ -871,6 +875,7 @@ __global__ void k_v0_prolong(V0 a, AmgLevel F, const float* __restrict__ e, floa
 template <int BS>
 __global__ void k_restrict(AmgLevel F, AmgLevel C, const float* __restrict__ t, const double* __restrict__ scal,
                            const double* __restrict__ omegaC, int presmooth) {
+    pdl_enter();
     const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (I >= C.n || seg_stopped(scal, C.seg[I])) return;
@@ -907,6 +912,7 @@ __global__ void k_restrict(AmgLevel F, AmgLevel C, const float* __restrict__ t, 
 
 // t = r - A x  (one warp per row)
 __global__ void k_v6_resid(AmgLevel L, const double* __restrict__ scal) {
+    pdl_enter();
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= L.n || seg_stopped(scal, L.seg[i])) return;
@@ -918,6 +924,7 @@ __global__ void k_v6_resid(AmgLevel L, const double* __restrict__ scal) {
 // out = x + omega D^-1 (r - A x)  (one warp per row)
 __global__ void k_v6_post(AmgLevel L, const double* __restrict__ scal, const double* __restrict__ omega,
                           const float* __restrict__ x, float* __restrict__ out) {
+    pdl_enter();
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= L.n || seg_stopped(scal, L.seg[i])) return;
@@ -931,6 +938,7 @@ __global__ void k_v6_post(AmgLevel L, const double* __restrict__ scal, const dou
 
 // x_i += P_i e_agg(i)  (6-DOF fine level)
 __global__ void k_v6_prolong(AmgLevel F, const double* __restrict__ scal, const float* __restrict__ e) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n || seg_stopped(scal, F.seg[i])) return;
     const int I = F.agg[i];
@@ -950,6 +958,7 @@ __global__ void k_v6_prolong(AmgLevel F, const double* __restrict__ scal, const 
 // e = C^-1 r on the coarsest level, one CTA per instance
 __global__ void k_coarse_solve(AmgLevel L, const double* __restrict__ scal, const int* __restrict__ cnode0,
                                const int* __restrict__ cinv0, const float* __restrict__ cinv) {
+    pdl_enter();
     const int g = blockIdx.x;
     if (seg_stopped(scal, g)) return;
     const int n0 = cnode0[g], m = 6 * (cnode0[g + 1] - n0);
@@ -1051,34 +1060,35 @@ void amg_vcycle(tf_handle* h, const double* r, double* out) {
     const int nl = a->nlev;
     V0 v0{d, a->omega, a->val32, a->dinv32};
     AmgLevel& L0 = a->L[0];
-    k_v0_pre<<<d.ncta, kNodeThreads, 0, st>>>(v0, r, L0.x);
-    k_v0_resid<<<d.ncta, kNodeThreads, 0, st>>>(v0, r, L0.x, L0.t);
-    k_restrict<3><<<cdiv(32 * (int64_t)a->L[1].n, kT), kT, 0, st>>>(L0, a->L[1], L0.t, d.scal, a->omega + 1,
-                                                                    (1 < nl - 1 || !a->coarse_exact) ? 1 : 0);
+    launch_pdl(k_v0_pre, d.ncta, kNodeThreads, st, v0, r, L0.x);
+    launch_pdl(k_v0_resid, d.ncta, kNodeThreads, st, v0, r, L0.x, L0.t);
+    launch_pdl(k_restrict<3>, cdiv(32 * (int64_t)a->L[1].n, kT), kT, st, L0, a->L[1], (const float*)L0.t,
+               (const double*)d.scal, (const double*)(a->omega + 1), (1 < nl - 1 || !a->coarse_exact) ? 1 : 0);
     for (int l = 1; l + 1 < nl; ++l) {
         AmgLevel& L = a->L[l];
-        k_v6_resid<<<cdiv(32 * (int64_t)L.n, kT), kT, 0, st>>>(L, d.scal);
-        k_restrict<6><<<cdiv(32 * (int64_t)a->L[l + 1].n, kT), kT, 0, st>>>(L, a->L[l + 1], L.t, d.scal,
-                                                                              a->omega + l + 1,
-                                                                              (l + 1 < nl - 1 || !a->coarse_exact) ? 1 : 0);
+        launch_pdl(k_v6_resid, cdiv(32 * (int64_t)L.n, kT), kT, st, L, (const double*)d.scal);
+        launch_pdl(k_restrict<6>, cdiv(32 * (int64_t)a->L[l + 1].n, kT), kT, st, L, a->L[l + 1], (const float*)L.t,
+                   (const double*)d.scal, (const double*)(a->omega + l + 1),
+                   (l + 1 < nl - 1 || !a->coarse_exact) ? 1 : 0);
     }
     AmgLevel& LC = a->L[nl - 1];
     if (a->coarse_exact) {
-        k_coarse_solve<<<a->nseg, 128, 0, st>>>(LC, d.scal, a->cnode0, a->cinv0, a->cinv);
+        launch_pdl(k_coarse_solve, a->nseg, 128, st, LC, d.scal, a->cnode0, a->cinv0, a->cinv);
     } else {
         // x from the restriction's pre-smoothing; three more sweeps into e
         const int nbc = cdiv(32 * (int64_t)LC.n, kT);
-        k_v6_post<<<nbc, kT, 0, st>>>(LC, d.scal, a->omega + nl - 1, LC.x, LC.e);
-        k_v6_post<<<nbc, kT, 0, st>>>(LC, d.scal, a->omega + nl - 1, LC.e, LC.t);
-        k_v6_post<<<nbc, kT, 0, st>>>(LC, d.scal, a->omega + nl - 1, LC.t, LC.e);
+        launch_pdl(k_v6_post, nbc, kT, st, LC, d.scal, a->omega + nl - 1, LC.x, LC.e);
+        launch_pdl(k_v6_post, nbc, kT, st, LC, d.scal, a->omega + nl - 1, LC.e, LC.t);
+        launch_pdl(k_v6_post, nbc, kT, st, LC, d.scal, a->omega + nl - 1, LC.t, LC.e);
     }
     for (int l = nl - 2; l >= 1; --l) {
         AmgLevel& L = a->L[l];
-        k_v6_prolong<<<cdiv(L.n, kT), kT, 0, st>>>(L, d.scal, a->L[l + 1].e);
-        k_v6_post<<<cdiv(32 * (int64_t)L.n, kT), kT, 0, st>>>(L, d.scal, a->omega + l, L.x, L.e);
+        launch_pdl(k_v6_prolong, cdiv(L.n, kT), kT, st, L, d.scal, a->L[l + 1].e);
+        launch_pdl(k_v6_post, cdiv(32 * (int64_t)L.n, kT), kT, st, L, (const double*)d.scal,
+                   (const double*)(a->omega + l), (const float*)L.x, L.e);
     }
-    k_v0_prolong<<<d.ncta, kNodeThreads, 0, st>>>(v0, L0, a->L[1].e, L0.x);
-    k_v0_post<<<d.ncta, kNodeThreads, 0, st>>>(v0, r, L0.x, out);
+    launch_pdl(k_v0_prolong, d.ncta, kNodeThreads, st, v0, L0, a->L[1].e, L0.x);
+    launch_pdl(k_v0_post, d.ncta, kNodeThreads, st, v0, r, L0.x, out);
 }
 
 }  // namespace tf

@@ -115,6 +115,31 @@ constexpr int kAmgMaxLevels = 10;
 
 struct Amg;  // multigrid hierarchy (tf_amg.cu)
 
+// Programmatic dependent launch for the chains of short kernels of the
+// linear solve: a kernel launched with launch_pdl may be scheduled as its
+// predecessor's blocks exit, hiding the launch gap; pdl_enter makes it wait
+// for the predecessor's completion (and memory) before anything else.  (An
+// explicit early trigger, letting the next kernel's blocks sit resident
+// while the current one runs, measured 10 % slower on the 320,000-prism
+// step; this form measured ~3 % faster than plain launches.)  A no-op for
+// ordinary launches.
+__device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // y = this thread's row of the sliced block matrix times x.  T is the
 // storage type of the values (double for the Krylov operator, float for the
 // copy the multigrid smoother reads); products and sums are FP64.  The thread is

@@ -190,6 +190,7 @@ __global__ void k_cg_init(Ctx c, const double* __restrict__ b, double* __restric
 
 // q = A p; alpha = rz / (p, q)
 __global__ void k_cg_spmv(Ctx c, const double* __restrict__ p, double* __restrict__ q) {
+    pdl_enter();
     const Where w = where(c);
     if (stopped(w)) return;
     double v[1] = {0.0};
@@ -218,6 +219,7 @@ __global__ void k_cg_spmv(Ctx c, const double* __restrict__ p, double* __restric
 // x += alpha p; r -= alpha q; z = M^-1 r;  beta = (r,z)_new / (r,z)
 __global__ void k_cg_update(Ctx c, double* __restrict__ x, double* __restrict__ r, double* __restrict__ z,
                             const double* __restrict__ p, const double* __restrict__ q, int jac) {
+    pdl_enter();
     const Where w = where(c);
     if (stopped(w)) return;
     const double alpha = __ldcg(&w.s[S_ALPHA]);
@@ -266,6 +268,7 @@ __global__ void k_cg_update(Ctx c, double* __restrict__ x, double* __restrict__ 
 // rz = (r, z), beta = rz / rz_old; start != 0 also sets p = z (first step).
 __global__ void k_cg_rz(Ctx c, const double* __restrict__ r, const double* __restrict__ z, double* __restrict__ p,
                         int start) {
+    pdl_enter();
     const Where w = where(c);
     if (stopped(w)) return;
     double v[1] = {0.0};
@@ -293,6 +296,7 @@ __global__ void k_cg_rz(Ctx c, const double* __restrict__ r, const double* __res
 
 // p = z + beta p
 __global__ void k_cg_direction(Ctx c, const double* __restrict__ z, double* __restrict__ p) {
+    pdl_enter();
     const Where w = where(c);
     if (stopped(w) || !w.valid) return;
     const double beta = __ldcg(&w.s[S_BETA]);
@@ -342,6 +346,7 @@ __global__ void k_bi_init(Ctx c, const double* __restrict__ b, double* __restric
 // p = r + beta (p - omega v); phat = M^-1 p
 __global__ void k_bi_dir(Ctx c, const double* __restrict__ r, const double* __restrict__ v, double* __restrict__ p,
                          double* __restrict__ phat, int jac) {
+    pdl_enter();
     const Where w = where(c);
     if (stopped(w) || !w.valid) return;
     const double beta = __ldcg(&w.s[S_BETA]), omega = __ldcg(&w.s[S_OMEGA]);
@@ -362,6 +367,7 @@ __global__ void k_bi_dir(Ctx c, const double* __restrict__ r, const double* __re
 // v = A phat; alpha = rho / (rhat, v)
 __global__ void k_bi_spmv1(Ctx c, const double* __restrict__ phat, const double* __restrict__ rhat,
                            double* __restrict__ v) {
+    pdl_enter();
     const Where w = where(c);
     if (stopped(w)) return;
     double s[1] = {0.0};
@@ -391,6 +397,7 @@ __global__ void k_bi_spmv1(Ctx c, const double* __restrict__ phat, const double*
 // omega would otherwise be formed from a vanishing s).
 __global__ void k_bi_s(Ctx c, const double* __restrict__ r, const double* __restrict__ v, double* __restrict__ s,
                        double* __restrict__ shat, double* __restrict__ x, const double* __restrict__ phat, int jac) {
+    pdl_enter();
     const Where w = where(c);
     if (stopped(w)) return;
     const double alpha = __ldcg(&w.s[S_ALPHA]);
@@ -424,6 +431,7 @@ __global__ void k_bi_s(Ctx c, const double* __restrict__ r, const double* __rest
 // Applies the half step x += alpha phat of instances flagged -1 by k_bi_s
 // and marks them converged.
 __global__ void k_bi_half(Ctx c, double* __restrict__ x, const double* __restrict__ phat) {
+    pdl_enter();
     const Where w = where(c);
     if (__ldcg(&w.s[S_FLAG]) != -1.0) return;
     const double alpha = __ldcg(&w.s[S_ALPHA]);
@@ -443,6 +451,7 @@ __global__ void k_bi_half(Ctx c, double* __restrict__ x, const double* __restric
 // t = A shat; omega = (t, s) / (t, t)
 __global__ void k_bi_spmv2(Ctx c, const double* __restrict__ shat, const double* __restrict__ s,
                            double* __restrict__ t) {
+    pdl_enter();
     const Where w = where(c);
     if (stopped(w)) return;
     double acc[2] = {0.0, 0.0};
@@ -468,6 +477,7 @@ __global__ void k_bi_spmv2(Ctx c, const double* __restrict__ shat, const double*
 __global__ void k_bi_x(Ctx c, double* __restrict__ x, double* __restrict__ r, const double* __restrict__ rhat,
                        const double* __restrict__ phat, const double* __restrict__ shat, const double* __restrict__ s,
                        const double* __restrict__ t) {
+    pdl_enter();
     const Where w = where(c);
     if (stopped(w)) return;
     const double alpha = __ldcg(&w.s[S_ALPHA]), omega = __ldcg(&w.s[S_OMEGA]);
@@ -586,22 +596,22 @@ void issue_iterations(tf_handle* h, const Ctx& c, int method, int n) {
     const int jac = h->amg ? 0 : 1;
     for (int it = 0; it < n; ++it) {
         if (method == 1) {
-            k_cg_spmv<<<nb, kThreads, 0, st>>>(c, d.p, d.q);
-            k_cg_update<<<nb, kThreads, 0, st>>>(c, d.du, d.r, d.z, d.p, d.q, jac);
+            launch_pdl(k_cg_spmv, nb, kThreads, st, c, d.p, d.q);
+            launch_pdl(k_cg_update, nb, kThreads, st, c, d.du, d.r, d.z, d.p, d.q, jac);
             if (!jac) {
                 amg_vcycle(h, d.r, d.z);
-                k_cg_rz<<<nb, kThreads, 0, st>>>(c, d.r, d.z, d.p, 0);
+                launch_pdl(k_cg_rz, nb, kThreads, st, c, d.r, d.z, d.p, 0);
             }
-            k_cg_direction<<<nb, kThreads, 0, st>>>(c, d.z, d.p);
+            launch_pdl(k_cg_direction, nb, kThreads, st, c, d.z, d.p);
         } else {
-            k_bi_dir<<<nb, kThreads, 0, st>>>(c, d.r, d.q, d.p, d.z, jac);
+            launch_pdl(k_bi_dir, nb, kThreads, st, c, d.r, d.q, d.p, d.z, jac);
             if (!jac) amg_vcycle(h, d.p, d.z);
-            k_bi_spmv1<<<nb, kThreads, 0, st>>>(c, d.z, d.rhat, d.q);
-            k_bi_s<<<nb, kThreads, 0, st>>>(c, d.r, d.q, d.s, d.sh, d.du, d.z, jac);
+            launch_pdl(k_bi_spmv1, nb, kThreads, st, c, d.z, d.rhat, d.q);
+            launch_pdl(k_bi_s, nb, kThreads, st, c, d.r, d.q, d.s, d.sh, d.du, d.z, jac);
             if (!jac) amg_vcycle(h, d.s, d.sh);
-            k_bi_half<<<nb, kThreads, 0, st>>>(c, d.du, d.z);
-            k_bi_spmv2<<<nb, kThreads, 0, st>>>(c, d.sh, d.s, d.t);
-            k_bi_x<<<nb, kThreads, 0, st>>>(c, d.du, d.r, d.rhat, d.z, d.sh, d.s, d.t);
+            launch_pdl(k_bi_half, nb, kThreads, st, c, d.du, d.z);
+            launch_pdl(k_bi_spmv2, nb, kThreads, st, c, d.sh, d.s, d.t);
+            launch_pdl(k_bi_x, nb, kThreads, st, c, d.du, d.r, d.rhat, d.z, d.sh, d.s, d.t);
         }
     }
 }
