@@ -48,6 +48,8 @@ constexpr int kT = 256;
 constexpr int kCoarseNodes = 16;  // nodes per instance at the coarsest level (96 DOFs)
 constexpr int kCoarseDofs = 6 * kCoarseNodes;
 constexpr int kPowerIters = 16;
+constexpr int kTailNodes = 256;   // levels with at most this many nodes per instance run fused
+constexpr int kTailThreads = 1024;
 
 // ---- host set-up -----------------------------------------------------------------
 
@@ -170,6 +172,7 @@ struct AmgLevel {
     int64_t nnzb = 0;
     float* dinv = nullptr;   // [n][36] block inverses (levels >= 1)
     int* seg = nullptr;      // [n] instance of each node (levels >= 1)
+    int* seg0 = nullptr;     // [nseg+1] node offsets per instance (levels >= 1)
     // transfer to level + 1 (absent at the coarsest level)
     int* agg = nullptr;      // [n]
     float* P = nullptr;      // [n][bs*6]
@@ -199,6 +202,7 @@ struct Amg {
     float* cinv = nullptr;     // coarsest inverses, m_g x m_g row-major
     bool coarse_exact = true;
     int max_cm = 0;
+    int tail = 0;              // levels tail..nlev-1 run in one kernel (one CTA per instance); 0: none
     std::vector<int> h_n;      // nodes per level (host)
     // what the next solve has to redo: 0 nothing, 1 the FP32 copies of the
     // level-0 matrix (new assembly, same time step), 2 the whole hierarchy
@@ -210,8 +214,8 @@ void amg_free(Amg* a) {
     if (!a) return;
     for (int l = 0; l < a->nlev; ++l) {
         AmgLevel& L = a->L[l];
-        void* ptrs[] = {L.rowptr, L.colidx, L.rowof, L.diag, L.val, L.seg, L.agg, L.P, L.mptr, L.mlist, L.gptr,
-                        L.glist, L.dead, L.r, L.x, L.t, L.e};
+        void* ptrs[] = {L.rowptr, L.colidx, L.rowof, L.diag, L.val, L.seg, L.seg0, L.agg, L.P, L.mptr, L.mlist,
+                        L.gptr, L.glist, L.dead, L.r, L.x, L.t, L.e};
         for (void* p : ptrs)
             if (p) cudaFree(p);
         if (l > 0 && L.dinv) cudaFree(L.dinv);
@@ -374,6 +378,7 @@ tf_status amg_build(tf_handle* h, const double* pos) {
         AMG_TRY(up(&CL.rowof, rowof));
         AMG_TRY(up(&CL.diag, diag));
         AMG_TRY(up(&CL.seg, seg));
+        AMG_TRY(up(&CL.seg0, C.seg0));
         AMG_TRY(up(&CL.dead, dead));
         AMG_TRY(zeros(&CL.val, (size_t)cnnzb * 36));  // float
         AMG_TRY(zeros(&CL.dinv, (size_t)na * 36));
@@ -424,6 +429,15 @@ tf_status amg_build(tf_handle* h, const double* pos) {
         cinv0[g + 1] = cinv0[g] + m * m;
     }
     a->coarse_exact = a->max_cm <= kCoarseDofs;
+    // the levels whose instances all have at most kTailNodes nodes run as
+    // one kernel per V-cycle, one CTA per instance
+    a->tail = a->coarse_exact ? a->nlev - 1 : 0;
+    for (int l = a->nlev - 1; l >= 1 && a->coarse_exact; --l) {
+        int maxn = 0;
+        for (int g = 0; g < d.nseg; ++g) maxn = std::max(maxn, H[l].seg0[g + 1] - H[l].seg0[g]);
+        if (maxn > kTailNodes) break;
+        a->tail = l;
+    }
     AMG_TRY(up(&a->cnode0, CH.seg0));
     AMG_TRY(up(&a->cinv0, cinv0));
     AMG_TRY(zeros(&a->cinv, (size_t)std::max(cinv0[d.nseg], 1)));
@@ -870,15 +884,12 @@ __global__ void k_v0_prolong(V0 a, AmgLevel F, const float* __restrict__ e, floa
 }
 
 // r_C(I) = sum over members i of P_i^T t_i; x_C = omega_C D_C^-1 r_C
-// (pre-smoothing).  One warp per coarse node: the lanes stride over the
-// (member, DOF) pairs.
+// (pre-smoothing), by one warp: the lanes stride over the (member, DOF)
+// pairs of coarse node I.
 template <int BS>
-__global__ void k_restrict(AmgLevel F, AmgLevel C, const float* __restrict__ t, const double* __restrict__ scal,
-                           const double* __restrict__ omegaC, int presmooth) {
-    pdl_enter();
-    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__device__ __forceinline__ void restrict_node(const AmgLevel& F, const AmgLevel& C, const float* __restrict__ t,
+                                              int I, const double* __restrict__ omegaC, int presmooth) {
     const int lane = threadIdx.x & 31;
-    if (I >= C.n || seg_stopped(scal, C.seg[I])) return;
     float rc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     const int q0 = F.mptr[I], np = BS * (F.mptr[I + 1] - q0);
     for (int qa = lane; qa < np; qa += 64) {
@@ -910,6 +921,44 @@ __global__ void k_restrict(AmgLevel F, AmgLevel C, const float* __restrict__ t, 
     }
 }
 
+// Restriction, one warp per coarse node.
+template <int BS>
+__global__ void k_restrict(AmgLevel F, AmgLevel C, const float* __restrict__ t, const double* __restrict__ scal,
+                           const double* __restrict__ omegaC, int presmooth) {
+    pdl_enter();
+    const int I = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (I >= C.n || seg_stopped(scal, C.seg[I])) return;
+    restrict_node<BS>(F, C, t, I, omegaC, presmooth);
+}
+
+// x_i += P_i e_agg(i) for node i of a 6-DOF level
+__device__ __forceinline__ void prolong_node(const AmgLevel& F, const float* __restrict__ e, int i) {
+    const int I = F.agg[i];
+    const float* __restrict__ P = F.P + 36 * (size_t)i;
+    float ec[6];
+#pragma unroll
+    for (int b = 0; b < 6; ++b) ec[b] = e[6 * I + b];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        float s = F.x[6 * i + k];
+#pragma unroll
+        for (int b = 0; b < 6; ++b) s = fmaf(__ldg(&P[6 * k + b]), ec[b], s);
+        F.x[6 * i + k] = s;
+    }
+}
+
+// out_i = x_i + omega D_i^-1 (r - A x)_i for row i, by one warp
+__device__ __forceinline__ void post_row(const AmgLevel& L, const double* __restrict__ omega,
+                                         const float* __restrict__ x, float* __restrict__ out, int i) {
+    const int lane = threadIdx.x & 31;
+    float y[6], rr[6];
+    row6_warp(L, i, x, y);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) rr[k] = L.r[6 * i + k] - y[k];
+    if (lane < 6)
+        out[6 * i + lane] = fmaf((float)__ldg(omega), lane_mul6(L.dinv + 36 * (size_t)i, rr, lane), x[6 * i + lane]);
+}
+
 // t = r - A x  (one warp per row)
 __global__ void k_v6_resid(AmgLevel L, const double* __restrict__ scal) {
     pdl_enter();
@@ -926,14 +975,8 @@ __global__ void k_v6_post(AmgLevel L, const double* __restrict__ scal, const dou
                           const float* __restrict__ x, float* __restrict__ out) {
     pdl_enter();
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
     if (i >= L.n || seg_stopped(scal, L.seg[i])) return;
-    float y[6], rr[6];
-    row6_warp(L, i, x, y);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) rr[k] = L.r[6 * i + k] - y[k];
-    if (lane < 6)
-        out[6 * i + lane] = fmaf((float)__ldg(omega), lane_mul6(L.dinv + 36 * (size_t)i, rr, lane), x[6 * i + lane]);
+    post_row(L, omega, x, out, i);
 }
 
 // x_i += P_i e_agg(i)  (6-DOF fine level)
@@ -941,18 +984,7 @@ __global__ void k_v6_prolong(AmgLevel F, const double* __restrict__ scal, const 
     pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n || seg_stopped(scal, F.seg[i])) return;
-    const int I = F.agg[i];
-    const float* __restrict__ P = F.P + 36 * (size_t)i;
-    float ec[6];
-#pragma unroll
-    for (int b = 0; b < 6; ++b) ec[b] = e[6 * I + b];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        float s = F.x[6 * i + k];
-#pragma unroll
-        for (int b = 0; b < 6; ++b) s = fmaf(__ldg(&P[6 * k + b]), ec[b], s);
-        F.x[6 * i + k] = s;
-    }
+    prolong_node(F, e, i);
 }
 
 // e = C^-1 r on the coarsest level, one CTA per instance
@@ -968,6 +1000,56 @@ __global__ void k_coarse_solve(AmgLevel L, const double* __restrict__ scal, cons
         float s = 0.f;
         for (int j = 0; j < m; ++j) s = fmaf(__ldg(&Mi[(size_t)k * m + j]), r[j], s);
         L.e[6 * (size_t)n0 + k] = s;
+    }
+}
+
+// The coarse tail of a V-cycle: levels T.first .. T.last of one instance
+// (one CTA each), block barriers instead of kernel boundaries.  Level
+// T.first arrives restricted and pre-smoothed; its corrected x goes out in e.
+struct Tail {
+    AmgLevel L[kAmgMaxLevels];
+    const double* omega;
+    const double* scal;
+    const int* cinv0;
+    const float* cinv;
+    int first, last;
+};
+
+__global__ void __launch_bounds__(kTailThreads) k_tail(Tail T) {
+    pdl_enter();
+    const int g = blockIdx.x;
+    if (seg_stopped(T.scal, g)) return;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int l = T.first; l < T.last; ++l) {
+        const AmgLevel& F = T.L[l];
+        const AmgLevel& C = T.L[l + 1];
+        for (int i = F.seg0[g] + warp; i < F.seg0[g + 1]; i += nw) {
+            float y[6];
+            row6_warp(F, i, F.x, y);
+            if (lane < 6) F.t[6 * i + lane] = F.r[6 * i + lane] - pick6(y, lane);
+        }
+        __syncthreads();
+        for (int I = C.seg0[g] + warp; I < C.seg0[g + 1]; I += nw)
+            restrict_node<6>(F, C, F.t, I, T.omega + l + 1, l + 1 < T.last ? 1 : 0);
+        __syncthreads();
+    }
+    {
+        const AmgLevel& C = T.L[T.last];
+        const int n0 = C.seg0[g], m = 6 * (C.seg0[g + 1] - n0);
+        const float* __restrict__ Mi = T.cinv + T.cinv0[g];
+        for (int k = threadIdx.x; k < m; k += blockDim.x) {
+            float s2 = 0.f;
+            for (int j = 0; j < m; ++j) s2 = fmaf(__ldg(&Mi[(size_t)k * m + j]), C.r[6 * (size_t)n0 + j], s2);
+            C.e[6 * (size_t)n0 + k] = s2;
+        }
+    }
+    __syncthreads();
+    for (int l = T.last - 1; l >= T.first; --l) {
+        const AmgLevel& F = T.L[l];
+        for (int i = F.seg0[g] + threadIdx.x; i < F.seg0[g + 1]; i += blockDim.x) prolong_node(F, T.L[l + 1].e, i);
+        __syncthreads();
+        for (int i = F.seg0[g] + warp; i < F.seg0[g + 1]; i += nw) post_row(F, T.omega + l, F.x, F.e, i);
+        __syncthreads();
     }
 }
 
@@ -1049,39 +1131,55 @@ tf_status amg_numeric(tf_handle* h) {
 
 int amg_vcycle_kernels(const tf_handle* h) {
     const Amg* a = h->amg;
+    if (a->tail > 0) return 4 * a->tail + 2;
     return 4 * (a->nlev - 2) + 6 + (a->coarse_exact ? 0 : 2);
 }
 
-// out = M^-1 r: one V-cycle (all launches on h->stream, no host work)
+// out = M^-1 r: one V-cycle (all launches on h->stream, no host work).
+// Levels below `tail` run kernel by kernel over all instances; the tail runs
+// as one kernel with a CTA per instance.
 void amg_vcycle(tf_handle* h, const double* r, double* out) {
     Amg* a = h->amg;
     Device& d = h->d;
     cudaStream_t st = h->stream;
     const int nl = a->nlev;
+    const int stop = a->tail > 0 ? a->tail : nl - 1;  // first level not handled kernel by kernel
     V0 v0{d, a->omega, a->val32, a->dinv32};
     AmgLevel& L0 = a->L[0];
+    auto presmooth = [&](int l) { return (l < nl - 1 || !a->coarse_exact) ? 1 : 0; };
     launch_pdl(k_v0_pre, d.ncta, kNodeThreads, st, v0, r, L0.x);
     launch_pdl(k_v0_resid, d.ncta, kNodeThreads, st, v0, r, L0.x, L0.t);
     launch_pdl(k_restrict<3>, cdiv(32 * (int64_t)a->L[1].n, kT), kT, st, L0, a->L[1], (const float*)L0.t,
-               (const double*)d.scal, (const double*)(a->omega + 1), (1 < nl - 1 || !a->coarse_exact) ? 1 : 0);
-    for (int l = 1; l + 1 < nl; ++l) {
+               (const double*)d.scal, (const double*)(a->omega + 1), presmooth(1));
+    for (int l = 1; l < stop; ++l) {
         AmgLevel& L = a->L[l];
         launch_pdl(k_v6_resid, cdiv(32 * (int64_t)L.n, kT), kT, st, L, (const double*)d.scal);
         launch_pdl(k_restrict<6>, cdiv(32 * (int64_t)a->L[l + 1].n, kT), kT, st, L, a->L[l + 1], (const float*)L.t,
-                   (const double*)d.scal, (const double*)(a->omega + l + 1),
-                   (l + 1 < nl - 1 || !a->coarse_exact) ? 1 : 0);
+                   (const double*)d.scal, (const double*)(a->omega + l + 1), presmooth(l + 1));
     }
-    AmgLevel& LC = a->L[nl - 1];
-    if (a->coarse_exact) {
-        launch_pdl(k_coarse_solve, a->nseg, 128, st, LC, d.scal, a->cnode0, a->cinv0, a->cinv);
+    if (a->tail > 0) {
+        Tail T;
+        for (int l = 0; l < nl; ++l) T.L[l] = a->L[l];
+        T.omega = a->omega;
+        T.scal = d.scal;
+        T.cinv0 = a->cinv0;
+        T.cinv = a->cinv;
+        T.first = a->tail;
+        T.last = nl - 1;
+        launch_pdl(k_tail, a->nseg, kTailThreads, st, T);
     } else {
-        // x from the restriction's pre-smoothing; three more sweeps into e
-        const int nbc = cdiv(32 * (int64_t)LC.n, kT);
-        launch_pdl(k_v6_post, nbc, kT, st, LC, d.scal, a->omega + nl - 1, LC.x, LC.e);
-        launch_pdl(k_v6_post, nbc, kT, st, LC, d.scal, a->omega + nl - 1, LC.e, LC.t);
-        launch_pdl(k_v6_post, nbc, kT, st, LC, d.scal, a->omega + nl - 1, LC.t, LC.e);
+        AmgLevel& LC = a->L[nl - 1];
+        if (a->coarse_exact) {
+            launch_pdl(k_coarse_solve, a->nseg, 128, st, LC, d.scal, a->cnode0, a->cinv0, a->cinv);
+        } else {
+            // x from the restriction's pre-smoothing; three more sweeps into e
+            const int nbc = cdiv(32 * (int64_t)LC.n, kT);
+            launch_pdl(k_v6_post, nbc, kT, st, LC, d.scal, a->omega + nl - 1, LC.x, LC.e);
+            launch_pdl(k_v6_post, nbc, kT, st, LC, d.scal, a->omega + nl - 1, LC.e, LC.t);
+            launch_pdl(k_v6_post, nbc, kT, st, LC, d.scal, a->omega + nl - 1, LC.t, LC.e);
+        }
     }
-    for (int l = nl - 2; l >= 1; --l) {
+    for (int l = stop - 1; l >= 1; --l) {
         AmgLevel& L = a->L[l];
         launch_pdl(k_v6_prolong, cdiv(L.n, kT), kT, st, L, d.scal, a->L[l + 1].e);
         launch_pdl(k_v6_post, cdiv(32 * (int64_t)L.n, kT), kT, st, L, (const double*)d.scal,
