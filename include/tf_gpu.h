@@ -134,6 +134,16 @@ TF_API tf_status tf_assemble(tf_handle* h);
  * not fixed -- the gExt hook of addMyosinForces/addPackingForces
  * (Simulation.cpp:6506-6540). */
 TF_API tf_status tf_add_external_forces(tf_handle* h, const double* gext);
+/* Adds n entries to K after tf_assemble -- the hook of the writers that add
+ * to NRSolver->K directly, e.g. Simulation::calculatePackingJacobian3D
+ * (Simulation.cpp:7205-7290): K(rows[k], cols[k]) += vals[k], DOF indices.
+ * Entries in a fixed DOF's row or column are dropped (calcutateFixedK runs
+ * after these writers).  Node pairs outside the element pattern are kept as
+ * extra blocks that the linear solve's products include (the multigrid
+ * preconditioner does not); their positions persist, their values are
+ * cleared by the next tf_assemble.  tf_export_csr includes them. */
+TF_API tf_status tf_add_K_triplets(tf_handle* h, int64_t n, const int32_t* rows, const int32_t* cols,
+                                   const double* vals);
 /* solveForDeltaU (NewtonRaphsonSolver.cpp:382-404): solves K^T du = g, the
  * transposed system Pardiso is asked for (iparm[11] = 1, :639). */
 TF_API tf_status tf_solve(tf_handle* h, int32_t* iters, double* relres);

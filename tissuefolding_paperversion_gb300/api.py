@@ -31,7 +31,7 @@ EXPORTED = [
     "tf_element_eval", "tf_get_sizes", "tf_get_stream", "tf_launch_count", "tf_time_assembly",
     "tf_solve_bsr_static", "tf_batch_create", "tf_batch_step", "tf_get_instances", "tf_elements_per_cta",
     "tf_adj_forward", "tf_adj_backward", "tf_adj_free", "tf_multigrid_info", "tf_read_mesh_file",
-    "tf_write_frame",
+    "tf_write_frame", "tf_add_K_triplets",
 ]
 
 
@@ -123,6 +123,8 @@ def load(build_if_missing: bool = True):
     L.tf_adj_free.argtypes = [vp]
     L.tf_multigrid_info.restype = C.c_int
     L.tf_multigrid_info.argtypes = [vp, ip, vp, vp]
+    L.tf_add_K_triplets.restype = C.c_int
+    L.tf_add_K_triplets.argtypes = [vp, i64, vp, vp, vp]
     L.tf_read_mesh_file.restype = C.c_int
     L.tf_read_mesh_file.argtypes = [C.c_char_p, ip, ip, vp, vp, vp, vp, vp, vp]
     L.tf_write_frame.restype = C.c_int
@@ -248,6 +250,13 @@ class Solver:
     def add_external_forces(self, gext):
         g = np.ascontiguousarray(gext, dtype=np.float64)
         self._check(self.L.tf_add_external_forces(self.h, _ptr(g)), "tf_add_external_forces")
+
+    def add_K_triplets(self, rows, cols, vals):
+        """K(rows[k], cols[k]) += vals[k] after assemble() (packing/myosin-type writers)."""
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        c = np.ascontiguousarray(cols, dtype=np.int32)
+        v = np.ascontiguousarray(vals, dtype=np.float64)
+        self._check(self.L.tf_add_K_triplets(self.h, r.size, _ptr(r), _ptr(c), _ptr(v)), "tf_add_K_triplets")
 
     def solve(self, allow_not_converged=False):
         it = C.c_int32(0)

@@ -80,7 +80,7 @@ void free_all(tf_handle* h) {
                     d.slot, d.bofs, d.wslot0, d.scol, d.val, d.eblk, d.ef, d.gptr, d.glist, d.fptr, d.flist, d.uk, d.un, d.vel, d.g,
                     d.du, d.dinv, d.r, d.p, d.z, d.q, d.rhat, d.s, d.t, d.sh, d.scal, d.part, d.tickets,
                     d.seg_node0, d.elem_seg, d.cta_seg, d.cta_node0, d.cta_node1, d.seg_cta0, d.seg_active, d.seg_solve,
-                    d.tblk, d.valT, d.lamv, d.carry, d.dldu, d.gr, d.ge, d.nu, d.apical};
+                    d.tblk, d.valT, d.lamv, d.carry, d.dldu, d.gr, d.ge, d.nu, d.apical, d.xrow, d.xcol, d.xval};
     destroy_graphs(h);
     if (h->amg) {
         amg_free(h->amg);
@@ -592,11 +592,135 @@ tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* ite
     return TF_OK;
 }
 
+// val[off[k]] += v[k]: K entries added at node pairs of the element pattern
+__global__ void k_add_entries(int n, const int* __restrict__ off, const double* __restrict__ v,
+                              double* __restrict__ val) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) atomicAdd(&val[off[k]], v[k]);
+}
+
+// Re-uploads the extra blocks (pattern and values) after a change.
+tf_status upload_extra(tf_handle* h, bool pattern_changed) {
+    Device& d = h->d;
+    if (pattern_changed) {
+        cudaFree(d.xrow);
+        cudaFree(d.xcol);
+        cudaFree(d.xval);
+        d.xrow = d.xcol = nullptr;
+        d.xval = nullptr;
+        std::vector<int> col;
+        h->h_xrow.assign(d.nn + 1, 0);
+        for (int i = 0; i < d.nn; ++i) {
+            col.insert(col.end(), h->h_xcols[i].begin(), h->h_xcols[i].end());
+            h->h_xrow[i + 1] = static_cast<int>(col.size());
+        }
+        d.nxb = static_cast<int64_t>(col.size());
+        TF_TRY(upload(&d.xrow, h->h_xrow));
+        TF_TRY(upload(&d.xcol, col));
+        TF_TRY(dev_alloc(&d.xval, 9 * (size_t)d.nxb));
+        destroy_graphs(h);  // the captured Krylov chunks hold the extra-block pointers
+    }
+    TF_CUDA(cudaMemcpyAsync(d.xval, h->h_xval.data(), sizeof(double) * 9 * (size_t)d.nxb, cudaMemcpyHostToDevice,
+                            h->stream));
+    return sync(h);
+}
+
 }  // namespace tf
 
 using namespace tf;
 
 extern "C" {
+
+tf_status tf_add_K_triplets(tf_handle* h, int64_t n, const int32_t* rows, const int32_t* cols, const double* vals) {
+    TF_TRY(check_handle(h));
+    if (n < 0 || (n > 0 && (!rows || !cols || !vals))) return set_error("tf_add_K_triplets: bad arguments"), TF_BAD_INPUT;
+    if (!h->assembled) return set_error("tf_add_K_triplets called before tf_assemble"), TF_BAD_INPUT;
+    Device& d = h->d;
+    const int64_t n3 = 3 * (int64_t)d.nn;
+    if (h->h_xcols.empty()) h->h_xcols.resize(d.nn);
+    std::vector<int> off;
+    std::vector<double> v;
+    struct Pending {
+        int J, I, e;
+        double v;
+    };
+    std::vector<Pending> extra;
+    bool changed = false;
+    for (int64_t k = 0; k < n; ++k) {
+        const int64_t r = rows[k], c = cols[k];
+        if (r < 0 || r >= n3 || c < 0 || c >= n3)
+            return set_error("tf_add_K_triplets: entry " + std::to_string(k) + " is out of range"), TF_BAD_INPUT;
+        if (h->h_fixed[r] || h->h_fixed[c]) continue;  // calcutateFixedK runs after these writers
+        // K(r, c) is A(c, r): block (J, I) = (c/3, r/3), entry (c%3, r%3)
+        const int J = static_cast<int>(c / 3), I = static_cast<int>(r / 3);
+        const int e = static_cast<int>(3 * (c % 3) + (r % 3));
+        auto b = h->h_colidx.begin() + h->h_rowptr[J], en = h->h_colidx.begin() + h->h_rowptr[J + 1];
+        auto it = std::lower_bound(b, en, I);
+        if (it != en && *it == I) {
+            off.push_back(h->h_bofs[it - h->h_colidx.begin()] + kSlice * e);
+            v.push_back(vals[k]);
+        } else {
+            std::vector<int>& xc = h->h_xcols[J];
+            auto jt = std::lower_bound(xc.begin(), xc.end(), I);
+            if (jt == xc.end() || *jt != I) {
+                xc.insert(jt, I);
+                changed = true;
+            }
+            extra.push_back({J, I, e, vals[k]});
+        }
+    }
+    if (changed) {
+        // new layout; the values accumulated so far in this assembly move with their blocks
+        int64_t nxb = 0;
+        for (const auto& xc : h->h_xcols) nxb += (int64_t)xc.size();
+        std::vector<double> nv(9 * (size_t)nxb, 0.0);
+        std::vector<int> row(d.nn + 1, 0);
+        for (int i = 0; i < d.nn; ++i) row[i + 1] = row[i] + static_cast<int>(h->h_xcols[i].size());
+        if (!h->h_xrow.empty())
+            for (int i = 0; i < d.nn; ++i)
+                for (int p = h->h_xrow[i]; p < h->h_xrow[i + 1]; ++p) {
+                    const auto& xc = h->h_xcols[i];
+                    const int q = row[i] + static_cast<int>(
+                                               std::lower_bound(xc.begin(), xc.end(), h->h_xcol_prev[p]) - xc.begin());
+                    for (int t = 0; t < 9; ++t) nv[9 * (size_t)q + t] = h->h_xval[9 * (size_t)p + t];
+                }
+        h->h_xval.swap(nv);
+        h->h_xcol_prev.clear();
+        for (const auto& xc : h->h_xcols) h->h_xcol_prev.insert(h->h_xcol_prev.end(), xc.begin(), xc.end());
+    }
+    if (!extra.empty() || changed) {
+        std::vector<int> row(d.nn + 1, 0);
+        for (int i = 0; i < d.nn; ++i) row[i + 1] = row[i] + static_cast<int>(h->h_xcols[i].size());
+        for (const Pending& q : extra) {
+            const auto& xc = h->h_xcols[q.J];
+            const int p = row[q.J] + static_cast<int>(std::lower_bound(xc.begin(), xc.end(), q.I) - xc.begin());
+            h->h_xval[9 * (size_t)p + q.e] += q.v;
+        }
+        TF_TRY(upload_extra(h, changed));
+    }
+    if (!off.empty()) {
+        int* doff = nullptr;
+        double* dv = nullptr;
+        TF_TRY(upload(&doff, off));
+        const tf_status s = upload(&dv, v);
+        if (s != TF_OK) {
+            cudaFree(doff);
+            return s;
+        }
+        const int m = static_cast<int>(off.size());
+        k_add_entries<<<cdiv(m, 256), 256, 0, h->stream>>>(m, doff, dv, d.val);
+        const cudaError_t e1 = cudaGetLastError();
+        const cudaError_t e2 = cudaStreamSynchronize(h->stream);
+        cudaFree(doff);
+        cudaFree(dv);
+        if (e1 != cudaSuccess) return cuda_fail(e1, "k_add_entries");
+        if (e2 != cudaSuccess) return cuda_fail(e2, "k_add_entries");
+        h->launches++;
+    }
+    amg_mark_stale(h, 1);
+    return TF_OK;
+}
+
 
 const char* tf_status_string(tf_status s) {
     switch (s) {
@@ -787,6 +911,10 @@ tf_status tf_begin_step(tf_handle* h, double dt) {
 tf_status tf_assemble(tf_handle* h) {
     TF_TRY(check_handle(h));
     amg_mark_stale(h, 1);
+    if (h->d.nxb > 0) {  // K entries added outside the element pattern belong to one assembly
+        std::fill(h->h_xval.begin(), h->h_xval.end(), 0.0);
+        TF_CUDA(cudaMemsetAsync(h->d.xval, 0, sizeof(double) * 9 * (size_t)h->d.nxb, h->stream));
+    }
     TF_TRY(autotune_element(h));
     TF_TRY(launch_prepare(h));
     TF_TRY(launch_element(h));
@@ -898,20 +1026,26 @@ tf_status tf_export_csr(tf_handle* h, double drop_tol, int32_t* ia, int32_t* ja,
         auto it = std::lower_bound(ci.begin() + rp[r], ci.begin() + rp[r + 1], c);
         return static_cast<int64_t>(it - ci.begin());
     };
+    // extra blocks A(J, I) from tf_add_K_triplets, listed by the K row I they touch
+    std::vector<std::vector<std::pair<int, int64_t>>> xby(d.nn);
+    if (d.nxb > 0)
+        for (int J = 0; J < d.nn; ++J)
+            for (int p = h->h_xrow[J]; p < h->h_xrow[J + 1]; ++p) xby[h->h_xcol_prev[p]].push_back({J, p});
+    for (auto& v : xby) std::sort(v.begin(), v.end());
     // K(3i+di, 3j+dj) = A(3j+dj, 3i+di): block (j, i) of A, entry (dj, di).
     int64_t q = 0;
     if (ia) ia[0] = 0;
     for (int i = 0; i < d.nn; ++i)
         for (int di = 0; di < 3; ++di) {
             const int r = 3 * i + di;
-            for (int p = rp[i]; p < rp[i + 1]; ++p) {
-                const int j = ci[p];
-                const int64_t bt = find_block(j, i);
+            size_t xk = 0;
+            const auto& xi = xby[i];
+            auto emit = [&](int j, const double* blk, int stride) {
                 for (int dj = 0; dj < 3; ++dj) {
                     const int c = 3 * j + dj;
                     double v;
                     if (h->h_fixed[r] || h->h_fixed[c]) v = (r == c) ? 1.0 : 0.0;
-                    else v = val[(size_t)h->h_bofs[bt] + kSlice * (3 * dj + di)];
+                    else v = blk[stride * (3 * dj + di)];
                     if (v > drop_tol || v < -drop_tol) {
                         if (ia) {
                             ja[q] = c;
@@ -920,7 +1054,14 @@ tf_status tf_export_csr(tf_handle* h, double drop_tol, int32_t* ia, int32_t* ja,
                         ++q;
                     }
                 }
+            };
+            for (int p = rp[i]; p < rp[i + 1]; ++p) {
+                const int j = ci[p];
+                for (; xk < xi.size() && xi[xk].first < j; ++xk)
+                    emit(xi[xk].first, &h->h_xval[9 * (size_t)xi[xk].second], 1);
+                emit(j, &val[(size_t)h->h_bofs[find_block(j, i)]], kSlice);
             }
+            for (; xk < xi.size(); ++xk) emit(xi[xk].first, &h->h_xval[9 * (size_t)xi[xk].second], 1);
             if (ia) ia[r + 1] = static_cast<int32_t>(q);
         }
     *nnz = q;

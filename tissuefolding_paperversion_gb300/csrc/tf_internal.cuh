@@ -91,6 +91,13 @@ struct Device {
     int* seg_cta0 = nullptr;    // [nseg+1] CTA ranges per instance
     int* seg_active = nullptr;  // [nseg] 1 while the instance's Newton loop runs
     int* seg_solve = nullptr;   // [nseg] instances a linear solve works on
+    // blocks of K entries added through tf_add_K_triplets at node pairs outside
+    // the element pattern (contact-type couplings): CSR over block rows of A,
+    // row-major 3x3 values, cleared at every assembly
+    int* xrow = nullptr;        // [nn+1] (null: none)
+    int* xcol = nullptr;        // [nxb]
+    double* xval = nullptr;     // [9 nxb]
+    int64_t nxb = 0;
     // adjoint (allocated by the first tf_adj_forward)
     int* tblk = nullptr;        // [nnzb] block index of the transposed block
     double* valT = nullptr;     // [9*nnzb] transposed block values
@@ -185,6 +192,10 @@ struct tf_handle {
     int method = 1;  // 1 CG, 2 BiCGStab
     std::vector<int> h_conn;
     std::vector<int> h_rowptr, h_colidx, h_bofs;
+    std::vector<std::vector<int>> h_xcols;      // extra block columns per block row (sorted)
+    std::vector<int> h_xrow;                    // CSR offsets of the extra blocks on the device
+    std::vector<int> h_xcol_prev;               // their columns in that layout
+    std::vector<double> h_xval;                 // their values of the current assembly
     std::vector<uint8_t> h_fixed;
     std::vector<double> h_nu;                   // Poisson ratios, clamped as the material setup does
     std::vector<int> h_apical;                  // 1 for apical nodes (tissue placement 1)

@@ -49,6 +49,9 @@ struct Ctx {
     const int* __restrict__ cta_node1;
     const int* __restrict__ seg_cta0;
     const int* __restrict__ seg_solve;
+    const int* __restrict__ xrow;     // extra blocks (tf_add_K_triplets), null: none
+    const int* __restrict__ xcol;
+    const double* __restrict__ xval;
 };
 
 struct Where {
@@ -129,8 +132,18 @@ __device__ __forceinline__ void apply_dinv(const double* __restrict__ D, const d
     z[2] = fma(D[6], r[0], fma(D[7], r[1], D[8] * r[2]));
 }
 
-__device__ __forceinline__ void bsr_row(const Ctx& c, const double* __restrict__ x, double y[3]) {
+__device__ __forceinline__ void bsr_row(const Ctx& c, int i, const double* __restrict__ x, double y[3]) {
     sliced_row(c.wslot0, c.scol, c.val, x, y);
+    if (c.xrow) {
+        for (int p = c.xrow[i]; p < c.xrow[i + 1]; ++p) {
+            const int j = c.xcol[p];
+            const double* __restrict__ a = c.xval + 9 * (size_t)p;
+            const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+            y[0] = fma(a[0], x0, fma(a[1], x1, fma(a[2], x2, y[0])));
+            y[1] = fma(a[3], x0, fma(a[4], x1, fma(a[5], x2, y[1])));
+            y[2] = fma(a[6], x0, fma(a[7], x1, fma(a[8], x2, y[2])));
+        }
+    }
 }
 
 // Sets an instance's stop flag from its first scalars (bb = |b|^2).
@@ -196,7 +209,7 @@ __global__ void k_cg_spmv(Ctx c, const double* __restrict__ p, double* __restric
     double v[1] = {0.0};
     if (w.valid) {
         double y[3];
-        bsr_row(c, p, y);
+        bsr_row(c, w.node, p, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             q[3 * w.node + d] = y[d];
@@ -373,7 +386,7 @@ __global__ void k_bi_spmv1(Ctx c, const double* __restrict__ phat, const double*
     double s[1] = {0.0};
     if (w.valid) {
         double y[3];
-        bsr_row(c, phat, y);
+        bsr_row(c, w.node, phat, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             v[3 * w.node + d] = y[d];
@@ -457,7 +470,7 @@ __global__ void k_bi_spmv2(Ctx c, const double* __restrict__ shat, const double*
     double acc[2] = {0.0, 0.0};
     if (w.valid) {
         double y[3];
-        bsr_row(c, shat, y);
+        bsr_row(c, w.node, shat, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             t[3 * w.node + d] = y[d];
@@ -585,6 +598,9 @@ Ctx make_ctx(tf_handle* h) {
     c.cta_node1 = d.cta_node1;
     c.seg_cta0 = d.seg_cta0;
     c.seg_solve = d.seg_solve;
+    c.xrow = d.nxb > 0 ? d.xrow : nullptr;
+    c.xcol = d.xcol;
+    c.xval = d.xval;
     return c;
 }
 
