@@ -293,48 +293,73 @@ def run_assembly_only(args, t):
 def run_batch(args):
     """Batched sweep: 256 tissues of 1k-50k prisms in one handle vs the plain
     GPU step looped over the instances (one handle each).  Metric: instance
-    time steps (implicit solves) per second."""
-    from tissuefolding_paperversion_gb300 import api, mesh
+    time steps (implicit solves) per second.  Under torchrun the instances are
+    sharded over the ranks (balanced by prism count, no exchange; timings are
+    the max over ranks), so the total work is fixed: strong scaling."""
+    from tissuefolding_paperversion_gb300 import api, mesh, shard
 
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # noqa: F811
+
+        dist.init_process_group("gloo")
     n = args.instances
-    ts = [mesh.config_batch_instance(s) for s in range(n)]
-    prisms = sum(t.n_elems for t in ts)
-    b = api.Batch(ts)
+    ts_all = [mesh.config_batch_instance(s) for s in range(n)]
+    mine = shard.shard_instances([t.n_elems for t in ts_all], world)[rank]
+    ts = [ts_all[i] for i in mine]
+    prisms = sum(t.n_elems for t in ts_all)
+    dev = local if world > 1 else 0
+
+    def slowest(x):
+        return shard.max_over_ranks(dist, x) if dist is not None else x
+
+    b = api.Batch(ts, device=dev)
     b.set_growth_rates()
     for _ in range(args.warmup):
         b.step(ts[0].dt)
+    if dist is not None:
+        dist.barrier()
     l0 = b.launch_count()
     w0 = time.perf_counter()
     outs = [b.step(ts[0].dt) for _ in range(args.steps)]
-    wall_b = time.perf_counter() - w0
+    wall_b = slowest(time.perf_counter() - w0)
     launches = b.launch_count() - l0
-    ms_b = sum(o["ms_total"] for o in outs)
+    ms_b = slowest(sum(o["ms_total"] for o in outs))
     ept = b.elements_per_cta()
     b.close()
     solvers = []
     for t in ts:
-        s = api.Solver(t)
+        s = api.Solver(t, device=dev)
         s.set_growth_rates(t.rates)
         solvers.append(s)
     for s, t in zip(solvers, ts):
         for _ in range(max(1, args.warmup)):
             s.newton_step(t.dt)
     loop_steps = max(1, min(args.steps, 2))
+    if dist is not None:
+        dist.barrier()
     w0 = time.perf_counter()
     ms_l = 0.0
     for _ in range(loop_steps):
         for s, t in zip(solvers, ts):
             ms_l += s.newton_step(t.dt)["ms_total"]
-    wall_l = time.perf_counter() - w0
+    wall_l = slowest(time.perf_counter() - w0)
+    ms_l = slowest(ms_l)
     for s in solvers:
         s.close()
     rate_b = n * args.steps / wall_b
     rate_l = n * loop_steps / wall_l
+    if rank != 0:
+        return
     print(json.dumps({
-        "metric": "batched implicit solves/s", "value": rate_b, "unit": "instance steps/s", "n_gpus": 1,
+        "metric": "batched implicit solves/s", "value": rate_b, "unit": "instance steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall_b / args.steps * 1e3, "higher_is_better": True,
-        "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"batch-{n}", "instances": n, "prisms": prisms, "elements_per_cta": ept},
+        "scaling": "strong", "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"batch-{n}", "instances": n, "prisms": prisms, "elements_per_cta": ept,
+                   "parallelism": f"instances sharded over {world} ranks" if world > 1 else "single"},
         "looped_plain": {"value": rate_l, "unit": "instance steps/s", "steps": loop_steps,
                          "device_ms_per_step": ms_l / loop_steps},
         "speedup_vs_looped": rate_b / rate_l,
