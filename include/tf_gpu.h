@@ -144,6 +144,12 @@ TF_API tf_status tf_add_external_forces(tf_handle* h, const double* gext);
  * cleared by the next tf_assemble.  tf_export_csr includes them. */
 TF_API tf_status tf_add_K_triplets(tf_handle* h, int64_t n, const int32_t* rows, const int32_t* cols,
                                    const double* vals);
+/* Bound DOF couples, NRSolver->slaveMasterList (Simulation.cpp:505-513):
+ * before each solve K_bound = N^T K N + I and g_bound = N^T g couple by couple
+ * (calculateBoundKWithSlavesMasterDoF, NewtonRaphsonSolver.cpp:154-235), after
+ * it du[slave] = du[master] (equateSlaveDisplacementsToMasters, :237-251).
+ * DOF indices (3*node + dim); n = 0 removes them. */
+TF_API tf_status tf_set_dof_bindings(tf_handle* h, int32_t n, const int32_t* slave_dofs, const int32_t* master_dofs);
 /* solveForDeltaU (NewtonRaphsonSolver.cpp:382-404): solves K^T du = g, the
  * transposed system Pardiso is asked for (iparm[11] = 1, :639). */
 TF_API tf_status tf_solve(tf_handle* h, int32_t* iters, double* relres);

@@ -285,6 +285,8 @@ class Ref:
             L.tfr_get_system.argtypes = [C.c_void_p, _ip, _ip, _dp, _dp]
             L.tfr_step.restype = C.c_int
             L.tfr_step.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.POINTER(C.c_int), _dp, C.c_int]
+            L.tfr_set_bindings.restype = None
+            L.tfr_set_bindings.argtypes = [C.c_void_p, C.c_int, _ip, _ip]
             cls._lib = L
         return cls._lib
 
@@ -367,6 +369,12 @@ class Ref:
         g = np.zeros(3 * self.nn)
         self.lib().tfr_get_system(self.h, ia, ja, a, g)
         return ia, ja, a, g
+
+    def set_bindings(self, slave_dofs, master_dofs):
+        s = _i32(slave_dofs)
+        m = _i32(master_dofs)
+        self._bind = (s, m)
+        self.lib().tfr_set_bindings(self.h, int(s.size), s, m)
 
     def step(self, dt, rates=None):
         it = C.c_int(0)

@@ -314,6 +314,15 @@ void tfr_get_system(void* h, int* ia, int* ja, double* a, double* g) {
 // Writes the number of Newton solves and the |du| of each into iters / dunorm
 // (capacity max_hist).  Returns 1 when the reference's non-convergence branch
 // was taken, else 0.
+// NRSolver->slaveMasterList and boundNodesWithSlaveMasterDefinition as
+// Simulation::initiateSystem sets them for bound nodes (Simulation.cpp:505-513).
+void tfr_set_bindings(void* h, int n, const int* slave_dofs, const int* master_dofs) {
+    RefSim* s = static_cast<RefSim*>(h);
+    s->nr->slaveMasterList.clear();
+    for (int k = 0; k < n; ++k) s->nr->slaveMasterList.push_back({slave_dofs[k], master_dofs[k]});
+    s->nr->boundNodesWithSlaveMasterDefinition = n > 0;
+}
+
 int tfr_step(void* h, double dt, const double* rates, int* iters, double* dunorm, int max_hist) {
     RefSim* s = static_cast<RefSim*>(h);
     if (rates) tfr_grow(h, dt, rates);

@@ -60,7 +60,41 @@ def steps_fixture(name, t, n_steps, seed_note):
     return time.time() - t0
 
 
+def bound_dofs(t):
+    """Slave/master DOF couples for the binding fixture: x of two apical nodes
+    that share an element, z of two apical nodes at opposite corners (not
+    element neighbours), y of two middle-layer nodes."""
+    pos = t.pos.reshape(-1, 3)
+    ap = np.flatnonzero(t.node_placement == 1)
+    mid = np.flatnonzero(t.node_placement == 2)
+    c = t.conn.reshape(-1, 6)
+    e0 = [e for e in range(c.shape[0]) if t.node_placement[c[e, 3]] == 1][0]
+    a_lo = ap[np.argmin(pos[ap, 0] + pos[ap, 1])]
+    a_hi = ap[np.argmax(pos[ap, 0] + pos[ap, 1])]
+    slaves = [3 * c[e0, 4] + 0, 3 * a_hi + 2, 3 * mid[-1] + 1]
+    masters = [3 * c[e0, 3] + 0, 3 * a_lo + 2, 3 * mid[0] + 1]
+    return np.array(slaves, dtype=np.int32), np.array(masters, dtype=np.int32)
+
+
+def bound_steps_fixture(name, t, n_steps, seed_note):
+    r = Ref(t)
+    s, m = bound_dofs(t)
+    r.set_bindings(s, m)
+    pos, iters = [], []
+    for _ in range(n_steps):
+        out = r.step(t.dt, t.rates)
+        pos.append(r.positions())
+        iters.append(out["iters"])
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), positions=np.array(pos), iters=np.array(iters),
+                        slaves=s, masters=m, note=seed_note)
+    r.close()
+
+
 def main():
+    if "--only-bound" in sys.argv:
+        t = mesh.config_tiny(seed=15, n=5, n_layers=2, eta=100.0)
+        bound_steps_fixture("steps_tiny_bound", t, 4, "config_tiny(seed=15,n=5,n_layers=2,eta=100), bound_dofs(t)")
+        return
     element_fixture("elem_tiny_elastic", 0.0, 11)
     element_fixture("elem_tiny_viscous", 100.0, 12)
     t = mesh.config_tiny(seed=13, n=4, n_layers=2, eta=0.0)
@@ -69,6 +103,8 @@ def main():
     print("tiny viscous steps", steps_fixture("steps_tiny_viscous", t, 5, "config_tiny(seed=14,n=4,n_layers=2,eta=100)"))
     t = mesh.config_small(seed=0)
     print("small steps", steps_fixture("steps_small", t, t.n_steps, "config_small(seed=0)"))
+    t = mesh.config_tiny(seed=15, n=5, n_layers=2, eta=100.0)
+    bound_steps_fixture("steps_tiny_bound", t, 4, "config_tiny(seed=15,n=5,n_layers=2,eta=100), bound_dofs(t)")
 
 
 if __name__ == "__main__":

@@ -152,3 +152,13 @@ def test_elastic_tangent_symmetric():
     ev = p.element_eval(uk, un, t.dt, LITERAL)
     Ke = ev["Ke"]
     assert _rel(Ke, np.transpose(Ke, (0, 2, 1))) <= 1e-12
+
+
+def test_bound_fixture_moves_couples_together():
+    """The binding fixture came from the reference's own solver: every slave
+    DOF moved by exactly its master's displacement."""
+    f = np.load(os.path.join(GOLD, "steps_tiny_bound.npz"))
+    t = mesh.config_tiny(seed=15, n=5, n_layers=2, eta=100.0)
+    d = f["positions"][-1] - t.pos
+    np.testing.assert_allclose(d[f["slaves"]], d[f["masters"]], rtol=0, atol=1e-12)
+    assert np.abs(d[f["slaves"]]).max() > 1e-3

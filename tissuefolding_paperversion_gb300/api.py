@@ -31,7 +31,7 @@ EXPORTED = [
     "tf_element_eval", "tf_get_sizes", "tf_get_stream", "tf_launch_count", "tf_time_assembly",
     "tf_solve_bsr_static", "tf_batch_create", "tf_batch_step", "tf_get_instances", "tf_elements_per_cta",
     "tf_adj_forward", "tf_adj_backward", "tf_adj_free", "tf_multigrid_info", "tf_read_mesh_file",
-    "tf_write_frame", "tf_add_K_triplets",
+    "tf_write_frame", "tf_add_K_triplets", "tf_set_dof_bindings",
 ]
 
 
@@ -123,6 +123,8 @@ def load(build_if_missing: bool = True):
     L.tf_adj_free.argtypes = [vp]
     L.tf_multigrid_info.restype = C.c_int
     L.tf_multigrid_info.argtypes = [vp, ip, vp, vp]
+    L.tf_set_dof_bindings.restype = C.c_int
+    L.tf_set_dof_bindings.argtypes = [vp, i32, vp, vp]
     L.tf_add_K_triplets.restype = C.c_int
     L.tf_add_K_triplets.argtypes = [vp, i64, vp, vp, vp]
     L.tf_read_mesh_file.restype = C.c_int
@@ -250,6 +252,13 @@ class Solver:
     def add_external_forces(self, gext):
         g = np.ascontiguousarray(gext, dtype=np.float64)
         self._check(self.L.tf_add_external_forces(self.h, _ptr(g)), "tf_add_external_forces")
+
+    def set_dof_bindings(self, slave_dofs, master_dofs):
+        """Bound DOF couples (slave follows master), applied at every solve."""
+        s = np.ascontiguousarray(slave_dofs, dtype=np.int32)
+        m = np.ascontiguousarray(master_dofs, dtype=np.int32)
+        self._bind = (s, m)
+        self._check(self.L.tf_set_dof_bindings(self.h, s.size, _ptr(s), _ptr(m)), "tf_set_dof_bindings")
 
     def add_K_triplets(self, rows, cols, vals):
         """K(rows[k], cols[k]) += vals[k] after assemble() (packing/myosin-type writers)."""

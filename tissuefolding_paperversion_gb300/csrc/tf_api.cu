@@ -4,6 +4,9 @@
 // sequence driven by Simulation::updateStepNR
 // (TissueFolding/TissueFolding/SourceCode/Simulation.cpp:6449-6590).
 #include <algorithm>
+#include <array>
+#include <map>
+#include <tuple>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -625,11 +628,221 @@ tf_status upload_extra(tf_handle* h, bool pattern_changed) {
     return sync(h);
 }
 
+// out[9k + e] = val[off[k] + 32 e] (gather of sliced blocks) and back
+__global__ void k_blocks_get(int n, const int* __restrict__ off, const double* __restrict__ val,
+                             double* __restrict__ out) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) out[9 * (size_t)k + e] = val[off[k] + kSlice * e];
+}
+
+__global__ void k_blocks_set(int n, const int* __restrict__ off, const double* __restrict__ in,
+                             double* __restrict__ val) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) val[off[k] + kSlice * e] = in[9 * (size_t)k + e];
+}
+
+// du[slave] = du[master], couple by couple in their order
+// (NewtonRaphsonSolver::equateSlaveDisplacementsToMasters, NewtonRaphsonSolver.cpp:237-251)
+__global__ void k_equate(int n, const int* __restrict__ slave, const int* __restrict__ master, double* du) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    for (int k = 0; k < n; ++k) du[slave[k]] = du[master[k]];
+}
+
+// K_bound = N^T K N + I, g_bound = N^T g couple by couple, as
+// NewtonRaphsonSolver::calculateBoundKWithSlavesMasterDoF
+// (NewtonRaphsonSolver.cpp:154-235) does on its dense K: the slave row is
+// added to the master row and zeroed, then the slave column to the master
+// column, then K(slave, slave) = 1.  The blocks of the nodes involved are
+// brought to the host, changed there and written back; blocks the merges
+// create outside the element pattern join the extra blocks.
+tf_status apply_bindings(tf_handle* h) {
+    Device& d = h->d;
+    const int nc = static_cast<int>(h->bind_slave.size());
+    std::vector<char> involved(d.nn, 0);
+    for (int k = 0; k < nc; ++k) {
+        involved[h->bind_slave[k] / 3] = 1;
+        involved[h->bind_master[k] / 3] = 1;
+    }
+    // blocks (J, I) with J or I involved: pattern blocks by offset, extras by index
+    using Key = std::pair<int, int>;
+    std::map<Key, std::array<double, 9>> blk;
+    std::vector<Key> pkeys;
+    std::vector<int> poff;
+    auto find_block = [&](int r, int c) -> int64_t {
+        auto b = h->h_colidx.begin() + h->h_rowptr[r], en = h->h_colidx.begin() + h->h_rowptr[r + 1];
+        auto it = std::lower_bound(b, en, c);
+        return (it != en && *it == c) ? static_cast<int64_t>(it - h->h_colidx.begin()) : -1;
+    };
+    for (int X = 0; X < d.nn; ++X) {
+        if (!involved[X]) continue;
+        for (int p = h->h_rowptr[X]; p < h->h_rowptr[X + 1]; ++p) {
+            const int C = h->h_colidx[p];
+            for (const Key& k : {Key{X, C}, Key{C, X}}) {
+                if (blk.count(k)) continue;
+                blk[k] = {};
+                pkeys.push_back(k);
+                poff.push_back(h->h_bofs[find_block(k.first, k.second)]);
+            }
+        }
+    }
+    // extra blocks in those rows and columns
+    std::vector<int> xrow(d.nn + 1, 0);
+    if (!h->h_xcols.empty())
+        for (int i = 0; i < d.nn; ++i) xrow[i + 1] = xrow[i] + static_cast<int>(h->h_xcols[i].size());
+    if (!h->h_xcols.empty())
+        for (int J = 0; J < d.nn; ++J)
+            for (size_t q = 0; q < h->h_xcols[J].size(); ++q) {
+                const int I = h->h_xcols[J][q];
+                if (!involved[J] && !involved[I]) continue;
+                std::array<double, 9> v;
+                for (int e = 0; e < 9; ++e) v[e] = h->h_xval[9 * (size_t)(xrow[J] + q) + e];
+                blk[{J, I}] = v;
+            }
+    const int npb = static_cast<int>(pkeys.size());
+    if (npb > 0) {
+        int* doff = nullptr;
+        double* dbuf = nullptr;
+        TF_TRY(upload(&doff, poff));
+        if (dev_alloc(&dbuf, 9 * (size_t)npb) != TF_OK) {
+            cudaFree(doff);
+            return TF_OUT_OF_MEMORY;
+        }
+        std::vector<double> hb(9 * (size_t)npb);
+        k_blocks_get<<<cdiv(npb, 256), 256, 0, h->stream>>>(npb, doff, d.val, dbuf);
+        cudaError_t e = cudaMemcpyAsync(hb.data(), dbuf, hb.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) {
+            cudaFree(doff);
+            cudaFree(dbuf);
+            return cuda_fail(e, "binding: block gather");
+        }
+        for (int k = 0; k < npb; ++k)
+            for (int q = 0; q < 9; ++q) blk[pkeys[k]][q] = hb[9 * (size_t)k + q];
+        // the couples, in order (K(r, c) is entry (c%3, r%3) of block (c/3, r/3))
+        std::vector<double> g(3 * (size_t)d.nn);
+        e = cudaMemcpyAsync(g.data(), d.g, g.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) {
+            cudaFree(doff);
+            cudaFree(dbuf);
+            return cuda_fail(e, "binding: rhs download");
+        }
+        bool changed = false;
+        for (int k = 0; k < nc; ++k) {
+            const int sd = h->bind_slave[k], md = h->bind_master[k];
+            const int S = sd / 3, M = md / 3, ds = sd % 3, dm = md % 3;
+            g[md] += g[sd];
+            g[sd] = 0.0;
+            // K row m += K row s; K row s = 0: column S of A into column M
+            std::vector<Key> colS;
+            for (auto& kv : blk)
+                if (kv.first.second == S) colS.push_back(kv.first);
+            for (const Key& key : colS)
+                for (int dc = 0; dc < 3; ++dc) {
+                    double& v = blk[key][3 * dc + ds];
+                    if (v == 0.0) continue;
+                    const Key tgt{key.first, M};
+                    if (!blk.count(tgt)) blk[tgt] = {};
+                    blk[tgt][3 * dc + dm] += v;
+                    v = 0.0;
+                }
+            // K column m += K column s; K column s = 0: row S of A into row M
+            std::vector<Key> rowS;
+            for (auto& kv : blk)
+                if (kv.first.first == S) rowS.push_back(kv.first);
+            for (const Key& key : rowS)
+                for (int dr = 0; dr < 3; ++dr) {
+                    double& v = blk[key][3 * ds + dr];
+                    if (v == 0.0) continue;
+                    const Key tgt{M, key.second};
+                    if (!blk.count(tgt)) blk[tgt] = {};
+                    blk[tgt][3 * dm + dr] += v;
+                    v = 0.0;
+                }
+            blk[{S, S}][3 * ds + ds] = 1.0;
+        }
+        // write back: pattern blocks through their offsets, the rest as extra blocks
+        for (int k = 0; k < npb; ++k)
+            for (int q = 0; q < 9; ++q) hb[9 * (size_t)k + q] = blk[pkeys[k]][q];
+        e = cudaMemcpyAsync(dbuf, hb.data(), hb.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream);
+        if (e == cudaSuccess) {
+            k_blocks_set<<<cdiv(npb, 256), 256, 0, h->stream>>>(npb, doff, dbuf, d.val);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(d.g, g.data(), g.size() * sizeof(double), cudaMemcpyHostToDevice,
+                                                  h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        cudaFree(doff);
+        cudaFree(dbuf);
+        if (e != cudaSuccess) return cuda_fail(e, "binding: write back");
+        h->launches += 2;
+        if (h->h_xcols.empty()) h->h_xcols.resize(d.nn);
+        std::vector<std::tuple<int, int, std::array<double, 9>>> extra;
+        for (auto& kv : blk) {
+            if (find_block(kv.first.first, kv.first.second) >= 0) continue;
+            std::vector<int>& xc = h->h_xcols[kv.first.first];
+            auto jt = std::lower_bound(xc.begin(), xc.end(), kv.first.second);
+            if (jt == xc.end() || *jt != kv.first.second) {
+                xc.insert(jt, kv.first.second);
+                changed = true;
+            }
+            extra.emplace_back(kv.first.first, kv.first.second, kv.second);
+        }
+        if (!extra.empty()) {
+            std::vector<int> row(d.nn + 1, 0);
+            for (int i = 0; i < d.nn; ++i) row[i + 1] = row[i] + static_cast<int>(h->h_xcols[i].size());
+            auto slot = [&](int J, int I) {
+                const auto& xc = h->h_xcols[J];
+                return row[J] + static_cast<int>(std::lower_bound(xc.begin(), xc.end(), I) - xc.begin());
+            };
+            if (changed) {  // new layout: the other extra blocks keep their values
+                std::vector<double> nv(9 * (size_t)row[d.nn], 0.0);
+                if (!h->h_xrow.empty())
+                    for (int i = 0; i < d.nn; ++i)
+                        for (int p = h->h_xrow[i]; p < h->h_xrow[i + 1]; ++p) {
+                            const int q = slot(i, h->h_xcol_prev[p]);
+                            for (int t = 0; t < 9; ++t) nv[9 * (size_t)q + t] = h->h_xval[9 * (size_t)p + t];
+                        }
+                h->h_xval.swap(nv);
+                h->h_xcol_prev.clear();
+                for (const auto& xc : h->h_xcols) h->h_xcol_prev.insert(h->h_xcol_prev.end(), xc.begin(), xc.end());
+            }
+            for (const auto& x : extra) {
+                const int p = slot(std::get<0>(x), std::get<1>(x));
+                for (int q = 0; q < 9; ++q) h->h_xval[9 * (size_t)p + q] = std::get<2>(x)[q];
+            }
+            TF_TRY(upload_extra(h, changed));
+        }
+    }
+    h->bound_applied = true;
+    amg_mark_stale(h, 1);
+    return TF_OK;
+}
+
 }  // namespace tf
 
 using namespace tf;
 
 extern "C" {
+
+tf_status tf_set_dof_bindings(tf_handle* h, int32_t n, const int32_t* slave_dofs, const int32_t* master_dofs) {
+    TF_TRY(check_handle(h));
+    if (n < 0 || (n > 0 && (!slave_dofs || !master_dofs))) return set_error("tf_set_dof_bindings: bad arguments"), TF_BAD_INPUT;
+    const int64_t n3 = 3 * (int64_t)h->d.nn;
+    for (int k = 0; k < n; ++k)
+        if (slave_dofs[k] < 0 || slave_dofs[k] >= n3 || master_dofs[k] < 0 || master_dofs[k] >= n3 ||
+            slave_dofs[k] == master_dofs[k])
+            return set_error("tf_set_dof_bindings: couple " + std::to_string(k) + " is invalid"), TF_BAD_INPUT;
+    h->bind_slave.assign(slave_dofs, slave_dofs + n);
+    h->bind_master.assign(master_dofs, master_dofs + n);
+    h->bound_applied = false;
+    return TF_OK;
+}
+
 
 tf_status tf_add_K_triplets(tf_handle* h, int64_t n, const int32_t* rows, const int32_t* cols, const double* vals) {
     TF_TRY(check_handle(h));
@@ -911,6 +1124,7 @@ tf_status tf_begin_step(tf_handle* h, double dt) {
 tf_status tf_assemble(tf_handle* h) {
     TF_TRY(check_handle(h));
     amg_mark_stale(h, 1);
+    h->bound_applied = false;
     if (h->d.nxb > 0) {  // K entries added outside the element pattern belong to one assembly
         std::fill(h->h_xval.begin(), h->h_xval.end(), 0.0);
         TF_CUDA(cudaMemsetAsync(h->d.xval, 0, sizeof(double) * 9 * (size_t)h->d.nxb, h->stream));
@@ -939,9 +1153,25 @@ tf_status tf_add_external_forces(tf_handle* h, const double* gext) {
 tf_status tf_solve(tf_handle* h, int32_t* iters, double* relres) {
     TF_TRY(check_handle(h));
     if (!h->assembled) return set_error("tf_solve called before tf_assemble"), TF_BAD_INPUT;
+    if (!h->bind_slave.empty() && !h->bound_applied) TF_TRY(apply_bindings(h));
     int it = 0;
     double rr = 0.0;
     tf_status s = krylov_solve(h, &it, &rr);
+    if (!h->bind_slave.empty() && (s == TF_OK || s == TF_KRYLOV_NOT_CONVERGED)) {
+        int* ds = nullptr;
+        int* dm = nullptr;
+        TF_TRY(upload(&ds, h->bind_slave));
+        if (upload(&dm, h->bind_master) != TF_OK) {
+            cudaFree(ds);
+            return TF_OUT_OF_MEMORY;
+        }
+        k_equate<<<1, 1, 0, h->stream>>>(static_cast<int>(h->bind_slave.size()), ds, dm, h->d.du);
+        const cudaError_t e = cudaStreamSynchronize(h->stream);
+        cudaFree(ds);
+        cudaFree(dm);
+        if (e != cudaSuccess) return cuda_fail(e, "k_equate");
+        h->launches++;
+    }
     if (iters) *iters = it;
     if (relres) *relres = rr;
     return s;

@@ -195,6 +195,8 @@ struct tf_handle {
     std::vector<std::vector<int>> h_xcols;      // extra block columns per block row (sorted)
     std::vector<int> h_xrow;                    // CSR offsets of the extra blocks on the device
     std::vector<int> h_xcol_prev;               // their columns in that layout
+    std::vector<int> bind_slave, bind_master;   // bound DOF couples (NRSolver::slaveMasterList)
+    bool bound_applied = false;                 // the couples are applied to the current assembly
     std::vector<double> h_xval;                 // their values of the current assembly
     std::vector<uint8_t> h_fixed;
     std::vector<double> h_nu;                   // Poisson ratios, clamped as the material setup does
