@@ -253,7 +253,8 @@ def run_gpu(args, t):
         "config": {"workload": t.name, "prisms": ne, "nodes": nn, "dof": 3 * nn, "block_nonzeros": nnzb,
                    "dt_s": t.dt, "l2": "inputs larger than L2 (no flush)", "parallelism": "replicas" if world > 1 else "single"},
         "newton": {"ms_per_step": step_ms, "assemblies_per_step": n_asm / len(stats),
-                   "preconditioner": "multigrid " + "/".join(map(str, mg_nodes)) if mg_nodes else "block-Jacobi",
+                   "preconditioner": (("plain-aggregation" if args.precond == 3 else "smoothed-aggregation")
+                                      + " multigrid " + "/".join(map(str, mg_nodes))) if mg_nodes else "block-Jacobi",
                    "krylov_iters_per_step": sum(x["krylov_total"] for x in stats) / len(stats),
                    "ms_assembly": ms_asm / n_asm, "wall_s": wall},
         "e2e": {"value": ne / e2e_s, "unit": "prisms/s", "h2d_bytes_per_step": 2 * 8 * 3 * nn,
@@ -445,7 +446,8 @@ def main():
                     help="step: Newton steps (the bench); assembly: back-to-back K+f assemblies only")
     ap.add_argument("--ref-seconds", type=float, default=15.0)
     ap.add_argument("--precond", type=int, default=0,
-                    help="0 auto (multigrid from 20,000 nodes), 1 block-Jacobi, 2 multigrid")
+                    help="0 auto (smoothed-aggregation multigrid from 20,000 nodes), 1 block-Jacobi, "
+                         "2 smoothed-aggregation multigrid, 3 plain-aggregation multigrid")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     from tissuefolding_paperversion_gb300 import mesh

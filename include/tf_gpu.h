@@ -75,8 +75,10 @@ typedef struct tf_options {
     int32_t deterministic;   /* 1: order-fixed assembly (no atomics); 0: atomic scatter */
     int32_t device;          /* CUDA device ordinal */
     int32_t autotune_off;    /* 1: keep 16 prisms per CTA instead of timing 8/16/32 on the mesh */
-    int32_t precond;         /* 0 auto (multigrid from 20,000 nodes on), 1 block-Jacobi,
-                                2 aggregation multigrid (no reference counterpart) */
+    int32_t precond;         /* 0 auto (smoothed-aggregation multigrid from 20,000 nodes on,
+                                else block-Jacobi), 1 block-Jacobi, 2 smoothed-aggregation
+                                multigrid, 3 plain-aggregation multigrid (no reference
+                                counterpart for 2 and 3); other values: TF_BAD_INPUT */
 } tf_options;
 
 /* Statistics of one time step (tf_newton_step). */

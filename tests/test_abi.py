@@ -43,6 +43,17 @@ def test_bad_input_is_rejected_before_any_device_work():
         raise AssertionError("out-of-range connectivity was accepted")
 
 
+def test_bad_options_are_rejected_before_any_device_work():
+    t = mesh.config_tiny(seed=1, n=3, n_layers=1)
+    for kw in ({"precond": 4}, {"precond": -1}, {"krylov_method": 3}):
+        try:
+            api.Solver(t, **kw)
+        except api.TfError as e:
+            assert e.status == api.TF_BAD_INPUT, kw
+        else:
+            raise AssertionError(f"{kw} was accepted")
+
+
 def test_status_strings():
     L = api.load()
     for code in range(9):

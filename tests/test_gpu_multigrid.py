@@ -1,11 +1,13 @@
-"""Aggregation multigrid preconditioner (tf_options.precond = 2).
+"""Aggregation multigrid preconditioners: smoothed (tf_options.precond = 2)
+and plain (3) aggregation.
 
 The preconditioner changes how the Krylov solve gets to its tolerance, not
 the system solved: Newton steps must still match the reference's golden
 positions to 1e-8 with the same Newton iteration counts, solutions must
 agree with the block-Jacobi solve to the Krylov tolerance, and the Krylov
 iteration count must drop well below block-Jacobi's on sheets of a few
-thousand nodes and more."""
+thousand nodes and more, and smoothing the prolongator must cut it below
+plain aggregation's."""
 import os
 
 import numpy as np
@@ -18,9 +20,9 @@ GOLD = os.path.join(os.path.dirname(__file__), "golden")
 TOL_POS = 1e-8
 
 
-def _steps(fixture, t):
+def _steps(fixture, t, precond=2):
     f = np.load(os.path.join(GOLD, fixture + ".npz"))
-    with api.Solver(t, precond=2) as s:
+    with api.Solver(t, precond=precond) as s:
         s.set_growth_rates(t.rates)
         for k in range(f["positions"].shape[0]):
             out = s.newton_step(t.dt, allow_not_converged=False)
@@ -30,13 +32,15 @@ def _steps(fixture, t):
             assert out["iters"] == f["iters"][k], (k, out["iters"])
 
 
-def test_multigrid_newton_steps_match_reference_small_config():
-    _steps("steps_small", mesh.config_small(seed=0))
+@pytest.mark.parametrize("precond", [2, 3])
+def test_multigrid_newton_steps_match_reference_small_config(precond):
+    _steps("steps_small", mesh.config_small(seed=0), precond)
 
 
+@pytest.mark.parametrize("precond", [2, 3])
 @pytest.mark.parametrize("name,seed,eta", [("steps_tiny_elastic", 13, 0.0), ("steps_tiny_viscous", 14, 100.0)])
-def test_multigrid_newton_steps_match_reference_tiny(name, seed, eta):
-    _steps(name, mesh.config_tiny(seed=seed, n=4, n_layers=2, eta=eta))
+def test_multigrid_newton_steps_match_reference_tiny(name, seed, eta, precond):
+    _steps(name, mesh.config_tiny(seed=seed, n=4, n_layers=2, eta=eta), precond)
 
 
 @pytest.mark.parametrize("eta", [0.0, 100.0])
@@ -46,7 +50,7 @@ def test_multigrid_solution_matches_block_jacobi(eta):
     Fg = mesh.growth_Fg(t, seed=5, amp=0.01)
     uk, un = mesh.perturbed_state(t, seed=6, amp=0.05)
     out = {}
-    for pc in (1, 2):
+    for pc in (1, 2, 3):
         with api.Solver(t, precond=pc, krylov_rtol=1e-11) as s:
             s.set_Fg(Fg)
             s.set_positions(un)
@@ -56,10 +60,13 @@ def test_multigrid_solution_matches_block_jacobi(eta):
             r = s.solve()
             out[pc] = (s.delta_u(), r["iters"], r["relres"])
     du1, it1, rr1 = out[1]
-    du2, it2, rr2 = out[2]
-    assert rr1 <= 1e-11 and rr2 <= 1e-11
-    assert np.abs(du2 - du1).max() <= 1e-7 * np.abs(du1).max()
-    assert it2 * 4 <= it1, (it1, it2)
+    for pc in (2, 3):
+        du2, it2, rr2 = out[pc]
+        assert rr1 <= 1e-11 and rr2 <= 1e-11
+        assert np.abs(du2 - du1).max() <= 1e-7 * np.abs(du1).max(), pc
+        assert it2 * 4 <= it1, (pc, it1, it2)
+    # the smoothed prolongator's coarse correction is the better one
+    assert out[2][1] < out[3][1], (out[2][1], out[3][1])
 
 
 def test_multigrid_is_bitwise_reproducible():

@@ -165,7 +165,10 @@ def _mesh_structs(t):
 
 
 class Solver:
-    """One GPU Newton solver over one tissue (a ``tf_handle``)."""
+    """One GPU Newton solver over one tissue (a ``tf_handle``).  ``precond``:
+    0 auto (smoothed-aggregation multigrid from 20,000 nodes on, else
+    block-Jacobi), 1 block-Jacobi, 2 smoothed-aggregation multigrid,
+    3 plain-aggregation multigrid."""
 
     def __init__(self, tissue, newton_tol=1e-8, newton_max_iter=20, krylov_rtol=1e-8, krylov_max_iter=20000,
                  krylov_method=0, deterministic=False, device=0, autotune=True, precond=0):

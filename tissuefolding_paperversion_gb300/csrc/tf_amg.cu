@@ -1,8 +1,8 @@
-// Aggregation algebraic multigrid: the preconditioner of the Krylov solve of
-// A du = g (A = K^T) on large meshes, in place of the block-Jacobi one.  No
-// counterpart in the reference, which factorises the system with Pardiso
-// (NewtonRaphsonSolver.cpp:418-683); the solution it converges to is the
-// same (the Krylov tolerance is unchanged).
+// Smoothed-aggregation algebraic multigrid: the preconditioner of the
+// Krylov solve of A du = g (A = K^T) on large meshes, in place of the
+// block-Jacobi one.  No counterpart in the reference, which factorises the
+// system with Pardiso (NewtonRaphsonSolver.cpp:418-683); the solution it
+// converges to is the same (the Krylov tolerance is unchanged).
 //
 // Set-up, once per handle, on the host from the block pattern and the
 // reference node positions:
@@ -16,22 +16,27 @@
 //   * tentative prolongator per aggregate from a modified Gram-Schmidt QR of
 //     its near-null-space rows (6 coarse DOFs per aggregate; a dependent
 //     column is dropped and its coarse DOF gets a unit diagonal);
-//   * coarse block patterns and, per coarse block, the ordered list of fine
-//     blocks contributing to it (Galerkin product without atomics).
-// Numeric phase, once per assembled matrix (all on the device):
-//   A_{l+1} = P_l^T A_l P_l block by block; 6x6 block inverses; lambda_max of
-//   D^-1 A per level by power iteration (smoother weight 4 / (3.15 lambda));
-//   Gauss-Jordan inverse of the coarsest level per instance (<= 16 nodes).
+//   * block patterns of the smoothed prolongator P = (I - omega D^-1 A) P_t
+//     (node i couples to the aggregates of its neighbours), of T = A P and of
+//     the coarse matrix P^T T, with per output block the ordered list of the
+//     products that make it (no atomics, reproducible).
+//   Plain aggregation (tf_options.precond 3) keeps P = P_t.
+// Numeric phase, once per time step (all on the device), level by level:
+//   lambda_max of D^-1 A by power iteration (smoother weight and prolongator
+//   smoothing weight omega = 4 / (3.15 lambda)); P; T = A P; A_{l+1} = P^T T;
+//   6x6 block inverses; Gauss-Jordan inverse of the coarsest level per
+//   instance (<= 16 nodes).
 // Application (one V-cycle per preconditioner call, all kernels, capturable
 // in a CUDA graph): damped block-Jacobi pre- and post-smoothing, residual,
 // restriction, coarse correction.  Kernels of an instance whose Krylov
 // solve has stopped return at once.
 // Precision: the preconditioner is any fixed linear operator as far as the
-// Krylov method is concerned, so the matrices it reads (a copy of the
-// level-0 values, the coarse operators, the level-0 block inverses) are
-// stored in FP32 -- half the bytes of its bandwidth-bound SpMVs -- while
-// every product, sum and vector stays FP64.  The Krylov recurrences, their
-// SpMVs with A and the convergence test are untouched FP64.
+// Krylov method is concerned, so the whole V-cycle -- its matrices (an FP32
+// copy of the level-0 values and block inverses, the coarse operators and
+// prolongators) and its vectors -- is FP32: half the bytes of its
+// bandwidth-bound sweeps, and no FP32/FP64 conversions on the FP64 pipe.
+// The Krylov recurrences, their SpMVs with A and the convergence test are
+// untouched FP64.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -159,8 +164,8 @@ tf_status zeros(T** dst, size_t n) {
 
 }  // namespace
 
-// Device view of one level.  Everything the V-cycle reads or writes is
-// FP32 (see the precision note above); the smoother weights are FP64 scalars.
+// Device view of one level: what the V-cycle reads and writes, all FP32
+// (see the precision note above); the smoother weights are FP64 scalars.
 struct AmgLevel {
     int n = 0, bs = 3;
     // matrix of levels >= 1: CSR of 6x6 row-major blocks
@@ -173,21 +178,45 @@ struct AmgLevel {
     float* dinv = nullptr;   // [n][36] block inverses (levels >= 1)
     int* seg = nullptr;      // [n] instance of each node (levels >= 1)
     int* seg0 = nullptr;     // [nseg+1] node offsets per instance (levels >= 1)
-    // transfer to level + 1 (absent at the coarsest level)
-    int* agg = nullptr;      // [n]
-    float* P = nullptr;      // [n][bs*6]
-    int* mptr = nullptr;     // [n_{l+1}+1] members of each next-level node
-    int* mlist = nullptr;
-    int* gptr = nullptr;     // [nnzb_{l+1}+1] fine blocks of each next-level block
-    int* glist = nullptr;
+    // prolongator to level + 1 (absent at the coarsest level): bs x 6
+    // row-major blocks, once by fine row and once by coarse column
+    int* prow = nullptr;     // [n+1] blocks of each fine node
+    int* pcol = nullptr;     // [npb] coarse node of each block
+    float* Pv = nullptr;     // [npb][bs*6]
+    int* pcptr = nullptr;    // [n_{l+1}+1] blocks of each coarse node (column order)
+    int* pcrow = nullptr;    // [npb] fine node of each block, column order
+    float* Pc = nullptr;     // [npb][bs*6] the blocks in column order
+    int64_t npb = 0;
     uint8_t* dead = nullptr; // [n * bs] (levels >= 1) DOFs with a zero prolongator column
     // vectors (levels >= 1: r input, e output; all levels: x, t work)
     float *r = nullptr, *x = nullptr, *t = nullptr, *e = nullptr;
 };
 
+// Lists of the numeric set-up of the transfer from level l to l + 1
+// (device arrays, built once on the host from the block patterns).
+struct AmgSetup {
+    float* Pt = nullptr;     // [n][bs*6] tentative prolongator (one block per fine node)
+    int* agg = nullptr;      // [n] aggregate of each fine node
+    int* pbrow = nullptr;    // [npb] fine node of each prolongator block
+    int* sptr = nullptr;     // [npb+1] fine-matrix blocks (i, j), agg(j) = column, per block (i, .)
+    int* slist = nullptr;
+    int* cperm = nullptr;    // [npb] row-order block at each column-order position
+    int64_t nT = 0;          // blocks of T = A P (bs x 6)
+    int* trow = nullptr;     // [nT] fine node of each T block
+    int* tptr = nullptr;     // [nT+1] pairs (fine-matrix block, prolongator block) per T block
+    int* ta = nullptr;
+    int* tb = nullptr;
+    float* T = nullptr;      // [nT][bs*6]
+    int* gptr = nullptr;     // [nnzb_{l+1}+1] pairs (prolongator block, T block) per coarse block
+    int* gp = nullptr;
+    int* gt = nullptr;
+};
+
 struct Amg {
     int nlev = 0;
+    bool smooth = true;        // smoothed (true) or plain (false) aggregation
     AmgLevel L[kAmgMaxLevels];
+    AmgSetup S[kAmgMaxLevels];
     double* omega = nullptr;   // [nlev] smoother weights
     double* pscal = nullptr;   // [nlev][2] power-iteration scalars (scale, lambda)
     float* pv = nullptr;       // power-iteration vectors (max n*bs each)
@@ -214,11 +243,16 @@ void amg_free(Amg* a) {
     if (!a) return;
     for (int l = 0; l < a->nlev; ++l) {
         AmgLevel& L = a->L[l];
-        void* ptrs[] = {L.rowptr, L.colidx, L.rowof, L.diag, L.val, L.seg, L.seg0, L.agg, L.P, L.mptr, L.mlist,
-                        L.gptr, L.glist, L.dead, L.r, L.x, L.t, L.e};
+        void* ptrs[] = {L.rowptr, L.colidx, L.rowof, L.diag, L.val, L.seg, L.seg0, L.prow, L.pcol, L.Pv,
+                        L.pcptr, L.pcrow, L.Pc, L.dead, L.r, L.x, L.t, L.e};
         for (void* p : ptrs)
             if (p) cudaFree(p);
         if (l > 0 && L.dinv) cudaFree(L.dinv);
+        AmgSetup& S = a->S[l];
+        void* sptrs[] = {S.Pt, S.agg, S.pbrow, S.sptr, S.slist, S.cperm, S.trow, S.tptr, S.ta, S.tb, S.T,
+                         S.gptr, S.gp, S.gt};
+        for (void* p : sptrs)
+            if (p) cudaFree(p);
     }
     void* ptrs[] = {a->omega, a->pscal, a->pv, a->pw, a->part, a->ticket, a->cnode0, a->cinv0, a->cinv,
                     a->val32, a->dinv32};
@@ -235,6 +269,7 @@ tf_status amg_build(tf_handle* h, const double* pos) {
     Amg* a = new Amg;
     h->amg = a;
     a->nseg = d.nseg;
+    a->smooth = h->opt.precond != 3;
     std::vector<HostLevel> H(1);
     H[0].n = d.nn;
     H[0].bs = 3;
@@ -303,7 +338,106 @@ tf_status amg_build(tf_handle* h, const double* pos) {
                         P[((size_t)i * bs + k) * 6 + col] = M[(size_t)(bs * (q - m0) + k) * 6 + col];
             }
         }
-        // coarse pattern
+        // prolongator pattern: block (i, J) for the aggregates J of node i's
+        // neighbours (smoothed: P = (I - omega D^-1 A) P_tentative) or for
+        // node i's own aggregate only (plain: P = P_tentative)
+        std::vector<int> prow(F.n + 1, 0), pcol, mark(na, -1), cols;
+        for (int i = 0; i < F.n; ++i) {
+            cols.assign(1, agg[i]);
+            mark[agg[i]] = i;
+            if (a->smooth)
+                for (int p = F.rowptr[i]; p < F.rowptr[i + 1]; ++p) {
+                    const int J = agg[F.colidx[p]];
+                    if (mark[J] != i) {
+                        mark[J] = i;
+                        cols.push_back(J);
+                    }
+                }
+            std::sort(cols.begin(), cols.end());
+            pcol.insert(pcol.end(), cols.begin(), cols.end());
+            prow[i + 1] = static_cast<int>(pcol.size());
+        }
+        const int npb = static_cast<int>(pcol.size());
+        std::vector<int> pbrow(npb);
+        for (int i = 0; i < F.n; ++i)
+            for (int b = prow[i]; b < prow[i + 1]; ++b) pbrow[b] = i;
+        // smoothing lists: fine block (i, j) adds to prolongator block (i, agg(j))
+        std::vector<int> sptr(npb + 1, 0), slist;
+        if (a->smooth) {
+            const int fnnzb = F.rowptr[F.n];
+            std::vector<int> sb(fnnzb);
+            for (int i = 0; i < F.n; ++i)
+                for (int p = F.rowptr[i]; p < F.rowptr[i + 1]; ++p) {
+                    const int J = agg[F.colidx[p]];
+                    sb[p] = static_cast<int>(std::lower_bound(pcol.begin() + prow[i], pcol.begin() + prow[i + 1], J) -
+                                             pcol.begin());
+                    sptr[sb[p] + 1]++;
+                }
+            for (int b = 0; b < npb; ++b) sptr[b + 1] += sptr[b];
+            slist.resize(fnnzb);
+            std::vector<int> fill(sptr.begin(), sptr.end() - 1);
+            for (int p = 0; p < fnnzb; ++p) slist[fill[sb[p]]++] = p;
+        }
+        // the same blocks by coarse column (fine nodes ascending within a column)
+        std::vector<int> pcptr(na + 1, 0), cperm(npb), pcrow(npb);
+        for (int b = 0; b < npb; ++b) pcptr[pcol[b] + 1]++;
+        for (int c = 0; c < na; ++c) pcptr[c + 1] += pcptr[c];
+        {
+            std::vector<int> fill(pcptr.begin(), pcptr.end() - 1);
+            for (int b = 0; b < npb; ++b) {
+                const int q = fill[pcol[b]]++;
+                cperm[q] = b;
+                pcrow[q] = pbrow[b];
+            }
+        }
+        // T = A P: pattern per fine row and, per T block, its pairs
+        // (fine-matrix block (i, j), prolongator block (j, J))
+        std::vector<int> trowptr(F.n + 1, 0), tcol;
+        std::fill(mark.begin(), mark.end(), -1);
+        for (int i = 0; i < F.n; ++i) {
+            cols.clear();
+            for (int p = F.rowptr[i]; p < F.rowptr[i + 1]; ++p) {
+                const int j = F.colidx[p];
+                for (int b = prow[j]; b < prow[j + 1]; ++b)
+                    if (mark[pcol[b]] != i) {
+                        mark[pcol[b]] = i;
+                        cols.push_back(pcol[b]);
+                    }
+            }
+            std::sort(cols.begin(), cols.end());
+            tcol.insert(tcol.end(), cols.begin(), cols.end());
+            trowptr[i + 1] = static_cast<int>(tcol.size());
+        }
+        const int64_t nT = (int64_t)tcol.size();
+        std::vector<int> trow(nT), tptr(nT + 1, 0), posJ(na, -1);
+        for (int i = 0; i < F.n; ++i) {
+            for (int t = trowptr[i]; t < trowptr[i + 1]; ++t) {
+                trow[t] = i;
+                posJ[tcol[t]] = t;
+            }
+            for (int p = F.rowptr[i]; p < F.rowptr[i + 1]; ++p) {
+                const int j = F.colidx[p];
+                for (int b = prow[j]; b < prow[j + 1]; ++b) tptr[posJ[pcol[b]] + 1]++;
+            }
+        }
+        for (int64_t t = 0; t < nT; ++t) tptr[t + 1] += tptr[t];
+        std::vector<int> ta(tptr[nT]), tb(tptr[nT]);
+        {
+            std::vector<int> fill(tptr.begin(), tptr.end() - 1);
+            for (int i = 0; i < F.n; ++i) {
+                for (int t = trowptr[i]; t < trowptr[i + 1]; ++t) posJ[tcol[t]] = t;
+                for (int p = F.rowptr[i]; p < F.rowptr[i + 1]; ++p) {
+                    const int j = F.colidx[p];
+                    for (int b = prow[j]; b < prow[j + 1]; ++b) {
+                        const int k = fill[posJ[pcol[b]]]++;
+                        ta[k] = p;
+                        tb[k] = b;
+                    }
+                }
+            }
+        }
+        // coarse pattern: row I joins the T rows of the fine nodes with a
+        // block in column I
         HostLevel C;
         C.n = na;
         C.bs = 6;
@@ -314,50 +448,72 @@ tf_status amg_build(tf_handle* h, const double* pos) {
         // aggregates of their own instance
         for (int g = 0; g <= d.nseg; ++g) C.seg0[g] = g < d.nseg ? (F.seg0[g] < F.n ? agg[F.seg0[g]] : na) : na;
         C.rowptr.assign(na + 1, 0);
-        {
-            std::vector<int> mark(na, -1), cols;
-            for (int c = 0; c < na; ++c) {
-                cols.clear();
-                for (int q = mptr[c]; q < mptr[c + 1]; ++q) {
-                    const int i = mlist[q];
-                    for (int p = F.rowptr[i]; p < F.rowptr[i + 1]; ++p) {
-                        const int J = agg[F.colidx[p]];
-                        if (mark[J] != c) {
-                            mark[J] = c;
-                            cols.push_back(J);
-                        }
+        std::fill(mark.begin(), mark.end(), -1);
+        for (int c = 0; c < na; ++c) {
+            cols.clear();
+            for (int q = pcptr[c]; q < pcptr[c + 1]; ++q) {
+                const int i = pcrow[q];
+                for (int t = trowptr[i]; t < trowptr[i + 1]; ++t)
+                    if (mark[tcol[t]] != c) {
+                        mark[tcol[t]] = c;
+                        cols.push_back(tcol[t]);
                     }
-                }
-                std::sort(cols.begin(), cols.end());
-                C.colidx.insert(C.colidx.end(), cols.begin(), cols.end());
-                C.rowptr[c + 1] = static_cast<int>(C.colidx.size());
             }
+            std::sort(cols.begin(), cols.end());
+            C.colidx.insert(C.colidx.end(), cols.begin(), cols.end());
+            C.rowptr[c + 1] = static_cast<int>(C.colidx.size());
         }
         const int64_t cnnzb = (int64_t)C.colidx.size();
-        // Galerkin lists: fine block b -> coarse block, grouped per coarse block
-        const int64_t fnnzb = (int64_t)F.colidx.size();
-        std::vector<int> cb(fnnzb);
-        for (int i = 0; i < F.n; ++i)
-            for (int p = F.rowptr[i]; p < F.rowptr[i + 1]; ++p) {
-                const int I = agg[i], J = agg[F.colidx[p]];
-                auto b = C.colidx.begin() + C.rowptr[I], e = C.colidx.begin() + C.rowptr[I + 1];
-                cb[p] = static_cast<int>(std::lower_bound(b, e, J) - C.colidx.begin());
+        // Galerkin pairs (prolongator block (i, I), T block (i, J)) per coarse block (I, J)
+        std::vector<int> gptr(cnnzb + 1, 0);
+        for (int c = 0; c < na; ++c) {
+            for (int p = C.rowptr[c]; p < C.rowptr[c + 1]; ++p) posJ[C.colidx[p]] = p;
+            for (int q = pcptr[c]; q < pcptr[c + 1]; ++q) {
+                const int i = pcrow[q];
+                for (int t = trowptr[i]; t < trowptr[i + 1]; ++t) gptr[posJ[tcol[t]] + 1]++;
             }
-        std::vector<int> gptr(cnnzb + 1, 0), glist(fnnzb);
-        for (int64_t b = 0; b < fnnzb; ++b) gptr[cb[b] + 1]++;
+        }
         for (int64_t c = 0; c < cnnzb; ++c) gptr[c + 1] += gptr[c];
+        std::vector<int> gp(gptr[cnnzb]), gt(gptr[cnnzb]);
         {
             std::vector<int> fill(gptr.begin(), gptr.end() - 1);
-            for (int64_t b = 0; b < fnnzb; ++b) glist[fill[cb[b]]++] = static_cast<int>(b);
+            for (int c = 0; c < na; ++c) {
+                for (int p = C.rowptr[c]; p < C.rowptr[c + 1]; ++p) posJ[C.colidx[p]] = p;
+                for (int q = pcptr[c]; q < pcptr[c + 1]; ++q) {
+                    const int i = pcrow[q];
+                    for (int t = trowptr[i]; t < trowptr[i + 1]; ++t) {
+                        const int k = fill[posJ[tcol[t]]]++;
+                        gp[k] = cperm[q];
+                        gt[k] = t;
+                    }
+                }
+            }
         }
         // device arrays of the fine level's transfer
         AmgLevel& DL = a->L[lev];
-        AMG_TRY(up(&DL.agg, agg));
-        AMG_TRY(up(&DL.P, std::vector<float>(P.begin(), P.end())));
-        AMG_TRY(up(&DL.mptr, mptr));
-        AMG_TRY(up(&DL.mlist, mlist));
-        AMG_TRY(up(&DL.gptr, gptr));
-        AMG_TRY(up(&DL.glist, glist));
+        DL.npb = npb;
+        AMG_TRY(up(&DL.prow, prow));
+        AMG_TRY(up(&DL.pcol, pcol));
+        AMG_TRY(zeros(&DL.Pv, (size_t)npb * bs * 6));
+        AMG_TRY(up(&DL.pcptr, pcptr));
+        AMG_TRY(up(&DL.pcrow, pcrow));
+        AMG_TRY(zeros(&DL.Pc, (size_t)npb * bs * 6));
+        AmgSetup& DS = a->S[lev];
+        DS.nT = nT;
+        AMG_TRY(up(&DS.Pt, std::vector<float>(P.begin(), P.end())));
+        AMG_TRY(up(&DS.agg, agg));
+        AMG_TRY(up(&DS.pbrow, pbrow));
+        AMG_TRY(up(&DS.sptr, sptr));
+        AMG_TRY(up(&DS.slist, slist));
+        AMG_TRY(up(&DS.cperm, cperm));
+        AMG_TRY(up(&DS.trow, trow));
+        AMG_TRY(up(&DS.tptr, tptr));
+        AMG_TRY(up(&DS.ta, ta));
+        AMG_TRY(up(&DS.tb, tb));
+        AMG_TRY(zeros(&DS.T, (size_t)nT * bs * 6));
+        AMG_TRY(up(&DS.gptr, gptr));
+        AMG_TRY(up(&DS.gp, gp));
+        AMG_TRY(up(&DS.gt, gt));
         // the coarse level's own arrays
         AmgLevel& CL = a->L[lev + 1];
         CL.n = na;
@@ -573,40 +729,116 @@ __global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restr
         b[k] = (float)a[k];
 }
 
-// Coarse block c, row p: sum over its fine blocks b = (i, j) of
-// (P_i^T A_b P_j)(p, :).  Level 0 reads the FP32 copy of the sliced storage.
+// Element (r, c) of fine-matrix block b: level 0 reads the FP32 copy of the
+// sliced storage, coarser levels their 6x6 CSR blocks.
 template <int BS, bool L0>
-__global__ void k_galerkin(AmgLevel F, AmgLevel C, const int* __restrict__ rowof0, const int* __restrict__ colidx0,
-                           const int* __restrict__ bofs0, const float* __restrict__ val0) {
+__device__ __forceinline__ const float* fine_block(const AmgLevel& F, const int* __restrict__ bofs0,
+                                                   const float* __restrict__ val0, int b) {
+    return L0 ? val0 + __ldg(&bofs0[b]) : F.val + 36 * (size_t)b;
+}
+template <int BS, bool L0>
+__device__ __forceinline__ float fine_at(const float* blk, int r, int c) {
+    return L0 ? __ldg(&blk[kSlice * (3 * r + c)]) : __ldg(&blk[6 * r + c]);
+}
+
+// Prolongator block b = (i, J): P_t(i) [agg(i) = J] - omega D_i^-1 sum over
+// the fine blocks (i, j) with agg(j) = J of A_ij P_t(j).  One thread per
+// block; plain aggregation has empty lists and omega 0 (a copy of P_t).
+template <int BS, bool L0>
+__global__ void k_smooth_p(AmgLevel F, AmgSetup S, const double* __restrict__ omega, int smooth,
+                           const int* __restrict__ colidx0, const int* __restrict__ bofs0,
+                           const float* __restrict__ val0, const float* __restrict__ dinv0) {
+    const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= F.npb) return;
+    const int i = S.pbrow[b], J = F.pcol[b];
+    float W[BS][6];
+#pragma unroll
+    for (int r = 0; r < BS; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) W[r][c] = 0.f;
+    for (int q = S.sptr[b]; q < S.sptr[b + 1]; ++q) {
+        const int ab = __ldg(&S.slist[q]);
+        const int j = L0 ? __ldg(&colidx0[ab]) : __ldg(&F.colidx[ab]);
+        const float* blk = fine_block<BS, L0>(F, bofs0, val0, ab);
+        const float* __restrict__ Pj = S.Pt + (size_t)j * BS * 6;
+#pragma unroll
+        for (int m = 0; m < BS; ++m) {
+            float pm[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) pm[c] = __ldg(&Pj[6 * m + c]);
+#pragma unroll
+            for (int r = 0; r < BS; ++r) {
+                const float av = fine_at<BS, L0>(blk, r, m);
+#pragma unroll
+                for (int c = 0; c < 6; ++c) W[r][c] = fmaf(av, pm[c], W[r][c]);
+            }
+        }
+    }
+    const float om = smooth ? (float)__ldg(omega) : 0.f;
+    const bool own = __ldg(&S.agg[i]) == J;
+    const float* __restrict__ Di = L0 ? dinv0 + 9 * (size_t)i : F.dinv + 36 * (size_t)i;
+    const float* __restrict__ Pi = S.Pt + (size_t)i * BS * 6;
+    float* __restrict__ out = F.Pv + (size_t)b * BS * 6;
+#pragma unroll
+    for (int r = 0; r < BS; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            float s = 0.f;
+#pragma unroll
+            for (int m = 0; m < BS; ++m) s = fmaf(__ldg(&Di[BS * r + m]), W[m][c], s);
+            out[6 * r + c] = fmaf(-om, s, own ? __ldg(&Pi[6 * r + c]) : 0.f);
+        }
+}
+
+// The prolongator blocks in coarse-column order (for the restriction).
+__global__ void k_p_columns(AmgLevel F, AmgSetup S, int bsz) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= F.npb * bsz) return;
+    const int64_t q = k / bsz;
+    F.Pc[k] = F.Pv[(size_t)__ldg(&S.cperm[q]) * bsz + (k - q * bsz)];
+}
+
+// T = A P, row r of T block t = (i, J): sum over its pairs (A_ij, P_jJ).
+template <int BS, bool L0>
+__global__ void k_ap(AmgLevel F, AmgSetup S, const int* __restrict__ bofs0, const float* __restrict__ val0) {
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= S.nT * BS) return;
+    const int64_t t = gid / BS;
+    const int r = static_cast<int>(gid - BS * t);
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int q = S.tptr[t]; q < S.tptr[t + 1]; ++q) {
+        const float* blk = fine_block<BS, L0>(F, bofs0, val0, __ldg(&S.ta[q]));
+        const float* __restrict__ Pb = F.Pv + (size_t)__ldg(&S.tb[q]) * BS * 6;
+#pragma unroll
+        for (int m = 0; m < BS; ++m) {
+            const float av = fine_at<BS, L0>(blk, r, m);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[c] = fmaf(av, __ldg(&Pb[6 * m + c]), acc[c]);
+        }
+    }
+    float* out = S.T + (size_t)t * BS * 6 + 6 * r;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) out[c] = acc[c];
+}
+
+// Coarse block c = (I, J), row p: sum over its pairs (P_iI, T_iJ) of
+// (P_iI^T T_iJ)(p, :).
+template <int BS>
+__global__ void k_ptap(AmgLevel F, AmgSetup S, AmgLevel C) {
     const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (gid >= C.nnzb * 6) return;
     const int64_t c = gid / 6;
     const int p = static_cast<int>(gid - 6 * c);
     float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int q = F.gptr[c]; q < F.gptr[c + 1]; ++q) {
-        const int b = __ldg(&F.glist[q]);
-        const int i = L0 ? __ldg(&rowof0[b]) : __ldg(&F.rowof[b]);
-        const int j = L0 ? __ldg(&colidx0[b]) : __ldg(&F.colidx[b]);
-        const float* __restrict__ Pi = F.P + (size_t)i * BS * 6;
-        const float* __restrict__ Pj = F.P + (size_t)j * BS * 6;
-        const int base = L0 ? __ldg(&bofs0[b]) : 0;
-        float t[BS];
+    for (int q = S.gptr[c]; q < S.gptr[c + 1]; ++q) {
+        const float* __restrict__ Pb = F.Pv + (size_t)__ldg(&S.gp[q]) * BS * 6;
+        const float* __restrict__ Tb = S.T + (size_t)__ldg(&S.gt[q]) * BS * 6;
 #pragma unroll
-        for (int s2 = 0; s2 < BS; ++s2) t[s2] = 0.f;
+        for (int k = 0; k < BS; ++k) {
+            const float pk = __ldg(&Pb[6 * k + p]);
 #pragma unroll
-        for (int r = 0; r < BS; ++r) {
-            const float pr = __ldg(&Pi[6 * r + p]);
-#pragma unroll
-            for (int s2 = 0; s2 < BS; ++s2) {
-                const float av = L0 ? __ldg(&val0[base + kSlice * (3 * r + s2)])
-                                    : __ldg(&F.val[36 * (size_t)b + 6 * r + s2]);
-                t[s2] = fmaf(pr, av, t[s2]);
-            }
+            for (int c2 = 0; c2 < 6; ++c2) acc[c2] = fmaf(pk, __ldg(&Tb[6 * k + c2]), acc[c2]);
         }
-#pragma unroll
-        for (int s2 = 0; s2 < BS; ++s2)
-#pragma unroll
-            for (int q2 = 0; q2 < 6; ++q2) acc[q2] = fmaf(t[s2], __ldg(&Pj[6 * s2 + q2]), acc[q2]);
     }
     const int I = C.rowof[c];
     if (C.colidx[c] == I && C.dead[6 * I + p]) acc[p] = 1.f;  // dropped coarse DOF: unit diagonal
@@ -864,46 +1096,49 @@ __global__ void k_v0_post(V0 a, const double* __restrict__ r, const float* __res
     for (int k = 0; k < 3; ++k) out[3 * q.i + k] = (double)fmaf(om, z[k], x[3 * q.i + k]);
 }
 
-// x_i += P_i e_agg(i)
+// x_i += sum over the prolongator blocks (i, J) of P_iJ e_J
 __global__ void k_v0_prolong(V0 a, AmgLevel F, const float* __restrict__ e, float* __restrict__ x) {
     pdl_enter();
     const Node0 q = node0(a.d);
     if (!q.valid || seg_stopped(a.d.scal, q.seg)) return;
-    const int I = F.agg[q.i];
-    const float* __restrict__ P = F.P + 18 * (size_t)q.i;
-    float ec[6];
+    float s[3] = {x[3 * q.i], x[3 * q.i + 1], x[3 * q.i + 2]};
+    for (int b = __ldg(&F.prow[q.i]); b < __ldg(&F.prow[q.i + 1]); ++b) {
+        const int J = __ldg(&F.pcol[b]);
+        const float* __restrict__ P = F.Pv + 18 * (size_t)b;
+        float ec[6];
 #pragma unroll
-    for (int b = 0; b < 6; ++b) ec[b] = e[6 * I + b];
+        for (int c = 0; c < 6; ++c) ec[c] = e[6 * J + c];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        float s = x[3 * q.i + k];
+        for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int b = 0; b < 6; ++b) s = fmaf(__ldg(&P[6 * k + b]), ec[b], s);
-        x[3 * q.i + k] = s;
+            for (int c = 0; c < 6; ++c) s[k] = fmaf(__ldg(&P[6 * k + c]), ec[c], s[k]);
     }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) x[3 * q.i + k] = s[k];
 }
 
-// r_C(I) = sum over members i of P_i^T t_i; x_C = omega_C D_C^-1 r_C
-// (pre-smoothing), by one warp: the lanes stride over the (member, DOF)
-// pairs of coarse node I.
+// r_C(I) = sum over the prolongator blocks (i, I) of P_iI^T t_i;
+// x_C = omega_C D_C^-1 r_C (pre-smoothing), by one warp: the lanes stride
+// over the (block, row) pairs of column I, stored contiguously.
 template <int BS>
 __device__ __forceinline__ void restrict_node(const AmgLevel& F, const AmgLevel& C, const float* __restrict__ t,
                                               int I, const double* __restrict__ omegaC, int presmooth) {
     const int lane = threadIdx.x & 31;
     float rc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    const int q0 = F.mptr[I], np = BS * (F.mptr[I + 1] - q0);
+    const int q0 = F.pcptr[I], np = BS * (F.pcptr[I + 1] - q0);
+    const float* __restrict__ Pc = F.Pc + (size_t)q0 * BS * 6;
     for (int qa = lane; qa < np; qa += 64) {
-        // two (member, DOF) pairs per lane and pass: their loads overlap
+        // two (block, row) pairs per lane and pass: their loads overlap
         float tk[2] = {0.f, 0.f};
-        const float* __restrict__ P[2] = {F.P, F.P};
+        const float* __restrict__ P[2] = {Pc, Pc};
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             const int q = qa + 32 * u;
             if (q < np) {
                 const int m = q / BS, k = q - BS * m;
-                const int i = __ldg(&F.mlist[q0 + m]);
+                const int i = __ldg(&F.pcrow[q0 + m]);
                 tk[u] = t[BS * (size_t)i + k];
-                P[u] = F.P + ((size_t)i * BS + k) * 6;
+                P[u] = Pc + 6 * (size_t)q;
             }
         }
 #pragma unroll
@@ -931,20 +1166,24 @@ __global__ void k_restrict(AmgLevel F, AmgLevel C, const float* __restrict__ t, 
     restrict_node<BS>(F, C, t, I, omegaC, presmooth);
 }
 
-// x_i += P_i e_agg(i) for node i of a 6-DOF level
+// x_i += sum over the prolongator blocks (i, J) of P_iJ e_J (6-DOF level)
 __device__ __forceinline__ void prolong_node(const AmgLevel& F, const float* __restrict__ e, int i) {
-    const int I = F.agg[i];
-    const float* __restrict__ P = F.P + 36 * (size_t)i;
-    float ec[6];
+    float s[6];
 #pragma unroll
-    for (int b = 0; b < 6; ++b) ec[b] = e[6 * I + b];
+    for (int k = 0; k < 6; ++k) s[k] = F.x[6 * i + k];
+    for (int b = __ldg(&F.prow[i]); b < __ldg(&F.prow[i + 1]); ++b) {
+        const int J = __ldg(&F.pcol[b]);
+        const float* __restrict__ P = F.Pv + 36 * (size_t)b;
+        float ec[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        float s = F.x[6 * i + k];
+        for (int c = 0; c < 6; ++c) ec[c] = e[6 * J + c];
 #pragma unroll
-        for (int b = 0; b < 6; ++b) s = fmaf(__ldg(&P[6 * k + b]), ec[b], s);
-        F.x[6 * i + k] = s;
+        for (int k = 0; k < 6; ++k)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) s[k] = fmaf(__ldg(&P[6 * k + c]), ec[c], s[k]);
     }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) F.x[6 * i + k] = s[k];
 }
 
 // out_i = x_i + omega D_i^-1 (r - A x)_i for row i, by one warp
@@ -1082,36 +1321,52 @@ tf_status amg_numeric(tf_handle* h) {
         a->stale = 0;
         return TF_OK;
     }
-    // Galerkin products and block inverses, level by level
-    for (int l = 0; l + 1 < a->nlev; ++l) {
-        AmgLevel& F = a->L[l];
+    // level by level: smoother weight from lambda_max(D^-1 A) (the
+    // prolongator smoothing uses it too), prolongator, Galerkin product
+    // A_{l+1} = P^T (A P) and the next level's block inverses
+    const int last = a->coarse_exact ? a->nlev - 1 : a->nlev;  // levels with a smoother
+    for (int l = 0; l < a->nlev; ++l) {
+        AmgLevel& L = a->L[l];
+        if (l < last) {
+            const int64_t m = (int64_t)L.n * L.bs;
+            double* scal = a->pscal + 2 * l;
+            float *v = a->pv, *w = a->pw;
+            k_pw_init<<<cdiv(m, kT), kT, 0, st>>>(m, v, a->part, a->ticket, scal);
+            TF_LAUNCH_CHECK(h);
+            for (int it = 0; it < kPowerIters; ++it) {
+                if (l == 0)
+                    k_pw_step0<<<d.ncta, kNodeThreads, 0, st>>>(d, a->val32, a->dinv32, v, w, a->part, a->ticket,
+                                                                scal, a->omega);
+                else
+                    k_pw_step6<<<cdiv(32 * (int64_t)L.n, kT), kT, 0, st>>>(L, v, w, a->part, a->ticket, scal,
+                                                                            a->omega + l);
+                TF_LAUNCH_CHECK(h);
+                std::swap(v, w);
+            }
+        }
+        if (l + 1 == a->nlev) break;
+        AmgSetup& S = a->S[l];
         AmgLevel& C = a->L[l + 1];
-        const int nb = cdiv(C.nnzb * 6, kT);
-        if (l == 0) k_galerkin<3, true><<<nb, kT, 0, st>>>(F, C, d.rowof, d.colidx, d.bofs, a->val32);
-        else k_galerkin<6, false><<<nb, kT, 0, st>>>(F, C, nullptr, nullptr, nullptr, nullptr);
+        const int sm = a->smooth ? 1 : 0;
+        if (l == 0) {
+            k_smooth_p<3, true><<<cdiv(L.npb, kT), kT, 0, st>>>(L, S, a->omega, sm, d.colidx, d.bofs, a->val32,
+                                                                a->dinv32);
+            TF_LAUNCH_CHECK(h);
+            k_ap<3, true><<<cdiv(S.nT * 3, kT), kT, 0, st>>>(L, S, d.bofs, a->val32);
+        } else {
+            k_smooth_p<6, false><<<cdiv(L.npb, kT), kT, 0, st>>>(L, S, a->omega + l, sm, nullptr, nullptr,
+                                                                 nullptr, nullptr);
+            TF_LAUNCH_CHECK(h);
+            k_ap<6, false><<<cdiv(S.nT * 6, kT), kT, 0, st>>>(L, S, nullptr, nullptr);
+        }
+        TF_LAUNCH_CHECK(h);
+        k_p_columns<<<cdiv(L.npb * L.bs * 6, kT), kT, 0, st>>>(L, S, L.bs * 6);
+        TF_LAUNCH_CHECK(h);
+        if (l == 0) k_ptap<3><<<cdiv(C.nnzb * 6, kT), kT, 0, st>>>(L, S, C);
+        else k_ptap<6><<<cdiv(C.nnzb * 6, kT), kT, 0, st>>>(L, S, C);
         TF_LAUNCH_CHECK(h);
         k_inv6<<<cdiv(C.n, kT), kT, 0, st>>>(C);
         TF_LAUNCH_CHECK(h);
-    }
-    // smoother weights from lambda_max(D^-1 A) per level
-    const int last = a->coarse_exact ? a->nlev - 1 : a->nlev;
-    for (int l = 0; l < last; ++l) {
-        AmgLevel& L = a->L[l];
-        const int64_t m = (int64_t)L.n * L.bs;
-        double* scal = a->pscal + 2 * l;
-        float *v = a->pv, *w = a->pw;
-        k_pw_init<<<cdiv(m, kT), kT, 0, st>>>(m, v, a->part, a->ticket, scal);
-        TF_LAUNCH_CHECK(h);
-        for (int it = 0; it < kPowerIters; ++it) {
-            if (l == 0)
-                k_pw_step0<<<d.ncta, kNodeThreads, 0, st>>>(d, a->val32, a->dinv32, v, w, a->part, a->ticket, scal,
-                                                            a->omega);
-            else
-                k_pw_step6<<<cdiv(32 * (int64_t)L.n, kT), kT, 0, st>>>(L, v, w, a->part, a->ticket, scal,
-                                                                        a->omega + l);
-            TF_LAUNCH_CHECK(h);
-            std::swap(v, w);
-        }
     }
     if (a->coarse_exact) {
         AmgLevel& L = a->L[a->nlev - 1];

@@ -470,6 +470,10 @@ constexpr int kAutoMultigridNodes = 20000;
 
 tf_status create_handle(const tf_mesh* mesh, const tf_material* mat, const tf_options* opts,
                         const std::vector<int>& seg_node0, const std::vector<int>& seg_elem0, tf_handle** out) {
+    if (opts && (opts->precond < 0 || opts->precond > 3 || opts->krylov_method < 0 || opts->krylov_method > 2)) {
+        set_error("tf_options: precond must be 0..3 and krylov_method 0..2");
+        return TF_BAD_INPUT;
+    }
     tf_handle* h = new tf_handle;
     if (opts) h->opt = *opts;
     if (h->opt.newton_tol <= 0) h->opt.newton_tol = 1e-8;
@@ -501,7 +505,7 @@ tf_status create_handle(const tf_mesh* mesh, const tf_material* mat, const tf_op
         return s;
     }
     tf_status s = build(h, mesh, mat, seg_node0, seg_elem0);
-    const bool amg = h->opt.precond == 2 || (h->opt.precond == 0 && mesh->n_nodes >= kAutoMultigridNodes);
+    const bool amg = h->opt.precond >= 2 || (h->opt.precond == 0 && mesh->n_nodes >= kAutoMultigridNodes);
     if (s == TF_OK && amg) s = amg_build(h, mesh->node_pos);
     if (s != TF_OK) {
         free_all(h);
