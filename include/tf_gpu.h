@@ -152,6 +152,27 @@ TF_API tf_status tf_add_K_triplets(tf_handle* h, int64_t n, const int32_t* rows,
  * it du[slave] = du[master] (equateSlaveDisplacementsToMasters, :237-251).
  * DOF indices (3*node + dim); n = 0 removes them. */
 TF_API tf_status tf_set_dof_bindings(tf_handle* h, int32_t n, const int32_t* slave_dofs, const int32_t* master_dofs);
+/* Implicit packing between tissue surfaces (implicitPacking, Simulation.cpp:37).
+ * enable = 1: every tf_begin_step detects the node couples at the step's start
+ * shape on the device -- Simulation::detectPacingNodes (Simulation.cpp:8167-8440)
+ * with the node masses of updateNodeMasses (:7552-7561), no fold-initiation
+ * branch and no collapsed nodes -- and every tf_assemble adds their forces to g
+ * and their Jacobian to K (calculatePackingForcesImplicit3D :7149-7203,
+ * calculatePackingJacobian3D :7205-7300, addPackingForces :8869-8900).
+ * flags bit 0 (TF_PACKING_REFERENCE_MERGE): leave out the couples found from
+ * the last of 16 node segments, as the reference's merge loop does (:8426).
+ * Single-mesh handles only; enable = 0 switches packing off. */
+#define TF_PACKING_REFERENCE_MERGE 1
+TF_API tf_status tf_set_packing(tf_handle* h, int32_t enable, int32_t flags);
+/* Couples of the last detection (pacingNodeCouples0/1, initialWeightPoint):
+ * their number in *n; node ids (2 per couple, first < second), weights (3 per
+ * couple, the unit vector from the second node to the first at detection),
+ * mean node masses, the force threshold (packingThreshold) and the detection
+ * distance.  Array arguments may be NULL. */
+TF_API tf_status tf_get_packing(tf_handle* h, int64_t* n, int32_t* nodes, double* weights, double* mbar,
+                                double* threshold, double* detect_distance);
+/* Node masses of the last detection (Node::mass), n_nodes values. */
+TF_API tf_status tf_packing_masses(tf_handle* h, double* mass);
 /* solveForDeltaU (NewtonRaphsonSolver.cpp:382-404): solves K^T du = g, the
  * transposed system Pardiso is asked for (iparm[11] = 1, :639). */
 TF_API tf_status tf_solve(tf_handle* h, int32_t* iters, double* relres);

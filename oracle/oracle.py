@@ -287,6 +287,13 @@ class Ref:
             L.tfr_step.argtypes = [C.c_void_p, C.c_double, C.c_void_p, C.POINTER(C.c_int), _dp, C.c_int]
             L.tfr_set_bindings.restype = None
             L.tfr_set_bindings.argtypes = [C.c_void_p, C.c_int, _ip, _ip]
+            L.tfr_set_packing.argtypes = [C.c_void_p, C.c_int, C.c_int]
+            L.tfr_pack_detect.argtypes = [C.c_void_p]
+            L.tfr_pack_count.restype = C.c_long
+            L.tfr_pack_count.argtypes = [C.c_void_p]
+            L.tfr_pack_get.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+            L.tfr_node_masses.argtypes = [C.c_void_p, _dp]
+            L.tfr_pack_forces.argtypes = [C.c_void_p, _dp]
             cls._lib = L
         return cls._lib
 
@@ -375,6 +382,41 @@ class Ref:
         m = _i32(master_dofs)
         self._bind = (s, m)
         self.lib().tfr_set_bindings(self.h, int(s.size), s, m)
+
+    def set_packing(self, on=True, drop_last_segment=True):
+        """Implicit packing between tissue surfaces in every later step and
+        assembly (Simulation::detectPacingNodes and the packing force and
+        Jacobian writers)."""
+        self.lib().tfr_set_packing(self.h, int(bool(on)), int(bool(drop_last_segment)))
+
+    def pack_detect(self):
+        """The start-of-step packing work at the current positions: bounding
+        box, node masses, couple detection."""
+        self.lib().tfr_pack_detect(self.h)
+
+    def packing(self):
+        """Couples of the last detection: dict with `nodes` (n, 2), `w`
+        (n, 3), `mbar` (n,), `threshold`, `detect`."""
+        L = self.lib()
+        n = int(L.tfr_pack_count(self.h))
+        nodes = np.zeros((n, 2), dtype=np.int32)
+        w = np.zeros((n, 3))
+        mbar = np.zeros(n)
+        thr = C.c_double(0.0)
+        det = C.c_double(0.0)
+        L.tfr_pack_get(self.h, nodes.ctypes.data_as(C.c_void_p), w.ctypes.data_as(C.c_void_p),
+                       mbar.ctypes.data_as(C.c_void_p), C.byref(thr), C.byref(det))
+        return {"nodes": nodes, "w": w, "mbar": mbar, "threshold": thr.value, "detect": det.value}
+
+    def node_masses(self):
+        m = np.zeros(self.nn)
+        self.lib().tfr_node_masses(self.h, m)
+        return m
+
+    def pack_forces(self):
+        f = np.zeros(3 * self.nn)
+        self.lib().tfr_pack_forces(self.h, f)
+        return f
 
     def step(self, dt, rates=None):
         it = C.c_int(0)

@@ -13,8 +13,20 @@
 //     ShapeBase.cpp:1215-1251);
 //   * updateNodeViscositySurfaces (Simulation.cpp:7563-7581);
 //   * updateStepNR (Simulation.cpp:6449-6590), restated call for call with
-//     packing, myosin, pipette and random forces switched off as in every
-//     configuration this build targets.
+//     myosin, pipette and random forces switched off as in every
+//     configuration this build targets;
+//   * implicit packing between tissue surfaces when switched on
+//     (tfr_set_packing): calculateBoundingBox :9148-9185 and the elements'
+//     bounding-box positions :5833-5843, updateNodeMasses :7552-7561,
+//     getAverageSideLength :3205-3265, detectPacingNodes :8167-8440 (without
+//     the fold-initiation branch, which needs emergent-ellipse marking or
+//     peripodial adhesion, and with no collapsed nodes),
+//     calculatePackingForcesImplicit3D :7149-7203,
+//     calculatePackingJacobian3D :7205-7300 and addPackingForces :8869-8900,
+//     in the order runOneStep / updateStepNR call them.  The reference's
+//     tissue alignment (alignTissueDVToXPositive), a rigid rotation outside
+//     the step, is not applied.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <iostream>
@@ -39,7 +51,23 @@ public:
     double muValue() const { return mu; }
 };
 
+// State of the packing restatement (Simulation's packing members).
+struct PackingRef {
+    bool on = false;
+    bool dropLastSegment = true;   // the reference's merge loop (Simulation.cpp:8426) skips the last segment
+    double bb[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    double bbSize[3] = {0, 0, 0};
+    double threshold = 0.0;        // packingThreshold
+    double detect = 0.0;           // detection distance of a master node in grid cell [0][0]
+    double multiplier = 5000.0;    // packingMultiplier
+    double saturation = 5.0;       // sigmoidSaturationForPacking
+    std::vector<int> c0, c1;       // pacingNodeCouples0 / 1
+    std::vector<double> wx, wy, wz;  // initialWeightPointx / y / z
+    std::vector<double> force;     // PackingForces, 3 per node
+};
+
 struct RefSim {
+    PackingRef pk;
     std::vector<Node*> nodes;
     std::vector<ShapeBase*> elements;
     NewtonRaphsonSolver* nr = nullptr;
@@ -66,6 +94,183 @@ void copyUkToPositions(RefSim* s) {
     }
     for (int i = 0; i < s->nNodes; ++i)
         for (int d = 0; d < 3; ++d) s->nodes[i]->Position[d] = gsl_matrix_get(s->nr->uk, 3 * i + d, 0);
+}
+
+// Simulation::calculateBoundingBox (Simulation.cpp:9148-9185): every node
+// counts (no ECM-mimicking elements), no y symmetry; note the running
+// "else if": a node that lowers the minimum is not tested for the maximum.
+void refBoundingBox(RefSim* s) {
+    PackingRef& p = s->pk;
+    for (int i = 0; i < 3; ++i) {
+        p.bb[0][i] = 100000.0;
+        p.bb[1][i] = -100000.0;
+    }
+    for (Node* n : s->nodes)
+        for (int i = 0; i < 3; ++i) {
+            if (n->Position[i] < p.bb[0][i]) p.bb[0][i] = n->Position[i];
+            else if (n->Position[i] > p.bb[1][i]) p.bb[1][i] = n->Position[i];
+        }
+    for (int i = 0; i < 3; ++i) p.bbSize[i] = p.bb[1][i] - p.bb[0][i];
+    for (ShapeBase* e : s->elements)
+        e->calculateRelativePosInBoundingBox(p.bb[0][0], p.bb[0][1], p.bbSize[0], p.bbSize[1]);
+}
+
+// Simulation::updateNodeMasses (Simulation.cpp:7552-7561)
+void refNodeMasses(RefSim* s) {
+    for (Node* n : s->nodes) n->mass = 0;
+    for (ShapeBase* e : s->elements)
+        if (!e->IsAblated) e->assignVolumesToNodes(s->nodes);
+}
+
+// Simulation::getAverageSideLength (Simulation.cpp:3205-3265) for a tissue of
+// columnar elements only: returns colAverageSideLength and fills the 10 x 5
+// detection grid.  (The reference declares its counter grid [10][4] while
+// indexing it [10][5]; both grids are 10 x 5 here.)
+double refAverageSideLength(RefSim* s, double grid[10][5]) {
+    double cnt[10][5];
+    for (int i = 0; i < 10; ++i)
+        for (int j = 0; j < 5; ++j) grid[i][j] = cnt[i][j] = 0.0;
+    double dsum = 0.0;
+    int n = 0;
+    for (ShapeBase* e : s->elements) {
+        if (e->IsAblated || e->tissueType != 0) continue;
+        double v = e->getApicalSideLengthAverage();
+        if (v > 0) {
+            dsum += v;
+            n++;
+        }
+        if (e->tissuePlacement == 0 || e->spansWholeTissue) {
+            v = e->getBasalSideLengthAverage();
+            if (v > 0) {
+                dsum += v;
+                n++;
+            }
+        }
+        double rel[2];
+        e->getRelativePosInBoundingBox(rel);
+        int rx = static_cast<int>(std::floor(rel[0])), ry = static_cast<int>(std::floor(rel[1] / 2.0));
+        rx = std::min(std::max(rx, 0), 9);
+        ry = std::min(std::max(ry, 0), 4);
+        grid[rx][ry] += v;
+        cnt[rx][ry] += 1.0;
+    }
+    for (int i = 0; i < 10; ++i)
+        for (int j = 0; j < 5; ++j)
+            if (cnt[i][j] > 0) grid[i][j] /= cnt[i][j];
+    return dsum / static_cast<double>(n);
+}
+
+// Simulation::detectPacingNodes (Simulation.cpp:8167-8440) without the
+// fold-initiation branch and with no collapsed nodes.
+void refDetectPacking(RefSim* s) {
+    PackingRef& p = s->pk;
+    double grid[10][5], gridSq[10][5];
+    const double col = refAverageSideLength(s, grid);
+    for (int i = 0; i < 10; ++i)
+        for (int j = 0; j < 5; ++j) {
+            grid[i][j] = 0.4 * grid[i][j];
+            gridSq[i][j] = grid[i][j] * grid[i][j];
+        }
+    p.threshold = 0.4 * col;
+    p.detect = grid[0][0];
+    p.c0.clear();
+    p.c1.clear();
+    p.wx.clear();
+    p.wy.clear();
+    p.wz.clear();
+    const int nNodes = s->nNodes;
+    int segSize = nNodes / 16;
+    if (segSize < 1) segSize = 1;
+    const int nSeg = nNodes / segSize;
+    const int lastStart = (nSeg - 1) * segSize;
+    for (int a = 0; a < nNodes; ++a) {
+        Node* m = s->nodes[a];
+        if (!m->checkIfNodeHasPacking()) continue;
+        if (p.dropLastSegment && a >= lastStart) continue;  // found, then dropped by the merge loop
+        const int gx = static_cast<int>(std::floor((m->Position[0] - p.bb[0][0]) / p.bbSize[0]));
+        const int gy = static_cast<int>(std::floor((m->Position[1] - p.bb[0][1]) / p.bbSize[1]));
+        // the reference indexes its 10 x 5 grid unchecked; no node lies outside it here
+        const double t2 = (gx >= 0 && gx < 10 && gy >= 0 && gy < 5) ? gridSq[gx][gy] : 0.0;
+        for (int b = a + 1; b < nNodes; ++b) {
+            Node* sl = s->nodes[b];
+            if (!sl->checkIfNodeHasPacking()) continue;
+            if (m->tissuePlacement != sl->tissuePlacement) continue;
+            if (m->isMyNeig(sl->Id)) continue;
+            const double dx = m->Position[0] - sl->Position[0];
+            const double dy = m->Position[1] - sl->Position[1];
+            const double dz = m->Position[2] - sl->Position[2];
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 < t2) {
+                const double d = std::pow(d2, 0.5);
+                p.c0.push_back(m->Id);
+                p.c1.push_back(sl->Id);
+                p.wx.push_back(dx / d);
+                p.wy.push_back(dy / d);
+                p.wz.push_back(dz / d);
+            }
+        }
+    }
+}
+
+// calculatePackingForcesImplicit3D (Simulation.cpp:7149-7203) after the
+// iteration's resetForces(true) (:6466), then calculatePackingJacobian3D
+// (:7205-7300) into K.
+void refPackingForcesAndJacobian(RefSim* s) {
+    PackingRef& p = s->pk;
+    std::fill(p.force.begin(), p.force.end(), 0.0);
+    const size_t n = p.c0.size();
+    for (size_t i = 0; i < n; ++i) {
+        const int a = p.c0[i], b = p.c1[i];
+        const double mbar = 0.5 * (s->nodes[a]->mass + s->nodes[b]->mass);
+        const double w[3] = {p.wx[i], p.wy[i], p.wz[i]};
+        for (int d = 0; d < 3; ++d) {
+            double dd = s->nodes[a]->Position[d] - s->nodes[b]->Position[d];
+            if (w[d] > 0) dd *= -1.0;
+            double F = p.multiplier * mbar / (1 + std::exp(p.saturation / p.threshold * (-1.0 * dd)));
+            F *= w[d];
+            p.force[3 * a + d] += F;
+            p.force[3 * b + d] -= F;
+        }
+    }
+    gsl_matrix* K = s->nr->K;
+    for (size_t i = 0; i < n; ++i) {
+        const int a = p.c0[i], b = p.c1[i];
+        const double mbar = 0.5 * (s->nodes[a]->mass + s->nodes[b]->mass);
+        const double w[3] = {p.wx[i], p.wy[i], p.wz[i]};
+        for (int d = 0; d < 3; ++d) {
+            double dd = s->nodes[a]->Position[d] - s->nodes[b]->Position[d];
+            if (w[d] > 0) dd *= -1.0;
+            const double sig = 1 / (1 + std::exp(p.saturation / p.threshold * (-1.0 * dd)));
+            double d0 = sig * (1 - sig) * p.multiplier * mbar * w[d] * (p.saturation / p.threshold);
+            double d1 = -1.0 * d0;
+            if (w[d] > 0) {
+                d0 *= -1.0;
+                d1 *= -1.0;
+            }
+            const int ra = 3 * a + d, rb = 3 * b + d;
+            gsl_matrix_set(K, ra, ra, gsl_matrix_get(K, ra, ra) - d0);
+            gsl_matrix_set(K, ra, rb, gsl_matrix_get(K, ra, rb) - d1);
+            gsl_matrix_set(K, rb, rb, gsl_matrix_get(K, rb, rb) - d0);
+            gsl_matrix_set(K, rb, ra, gsl_matrix_get(K, rb, ra) - d1);
+        }
+    }
+}
+
+// Simulation::addPackingForces (Simulation.cpp:8869-8900)
+void refAddPackingForces(RefSim* s) {
+    for (int j = 0; j < s->nNodes; ++j)
+        for (int d = 0; d < 3; ++d)
+            gsl_matrix_set(s->nr->gExt, 3 * j + d, 0,
+                           s->pk.force[3 * j + d] + gsl_matrix_get(s->nr->gExt, 3 * j + d, 0));
+}
+
+// Start-of-step packing work of runOneStep (Simulation.cpp:5833-5843,
+// 5911, 5920): bounding box and element positions in it, node masses,
+// couple detection.  Growth has already updated the element volumes.
+void refPackingStepStart(RefSim* s) {
+    refBoundingBox(s);
+    refNodeMasses(s);
+    refDetectPacking(s);
 }
 
 }  // namespace
@@ -111,6 +316,9 @@ void* tfr_create(int n_nodes, int n_elems, const double* pos, const int* conn,
         e->calculateElementShapeFunctionDerivatives();
         static_cast<PrismRef*>(e)->exposeSurfaces(s->nodes);
     }
+    // Simulation::fillInNodeNeighbourhood (Simulation.cpp:7595-7600)
+    for (auto* e : s->elements) e->fillNodeNeighbourhood(s->nodes);
+    s->pk.force.assign(3 * (size_t)n_nodes, 0.0);
     s->nr = new NewtonRaphsonSolver(3, n_nodes);
     s->systemForces = new double*[n_nodes];
     s->fixedNodeForces = new double*[n_nodes];
@@ -279,8 +487,10 @@ long tfr_assemble(void* h, const double* uk, const double* un, double dt) {
     nr->writeImplicitElementalKToJacobian(s->elements);
     nr->calculateExternalViscousForcesForNR(s->nodes);
     nr->addImplicitKViscousExternalToJacobian(s->nodes, dt);
+    if (s->pk.on) refPackingForcesAndJacobian(s);
     nr->checkJacobianForAblatedNodes(s->ablated);
     nr->calculateSumOfInternalForces();
+    if (s->pk.on) refAddPackingForces(s);
     nr->addExernalForces();
     nr->calcutateFixedK(s->nodes);
     nr->calculateBoundKWithSlavesMasterDoF();
@@ -325,8 +535,17 @@ void tfr_set_bindings(void* h, int n, const int* slave_dofs, const int* master_d
 
 int tfr_step(void* h, double dt, const double* rates, int* iters, double* dunorm, int max_hist) {
     RefSim* s = static_cast<RefSim*>(h);
-    if (rates) tfr_grow(h, dt, rates);
+    if (rates) {
+        tfr_grow(h, dt, rates);
+    } else if (s->pk.on) {
+        // runOneStep calls growShapeByFg on every element at every step
+        // (Simulation.cpp:5901-5906), which sets the volumes the node masses
+        // are made of (the Prism constructor leaves them 0, Prism.cpp:218)
+        std::vector<double> zero(3 * (size_t)s->nElems, 0.0);
+        tfr_grow(h, dt, zero.data());
+    }
     tfr_update_viscosity_surfaces(h, nullptr);
+    if (s->pk.on) refPackingStepStart(s);
     QuietCout q;
     std::ostringstream err;
     std::streambuf* oldErr = std::cerr.rdbuf(err.rdbuf());
@@ -348,8 +567,10 @@ int tfr_step(void* h, double dt, const double* rates, int* iters, double* dunorm
         nr->writeImplicitElementalKToJacobian(s->elements);
         nr->calculateExternalViscousForcesForNR(s->nodes);
         nr->addImplicitKViscousExternalToJacobian(s->nodes, dt);
+        if (s->pk.on) refPackingForcesAndJacobian(s);
         nr->checkJacobianForAblatedNodes(s->ablated);
         nr->calculateSumOfInternalForces();
+        if (s->pk.on) refAddPackingForces(s);
         nr->addExernalForces();
         nr->calcutateFixedK(s->nodes);
         nr->calculateBoundKWithSlavesMasterDoF();
@@ -368,6 +589,59 @@ int tfr_step(void* h, double dt, const double* rates, int* iters, double* dunorm
     std::cerr.rdbuf(oldErr);
     *iters = iteratorK;
     return notConverged;
+}
+
+// Packing on / off; drop_last_segment reproduces the reference's merge of
+// its 16 detection segments (Simulation.cpp:8426), which leaves out the
+// couples found from the nodes of the last segment.
+void tfr_set_packing(void* h, int on, int drop_last_segment) {
+    RefSim* s = static_cast<RefSim*>(h);
+    s->pk.on = on != 0;
+    s->pk.dropLastSegment = drop_last_segment != 0;
+}
+
+// The start-of-step packing work at the current positions and growth (a
+// zero-rate growShapeByFg first, as every step of runOneStep does).
+void tfr_pack_detect(void* h) {
+    RefSim* s = static_cast<RefSim*>(h);
+    std::vector<double> zero(3 * (size_t)s->nElems, 0.0);
+    tfr_grow(h, 1.0, zero.data());
+    QuietCout q;
+    refPackingStepStart(s);
+}
+
+long tfr_pack_count(void* h) { return static_cast<long>(static_cast<RefSim*>(h)->pk.c0.size()); }
+
+// Couples of the last detection: node ids (2 per couple), weights (3),
+// average masses, the force threshold and the detection distance.
+void tfr_pack_get(void* h, int* nodes, double* w, double* mbar, double* threshold, double* detect) {
+    RefSim* s = static_cast<RefSim*>(h);
+    const PackingRef& p = s->pk;
+    for (size_t i = 0; i < p.c0.size(); ++i) {
+        if (nodes) {
+            nodes[2 * i] = p.c0[i];
+            nodes[2 * i + 1] = p.c1[i];
+        }
+        if (w) {
+            w[3 * i] = p.wx[i];
+            w[3 * i + 1] = p.wy[i];
+            w[3 * i + 2] = p.wz[i];
+        }
+        if (mbar) mbar[i] = 0.5 * (s->nodes[p.c0[i]]->mass + s->nodes[p.c1[i]]->mass);
+    }
+    if (threshold) *threshold = p.threshold;
+    if (detect) *detect = p.detect;
+}
+
+void tfr_node_masses(void* h, double* mass) {
+    RefSim* s = static_cast<RefSim*>(h);
+    for (int i = 0; i < s->nNodes; ++i) mass[i] = s->nodes[i]->mass;
+}
+
+// PackingForces of the last assembly (3 per node).
+void tfr_pack_forces(void* h, double* f) {
+    RefSim* s = static_cast<RefSim*>(h);
+    std::copy(s->pk.force.begin(), s->pk.force.end(), f);
 }
 
 }  // extern "C"

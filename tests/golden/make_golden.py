@@ -4,7 +4,7 @@ Run where the reference checkout is present (it builds oracle/_ref from the
 reference's own sources with the project-written GSL/uBLAS/Pardiso
 stand-ins):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--only-bound | --only-packing]
 
 Every fixture records the seeded inputs that produced it, so tests rebuild
 the same inputs with tissuefolding_paperversion_gb300.mesh and compare.
@@ -90,7 +90,61 @@ def bound_steps_fixture(name, t, n_steps, seed_note):
     r.close()
 
 
+def packing_steps_fixture(name, t, n_steps, drop_last_segment, seed_note):
+    """Steps with the reference's implicit packing (couples detected at each
+    step start), plus the couples, node masses and one assembled system with
+    its packing forces at a perturbed state of the first step."""
+    r = Ref(t)
+    r.set_packing(True, drop_last_segment)
+    pos, iters, pk_nodes, pk_w, pk_mbar, pk_thr, pk_det, pk_n = [], [], [], [], [], [], [], []
+    for _ in range(n_steps):
+        out = r.step(t.dt, t.rates)
+        p = r.packing()
+        pk_n.append(len(p["nodes"]))
+        pk_nodes.append(p["nodes"])
+        pk_w.append(p["w"])
+        pk_mbar.append(p["mbar"])
+        pk_thr.append(p["threshold"])
+        pk_det.append(p["detect"])
+        pos.append(r.positions())
+        iters.append(out["iters"])
+    r.close()
+    # one assembly at a perturbed state, couples detected at un
+    r = Ref(t)
+    r.set_packing(True, drop_last_segment)
+    uk, un = mesh.perturbed_state(t, seed=7, amp=0.05)
+    r.set_positions(un)
+    r.pack_detect()
+    p0 = r.packing()
+    masses = r.node_masses()
+    r.update_viscosity_surfaces()
+    ia, ja, a, g = r.assemble(uk, un, t.dt)
+    f = r.pack_forces()
+    r.close()
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), positions=np.array(pos), iters=np.array(iters),
+                        pk_n=np.array(pk_n), pk_nodes=np.concatenate(pk_nodes), pk_w=np.concatenate(pk_w),
+                        pk_mbar=np.concatenate(pk_mbar), pk_threshold=np.array(pk_thr), pk_detect=np.array(pk_det),
+                        asm_nodes=p0["nodes"], asm_w=p0["w"], asm_mbar=p0["mbar"], asm_threshold=p0["threshold"],
+                        asm_masses=masses, asm_ia=ia, asm_ja=ja, asm_a=a, asm_g=g, asm_forces=f,
+                        drop_last_segment=drop_last_segment, note=seed_note)
+
+
+def packing_fixtures():
+    # stiff sheets (E = 1e5 Pa): the reference's packing force (5000 x the
+    # couple's mean node mass) deforms softer sheets by several µm per step
+    # and makes later steps diverge
+    t = mesh.config_facing_sheets(seed=12, gap=1.5, E=100000.0, eta=0.0)
+    packing_steps_fixture("steps_facing_packing", t, 3, True,
+                          "config_facing_sheets(seed=12, gap=1.5, E=1e5, eta=0), packing on, last segment dropped")
+    t = mesh.config_facing_sheets(seed=13, gap=1.5, E=100000.0, eta=100.0)
+    packing_steps_fixture("steps_facing_packing_viscous", t, 2, False,
+                          "config_facing_sheets(seed=13, gap=1.5, E=1e5, eta=100), packing on, every segment kept")
+
+
 def main():
+    if "--only-packing" in sys.argv:
+        packing_fixtures()
+        return
     if "--only-bound" in sys.argv:
         t = mesh.config_tiny(seed=15, n=5, n_layers=2, eta=100.0)
         bound_steps_fixture("steps_tiny_bound", t, 4, "config_tiny(seed=15,n=5,n_layers=2,eta=100), bound_dofs(t)")
@@ -105,6 +159,7 @@ def main():
     print("small steps", steps_fixture("steps_small", t, t.n_steps, "config_small(seed=0)"))
     t = mesh.config_tiny(seed=15, n=5, n_layers=2, eta=100.0)
     bound_steps_fixture("steps_tiny_bound", t, 4, "config_tiny(seed=15,n=5,n_layers=2,eta=100), bound_dofs(t)")
+    packing_fixtures()
 
 
 if __name__ == "__main__":

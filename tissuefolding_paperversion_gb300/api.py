@@ -31,7 +31,8 @@ EXPORTED = [
     "tf_element_eval", "tf_get_sizes", "tf_get_stream", "tf_launch_count", "tf_time_assembly",
     "tf_solve_bsr_static", "tf_batch_create", "tf_batch_step", "tf_get_instances", "tf_elements_per_cta",
     "tf_adj_forward", "tf_adj_backward", "tf_adj_free", "tf_multigrid_info", "tf_read_mesh_file",
-    "tf_write_frame", "tf_add_K_triplets", "tf_set_dof_bindings",
+    "tf_write_frame", "tf_add_K_triplets", "tf_set_dof_bindings", "tf_set_packing", "tf_get_packing",
+    "tf_packing_masses",
 ]
 
 
@@ -127,6 +128,13 @@ def load(build_if_missing: bool = True):
     L.tf_set_dof_bindings.argtypes = [vp, i32, vp, vp]
     L.tf_add_K_triplets.restype = C.c_int
     L.tf_add_K_triplets.argtypes = [vp, i64, vp, vp, vp]
+    L.tf_set_packing.restype = C.c_int
+    L.tf_set_packing.argtypes = [vp, i32, i32]
+    L.tf_get_packing.restype = C.c_int
+    L.tf_get_packing.argtypes = [vp, C.POINTER(C.c_int64), vp, vp, vp, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double)]
+    L.tf_packing_masses.restype = C.c_int
+    L.tf_packing_masses.argtypes = [vp, vp]
     L.tf_read_mesh_file.restype = C.c_int
     L.tf_read_mesh_file.argtypes = [C.c_char_p, ip, ip, vp, vp, vp, vp, vp, vp]
     L.tf_write_frame.restype = C.c_int
@@ -262,6 +270,34 @@ class Solver:
         m = np.ascontiguousarray(master_dofs, dtype=np.int32)
         self._bind = (s, m)
         self._check(self.L.tf_set_dof_bindings(self.h, s.size, _ptr(s), _ptr(m)), "tf_set_dof_bindings")
+
+    def set_packing(self, enable=True, reference_merge=True):
+        """Implicit packing between tissue surfaces: couples detected at every
+        begin_step, their forces and Jacobian added at every assemble.
+        reference_merge keeps the reference's merge, which leaves out the
+        couples found from the last of its 16 node segments."""
+        self._check(self.L.tf_set_packing(self.h, 1 if enable else 0, 1 if reference_merge else 0),
+                    "tf_set_packing")
+
+    def packing(self):
+        """Couples of the last detection: dict with nodes (n, 2), w (n, 3),
+        mbar (n,), threshold, detect."""
+        n = C.c_int64(0)
+        thr = C.c_double(0.0)
+        det = C.c_double(0.0)
+        self._check(self.L.tf_get_packing(self.h, C.byref(n), None, None, None, C.byref(thr), C.byref(det)),
+                    "tf_get_packing")
+        nodes = np.zeros((n.value, 2), dtype=np.int32)
+        w = np.zeros((n.value, 3))
+        mbar = np.zeros(n.value)
+        self._check(self.L.tf_get_packing(self.h, C.byref(n), _ptr(nodes), _ptr(w), _ptr(mbar), C.byref(thr),
+                                          C.byref(det)), "tf_get_packing")
+        return {"nodes": nodes, "w": w, "mbar": mbar, "threshold": thr.value, "detect": det.value}
+
+    def packing_masses(self):
+        m = np.zeros(self.nn)
+        self._check(self.L.tf_packing_masses(self.h, _ptr(m)), "tf_packing_masses")
+        return m
 
     def add_K_triplets(self, rows, cols, vals):
         """K(rows[k], cols[k]) += vals[k] after assemble() (packing/myosin-type writers)."""

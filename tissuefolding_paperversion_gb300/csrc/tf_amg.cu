@@ -677,6 +677,24 @@ __device__ __forceinline__ void sliced_row32(const int* __restrict__ wslot0, con
     y[2] = y2;
 }
 
+// Level-0 row product of the smoother: the FP32 copy of the sliced storage
+// plus the extra blocks outside the element pattern (K entries of packing
+// couples and tf_add_K_triplets, few and FP64, converted on the fly), so that
+// the smoother works on the operator the Krylov method solves.
+__device__ __forceinline__ void row0(const Device& d, const float* __restrict__ val32, const float* __restrict__ x,
+                                     int i, float y[3]) {
+    sliced_row32(d.wslot0, d.scol, val32, x, y);
+    if (!d.xrow) return;
+    for (int q = d.xrow[i]; q < d.xrow[i + 1]; ++q) {
+        const int j = d.xcol[q];
+        const double* __restrict__ v = d.xval + 9 * (size_t)q;
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+            y[r] = fmaf((float)v[3 * r], x[3 * j],
+                        fmaf((float)v[3 * r + 1], x[3 * j + 1], fmaf((float)v[3 * r + 2], x[3 * j + 2], y[r])));
+    }
+}
+
 // Warp-cooperative product of row i of a 6x6-block CSR matrix with x.
 // Lane 6 k + a (< 30) takes row a of blocks k, k + 5, k + 10, ... of the
 // row: six FMAs per block row, every value used once (lane groups read
@@ -932,7 +950,7 @@ __global__ void k_pw_step0(Device d, const float* __restrict__ val32, const floa
     const Node0 q = node0(d);
     double s = 0.0;
     float y[3] = {0.f, 0.f, 0.f};
-    if (q.valid) sliced_row32(d.wslot0, d.scol, val32, v, y);
+    if (q.valid) row0(d, val32, v, q.i, y);
     if (q.valid) {
         const float sc = (float)__ldcg(&scal[0]);
         float yy[3] = {sc * y[0], sc * y[1], sc * y[2]}, z[3];
@@ -1073,7 +1091,7 @@ __global__ void k_v0_resid(V0 a, const double* __restrict__ r, const float* __re
     const Node0 q = node0(a.d);
     if (seg_stopped(a.d.scal, q.seg)) return;
     float y[3];
-    if (q.valid) sliced_row32(a.d.wslot0, a.d.scol, a.val32, x, y);
+    if (q.valid) row0(a.d, a.val32, x, q.i, y);
     if (!q.valid) return;
 #pragma unroll
     for (int k = 0; k < 3; ++k) t[3 * q.i + k] = (float)r[3 * q.i + k] - y[k];
@@ -1085,7 +1103,7 @@ __global__ void k_v0_post(V0 a, const double* __restrict__ r, const float* __res
     const Node0 q = node0(a.d);
     if (seg_stopped(a.d.scal, q.seg)) return;
     float y[3];
-    if (q.valid) sliced_row32(a.d.wslot0, a.d.scol, a.val32, x, y);
+    if (q.valid) row0(a.d, a.val32, x, q.i, y);
     if (!q.valid) return;
     const float om = (float)__ldg(a.omega);
     float rr[3], z[3];

@@ -55,6 +55,35 @@ bool inverse3(const double M[9], double inv[9], double* det_out) {
     return true;
 }
 
+// Prism::calculateReferenceVolume (Prism.cpp:876-908) with
+// ShapeBase::calculateVolumeForInputShapeStructure (ShapeBase.cpp:3362-3395):
+// 8 triangles (2 bases, 3 split quads), each the base of a tetrahedron with
+// the prism's centre.
+double prism_volume(const double X[6][3]) {
+    static const int faces[8][3] = {{0, 1, 2}, {3, 4, 5}, {0, 1, 3}, {1, 3, 4},
+                                    {1, 2, 4}, {2, 4, 5}, {0, 2, 3}, {2, 3, 5}};
+    double c[3] = {0.0, 0.0, 0.0};
+    for (int a = 0; a < 6; ++a)
+        for (int k = 0; k < 3; ++k) c[k] += X[a][k];
+    for (int k = 0; k < 3; ++k) c[k] /= 6;
+    double vol = 0.0;
+    for (const auto& f : faces) {
+        double v1[3], v2[3], vm[3];
+        for (int k = 0; k < 3; ++k) {
+            v1[k] = X[f[1]][k] - X[f[0]][k];
+            v2[k] = X[f[2]][k] - X[f[0]][k];
+            vm[k] = c[k] - X[f[0]][k];
+        }
+        const double b[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2],
+                             v1[0] * v2[1] - v1[1] * v2[0]};
+        const double nb = std::sqrt(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+        double hgt = (vm[0] * b[0] + vm[1] * b[1] + vm[2] * b[2]) / nb;
+        if (hgt < 0) hgt *= -1.0;
+        vol += 1.0 / 3.0 * (hgt * (nb / 2));
+    }
+    return vol;
+}
+
 template <class T>
 tf_status dev_alloc(T** p, size_t n) {
     if (n == 0) n = 1;
@@ -88,6 +117,10 @@ void free_all(tf_handle* h) {
     if (h->amg) {
         amg_free(h->amg);
         h->amg = nullptr;
+    }
+    if (h->pk) {
+        packing_free(h->pk);
+        h->pk = nullptr;
     }
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -183,6 +216,7 @@ tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat, const st
     }
     // ---- reference geometry: dN_X per Gauss point --------------------------
     std::vector<double> gx(18 * 6 * (size_t)ne), wdet(6 * (size_t)ne), detd(6 * (size_t)ne);
+    h->h_vref.assign(ne, 0.0);
     double dN[6][3][6];
     for (int gp = 0; gp < 6; ++gp) shape_derivatives(gp, dN[gp]);
     for (int e = 0; e < ne; ++e) {
@@ -191,6 +225,7 @@ tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat, const st
             for (int c = 0; c < 3; ++c)
                 X[a][c] = m->ref_pos ? m->ref_pos[18 * (size_t)e + 3 * a + c]
                                      : m->node_pos[3 * (size_t)m->conn[6 * (size_t)e + a] + c];
+        h->h_vref[e] = prism_volume(X);
         for (int gp = 0; gp < 6; ++gp) {
             // dX/dxi = (dN X)^T   (Prism.cpp:705-728)
             double J[9];
@@ -222,6 +257,7 @@ tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat, const st
     h->h_nu.resize(ne);
     h->h_apical.resize(nn);
     for (int i = 0; i < nn; ++i) h->h_apical[i] = m->node_placement[i] == 1 ? 1 : 0;
+    h->h_place.assign(m->node_placement, m->node_placement + nn);
     for (int e = 0; e < ne; ++e) {
         double v = mat->nu[e];
         if (v > 0.5) v = 0.5;
@@ -606,6 +642,25 @@ __global__ void k_add_entries(int n, const int* __restrict__ off, const double* 
     if (k < n) atomicAdd(&val[off[k]], v[k]);
 }
 
+// The extra-block values of the current assembly back to the host copy
+// (needed before a host-side change when the device wrote some of them:
+// the packing Jacobian).
+tf_status sync_extra_to_host(tf_handle* h) {
+    if (!h->pk || h->d.nxb == 0) return TF_OK;
+    TF_CUDA(cudaMemcpyAsync(h->h_xval.data(), h->d.xval, sizeof(double) * 9 * (size_t)h->d.nxb,
+                            cudaMemcpyDeviceToHost, h->stream));
+    return sync(h);
+}
+
+// Adds block (J, I) to the user's extra pattern (kept apart from the
+// packing blocks, which change every step).
+void note_user_block(tf_handle* h, int J, int I) {
+    if (h->h_xuser.empty()) h->h_xuser.resize(h->d.nn);
+    std::vector<int>& xu = h->h_xuser[J];
+    auto it = std::lower_bound(xu.begin(), xu.end(), I);
+    if (it == xu.end() || *it != I) xu.insert(it, I);
+}
+
 // Re-uploads the extra blocks (pattern and values) after a change.
 tf_status upload_extra(tf_handle* h, bool pattern_changed) {
     Device& d = h->d;
@@ -626,6 +681,7 @@ tf_status upload_extra(tf_handle* h, bool pattern_changed) {
         TF_TRY(upload(&d.xcol, col));
         TF_TRY(dev_alloc(&d.xval, 9 * (size_t)d.nxb));
         destroy_graphs(h);  // the captured Krylov chunks hold the extra-block pointers
+        TF_TRY(packing_relink(h));
     }
     TF_CUDA(cudaMemcpyAsync(d.xval, h->h_xval.data(), sizeof(double) * 9 * (size_t)d.nxb, cudaMemcpyHostToDevice,
                             h->stream));
@@ -665,6 +721,7 @@ __global__ void k_equate(int n, const int* __restrict__ slave, const int* __rest
 // create outside the element pattern join the extra blocks.
 tf_status apply_bindings(tf_handle* h) {
     Device& d = h->d;
+    TF_TRY(sync_extra_to_host(h));
     const int nc = static_cast<int>(h->bind_slave.size());
     std::vector<char> involved(d.nn, 0);
     for (int k = 0; k < nc; ++k) {
@@ -788,6 +845,7 @@ tf_status apply_bindings(tf_handle* h) {
         std::vector<std::tuple<int, int, std::array<double, 9>>> extra;
         for (auto& kv : blk) {
             if (find_block(kv.first.first, kv.first.second) >= 0) continue;
+            note_user_block(h, kv.first.first, kv.first.second);
             std::vector<int>& xc = h->h_xcols[kv.first.first];
             auto jt = std::lower_bound(xc.begin(), xc.end(), kv.first.second);
             if (jt == xc.end() || *jt != kv.first.second) {
@@ -833,6 +891,52 @@ using namespace tf;
 
 extern "C" {
 
+tf_status tf_set_packing(tf_handle* h, int32_t enable, int32_t flags) {
+    TF_TRY(check_handle(h));
+    if (flags & ~1) return set_error("tf_set_packing: unknown flags"), TF_BAD_INPUT;
+    if (h->d.nseg != 1) return set_error("tf_set_packing: packing works on single-mesh handles"), TF_BAD_INPUT;
+    TF_CUDA(cudaSetDevice(h->device));
+    TF_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->pk) {
+        packing_free(h->pk);
+        h->pk = nullptr;
+    }
+    if (enable) {
+        const tf_status s = packing_setup(h, flags);
+        if (s != TF_OK) {
+            packing_free(h->pk);
+            h->pk = nullptr;
+            return s;
+        }
+    } else if (!h->h_xuser.empty() || !h->h_xcols.empty()) {
+        // back to the user's extra blocks only
+        if (h->h_xuser.empty()) h->h_xuser.resize(h->d.nn);
+        h->h_xcols = h->h_xuser;
+        int64_t nxb = 0;
+        for (const auto& xc : h->h_xcols) nxb += (int64_t)xc.size();
+        h->h_xval.assign(9 * (size_t)nxb, 0.0);
+        h->h_xcol_prev.clear();
+        for (const auto& xc : h->h_xcols) h->h_xcol_prev.insert(h->h_xcol_prev.end(), xc.begin(), xc.end());
+        TF_TRY(upload_extra(h, true));
+    }
+    return TF_OK;
+}
+
+tf_status tf_get_packing(tf_handle* h, int64_t* n, int32_t* nodes, double* weights, double* mbar, double* threshold,
+                         double* detect_distance) {
+    TF_TRY(check_handle(h));
+    if (!n) return set_error("tf_get_packing: n is required"), TF_BAD_INPUT;
+    TF_CUDA(cudaSetDevice(h->device));
+    return packing_get(h, n, nodes, weights, mbar, threshold, detect_distance);
+}
+
+tf_status tf_packing_masses(tf_handle* h, double* mass) {
+    TF_TRY(check_handle(h));
+    if (!mass) return set_error("tf_packing_masses: bad arguments"), TF_BAD_INPUT;
+    TF_CUDA(cudaSetDevice(h->device));
+    return packing_masses(h, mass);
+}
+
 tf_status tf_set_dof_bindings(tf_handle* h, int32_t n, const int32_t* slave_dofs, const int32_t* master_dofs) {
     TF_TRY(check_handle(h));
     if (n < 0 || (n > 0 && (!slave_dofs || !master_dofs))) return set_error("tf_set_dof_bindings: bad arguments"), TF_BAD_INPUT;
@@ -855,6 +959,7 @@ tf_status tf_add_K_triplets(tf_handle* h, int64_t n, const int32_t* rows, const 
     Device& d = h->d;
     const int64_t n3 = 3 * (int64_t)d.nn;
     if (h->h_xcols.empty()) h->h_xcols.resize(d.nn);
+    TF_TRY(sync_extra_to_host(h));
     std::vector<int> off;
     std::vector<double> v;
     struct Pending {
@@ -877,6 +982,7 @@ tf_status tf_add_K_triplets(tf_handle* h, int64_t n, const int32_t* rows, const 
             off.push_back(h->h_bofs[it - h->h_colidx.begin()] + kSlice * e);
             v.push_back(vals[k]);
         } else {
+            note_user_block(h, J, I);
             std::vector<int>& xc = h->h_xcols[J];
             auto jt = std::lower_bound(xc.begin(), xc.end(), I);
             if (jt == xc.end() || *jt != I) {
@@ -1122,6 +1228,7 @@ tf_status tf_begin_step(tf_handle* h, double dt) {
     TF_CUDA(cudaMemcpyAsync(h->d.un, h->d.uk, sizeof(double) * 3 * (size_t)h->d.nn, cudaMemcpyDeviceToDevice,
                             h->stream));
     h->assembled = false;
+    if (h->pk) TF_TRY(packing_detect(h));  // runOneStep: detectPacingNodes after growth (Simulation.cpp:5920)
     return TF_OK;
 }
 
@@ -1137,6 +1244,7 @@ tf_status tf_assemble(tf_handle* h) {
     TF_TRY(launch_prepare(h));
     TF_TRY(launch_element(h));
     if (h->opt.deterministic) TF_TRY(launch_deterministic_gather(h));
+    if (h->pk) TF_TRY(packing_assemble(h));  // after addImplicitKViscousExternalToJacobian (Simulation.cpp:6489-6493)
     h->assembled = true;
     return TF_OK;
 }
@@ -1251,6 +1359,7 @@ tf_status tf_export_csr(tf_handle* h, double drop_tol, int32_t* ia, int32_t* ja,
     if (!h->assembled) return set_error("tf_export_csr called before tf_assemble"), TF_BAD_INPUT;
     if (!nnz || (ia && (!ja || !a))) return set_error("bad output arrays"), TF_BAD_INPUT;
     const Device& d = h->d;
+    TF_TRY(sync_extra_to_host(h));
     std::vector<double> val((size_t)d.nval);
     TF_CUDA(cudaMemcpyAsync(val.data(), d.val, val.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     TF_TRY(sync(h));

@@ -120,7 +120,8 @@ constexpr int kNodeThreads = 256;    // nodes per CTA of the node-parallel kerne
 constexpr int kWarps = kNodeThreads / 32;
 constexpr int kAmgMaxLevels = 10;
 
-struct Amg;  // multigrid hierarchy (tf_amg.cu)
+struct Amg;      // multigrid hierarchy (tf_amg.cu)
+struct Packing;  // packing between tissue surfaces (tf_packing.cu)
 
 // Programmatic dependent launch for the chains of short kernels of the
 // linear solve: a kernel launched with launch_pdl may be scheduled as its
@@ -201,6 +202,9 @@ struct tf_handle {
     std::vector<uint8_t> h_fixed;
     std::vector<double> h_nu;                   // Poisson ratios, clamped as the material setup does
     std::vector<int> h_apical;                  // 1 for apical nodes (tissue placement 1)
+    std::vector<int> h_place;                   // node placement (0 basal, 1 apical, 2 mid, 3 lateral)
+    std::vector<double> h_vref;                 // reference volume of each prism
+    std::vector<std::vector<int>> h_xuser;      // extra blocks of tf_add_K_triplets and DOF bindings
     std::vector<int> h_seg_node0, h_seg_elem0;  // host copies of the instance offsets
     std::vector<int> h_active;                  // host mirror of seg_active
     int elem_cta = 16;                          // prisms per CTA of the element kernel (autotuned)
@@ -209,6 +213,7 @@ struct tf_handle {
     int64_t graph_kernels[2][4] = {};
     int last_iters[2] = {0, 0};                 // iterations of the last solve per method (chunk planning)
     tf::Amg* amg = nullptr;                     // multigrid preconditioner (null: block-Jacobi)
+    tf::Packing* pk = nullptr;                  // packing between tissue surfaces (null: off)
 };
 
 namespace tf {
@@ -246,6 +251,20 @@ void amg_vcycle(tf_handle* h, const double* r, double* out);
 int amg_vcycle_kernels(const tf_handle* h);
 void amg_free(Amg* a);
 void amg_mark_stale(tf_handle* h, int level);  // 1: new assembly, 2: rebuild the hierarchy
+tf_status packing_setup(tf_handle* h, int flags); // switch packing on (device tables)
+tf_status packing_detect(tf_handle* h);          // couples at the current positions (step start)
+tf_status packing_get(tf_handle* h, int64_t* n, int32_t* nodes, double* w, double* mbar, double* threshold,
+                      double* detect);
+tf_status packing_masses(tf_handle* h, double* mass);
+tf_status packing_assemble(tf_handle* h);        // forces and Jacobian into g and K
+tf_status packing_relink(tf_handle* h);          // couple blocks in the current extra-block layout
+// The multigrid preconditioner is used unless packing couples are present:
+// its hierarchy follows the element graph, which never joins the coupled
+// surfaces, so its coarse correction would miss their (stiff) coupling.
+bool use_multigrid(const tf_handle* h);
+void packing_free(Packing* p);
+tf_status upload_extra(tf_handle* h, bool pattern_changed);
+tf_status sync_extra_to_host(tf_handle* h);      // device extra-block values -> h_xval
 bool amg_reused(const tf_handle* h);
 tf_status launch_adjoint_element(tf_handle* h, const double* lamv, double* carry, double* gr, double* ge, double ndt);
 void destroy_graphs(tf_handle* h);

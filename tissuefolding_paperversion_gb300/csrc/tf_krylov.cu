@@ -609,7 +609,7 @@ void issue_iterations(tf_handle* h, const Ctx& c, int method, int n) {
     Device& d = h->d;
     cudaStream_t st = h->stream;
     const int nb = d.ncta;
-    const int jac = h->amg ? 0 : 1;
+    const int jac = use_multigrid(h) ? 0 : 1;
     for (int it = 0; it < n; ++it) {
         if (method == 1) {
             launch_pdl(k_cg_spmv, nb, kThreads, st, c, d.p, d.q);
@@ -633,7 +633,7 @@ void issue_iterations(tf_handle* h, const Ctx& c, int method, int n) {
 }
 
 int kernels_per_iteration(const tf_handle* h, int method) {
-    if (!h->amg) return method == 1 ? 3 : 6;
+    if (!use_multigrid(h)) return method == 1 ? 3 : 6;
     const int v = amg_vcycle_kernels(h);
     return method == 1 ? 4 + v : 6 + 2 * v;
 }
@@ -666,13 +666,13 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
     const Ctx c = make_ctx(h);
     cudaStream_t st = h->stream;
     const double tol2 = h->opt.krylov_rtol * h->opt.krylov_rtol;
-    const int jac = h->amg ? 0 : 1;
+    const int jac = use_multigrid(h) ? 0 : 1;
     if (keep == 2) {  // BiCGStab restart: block inverse and x are kept
         k_bi_restart<<<d.ncta, kThreads, 0, st>>>(c, d.r, d.rhat, d.p, d.q);
     } else {
         const tf_status sb = launch_block_inverse(h);
         if (sb != TF_OK) return sb;
-        if (h->amg) {
+        if (use_multigrid(h)) {
             const tf_status sa = amg_numeric(h);
             if (sa != TF_OK) return sa;
         }
@@ -776,7 +776,7 @@ tf_status krylov_solve(tf_handle* h, int* iters, double* relres) {
     TF_CUDA(cudaMemcpyAsync(d.seg_solve, d.seg_active, sizeof(int) * (size_t)d.nseg, cudaMemcpyDeviceToDevice,
                             h->stream));
     tf_status s = krylov_run(h, h->method, 0, iters, relres);
-    if (s != TF_OK && amg_reused(h)) {
+    if (s != TF_OK && use_multigrid(h) && amg_reused(h)) {
         // the coarse levels came from an earlier Newton iteration: rebuild
         // them for this matrix and solve again
         amg_mark_stale(h, 2);

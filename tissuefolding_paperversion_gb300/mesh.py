@@ -269,6 +269,46 @@ def config_tiny(seed: int = 0, n: int = 4, n_layers: int = 2, eta: float = 0.0,
                   name=f"tiny-{ne}")
 
 
+def config_facing_sheets(seed: int = 0, n: int = 5, n_layers: int = 2, gap: float = 1.2, eta: float = 0.0,
+                         E: float = 1000.0, nu: float = 0.3, jitter: float = 0.3, spacing: float = 5.0,
+                         offset=(0.0, 0.0), shuffle: bool = True) -> Tissue:
+    """Two n x n sheets whose apical surfaces face each other across `gap`
+    (µm): the lower one as config_tiny builds it, the upper one mirrored in z
+    (its basal surface on top, its prisms re-ordered so their basal triangle
+    stays counter-clockwise seen from the apical side) and shifted in xy by
+    `offset`.  Both basal surfaces are fixed in z.  Apical nodes of the two
+    sheets closer than the packing detection distance are what the
+    reference's packing (Simulation::detectPacingNodes) couples.  `shuffle`
+    renumbers the nodes by a seeded permutation, so that packing couples
+    start from nodes all over the node order (node 0 keeps its place: the
+    reference's bounding box never tests node 0 for the maximum)."""
+    rng = np.random.default_rng(seed)
+    thick = spacing * n_layers
+    pa, ca, la = rect_sheet(n, n, spacing, n_layers, thick, jitter, rng)
+    pb, cb, lb = rect_sheet(n, n, spacing, n_layers, thick, jitter, rng)
+    pb = pb.reshape(-1, 3).copy()
+    pb[:, 0] += offset[0]
+    pb[:, 1] += offset[1]
+    pb[:, 2] = 2.0 * thick + gap - pb[:, 2]
+    cb = cb.reshape(-1, 6)[:, [0, 2, 1, 3, 5, 4]] + pa.size // 3
+    pos = np.concatenate([pa.reshape(-1, 3), pb]).reshape(-1)
+    conn = np.concatenate([ca.reshape(-1, 6), cb]).reshape(-1).astype(np.int32)
+    pl = np.concatenate([la, lb]).astype(np.int32)
+    nn = pl.size
+    if shuffle:
+        perm = np.concatenate([[0], 1 + rng.permutation(nn - 1)])  # new id of each old node
+        inv = np.argsort(perm)
+        pos = pos.reshape(-1, 3)[inv].reshape(-1)
+        pl = pl[inv]
+        conn = perm[conn].astype(np.int32)
+    ne = conn.size // 6
+    rates = np.zeros((ne, 3))
+    rates[:, 0] = rates[:, 1] = 0.01 / HOUR
+    return Tissue(pos=pos, conn=conn, fixed=_bc_basal_z_fixed(pl), ext_visc=_ext_visc_surfaces(pl, 10.0, 10.0),
+                  node_placement=pl, E=np.full(ne, E) * rng.uniform(0.8, 1.2, size=ne), nu=np.full(ne, nu),
+                  eta=np.full(ne, eta), rates=rates.reshape(-1), dt=60.0, n_steps=3, name=f"facing-{ne}")
+
+
 def config_batch_instance(seed: int, min_prisms: int = 1000, max_prisms: int = 50000) -> Tissue:
     """One instance of the batched sweep: prism count log-uniform in
     [1k, 50k], 2-4 layers, rectangular or elliptical, seeded E, nu in
