@@ -428,6 +428,72 @@ def run_adjoint(args, t):
     }))
 
 
+def run_packing(args):
+    """Implicit packing between two facing sheets: the per-step couple
+    detection (the reference's O(N^2) detectPacingNodes) and the packing terms
+    of an assembly, on the GPU; the CPU baseline is the restatement of the
+    reference's scan timed on a sample of first nodes."""
+    from tissuefolding_paperversion_gb300 import api, mesh
+
+    t = mesh.config_facing_sheets(seed=0, n=args.pack_n, gap=1.5, E=100000.0)
+    nn = t.n_nodes
+    times = {}
+    with api.Solver(t, precond=1) as s:
+        s.set_positions(t.pos)
+        for pack in (False, True):
+            s.set_packing(pack)
+            for _ in range(args.warmup):
+                s.begin_step(t.dt)
+            w = []
+            a = []
+            for _ in range(args.steps):
+                w0 = time.perf_counter()
+                s.begin_step(t.dt)            # synchronous: detection reads the couple count back
+                w.append(time.perf_counter() - w0)
+                s.set_state(t.pos, t.pos, t.dt)
+                s.residual()
+                w0 = time.perf_counter()
+                s.assemble()
+                s.residual()                   # waits for the assembly
+                a.append(time.perf_counter() - w0)
+            times[pack] = (float(np.median(w)), float(np.median(a)))
+        pk = s.packing()
+        l0 = s.launch_count()
+        s.begin_step(t.dt)
+        launches = s.launch_count() - l0
+    detect_s = times[True][0] - times[False][0]
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import packing as op
+        vref = op.reference_volumes(t.pos.reshape(-1, 3)[t.conn.reshape(-1, 6)])
+        m = op.node_masses(t.conn, nn, vref, np.tile(np.eye(3), (t.n_elems, 1, 1)))
+        elig = np.flatnonzero((m != 0) & ((t.node_placement == 0) | (t.node_placement == 1)))
+        sample = np.random.default_rng(0).choice(elig, size=min(400, elig.size), replace=False)
+        sample.sort()
+        nb = op.neighbours(t.conn, nn)
+        w0 = time.perf_counter()
+        op.detect(t.pos, t.conn, t.node_placement, m, True, masters=sample, nb=nb)
+        per = (time.perf_counter() - w0) / sample.size
+        full_s = per * elig.size
+        cpu = {"value": nn / full_s, "unit": "nodes/s", "cores": 1, "kind": "port",
+               "sample": f"O(N^2) scan (numpy over the partners of each first node) from {sample.size} of "
+                         f"{elig.size} eligible first nodes, {per * sample.size:.1f} s; full scan estimated "
+                         f"{full_s:.0f} s"}
+    print(json.dumps({
+        "metric": "packing couple detection, nodes/s", "value": nn / detect_s, "unit": "nodes/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": detect_s * 1e3, "higher_is_better": True,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"packing-facing-sheets-{t.n_elems}", "nodes": nn, "prisms": t.n_elems,
+                   "gap_um": 1.5, "couples": int(len(pk["nodes"])), "detect_distance_um": pk["detect"]},
+        "detection_ms": detect_s * 1e3,
+        "packing_assembly_ms": (times[True][1] - times[False][1]) * 1e3,
+        "begin_step_ms": {"without": times[False][0] * 1e3, "with": times[True][0] * 1e3},
+        "timing": "host wall clock around synchronous calls, median of the timed steps",
+        "gpu_launches": launches,
+        "cpu_baseline": cpu,
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -435,9 +501,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="large", choices=["large", "medium", "small", "wing"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint", "packing"],
                     help="plain: the 320k-prism Newton step; batch: the 256-instance sweep; "
-                         "adjoint: gradient of an apical shape loss through n steps")
+                         "adjoint: gradient of an apical shape loss through n steps; "
+                         "packing: couple detection between two facing sheets")
+    ap.add_argument("--pack-n", type=int, default=200, help="nodes per side of each sheet (packing workload)")
     ap.add_argument("--adj-steps", type=int, default=50)
     ap.add_argument("--adj-every", type=int, default=10)
     ap.add_argument("--adj-fd", type=int, default=0, help="central-difference checks along random directions")
@@ -454,6 +522,9 @@ def main():
 
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "packing":
+        run_packing(args)
         return
     if args.config == "large":
         t = mesh.config_large(seed=0)

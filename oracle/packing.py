@@ -71,32 +71,38 @@ def node_masses(conn, n_nodes, vref, Fg):
     return m
 
 
-def _side_avg(p, pairs):
-    s, n = 0.0, 0
+def _side_avg(P, c, pairs):
+    """Prism::getApicalSideLengthAverage / getBasalSideLengthAverage
+    (Prism.cpp:1443-1490) for every prism: mean of the non-zero side lengths
+    of the triangle (0 if all are zero)."""
+    s = np.zeros(c.shape[0])
+    n = np.zeros(c.shape[0])
     for a, b in pairs:
-        d = p[a] - p[b]
-        d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2]
-        if d2 > 0:
-            s += d2 ** 0.5
-            n += 1
-    return s / n if n > 0 else s
+        d = P[c[:, a]] - P[c[:, b]]
+        d2 = d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2]
+        pos = d2 > 0
+        s = np.where(pos, s + np.sqrt(d2), s)
+        n = n + pos
+    return np.where(n > 0, s / np.maximum(n, 1), s)
 
 
 def side_lengths(pos, conn, placement):
     """(colAverageSideLength, grid[0][0]) of getAverageSideLength for a
-    tissue of columnar prisms."""
+    tissue of columnar prisms (sums in prism order)."""
     P = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
     c = np.asarray(conn).reshape(-1, 6)
     pl = np.asarray(placement)
+    ap = _side_avg(P, c, [(3, 4), (3, 5), (4, 5)])
+    bs = _side_avg(P, c, [(0, 1), (0, 2), (1, 2)])
+    basal = np.any(pl[c] == 0, axis=1)            # basal placement or spans the whole tissue
     dsum, n, gsum = 0.0, 0, 0.0
     for e in range(c.shape[0]):
-        p = P[c[e]]
-        v = _side_avg(p, [(3, 4), (3, 5), (4, 5)])
+        v = ap[e]
         if v > 0:
             dsum += v
             n += 1
-        if np.any(pl[c[e]] == 0):          # basal placement or spans the whole tissue
-            v = _side_avg(p, [(0, 1), (0, 2), (1, 2)])
+        if basal[e]:
+            v = bs[e]
             if v > 0:
                 dsum += v
                 n += 1
@@ -113,9 +119,11 @@ def neighbours(conn, n_nodes):
     return nb
 
 
-def detect(pos, conn, placement, masses, drop_last_segment=True):
+def detect(pos, conn, placement, masses, drop_last_segment=True, masters=None, nb=None):
     """Couples of detectPacingNodes at positions `pos`: dict with nodes
-    (n, 2), w (n, 3), mbar (n,), threshold, detect."""
+    (n, 2), w (n, 3), mbar (n,), threshold, detect.  `masters` restricts the
+    scan to those first nodes (a timing sample); `nb` passes precomputed
+    neighbour sets."""
     P = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
     nn = P.shape[0]
     pl = np.asarray(placement)
@@ -125,11 +133,12 @@ def detect(pos, conn, placement, masses, drop_last_segment=True):
     bb0 = P.min(axis=0)
     bbs = P.max(axis=0) - bb0
     eligible = (masses != 0) & ((pl == 0) | (pl == 1))
-    nb = neighbours(conn, nn)
+    if nb is None:
+        nb = neighbours(conn, nn)
     seg = max(nn // 16, 1)
     last = (nn // seg - 1) * seg
     c0, c1, w = [], [], []
-    for a in range(nn):
+    for a in (range(nn) if masters is None else masters):
         if not eligible[a] or (drop_last_segment and a >= last):
             continue
         gx = np.floor((P[a, 0] - bb0[0]) / bbs[0])

@@ -47,7 +47,6 @@ namespace {
 constexpr double kMultiplier = 5000.0;  // packingMultiplier (Simulation.cpp:8187)
 constexpr double kSaturation = 5.0;     // sigmoidSaturationForPacking (:8188)
 constexpr int kT = 256;
-constexpr int kRed = 1024;               // threads of the one-CTA reductions
 enum Par { P_THR = 0, P_DET, P_T2, P_BB0X, P_BB0Y, P_BBSX, P_BBSY, P_CELL, P_COUNT = 8 };
 
 #define PK_TRY(expr)                \
@@ -87,6 +86,8 @@ struct Packing {
     int* nelem = nullptr;
     double* mass = nullptr;    // [nn] node masses of the step
     double* par = nullptr;     // [P_COUNT] parameters of the detection
+    double* part = nullptr;    // per-CTA partials of the parameter reduction
+    unsigned* ticket = nullptr;
     int T = 0;                 // hash table size (power of two)
     int* hoff = nullptr;       // [T+1] counts, then offsets
     int* hcur = nullptr;       // [T] fill cursors
@@ -109,11 +110,13 @@ struct Packing {
     double h_par[P_COUNT] = {};
     std::vector<int> h_c0, h_c1;
     std::vector<std::pair<int, int>> h_blocks;  // extra blocks (J, I) of the current couples
+    bool linked = false;       // incidence tables and block positions match h_c0 / h_c1
 };
 
 void packing_free(Packing* p) {
     if (!p) return;
-    void* ptrs[] = {p->place, p->vref, p->ebasal, p->nptr, p->nelem, p->mass, p->par, p->hoff, p->hcur, p->hids,
+    void* ptrs[] = {p->place, p->vref, p->ebasal, p->nptr, p->nelem, p->mass, p->par, p->part, p->ticket,
+                    p->hoff, p->hcur, p->hids,
                     p->ccount, p->scan_tmp, p->c0, p->c1, p->w, p->mbar, p->x01, p->x10, p->pnode, p->pptr,
                     p->plist};
     for (void* q : ptrs)
@@ -246,13 +249,22 @@ __device__ double block_sum(double v, double* sm) {
     return t;
 }
 
-// One CTA: side-length means, bounding box and the detection parameters.
-__global__ void __launch_bounds__(kRed) k_pk_params(int nn, int ne, const double* __restrict__ pos,
-                                                    const int* __restrict__ conn, const uint8_t* __restrict__ ebasal,
-                                                    double* __restrict__ par) {
-    __shared__ double sm[kRed / 32];
+// Side-length sums and the bounding box over the whole grid: per-CTA
+// partials, folded in CTA order by the last CTA to arrive (no waiting), which
+// writes the detection parameters.
+constexpr int kParCtas = 2 * 152;
+constexpr int kPart = 7;  // dsum, count, grid sum, min x, min y, max x, max y
+
+__global__ void __launch_bounds__(kT) k_pk_params(int nn, int ne, const double* __restrict__ pos,
+                                                  const int* __restrict__ conn, const uint8_t* __restrict__ ebasal,
+                                                  double* __restrict__ part, unsigned* __restrict__ ticket,
+                                                  double* __restrict__ par) {
+    __shared__ double sm[kT / 32];
+    __shared__ double smn[2][kT / 32], smx[2][kT / 32];
+    __shared__ bool last;
     double ds = 0.0, dn = 0.0, gs = 0.0;
-    for (int e = threadIdx.x; e < ne; e += blockDim.x) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
         double v = side_avg(pos, conn, ne, e, 3);
         if (v > 0) {
             ds += v;
@@ -268,14 +280,13 @@ __global__ void __launch_bounds__(kRed) k_pk_params(int nn, int ne, const double
         gs += v;
     }
     double mn[2] = {INFINITY, INFINITY}, mx[2] = {-INFINITY, -INFINITY};
-    for (int i = threadIdx.x; i < nn; i += blockDim.x)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += stride)
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             mn[k] = fmin(mn[k], pos[3 * i + k]);
             mx[k] = fmax(mx[k], pos[3 * i + k]);
         }
     const double tds = block_sum(ds, sm), tdn = block_sum(dn, sm), tgs = block_sum(gs, sm);
-    __shared__ double smn[2][kRed / 32], smx[2][kRed / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
@@ -291,25 +302,45 @@ __global__ void __launch_bounds__(kRed) k_pk_params(int nn, int ne, const double
         }
     }
     __syncthreads();
-    if (threadIdx.x != 0) return;
-    double bmn[2], bmx[2];
-    for (int k = 0; k < 2; ++k) {
-        bmn[k] = INFINITY;
-        bmx[k] = -INFINITY;
-        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
-            bmn[k] = fmin(bmn[k], smn[k][q]);
-            bmx[k] = fmax(bmx[k], smx[k][q]);
+    if (threadIdx.x == 0) {
+        double* pp = part + (size_t)kPart * blockIdx.x;
+        pp[0] = tds;
+        pp[1] = tdn;
+        pp[2] = tgs;
+        for (int k = 0; k < 2; ++k) {
+            double a = INFINITY, b = -INFINITY;
+            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+                a = fmin(a, smn[k][q]);
+                b = fmax(b, smx[k][q]);
+            }
+            pp[3 + k] = a;
+            pp[5 + k] = b;
+        }
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double t[kPart] = {0.0, 0.0, 0.0, INFINITY, INFINITY, -INFINITY, -INFINITY};
+    for (unsigned c = 0; c < gridDim.x; ++c) {
+        const double* pp = part + (size_t)kPart * c;
+        for (int k = 0; k < 3; ++k) t[k] += __ldcg(&pp[k]);
+        for (int k = 0; k < 2; ++k) {
+            t[3 + k] = fmin(t[3 + k], __ldcg(&pp[3 + k]));
+            t[5 + k] = fmax(t[5 + k], __ldcg(&pp[5 + k]));
         }
     }
-    const double col = tds / tdn;
-    const double g00 = 0.4 * (tgs / ne);
+    *ticket = 0u;
+    const double col = t[0] / t[1];
+    const double g00 = 0.4 * (t[2] / ne);
     par[P_THR] = 0.4 * col;
     par[P_DET] = g00;
     par[P_T2] = g00 * g00;
-    par[P_BB0X] = bmn[0];
-    par[P_BB0Y] = bmn[1];
-    par[P_BBSX] = bmx[0] - bmn[0];
-    par[P_BBSY] = bmx[1] - bmn[1];
+    par[P_BB0X] = t[3];
+    par[P_BB0Y] = t[4];
+    par[P_BBSX] = t[5] - t[3];
+    par[P_BBSY] = t[6] - t[4];
     par[P_CELL] = g00 * (1.0 + 1e-9);  // cells a hair wider than the distance: no pair is missed by rounding
 }
 
@@ -566,6 +597,9 @@ tf_status packing_setup(tf_handle* h, int flags) {
     PK_TRY(put(&p->nelem, nelem));
     PK_TRY(alloc(&p->mass, d.nn));
     PK_TRY(alloc(&p->par, P_COUNT));
+    PK_TRY(alloc(&p->part, (size_t)kPart * kParCtas));
+    PK_TRY(alloc(&p->ticket, 1));
+    TF_CUDA(cudaMemset(p->ticket, 0, sizeof(unsigned)));
     PK_TRY(alloc(&p->hoff, (size_t)T + 1));
     PK_TRY(alloc(&p->hcur, (size_t)T));
     PK_TRY(alloc(&p->hids, d.nn));
@@ -583,7 +617,7 @@ tf_status packing_detect(tf_handle* h) {
     const int nn = d.nn;
     k_pk_mass<<<cdiv(nn, kT), kT, 0, st>>>(nn, d.ne, d.Fg, p->vref, p->nptr, p->nelem, p->mass);
     TF_LAUNCH_CHECK(h);
-    k_pk_params<<<1, kRed, 0, st>>>(nn, d.ne, d.uk, d.conn, p->ebasal, p->par);
+    k_pk_params<<<kParCtas, kT, 0, st>>>(nn, d.ne, d.uk, d.conn, p->ebasal, p->part, p->ticket, p->par);
     TF_LAUNCH_CHECK(h);
     TF_CUDA(cudaMemsetAsync(p->hoff, 0, sizeof(int) * ((size_t)p->T + 1), st));
     k_pk_hcount<<<cdiv(nn, kT), kT, 0, st>>>(nn, d.uk, p->mass, p->place, p->par, p->T, p->hoff);
@@ -620,13 +654,16 @@ tf_status packing_detect(tf_handle* h) {
         k_pk_fill<<<cdiv(nn, kT), kT, 0, st>>>(S, p->ccount, p->c0, p->c1, p->w, p->mbar);
         TF_LAUNCH_CHECK(h);
     }
-    p->h_c0.resize(total);
-    p->h_c1.resize(total);
+    std::vector<int> c0(total), c1(total);
     if (total > 0) {
-        TF_CUDA(cudaMemcpyAsync(p->h_c0.data(), p->c0, sizeof(int) * (size_t)total, cudaMemcpyDeviceToHost, st));
-        TF_CUDA(cudaMemcpyAsync(p->h_c1.data(), p->c1, sizeof(int) * (size_t)total, cudaMemcpyDeviceToHost, st));
+        TF_CUDA(cudaMemcpyAsync(c0.data(), p->c0, sizeof(int) * (size_t)total, cudaMemcpyDeviceToHost, st));
+        TF_CUDA(cudaMemcpyAsync(c1.data(), p->c1, sizeof(int) * (size_t)total, cudaMemcpyDeviceToHost, st));
     }
     TF_CUDA(cudaStreamSynchronize(st));
+    if (p->linked && c0 == p->h_c0 && c1 == p->h_c1) return TF_OK;  // same couples: tables still valid
+    p->h_c0.swap(c0);
+    p->h_c1.swap(c1);
+    p->linked = true;
     // per-node incidence in couple order
     {
         std::vector<int> cnt(nn, 0);
