@@ -27,7 +27,8 @@
 //   6x6 block inverses; Gauss-Jordan inverse of the coarsest level per
 //   instance (<= 16 nodes).
 // Application (one V-cycle per preconditioner call, all kernels, capturable
-// in a CUDA graph): damped block-Jacobi pre- and post-smoothing, residual,
+// in a CUDA graph): damped block-Jacobi pre- and post-smoothing (one sweep
+// each way at level 0, kCoarseSweeps on the coarser levels), residual,
 // restriction, coarse correction.  Kernels of an instance whose Krylov
 // solve has stopped return at once.
 // Precision: the preconditioner is any fixed linear operator as far as the
@@ -55,6 +56,13 @@ constexpr int kCoarseDofs = 6 * kCoarseNodes;
 constexpr int kPowerIters = 16;
 constexpr int kTailNodes = 256;   // levels with at most this many nodes per instance run fused
 constexpr int kTailThreads = 1024;
+// damped block-Jacobi sweeps before and after the coarse correction on the
+// levels >= 1 (level 0 sweeps once each way): more sweeps on the small,
+// launch-bound coarse levels cut the Krylov iterations (320,000-prism sheet:
+// 88 / 64 / 58 per step with 1 / 2 / 3 sweeps, 80 / 68.7 / 68.4 ms; 1M-prism
+// wing: 201 / 150 / 128, 177 / 153 / 144 ms) while extra level-0 sweeps,
+// which cost a full-size SpMV each, barely do
+constexpr int kCoarseSweeps = 3;
 
 // ---- host set-up -----------------------------------------------------------------
 
@@ -1185,10 +1193,10 @@ __global__ void k_restrict(AmgLevel F, AmgLevel C, const float* __restrict__ t, 
 }
 
 // x_i += sum over the prolongator blocks (i, J) of P_iJ e_J (6-DOF level)
-__device__ __forceinline__ void prolong_node(const AmgLevel& F, const float* __restrict__ e, int i) {
+__device__ __forceinline__ void prolong_node(const AmgLevel& F, const float* __restrict__ e, int i, float* x) {
     float s[6];
 #pragma unroll
-    for (int k = 0; k < 6; ++k) s[k] = F.x[6 * i + k];
+    for (int k = 0; k < 6; ++k) s[k] = x[6 * i + k];
     for (int b = __ldg(&F.prow[i]); b < __ldg(&F.prow[i + 1]); ++b) {
         const int J = __ldg(&F.pcol[b]);
         const float* __restrict__ P = F.Pv + 36 * (size_t)b;
@@ -1201,7 +1209,7 @@ __device__ __forceinline__ void prolong_node(const AmgLevel& F, const float* __r
             for (int c = 0; c < 6; ++c) s[k] = fmaf(__ldg(&P[6 * k + c]), ec[c], s[k]);
     }
 #pragma unroll
-    for (int k = 0; k < 6; ++k) F.x[6 * i + k] = s[k];
+    for (int k = 0; k < 6; ++k) x[6 * i + k] = s[k];
 }
 
 // out_i = x_i + omega D_i^-1 (r - A x)_i for row i, by one warp
@@ -1217,13 +1225,13 @@ __device__ __forceinline__ void post_row(const AmgLevel& L, const double* __rest
 }
 
 // t = r - A x  (one warp per row)
-__global__ void k_v6_resid(AmgLevel L, const double* __restrict__ scal) {
+__global__ void k_v6_resid(AmgLevel L, const double* __restrict__ scal, const float* __restrict__ x) {
     pdl_enter();
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= L.n || seg_stopped(scal, L.seg[i])) return;
     float y[6];
-    row6_warp(L, i, L.x, y);
+    row6_warp(L, i, x, y);
     if (lane < 6) L.t[6 * i + lane] = L.r[6 * i + lane] - pick6(y, lane);
 }
 
@@ -1236,12 +1244,24 @@ __global__ void k_v6_post(AmgLevel L, const double* __restrict__ scal, const dou
     post_row(L, omega, x, out, i);
 }
 
-// x_i += P_i e_agg(i)  (6-DOF fine level)
-__global__ void k_v6_prolong(AmgLevel F, const double* __restrict__ scal, const float* __restrict__ e) {
+// x_i += P_i e  (6-DOF fine level)
+__global__ void k_v6_prolong(AmgLevel F, const double* __restrict__ scal, const float* __restrict__ e, float* x) {
     pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= F.n || seg_stopped(scal, F.seg[i])) return;
-    prolong_node(F, e, i);
+    prolong_node(F, e, i, x);
+}
+
+// Buffers of the damped-Jacobi sweeps of a coarse level (a sweep reads one
+// vector and writes another): the pre-sweeps after the first (fused into the
+// restriction, into x) alternate x and e; the post-sweeps alternate x and t
+// and the last writes e, the level's output.
+__host__ __device__ __forceinline__ float* pre_sweep_out(const AmgLevel& L, const float* cur) {
+    return cur == L.x ? L.e : L.x;
+}
+__host__ __device__ __forceinline__ float* post_sweep_out(const AmgLevel& L, const float* cur, int s, int sweeps) {
+    if (s == sweeps) return L.e;
+    return cur == L.x ? L.t : L.x;
 }
 
 // e = C^-1 r on the coarsest level, one CTA per instance
@@ -1270,6 +1290,7 @@ struct Tail {
     const int* cinv0;
     const float* cinv;
     int first, last;
+    int sweeps;  // pre- and post-smoothing sweeps per level
 };
 
 __global__ void __launch_bounds__(kTailThreads) k_tail(Tail T) {
@@ -1277,12 +1298,21 @@ __global__ void __launch_bounds__(kTailThreads) k_tail(Tail T) {
     const int g = blockIdx.x;
     if (seg_stopped(T.scal, g)) return;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    float* cur[kAmgMaxLevels];
     for (int l = T.first; l < T.last; ++l) {
         const AmgLevel& F = T.L[l];
         const AmgLevel& C = T.L[l + 1];
+        float* x = F.x;
+        for (int s = 2; s <= T.sweeps; ++s) {
+            float* out = pre_sweep_out(F, x);
+            for (int i = F.seg0[g] + warp; i < F.seg0[g + 1]; i += nw) post_row(F, T.omega + l, x, out, i);
+            __syncthreads();
+            x = out;
+        }
+        cur[l] = x;
         for (int i = F.seg0[g] + warp; i < F.seg0[g + 1]; i += nw) {
             float y[6];
-            row6_warp(F, i, F.x, y);
+            row6_warp(F, i, x, y);
             if (lane < 6) F.t[6 * i + lane] = F.r[6 * i + lane] - pick6(y, lane);
         }
         __syncthreads();
@@ -1303,10 +1333,15 @@ __global__ void __launch_bounds__(kTailThreads) k_tail(Tail T) {
     __syncthreads();
     for (int l = T.last - 1; l >= T.first; --l) {
         const AmgLevel& F = T.L[l];
-        for (int i = F.seg0[g] + threadIdx.x; i < F.seg0[g + 1]; i += blockDim.x) prolong_node(F, T.L[l + 1].e, i);
+        float* x = cur[l];
+        for (int i = F.seg0[g] + threadIdx.x; i < F.seg0[g + 1]; i += blockDim.x) prolong_node(F, T.L[l + 1].e, i, x);
         __syncthreads();
-        for (int i = F.seg0[g] + warp; i < F.seg0[g + 1]; i += nw) post_row(F, T.omega + l, F.x, F.e, i);
-        __syncthreads();
+        for (int s = 1; s <= T.sweeps; ++s) {
+            float* out = post_sweep_out(F, x, s, T.sweeps);
+            for (int i = F.seg0[g] + warp; i < F.seg0[g + 1]; i += nw) post_row(F, T.omega + l, x, out, i);
+            __syncthreads();
+            x = out;
+        }
     }
 }
 
@@ -1404,8 +1439,9 @@ tf_status amg_numeric(tf_handle* h) {
 
 int amg_vcycle_kernels(const tf_handle* h) {
     const Amg* a = h->amg;
-    if (a->tail > 0) return 4 * a->tail + 2;
-    return 4 * (a->nlev - 2) + 6 + (a->coarse_exact ? 0 : 2);
+    const int per = 2 * kCoarseSweeps + 2;  // kernels of a coarse level run kernel by kernel
+    if (a->tail > 0) return 5 + per * (a->tail - 1) + 1;
+    return 5 + per * (a->nlev - 2) + (a->coarse_exact ? 1 : 3);
 }
 
 // out = M^-1 r: one V-cycle (all launches on h->stream, no host work).
@@ -1424,9 +1460,19 @@ void amg_vcycle(tf_handle* h, const double* r, double* out) {
     launch_pdl(k_v0_resid, d.ncta, kNodeThreads, st, v0, r, L0.x, L0.t);
     launch_pdl(k_restrict<3>, cdiv(32 * (int64_t)a->L[1].n, kT), kT, st, L0, a->L[1], (const float*)L0.t,
                (const double*)d.scal, (const double*)(a->omega + 1), presmooth(1));
+    float* cur[kAmgMaxLevels] = {};
     for (int l = 1; l < stop; ++l) {
         AmgLevel& L = a->L[l];
-        launch_pdl(k_v6_resid, cdiv(32 * (int64_t)L.n, kT), kT, st, L, (const double*)d.scal);
+        const int nb = cdiv(32 * (int64_t)L.n, kT);
+        float* x = L.x;  // first pre-sweep: fused into the restriction
+        for (int s = 2; s <= kCoarseSweeps; ++s) {
+            float* o = pre_sweep_out(L, x);
+            launch_pdl(k_v6_post, nb, kT, st, L, (const double*)d.scal, (const double*)(a->omega + l),
+                       (const float*)x, o);
+            x = o;
+        }
+        cur[l] = x;
+        launch_pdl(k_v6_resid, nb, kT, st, L, (const double*)d.scal, (const float*)x);
         launch_pdl(k_restrict<6>, cdiv(32 * (int64_t)a->L[l + 1].n, kT), kT, st, L, a->L[l + 1], (const float*)L.t,
                    (const double*)d.scal, (const double*)(a->omega + l + 1), presmooth(l + 1));
     }
@@ -1439,6 +1485,7 @@ void amg_vcycle(tf_handle* h, const double* r, double* out) {
         T.cinv = a->cinv;
         T.first = a->tail;
         T.last = nl - 1;
+        T.sweeps = kCoarseSweeps;
         launch_pdl(k_tail, a->nseg, kTailThreads, st, T);
     } else {
         AmgLevel& LC = a->L[nl - 1];
@@ -1454,9 +1501,14 @@ void amg_vcycle(tf_handle* h, const double* r, double* out) {
     }
     for (int l = stop - 1; l >= 1; --l) {
         AmgLevel& L = a->L[l];
-        launch_pdl(k_v6_prolong, cdiv(L.n, kT), kT, st, L, d.scal, a->L[l + 1].e);
-        launch_pdl(k_v6_post, cdiv(32 * (int64_t)L.n, kT), kT, st, L, (const double*)d.scal,
-                   (const double*)(a->omega + l), (const float*)L.x, L.e);
+        float* x = cur[l];
+        launch_pdl(k_v6_prolong, cdiv(L.n, kT), kT, st, L, d.scal, (const float*)a->L[l + 1].e, x);
+        for (int s = 1; s <= kCoarseSweeps; ++s) {
+            float* o = post_sweep_out(L, x, s, kCoarseSweeps);
+            launch_pdl(k_v6_post, cdiv(32 * (int64_t)L.n, kT), kT, st, L, (const double*)d.scal,
+                       (const double*)(a->omega + l), (const float*)x, o);
+            x = o;
+        }
     }
     launch_pdl(k_v0_prolong, d.ncta, kNodeThreads, st, v0, L0, a->L[1].e, L0.x);
     launch_pdl(k_v0_post, d.ncta, kNodeThreads, st, v0, r, L0.x, out);
