@@ -239,6 +239,7 @@ struct Amg {
     float* cinv = nullptr;     // coarsest inverses, m_g x m_g row-major
     bool coarse_exact = true;
     int max_cm = 0;
+    int v0_smem = 0;           // shared memory of the level-0 prolongation (3 floats per block of a CTA)
     int tail = 0;              // levels tail..nlev-1 run in one kernel (one CTA per instance); 0: none
     std::vector<int> h_n;      // nodes per level (host)
     // what the next solve has to redo: 0 nothing, 1 the FP32 copies of the
@@ -560,6 +561,16 @@ tf_status amg_build(tf_handle* h, const double* pos) {
     L0.n = d.nn;
     L0.bs = 3;
     L0.nnzb = d.nnzb;
+    {
+        // blocks of the prolongator rows of each node-parallel CTA
+        std::vector<int> c0(d.ncta), c1(d.ncta), prow0(d.nn + 1);
+        TF_CUDA(cudaMemcpy(c0.data(), d.cta_node0, sizeof(int) * (size_t)d.ncta, cudaMemcpyDeviceToHost));
+        TF_CUDA(cudaMemcpy(c1.data(), d.cta_node1, sizeof(int) * (size_t)d.ncta, cudaMemcpyDeviceToHost));
+        TF_CUDA(cudaMemcpy(prow0.data(), L0.prow, sizeof(int) * (size_t)(d.nn + 1), cudaMemcpyDeviceToHost));
+        int maxb = 1;
+        for (int c = 0; c < d.ncta; ++c) maxb = std::max(maxb, prow0[c1[c]] - prow0[c0[c]]);
+        a->v0_smem = static_cast<int>(3 * sizeof(float) * (size_t)maxb);
+    }
     size_t maxv = 0;
     for (int l = 0; l < a->nlev; ++l) {
         AmgLevel& L = a->L[l];
@@ -1122,25 +1133,36 @@ __global__ void k_v0_post(V0 a, const double* __restrict__ r, const float* __res
     for (int k = 0; k < 3; ++k) out[3 * q.i + k] = (double)fmaf(om, z[k], x[3 * q.i + k]);
 }
 
-// x_i += sum over the prolongator blocks (i, J) of P_iJ e_J
+// x_i += sum over the prolongator blocks (i, J) of P_iJ e_J.  The CTA's
+// nodes own a contiguous range of blocks: consecutive threads take
+// consecutive (block, row) pairs -- coalesced reads of the prolongator --
+// into shared memory, then each node adds its blocks' rows in block order.
 __global__ void k_v0_prolong(V0 a, AmgLevel F, const float* __restrict__ e, float* __restrict__ x) {
+    extern __shared__ float part[];  // [3 * blocks of the CTA's nodes]
     pdl_enter();
-    const Node0 q = node0(a.d);
-    if (!q.valid || seg_stopped(a.d.scal, q.seg)) return;
-    float s[3] = {x[3 * q.i], x[3 * q.i + 1], x[3 * q.i + 2]};
-    for (int b = __ldg(&F.prow[q.i]); b < __ldg(&F.prow[q.i + 1]); ++b) {
-        const int J = __ldg(&F.pcol[b]);
-        const float* __restrict__ P = F.Pv + 18 * (size_t)b;
-        float ec[6];
+    if (seg_stopped(a.d.scal, a.d.cta_seg[blockIdx.x])) return;
+    const int n0 = a.d.cta_node0[blockIdx.x], n1 = a.d.cta_node1[blockIdx.x];
+    const int b0 = __ldg(&F.prow[n0]);
+    const int nitem = 3 * (__ldg(&F.prow[n1]) - b0);
+    for (int q = threadIdx.x; q < nitem; q += blockDim.x) {
+        const int bq = q / 3, k = q - 3 * bq;
+        const int J = __ldg(&F.pcol[b0 + bq]);
+        const float* __restrict__ P = F.Pv + 18 * (size_t)(b0 + bq) + 6 * k;
+        float s = 0.f;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) ec[c] = e[6 * J + c];
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-#pragma unroll
-            for (int c = 0; c < 6; ++c) s[k] = fmaf(__ldg(&P[6 * k + c]), ec[c], s[k]);
+        for (int c = 0; c < 6; ++c) s = fmaf(__ldg(&P[c]), e[6 * J + c], s);
+        part[q] = s;
     }
+    __syncthreads();
+    const int i = n0 + threadIdx.x;
+    if (i >= n1) return;
+    const int p0 = __ldg(&F.prow[i]) - b0, p1 = __ldg(&F.prow[i + 1]) - b0;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) x[3 * q.i + k] = s[k];
+    for (int k = 0; k < 3; ++k) {
+        float s = x[3 * i + k];
+        for (int b = p0; b < p1; ++b) s += part[3 * b + k];
+        x[3 * i + k] = s;
+    }
 }
 
 // r_C(I) = sum over the prolongator blocks (i, I) of P_iI^T t_i;
@@ -1362,6 +1384,8 @@ bool amg_reused(const tf_handle* h) { return h->amg && h->amg->reused; }
 tf_status amg_numeric(tf_handle* h) {
     Amg* a = h->amg;
     if (a->stale == 0) return TF_OK;
+    if (a->v0_smem > 48 * 1024)  // outside any stream capture: the V-cycles launched later need it
+        TF_CUDA(cudaFuncSetAttribute(k_v0_prolong, cudaFuncAttributeMaxDynamicSharedMemorySize, a->v0_smem));
     Device& d = h->d;
     cudaStream_t st = h->stream;
     // FP32 copies of the level-0 values and block inverses for the smoother
@@ -1510,7 +1534,8 @@ void amg_vcycle(tf_handle* h, const double* r, double* out) {
             x = o;
         }
     }
-    launch_pdl(k_v0_prolong, d.ncta, kNodeThreads, st, v0, L0, a->L[1].e, L0.x);
+    launch_pdl_smem(k_v0_prolong, d.ncta, kNodeThreads, (size_t)a->v0_smem, st, v0, L0, (const float*)a->L[1].e,
+                    L0.x);
     launch_pdl(k_v0_post, d.ncta, kNodeThreads, st, v0, r, L0.x, out);
 }
 

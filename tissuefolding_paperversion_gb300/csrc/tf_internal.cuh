@@ -134,11 +134,12 @@ struct Packing;  // packing between tissue surfaces (tf_packing.cu)
 __device__ __forceinline__ void pdl_enter() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 template <typename... KArgs, typename... Args>
-inline void launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+inline void launch_pdl_smem(void (*kernel)(KArgs...), int grid, int block, size_t smem, cudaStream_t st,
+                            Args... args) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
     cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = 0;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
@@ -146,6 +147,11 @@ inline void launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+template <class... KArgs, class... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream_t st, Args... args) {
+    launch_pdl_smem(kernel, grid, block, 0, st, args...);
 }
 
 // y = this thread's row of the sliced block matrix times x.  T is the
