@@ -302,6 +302,7 @@ tf_status copy_state(tf_handle* h, double* u, double* F, double* iF, const doubl
 }
 
 tf_status adj_forward(tf_handle* h, tf_adjoint* a, const double* rate, const double* logE) {
+    NvtxRange nvtx_range("tf adjoint forward");
     Device& d = h->d;
     const int ne = d.ne;
     const size_t n3 = 3 * (size_t)d.nn, n9 = 9 * (size_t)ne;
@@ -341,6 +342,7 @@ tf_status adj_forward(tf_handle* h, tf_adjoint* a, const double* rate, const dou
 }
 
 tf_status adj_backward(tf_handle* h, tf_adjoint* a, double dloss, double* grad_rate, double* grad_logE) {
+    NvtxRange nvtx_range("tf adjoint backward");
     Device& d = h->d;
     const int ne = d.ne;
     const size_t n3 = 3 * (size_t)d.nn, n9 = 9 * (size_t)ne;

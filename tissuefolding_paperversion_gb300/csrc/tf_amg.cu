@@ -1382,6 +1382,7 @@ bool amg_reused(const tf_handle* h) { return h->amg && h->amg->reused; }
 // first solve of each time step (and whenever a solve with reused coarse
 // levels fails, see krylov_solve).
 tf_status amg_numeric(tf_handle* h) {
+    NvtxRange nvtx_range("tf multigrid numeric");
     Amg* a = h->amg;
     if (a->stale == 0) return TF_OK;
     if (a->v0_smem > 48 * 1024)  // outside any stream capture: the V-cycles launched later need it

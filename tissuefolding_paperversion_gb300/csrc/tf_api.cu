@@ -557,6 +557,7 @@ tf_status create_handle(const tf_mesh* mesh, const tf_material* mat, const tf_op
 // after max_iter+1 solves; the others continue.  Per-instance iteration
 // counts and convergence go to iters / conv (may be NULL).
 tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* iters, int32_t* conv) {
+    NvtxRange nvtx_range("tf newton step");
     Device& d = h->d;
     tf_step_stats st;
     std::memset(&st, 0, sizeof(st));
@@ -1219,6 +1220,7 @@ tf_status tf_set_growth_rates(tf_handle* h, const double* rates) {
 }
 
 tf_status tf_begin_step(tf_handle* h, double dt) {
+    NvtxRange nvtx_range("tf begin_step");
     TF_TRY(check_handle(h));
     if (!(dt > 0.0) || !std::isfinite(dt)) return set_error("dt must be positive"), TF_BAD_INPUT;
     h->dt = dt;
@@ -1233,6 +1235,7 @@ tf_status tf_begin_step(tf_handle* h, double dt) {
 }
 
 tf_status tf_assemble(tf_handle* h) {
+    NvtxRange nvtx_range("tf assemble");
     TF_TRY(check_handle(h));
     amg_mark_stale(h, 1);
     h->bound_applied = false;
@@ -1263,6 +1266,7 @@ tf_status tf_add_external_forces(tf_handle* h, const double* gext) {
 }
 
 tf_status tf_solve(tf_handle* h, int32_t* iters, double* relres) {
+    NvtxRange nvtx_range("tf solve");
     TF_TRY(check_handle(h));
     if (!h->assembled) return set_error("tf_solve called before tf_assemble"), TF_BAD_INPUT;
     if (!h->bind_slave.empty() && !h->bound_applied) TF_TRY(apply_bindings(h));

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <string>
@@ -10,6 +11,16 @@
 #include "../../include/tf_gpu.h"
 
 namespace tf {
+
+// NVTX range for the phases of a step (begin_step, assembly, solve, Newton
+// iteration, multigrid set-up, packing detection, adjoint passes): visible
+// to profilers, a no-op without one.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Sliced block storage: a slot holds one 3x3 block for each of 32 rows.
 constexpr int kSlice = 32;

@@ -611,6 +611,7 @@ tf_status packing_setup(tf_handle* h, int flags) {
 // Couples at the current positions (the step's start shape) and their
 // extra blocks.
 tf_status packing_detect(tf_handle* h) {
+    NvtxRange nvtx_range("tf packing detection");
     Packing* p = h->pk;
     Device& d = h->d;
     cudaStream_t st = h->stream;
