@@ -61,8 +61,8 @@ def test_detection_and_assembled_system_match_the_reference(name, kw):
 @pytest.mark.parametrize("name,kw", CASES)
 @pytest.mark.parametrize("precond", [1, 2])
 def test_newton_steps_with_packing_match_the_reference(name, kw, precond):
-    # with precond 2 the handle has a multigrid hierarchy; solves with packing
-    # couples use block-Jacobi (the hierarchy follows the element graph)
+    # precond 2: the multigrid's coarse levels carry the couples' blocks as
+    # P^T X P (the element graph never joins the two sheets)
     f = np.load(os.path.join(GOLD, name + ".npz"))
     t = mesh.config_facing_sheets(**kw)
     off = np.concatenate([[0], np.cumsum(f["pk_n"])])
@@ -95,6 +95,22 @@ def test_cell_list_finds_the_couples_of_the_full_scan(seed, n, merge):
     np.testing.assert_allclose(got["w"], want["w"], rtol=0, atol=1e-15)
     np.testing.assert_allclose(got["mbar"], want["mbar"], rtol=1e-14)
     assert abs(got["threshold"] - want["threshold"]) <= 1e-13 * want["threshold"]
+
+
+def test_multigrid_sees_the_couples():
+    # without the couples' coarse images the V-cycle's coarse correction misses
+    # the stiff coupling between the sheets and the solve diverges; with them
+    # it needs a fraction of block-Jacobi's iterations
+    t = mesh.config_facing_sheets(seed=12, gap=1.5, E=100000.0)
+    tot = {}
+    for pc in (1, 2):
+        with api.Solver(t, precond=pc) as s:
+            s.set_growth_rates(t.rates)
+            s.set_packing(True)
+            tot[pc] = sum(s.newton_step(t.dt, allow_not_converged=False)["krylov_total"] for _ in range(2))
+            if pc == 2:
+                assert s.multigrid_info()[0]
+    assert 3 * tot[2] < tot[1], tot
 
 
 def test_packing_is_bitwise_reproducible_and_switches_off():

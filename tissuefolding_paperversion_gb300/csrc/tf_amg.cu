@@ -196,6 +196,12 @@ struct AmgLevel {
     float* Pc = nullptr;     // [npb][bs*6] the blocks in column order
     int64_t npb = 0;
     uint8_t* dead = nullptr; // [n * bs] (levels >= 1) DOFs with a zero prolongator column
+    // coarse image of the extra blocks outside the element pattern (levels >=
+    // 1): X_l = P^T X_{l-1} P, CSR of 6x6 blocks (null: none)
+    int* xrow = nullptr;
+    int* xcol = nullptr;
+    float* xval = nullptr;
+    int64_t nx = 0;
     // vectors (levels >= 1: r input, e output; all levels: x, t work)
     float *r = nullptr, *x = nullptr, *t = nullptr, *e = nullptr;
 };
@@ -218,6 +224,8 @@ struct AmgSetup {
     int* gptr = nullptr;     // [nnzb_{l+1}+1] pairs (prolongator block, T block) per coarse block
     int* gp = nullptr;
     int* gt = nullptr;
+    int* xptr = nullptr;     // [nx_{l+1}+1] triples (extra block (J, I), P block (J, K), P block (I, M))
+    int* xtrip = nullptr;    // per coarse extra block (K, M)
 };
 
 struct Amg {
@@ -242,6 +250,8 @@ struct Amg {
     int v0_smem = 0;           // shared memory of the level-0 prolongation (3 floats per block of a CTA)
     int tail = 0;              // levels tail..nlev-1 run in one kernel (one CTA per instance); 0: none
     std::vector<int> h_n;      // nodes per level (host)
+    std::vector<int> h_prow[kAmgMaxLevels], h_pcol[kAmgMaxLevels];  // prolongator patterns (host)
+    int64_t x_version = -1;    // extra-block layout the coarse extra blocks were built for
     // what the next solve has to redo: 0 nothing, 1 the FP32 copies of the
     // level-0 matrix (new assembly, same time step), 2 the whole hierarchy
     int stale = 2;
@@ -259,7 +269,7 @@ void amg_free(Amg* a) {
         if (l > 0 && L.dinv) cudaFree(L.dinv);
         AmgSetup& S = a->S[l];
         void* sptrs[] = {S.Pt, S.agg, S.pbrow, S.sptr, S.slist, S.cperm, S.trow, S.tptr, S.ta, S.tb, S.T,
-                         S.gptr, S.gp, S.gt};
+                         S.gptr, S.gp, S.gt, S.xptr, S.xtrip, L.xrow, L.xcol, L.xval};
         for (void* p : sptrs)
             if (p) cudaFree(p);
     }
@@ -501,6 +511,8 @@ tf_status amg_build(tf_handle* h, const double* pos) {
         // device arrays of the fine level's transfer
         AmgLevel& DL = a->L[lev];
         DL.npb = npb;
+        a->h_prow[lev] = prow;
+        a->h_pcol[lev] = pcol;
         AMG_TRY(up(&DL.prow, prow));
         AMG_TRY(up(&DL.pcol, pcol));
         AMG_TRY(zeros(&DL.Pv, (size_t)npb * bs * 6));
@@ -619,6 +631,78 @@ tf_status amg_build(tf_handle* h, const double* pos) {
     return TF_OK;
 }
 
+// Patterns of the coarse images X_{l+1} = P_l^T X_l P_l of the extra blocks
+// (packing couples, tf_add_K_triplets, DOF-binding merges), rebuilt on the
+// host whenever the extra-block layout changes: per coarse extra block the
+// list of triples (X_l block (J, I), P_l block (J, K), P_l block (I, M))
+// whose products it sums.  The coarse operators then see the couplings the
+// element graph does not have (e.g. between two surfaces pressed together).
+tf_status amg_extra_symbolic(tf_handle* h) {
+    Amg* a = h->amg;
+    for (int l = 0; l < a->nlev; ++l) {
+        AmgLevel& L = a->L[l];
+        AmgSetup& S = a->S[l];
+        void* ptrs[] = {S.xptr, S.xtrip, l > 0 ? L.xrow : nullptr, l > 0 ? L.xcol : nullptr,
+                        l > 0 ? L.xval : nullptr};
+        for (void* q : ptrs)
+            if (q) cudaFree(q);
+        S.xptr = S.xtrip = nullptr;
+        if (l > 0) {
+            L.xrow = L.xcol = nullptr;
+            L.xval = nullptr;
+            L.nx = 0;
+        }
+    }
+    a->x_version = h->extra_version;
+    if (h->d.nxb == 0 || h->h_xcols.empty()) return TF_OK;
+    // level 0: (column, block index) per row, in the device layout
+    std::vector<std::vector<std::pair<int, int>>> X(h->d.nn);
+    for (int J = 0; J < h->d.nn; ++J)
+        for (size_t q = 0; q < h->h_xcols[J].size(); ++q)
+            X[J].emplace_back(h->h_xcols[J][q], h->h_xrow[J] + static_cast<int>(q));
+    for (int l = 0; l + 1 < a->nlev; ++l) {
+        const std::vector<int>& prow = a->h_prow[l];
+        const std::vector<int>& pcol = a->h_pcol[l];
+        const int nc = a->h_n[l + 1];
+        struct Trip {
+            int K, M, q, b1, b2;
+        };
+        std::vector<Trip> trips;
+        for (size_t J = 0; J < X.size(); ++J)
+            for (const auto& e : X[J])
+                for (int b1 = prow[J]; b1 < prow[J + 1]; ++b1)
+                    for (int b2 = prow[e.first]; b2 < prow[e.first + 1]; ++b2)
+                        trips.push_back({pcol[b1], pcol[b2], e.second, b1, b2});
+        if (trips.empty()) break;
+        std::sort(trips.begin(), trips.end(), [](const Trip& u, const Trip& v) {
+            return u.K != v.K ? u.K < v.K : (u.M != v.M ? u.M < v.M : u.q < v.q);
+        });
+        std::vector<int> xrow(nc + 1, 0), xcol, xptr(1, 0), xtrip;
+        std::vector<std::vector<std::pair<int, int>>> Xn(nc);
+        for (size_t t = 0; t < trips.size(); ++t) {
+            const Trip& u = trips[t];
+            if (t == 0 || u.K != trips[t - 1].K || u.M != trips[t - 1].M) {
+                if (t > 0) xptr.push_back(static_cast<int>(xtrip.size() / 3));
+                Xn[u.K].emplace_back(u.M, static_cast<int>(xcol.size()));
+                xcol.push_back(u.M);
+                xrow[u.K + 1]++;
+            }
+            xtrip.insert(xtrip.end(), {u.q, u.b1, u.b2});
+        }
+        xptr.push_back(static_cast<int>(xtrip.size() / 3));
+        for (int K = 0; K < nc; ++K) xrow[K + 1] += xrow[K];
+        AmgLevel& C = a->L[l + 1];
+        AmgSetup& S = a->S[l];
+        C.nx = static_cast<int64_t>(xcol.size());
+        AMG_TRY(up(&C.xrow, xrow));
+        AMG_TRY(up(&C.xcol, xcol));
+        AMG_TRY(zeros(&C.xval, 36 * (size_t)C.nx));
+        AMG_TRY(up(&S.xptr, xptr));
+        AMG_TRY(up(&S.xtrip, xtrip));
+        X.swap(Xn);
+    }
+    return TF_OK;
+}
 
 namespace {
 
@@ -741,6 +825,15 @@ __device__ __forceinline__ void row6_warp(const AmgLevel& L, int i, const float*
         for (int g = 0; g < 5; ++g) s2 += __shfl_sync(0xffffffffu, acc, 6 * g + k);
         y[k] = s2;
     }
+    if (L.xrow)  // coarse image of the extra blocks (few; every lane adds them)
+        for (int q = L.xrow[i]; q < L.xrow[i + 1]; ++q) {
+            const float* __restrict__ v = L.xval + 36 * (size_t)q;
+            const float* __restrict__ xj = x + 6 * (size_t)L.xcol[q];
+#pragma unroll
+            for (int k = 0; k < 6; ++k)
+#pragma unroll
+                for (int m = 0; m < 6; ++m) y[k] = fmaf(v[6 * k + m], xj[m], y[k]);
+        }
 }
 
 // r[a] without dynamic register indexing (which would go to local memory).
@@ -884,6 +977,38 @@ __global__ void k_ptap(AmgLevel F, AmgSetup S, AmgLevel C) {
     for (int q2 = 0; q2 < 6; ++q2) out[q2] = acc[q2];
 }
 
+// Coarse extra block c = (K, M), row p: sum over its triples (X_JI, P_JK,
+// P_IM) of (P_JK^T X_JI P_IM)(p, :).  Level 0's extra blocks are the FP64
+// 3x3 blocks of the Krylov operator.
+template <int BS, bool L0>
+__global__ void k_xgal(AmgLevel F, AmgSetup S, AmgLevel C, const double* __restrict__ x0) {
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= C.nx * 6) return;
+    const int64_t c = gid / 6;
+    const int p = static_cast<int>(gid - 6 * c);
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int t = S.xptr[c]; t < S.xptr[c + 1]; ++t) {
+        const int q = __ldg(&S.xtrip[3 * t]);
+        const float* __restrict__ P1 = F.Pv + (size_t)__ldg(&S.xtrip[3 * t + 1]) * BS * 6;
+        const float* __restrict__ P2 = F.Pv + (size_t)__ldg(&S.xtrip[3 * t + 2]) * BS * 6;
+#pragma unroll
+        for (int r = 0; r < BS; ++r) {
+            const float pr = __ldg(&P1[6 * r + p]);
+#pragma unroll
+            for (int s2 = 0; s2 < BS; ++s2) {
+                const float xv = L0 ? (float)__ldg(&x0[9 * (size_t)q + 3 * r + s2])
+                                    : __ldg(&F.xval[36 * (size_t)q + 6 * r + s2]);
+                const float px = pr * xv;
+#pragma unroll
+                for (int m = 0; m < 6; ++m) acc[m] = fmaf(px, __ldg(&P2[6 * s2 + m]), acc[m]);
+            }
+        }
+    }
+    float* out = C.xval + 36 * (size_t)c + 6 * p;
+#pragma unroll
+    for (int m = 0; m < 6; ++m) out[m] = acc[m];
+}
+
 // Inverse of a 6x6 block by Gauss-Jordan with partial pivoting (FP64 work).
 __device__ void inv6(const float* __restrict__ A, float* __restrict__ out) {
     double M[6][12];
@@ -1022,13 +1147,22 @@ __global__ void k_coarse_invert(AmgLevel L, const int* __restrict__ cnode0, cons
         M[k] = (c - m == r) ? 1.0 : 0.0;
     }
     __syncthreads();
-    for (int I = n0 + threadIdx.x; I < n1; I += blockDim.x)
+    for (int I = n0 + threadIdx.x; I < n1; I += blockDim.x) {
         for (int p = L.rowptr[I]; p < L.rowptr[I + 1]; ++p) {
             const int J = L.colidx[p] - n0;
             const float* v = L.val + 36 * (size_t)p;
             for (int a = 0; a < 6; ++a)
                 for (int b = 0; b < 6; ++b) M[(6 * (I - n0) + a) * w + 6 * J + b] = (double)v[6 * a + b];
         }
+        if (L.xrow)
+            for (int q = L.xrow[I]; q < L.xrow[I + 1]; ++q) {
+                const int J = L.xcol[q] - n0;
+                if (J < 0 || J >= n1 - n0) continue;  // couples another instance: outside this inverse
+                const float* v = L.xval + 36 * (size_t)q;
+                for (int a = 0; a < 6; ++a)
+                    for (int b = 0; b < 6; ++b) M[(6 * (I - n0) + a) * w + 6 * J + b] += (double)v[6 * a + b];
+            }
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         double dmax = 0.0;
@@ -1399,6 +1533,7 @@ tf_status amg_numeric(tf_handle* h) {
         a->stale = 0;
         return TF_OK;
     }
+    if (a->x_version != h->extra_version) AMG_TRY(amg_extra_symbolic(h));
     // level by level: smoother weight from lambda_max(D^-1 A) (the
     // prolongator smoothing uses it too), prolongator, Galerkin product
     // A_{l+1} = P^T (A P) and the next level's block inverses
@@ -1443,6 +1578,11 @@ tf_status amg_numeric(tf_handle* h) {
         if (l == 0) k_ptap<3><<<cdiv(C.nnzb * 6, kT), kT, 0, st>>>(L, S, C);
         else k_ptap<6><<<cdiv(C.nnzb * 6, kT), kT, 0, st>>>(L, S, C);
         TF_LAUNCH_CHECK(h);
+        if (C.nx > 0) {
+            if (l == 0) k_xgal<3, true><<<cdiv(C.nx * 6, kT), kT, 0, st>>>(L, S, C, d.xval);
+            else k_xgal<6, false><<<cdiv(C.nx * 6, kT), kT, 0, st>>>(L, S, C, nullptr);
+            TF_LAUNCH_CHECK(h);
+        }
         k_inv6<<<cdiv(C.n, kT), kT, 0, st>>>(C);
         TF_LAUNCH_CHECK(h);
     }

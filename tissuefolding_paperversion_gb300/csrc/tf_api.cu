@@ -683,6 +683,8 @@ tf_status upload_extra(tf_handle* h, bool pattern_changed) {
         TF_TRY(dev_alloc(&d.xval, 9 * (size_t)d.nxb));
         destroy_graphs(h);  // the captured Krylov chunks hold the extra-block pointers
         TF_TRY(packing_relink(h));
+        h->extra_version++;
+        amg_mark_stale(h, 2);  // the coarse images of the extra blocks follow the new layout
     }
     TF_CUDA(cudaMemcpyAsync(d.xval, h->h_xval.data(), sizeof(double) * 9 * (size_t)d.nxb, cudaMemcpyHostToDevice,
                             h->stream));

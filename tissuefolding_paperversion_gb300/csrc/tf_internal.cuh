@@ -216,6 +216,7 @@ struct tf_handle {
     std::vector<int> bind_slave, bind_master;   // bound DOF couples (NRSolver::slaveMasterList)
     bool bound_applied = false;                 // the couples are applied to the current assembly
     std::vector<double> h_xval;                 // their values of the current assembly
+    int64_t extra_version = 0;                  // changes with every new extra-block layout
     std::vector<uint8_t> h_fixed;
     std::vector<double> h_nu;                   // Poisson ratios, clamped as the material setup does
     std::vector<int> h_apical;                  // 1 for apical nodes (tissue placement 1)
@@ -275,9 +276,9 @@ tf_status packing_get(tf_handle* h, int64_t* n, int32_t* nodes, double* w, doubl
 tf_status packing_masses(tf_handle* h, double* mass);
 tf_status packing_assemble(tf_handle* h);        // forces and Jacobian into g and K
 tf_status packing_relink(tf_handle* h);          // couple blocks in the current extra-block layout
-// The multigrid preconditioner is used unless packing couples are present:
-// its hierarchy follows the element graph, which never joins the coupled
-// surfaces, so its coarse correction would miss their (stiff) coupling.
+// The multigrid preconditioner is used whenever the handle has a hierarchy
+// (the extra blocks -- packing couples among them -- reach its coarse levels
+// as X_{l+1} = P^T X_l P).
 bool use_multigrid(const tf_handle* h);
 void packing_free(Packing* p);
 tf_status upload_extra(tf_handle* h, bool pattern_changed);

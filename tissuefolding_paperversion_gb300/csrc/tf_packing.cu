@@ -743,7 +743,7 @@ tf_status packing_relink(tf_handle* h) {
     return TF_OK;
 }
 
-bool use_multigrid(const tf_handle* h) { return h->amg && !(h->pk && h->pk->n > 0); }
+bool use_multigrid(const tf_handle* h) { return h->amg != nullptr; }
 
 tf_status packing_assemble(tf_handle* h) {
     Packing* p = h->pk;
