@@ -35,7 +35,9 @@
 // Krylov method is concerned, so the whole V-cycle -- its matrices (an FP32
 // copy of the level-0 values and block inverses, the coarse operators and
 // prolongators) and its vectors -- is FP32: half the bytes of its
-// bandwidth-bound sweeps, and no FP32/FP64 conversions on the FP64 pipe.
+// bandwidth-bound sweeps, and no FP32/FP64 conversions on the FP64 pipe.  The
+// level-0 smoother reads S = D^-1 A in FP16 (entries of order one), a quarter
+// of the FP64 bytes.
 // The Krylov recurrences, their SpMVs with A and the convergence test are
 // untouched FP64.
 #include <algorithm>
@@ -43,6 +45,8 @@
 #include <cstring>
 #include <numeric>
 #include <vector>
+
+#include <cuda_fp16.h>
 
 #include "tf_internal.cuh"
 
@@ -240,6 +244,7 @@ struct Amg {
     double* part = nullptr;    // per-CTA partial sums
     unsigned* ticket = nullptr;
     float* val32 = nullptr;    // FP32 copy of the level-0 values (sliced layout)
+    __half* valh = nullptr;    // the smoother's level-0 operator S = D^-1 A in FP16 (sliced layout)
     float* dinv32 = nullptr;   // FP32 copy of the level-0 block inverses
     int nseg = 1;
     int* cnode0 = nullptr;     // [nseg+1] coarsest-level node offsets per instance
@@ -274,7 +279,7 @@ void amg_free(Amg* a) {
             if (p) cudaFree(p);
     }
     void* ptrs[] = {a->omega, a->pscal, a->pv, a->pw, a->part, a->ticket, a->cnode0, a->cinv0, a->cinv,
-                    a->val32, a->dinv32};
+                    a->val32, a->dinv32, a->valh};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete a;
@@ -598,6 +603,7 @@ tf_status amg_build(tf_handle* h, const double* pos) {
     }
     AMG_TRY(zeros(&a->omega, (size_t)a->nlev));
     AMG_TRY(zeros(&a->val32, (size_t)d.nval));
+    AMG_TRY(zeros(&a->valh, (size_t)d.nval));
     AMG_TRY(zeros(&a->dinv32, 9 * (size_t)d.nn));
     AMG_TRY(zeros(&a->pscal, 2 * (size_t)a->nlev));
     AMG_TRY(zeros(&a->pv, maxv));
@@ -780,22 +786,42 @@ __device__ __forceinline__ void sliced_row32(const int* __restrict__ wslot0, con
     y[2] = y2;
 }
 
-// Level-0 row product of the smoother: the FP32 copy of the sliced storage
-// plus the extra blocks outside the element pattern (K entries of packing
-// couples and tf_add_K_triplets, few and FP64, converted on the fly), so that
-// the smoother works on the operator the Krylov method solves.
-__device__ __forceinline__ void row0(const Device& d, const float* __restrict__ val32, const float* __restrict__ x,
-                                     int i, float y[3]) {
-    sliced_row32(d.wslot0, d.scol, val32, x, y);
-    if (!d.xrow) return;
+// Row of S = D^-1 A (FP16, sliced) times x, FP32 sums; the extra blocks X
+// (FP64) enter as D^-1 (X x).
+__device__ __forceinline__ void row0s(const Device& d, const __half* __restrict__ valh,
+                                      const float* __restrict__ dinv32, const float* __restrict__ x, int i,
+                                      float y[3]) {
+    const int lane = threadIdx.x & 31;
+    const int wg = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const int s0 = __ldg(&d.wslot0[wg]), s1 = __ldg(&d.wslot0[wg + 1]);
+    float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+    const int* __restrict__ col = d.scol + lane;
+    const __half* __restrict__ a = valh + lane;
+#pragma unroll 4
+    for (int s = s0; s < s1; ++s) {
+        const int j = __ldg(&col[(size_t)s * kSlice]);
+        const __half* __restrict__ v = a + (size_t)s * kSlotDoubles;
+        const float x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
+        y0 = fmaf(__half2float(v[0]), x0, fmaf(__half2float(v[32]), x1, fmaf(__half2float(v[64]), x2, y0)));
+        y1 = fmaf(__half2float(v[96]), x0, fmaf(__half2float(v[128]), x1, fmaf(__half2float(v[160]), x2, y1)));
+        y2 = fmaf(__half2float(v[192]), x0, fmaf(__half2float(v[224]), x1, fmaf(__half2float(v[256]), x2, y2)));
+    }
+    y[0] = y0;
+    y[1] = y1;
+    y[2] = y2;
+    if (!d.xrow || d.xrow[i] == d.xrow[i + 1]) return;
+    float e[3] = {0.f, 0.f, 0.f}, z[3];
     for (int q = d.xrow[i]; q < d.xrow[i + 1]; ++q) {
         const int j = d.xcol[q];
         const double* __restrict__ v = d.xval + 9 * (size_t)q;
 #pragma unroll
         for (int r = 0; r < 3; ++r)
-            y[r] = fmaf((float)v[3 * r], x[3 * j],
-                        fmaf((float)v[3 * r + 1], x[3 * j + 1], fmaf((float)v[3 * r + 2], x[3 * j + 2], y[r])));
+            e[r] = fmaf((float)v[3 * r], x[3 * j],
+                        fmaf((float)v[3 * r + 1], x[3 * j + 1], fmaf((float)v[3 * r + 2], x[3 * j + 2], e[r])));
     }
+    mul3(dinv32 + 9 * (size_t)i, e, z);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) y[r] += z[r];
 }
 
 // Warp-cooperative product of row i of a 6x6-block CSR matrix with x.
@@ -857,6 +883,32 @@ __device__ __forceinline__ float lane_mul6(const float* __restrict__ D, const fl
 __global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
         b[k] = (float)a[k];
+}
+
+// S = D^-1 A for the smoother, block by block in the sliced layout, FP16
+// (its entries are O(1): the FP16 range and 11-bit mantissa suffice for a
+// preconditioner; the Krylov operator itself stays FP64).
+__global__ void k_to_h(Device d, const float* __restrict__ val32, const float* __restrict__ dinv32,
+                       __half* __restrict__ valh) {
+    const Node0 q = node0(d);
+    const int lane = threadIdx.x & 31;
+    const int wg = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    const int s0 = d.wslot0[wg], s1 = d.wslot0[wg + 1];
+    float D[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) D[k] = q.valid ? dinv32[9 * (size_t)q.i + k] : 0.f;
+    for (int s = s0; s < s1; ++s) {
+        const size_t base = (size_t)s * kSlotDoubles + lane;
+        float A[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) A[k] = val32[base + 32 * k];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                valh[base + 32 * (3 * r + c)] =
+                    __float2half_rn(fmaf(D[3 * r], A[c], fmaf(D[3 * r + 1], A[3 + c], D[3 * r + 2] * A[6 + c])));
+    }
 }
 
 // Element (r, c) of fine-matrix block b: level 0 reads the FP32 copy of the
@@ -1088,21 +1140,20 @@ __device__ __forceinline__ void pw_finish(double tot, double* scal, double* omeg
     *omega = lam > 0.0 ? (4.0 / 3.0) / (1.05 * lam) : 1.0;
 }
 
-__global__ void k_pw_step0(Device d, const float* __restrict__ val32, const float* __restrict__ dinv32,
+__global__ void k_pw_step0(Device d, const __half* __restrict__ valh, const float* __restrict__ dinv32,
                            const float* __restrict__ v, float* __restrict__ w, double* part, unsigned* ticket,
                            double* scal, double* omega) {
     const Node0 q = node0(d);
     double s = 0.0;
     float y[3] = {0.f, 0.f, 0.f};
-    if (q.valid) row0(d, val32, v, q.i, y);
+    if (q.valid) row0s(d, valh, dinv32, v, q.i, y);  // D^-1 A v = S v, the smoother's operator
     if (q.valid) {
         const float sc = (float)__ldcg(&scal[0]);
-        float yy[3] = {sc * y[0], sc * y[1], sc * y[2]}, z[3];
-        mul3(dinv32 + 9 * (size_t)q.i, yy, z);
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
-            w[3 * q.i + k] = z[k];
-            s += (double)z[k] * z[k];
+            const float z = sc * y[k];
+            w[3 * q.i + k] = z;
+            s += (double)z * z;
         }
     }
     double tot;
@@ -1222,8 +1273,9 @@ __global__ void k_coarse_invert(AmgLevel L, const int* __restrict__ cnode0, cons
 struct V0 {  // level-0 operands
     Device d;
     const double* omega;
-    const float* val32;   // FP32 copy of the values
+    const float* val32;   // FP32 copy of the values (diagonal blocks for the residual)
     const float* dinv32;  // FP32 copy of the block inverses
+    const __half* valh;   // S = D^-1 A, FP16
 };
 
 // x = omega D^-1 r  (r is the Krylov method's FP64 vector)
@@ -1244,10 +1296,14 @@ __global__ void k_v0_resid(V0 a, const double* __restrict__ r, const float* __re
     const Node0 q = node0(a.d);
     if (seg_stopped(a.d.scal, q.seg)) return;
     float y[3];
-    if (q.valid) row0(a.d, a.val32, x, q.i, y);
+    if (q.valid) row0s(a.d, a.valh, a.dinv32, x, q.i, y);
     if (!q.valid) return;
+    // A x = D (S x), D the diagonal block
+    const float* __restrict__ Dg = a.val32 + __ldg(&a.d.diag[q.i]);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) t[3 * q.i + k] = (float)r[3 * q.i + k] - y[k];
+    for (int k = 0; k < 3; ++k)
+        t[3 * q.i + k] = (float)r[3 * q.i + k] - fmaf(Dg[kSlice * (3 * k)], y[0],
+                                                      fmaf(Dg[kSlice * (3 * k + 1)], y[1], Dg[kSlice * (3 * k + 2)] * y[2]));
 }
 
 // out = x + omega D^-1 (r - A x), written back as the FP64 preconditioned vector
@@ -1256,15 +1312,14 @@ __global__ void k_v0_post(V0 a, const double* __restrict__ r, const float* __res
     const Node0 q = node0(a.d);
     if (seg_stopped(a.d.scal, q.seg)) return;
     float y[3];
-    if (q.valid) row0(a.d, a.val32, x, q.i, y);
+    if (q.valid) row0s(a.d, a.valh, a.dinv32, x, q.i, y);
     if (!q.valid) return;
+    // x + omega D^-1 (r - A x) = x + omega (D^-1 r - S x)
     const float om = (float)__ldg(a.omega);
-    float rr[3], z[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) rr[k] = (float)r[3 * q.i + k] - y[k];
+    float rr[3] = {(float)r[3 * q.i], (float)r[3 * q.i + 1], (float)r[3 * q.i + 2]}, z[3];
     mul3(a.dinv32 + 9 * (size_t)q.i, rr, z);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) out[3 * q.i + k] = (double)fmaf(om, z[k], x[3 * q.i + k]);
+    for (int k = 0; k < 3; ++k) out[3 * q.i + k] = (double)fmaf(om, z[k] - y[k], x[3 * q.i + k]);
 }
 
 // x_i += sum over the prolongator blocks (i, J) of P_iJ e_J.  The CTA's
@@ -1528,6 +1583,8 @@ tf_status amg_numeric(tf_handle* h) {
     TF_LAUNCH_CHECK(h);
     k_to_f32<<<4 * 152, kT, 0, st>>>(9 * (int64_t)d.nn, d.dinv, a->dinv32);
     TF_LAUNCH_CHECK(h);
+    k_to_h<<<d.ncta, kNodeThreads, 0, st>>>(d, a->val32, a->dinv32, a->valh);
+    TF_LAUNCH_CHECK(h);
     a->reused = a->stale == 1;
     if (a->reused) {
         a->stale = 0;
@@ -1548,7 +1605,7 @@ tf_status amg_numeric(tf_handle* h) {
             TF_LAUNCH_CHECK(h);
             for (int it = 0; it < kPowerIters; ++it) {
                 if (l == 0)
-                    k_pw_step0<<<d.ncta, kNodeThreads, 0, st>>>(d, a->val32, a->dinv32, v, w, a->part, a->ticket,
+                    k_pw_step0<<<d.ncta, kNodeThreads, 0, st>>>(d, a->valh, a->dinv32, v, w, a->part, a->ticket,
                                                                 scal, a->omega);
                 else
                     k_pw_step6<<<cdiv(32 * (int64_t)L.n, kT), kT, 0, st>>>(L, v, w, a->part, a->ticket, scal,
@@ -1618,7 +1675,7 @@ void amg_vcycle(tf_handle* h, const double* r, double* out) {
     cudaStream_t st = h->stream;
     const int nl = a->nlev;
     const int stop = a->tail > 0 ? a->tail : nl - 1;  // first level not handled kernel by kernel
-    V0 v0{d, a->omega, a->val32, a->dinv32};
+    V0 v0{d, a->omega, a->val32, a->dinv32, a->valh};
     AmgLevel& L0 = a->L[0];
     auto presmooth = [&](int l) { return (l < nl - 1 || !a->coarse_exact) ? 1 : 0; };
     launch_pdl(k_v0_pre, d.ncta, kNodeThreads, st, v0, r, L0.x);
