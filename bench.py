@@ -415,6 +415,28 @@ def run_adjoint(args, t):
         f = (out[0] - out[1]) / (2 * h)
         fd.append({"adjoint": float(gr @ d), "fd": f, "rel": abs(float(gr @ d) - f) / max(abs(f), 1e-300)})
     s.close()
+    if args.adj_fd:
+        # the same check with the step solved tightly (Newton |du| <= 1e-11, Krylov 1e-13): at the
+        # default tolerances the central differences carry the solver's error over n steps
+        ts = api.Solver(t, newton_tol=1e-11, krylov_rtol=1e-13)
+        ts.set_positions(t.pos)
+        _, sv = ts.adjoint_forward(rate, logE, n, t.dt, every, params)
+        gt, _ = ts.adjoint_backward(sv)
+        sv.free()
+        rng = np.random.default_rng(1234)
+        for k in range(args.adj_fd):
+            d = rng.standard_normal(t.n_elems)
+            h = 1e-3 * np.abs(rate).mean()
+            out = []
+            for sgn in (1.0, -1.0):
+                ts.set_positions(t.pos)
+                lv, sp = ts.adjoint_forward(rate + sgn * h * d, logE, n, t.dt, every, params)
+                sp.free()
+                out.append(lv)
+            f = (out[0] - out[1]) / (2 * h)
+            fd[k]["tight_solve"] = {"adjoint": float(gt @ d), "fd": f,
+                                    "rel": abs(float(gt @ d) - f) / max(abs(f), 1e-300)}
+        ts.close()
     print(json.dumps({
         "metric": "adjoint backward / forward cost", "value": bwd / fwd, "unit": "ratio", "n_gpus": 1,
         "steps": n, "warmup": 1, "ms_per_step": (fwd + bwd) / n * 1e3, "higher_is_better": False,

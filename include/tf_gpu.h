@@ -265,8 +265,10 @@ TF_API tf_status tf_solve_bsr_static(int32_t n_block_rows, const int32_t* rowptr
  * moduli (E_e = exp(logE_e), Poisson ratios kept), runs n_steps Newton steps
  * of length dt from the current positions and keeps the state every `every`
  * steps in *saved.  tf_adj_backward recomputes each span of `every` steps
- * from its saved state and solves A^T lambda = rhs per step, scaling dL by
- * dloss; it leaves the handle at the final state.  Single-mesh handles only. */
+ * from its saved state and solves A^T lambda = rhs per step (to a relative
+ * residual of min(krylov_rtol, 1e-12): the errors of these solves are carried
+ * through the earlier steps), scaling dL by dloss; it leaves the handle at the
+ * final state.  Single-mesh handles only. */
 /* The reference's mesh input file (.mesh; Simulation.cpp:2074-2239): node
  * positions, tissue placement / type / circumference flags, prism node ids
  * (after Prism::checkRotationConsistency3D, Prism.cpp:364-410) and the 6 x 3

@@ -171,6 +171,26 @@ def config5():
             "adjoint_vs_oracle_central_differences_max_rel_err": worst_ora}
 
 
+def packing(name, kw, precond):
+    """steps with implicit packing against the reference's own
+    classes (fixtures tests/golden/steps_facing_packing*.npz)."""
+    f = np.load(os.path.join(GOLD, name + ".npz"))
+    t = mesh.config_facing_sheets(**kw)
+    off = np.concatenate([[0], np.cumsum(f["pk_n"])])
+    err, same, couples = 0.0, True, True
+    with api.Solver(t, krylov_rtol=1e-12, precond=precond) as s:
+        s.set_growth_rates(t.rates)
+        s.set_packing(True, reference_merge=bool(f["drop_last_segment"]))
+        for k in range(f["positions"].shape[0]):
+            out = s.newton_step(t.dt)
+            err = max(err, rel(s.positions(), f["positions"][k]))
+            same &= out["iters"] == f["iters"][k]
+            couples &= bool(np.array_equal(s.packing()["nodes"], f["pk_nodes"][off[k]:off[k + 1]]))
+    return {"config": f"f3 packing: {name} ({t.n_elems} prisms, {f['positions'].shape[0]} steps), "
+                      f"{'multigrid' if precond == 2 else 'block-Jacobi'}",
+            "positions_max_rel_err": err, "newton_iters_identical": bool(same), "couples_identical": couples}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true", help="skip the 1.0M-prism wing")
@@ -182,6 +202,9 @@ def main():
         runs.append(lambda: full_size(mesh.config_wing(seed=0), "3: 995,824-prism wing, first Newton step",
                                       csr=False))
     runs += [config4, config5]
+    for name, kw in (("steps_facing_packing", dict(seed=12, gap=1.5, E=100000.0, eta=0.0)),
+                     ("steps_facing_packing_viscous", dict(seed=13, gap=1.5, E=100000.0, eta=100.0))):
+        runs += [lambda name=name, kw=kw, pc=pc: packing(name, kw, pc) for pc in (1, 2)]
     out = []
     for r in runs:
         out.append(r())
