@@ -67,8 +67,13 @@ class tf_step_stats(C.Structure):
 _lib = None
 
 
+def checked() -> bool:
+    """TF_CHECKED=1 in the environment selects the checked build."""
+    return os.environ.get("TF_CHECKED") == "1"
+
+
 def library_path() -> str:
-    return _build.LIB
+    return _build.LIB_CHECKED if checked() else _build.LIB
 
 
 def load(build_if_missing: bool = True):
@@ -80,7 +85,7 @@ def load(build_if_missing: bool = True):
     if not os.path.exists(path):
         if not build_if_missing:
             raise RuntimeError(f"{path} is missing; run tissuefolding_paperversion_gb300.build.build()")
-        _build.build()
+        _build.build(checked=checked())
     L = C.CDLL(path)
     vp, dp, ip, i32, i64 = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int32), C.c_int32, C.c_int64
     L.tf_status_string.restype = C.c_char_p

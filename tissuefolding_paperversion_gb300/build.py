@@ -2,6 +2,9 @@
 
 The library is built in-tree into ``tissuefolding_paperversion_gb300/_lib``;
 object files go to ``_build``.  Translation units compile in parallel.
+``build(checked=True)`` builds libtfgpu_checked.so (-DTF_CHECKED: every
+checked index is tested before its access; a failed test is reported as
+TF_CUDA_ERROR instead of touching memory out of bounds) into ``_build_checked``.
 """
 from __future__ import annotations
 
@@ -16,6 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libtfgpu.so")
+LIB_CHECKED = os.path.join(LIBDIR, "libtfgpu_checked.so")
 SOURCES = ["tf_api.cu", "tf_element.cu", "tf_assembly.cu", "tf_krylov.cu", "tf_static_solve.cu", "tf_adjoint.cu", "tf_amg.cu",
            "tf_packing.cu", "tf_meshio.cpp"]
 HEADERS = ["tf_internal.cuh"]
@@ -38,18 +42,21 @@ def _stale(target: str, deps) -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    os.makedirs(OBJ, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> str:
+    obj_dir = OBJ + "_checked" if checked else OBJ
+    lib = LIB_CHECKED if checked else LIB
+    flags = FLAGS + (["-DTF_CHECKED"] if checked else [])
+    os.makedirs(obj_dir, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(ROOT, "include", "tf_gpu.h")]
     jobs = []
     objs = []
     for s in SOURCES:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(OBJ, os.path.splitext(s)[0] + ".o")
+        obj = os.path.join(obj_dir, os.path.splitext(s)[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src, *hdrs]):
-            jobs.append([nvcc(), *ARCH, *FLAGS, "-c", src, "-o", obj])
+            jobs.append([nvcc(), *ARCH, *flags, "-c", src, "-o", obj])
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -58,9 +65,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
             print(r.stdout + r.stderr)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         list(ex.map(run, jobs))
-    if force or jobs or _stale(LIB, objs):
-        run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs])
-    return LIB
+    if force or jobs or _stale(lib, objs):
+        run([nvcc(), *ARCH, "-shared", "-o", lib, *objs])
+    return lib
 
 
 if __name__ == "__main__":

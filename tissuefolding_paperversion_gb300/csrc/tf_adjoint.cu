@@ -284,6 +284,7 @@ tf_status solve_transposed(tf_handle* h, int* iters) {
     h->opt.krylov_rtol = std::min(rtol, kAdjointRtol);
     const tf_status s = krylov_solve(h, iters, &rr);
     h->opt.krylov_rtol = rtol;
+    TFA_TRY(take_check(h));
     return s == TF_KRYLOV_NOT_CONVERGED ? TF_OK : s;
 }
 

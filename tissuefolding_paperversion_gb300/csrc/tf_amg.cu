@@ -208,6 +208,8 @@ struct AmgLevel {
     int64_t nx = 0;
     // vectors (levels >= 1: r input, e output; all levels: x, t work)
     float *r = nullptr, *x = nullptr, *t = nullptr, *e = nullptr;
+    int ncoarse = 0;         // nodes of level + 1
+    int* check = nullptr;    // checked build: failed index checks
 };
 
 // Lists of the numeric set-up of the transfer from level l to l + 1
@@ -601,6 +603,10 @@ tf_status amg_build(tf_handle* h, const double* pos) {
         }
         a->h_n.push_back(L.n);
     }
+    for (int l = 0; l < a->nlev; ++l) {
+        a->L[l].ncoarse = l + 1 < a->nlev ? a->L[l + 1].n : 0;
+        a->L[l].check = d.check;
+    }
     AMG_TRY(zeros(&a->omega, (size_t)a->nlev));
     AMG_TRY(zeros(&a->val32, (size_t)d.nval));
     AMG_TRY(zeros(&a->valh, (size_t)d.nval));
@@ -800,6 +806,7 @@ __device__ __forceinline__ void row0s(const Device& d, const __half* __restrict_
 #pragma unroll 4
     for (int s = s0; s < s1; ++s) {
         const int j = __ldg(&col[(size_t)s * kSlice]);
+        if (!TF_IN(d.check, j, d.nn, CK_V0_COL)) continue;
         const __half* __restrict__ v = a + (size_t)s * kSlotDoubles;
         const float x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
         y0 = fmaf(__half2float(v[0]), x0, fmaf(__half2float(v[32]), x1, fmaf(__half2float(v[64]), x2, y0)));
@@ -813,6 +820,7 @@ __device__ __forceinline__ void row0s(const Device& d, const __half* __restrict_
     float e[3] = {0.f, 0.f, 0.f}, z[3];
     for (int q = d.xrow[i]; q < d.xrow[i + 1]; ++q) {
         const int j = d.xcol[q];
+        if (!TF_IN(d.check, j, d.nn, CK_EXTRA_COL)) continue;
         const double* __restrict__ v = d.xval + 9 * (size_t)q;
 #pragma unroll
         for (int r = 0; r < 3; ++r)
@@ -1338,6 +1346,10 @@ __global__ void k_v0_prolong(V0 a, AmgLevel F, const float* __restrict__ e, floa
         const int J = __ldg(&F.pcol[b0 + bq]);
         const float* __restrict__ P = F.Pv + 18 * (size_t)(b0 + bq) + 6 * k;
         float s = 0.f;
+        if (!TF_IN(F.check, J, F.ncoarse, CK_PROLONG_COL)) {
+            part[q] = 0.f;
+            continue;
+        }
 #pragma unroll
         for (int c = 0; c < 6; ++c) s = fmaf(__ldg(&P[c]), e[6 * J + c], s);
         part[q] = s;
@@ -1374,6 +1386,7 @@ __device__ __forceinline__ void restrict_node(const AmgLevel& F, const AmgLevel&
             if (q < np) {
                 const int m = q / BS, k = q - BS * m;
                 const int i = __ldg(&F.pcrow[q0 + m]);
+                if (!TF_IN(F.check, i, F.n, CK_RESTRICT_ROW)) continue;
                 tk[u] = t[BS * (size_t)i + k];
                 P[u] = Pc + 6 * (size_t)q;
             }
@@ -1410,6 +1423,7 @@ __device__ __forceinline__ void prolong_node(const AmgLevel& F, const float* __r
     for (int k = 0; k < 6; ++k) s[k] = x[6 * i + k];
     for (int b = __ldg(&F.prow[i]); b < __ldg(&F.prow[i + 1]); ++b) {
         const int J = __ldg(&F.pcol[b]);
+        if (!TF_IN(F.check, J, F.ncoarse, CK_PROLONG_COL)) continue;
         const float* __restrict__ P = F.Pv + 36 * (size_t)b;
         float ec[6];
 #pragma unroll

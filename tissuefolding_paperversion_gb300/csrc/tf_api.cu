@@ -112,7 +112,8 @@ void free_all(tf_handle* h) {
                     d.slot, d.bofs, d.wslot0, d.scol, d.val, d.eblk, d.ef, d.gptr, d.glist, d.fptr, d.flist, d.uk, d.un, d.vel, d.g,
                     d.du, d.dinv, d.r, d.p, d.z, d.q, d.rhat, d.s, d.t, d.sh, d.scal, d.part, d.tickets,
                     d.seg_node0, d.elem_seg, d.cta_seg, d.cta_node0, d.cta_node1, d.seg_cta0, d.seg_active, d.seg_solve,
-                    d.tblk, d.valT, d.lamv, d.carry, d.dldu, d.gr, d.ge, d.nu, d.apical, d.xrow, d.xcol, d.xval};
+                    d.tblk, d.valT, d.lamv, d.carry, d.dldu, d.gr, d.ge, d.nu, d.apical, d.xrow, d.xcol, d.xval,
+                    d.check};
     destroy_graphs(h);
     if (h->amg) {
         amg_free(h->amg);
@@ -173,6 +174,8 @@ tf_status setup_instances(tf_handle* h, const std::vector<int>& seg_node0, const
     TF_TRY(upload(&d.seg_active, h->h_active));
     TF_TRY(upload(&d.seg_solve, h->h_active));
     TF_TRY(dev_alloc(&d.tickets, nseg));
+    TF_TRY(dev_alloc(&d.check, 1));
+    TF_CUDA(cudaMemset(d.check, 0, sizeof(int)));
     TF_CUDA(cudaMemset(d.tickets, 0, sizeof(unsigned) * (size_t)nseg));
     TF_TRY(dev_alloc(&d.scal, (size_t)nseg * S_COUNT));
     TF_CUDA(cudaMemset(d.scal, 0, sizeof(double) * (size_t)nseg * S_COUNT));
@@ -641,6 +644,26 @@ __global__ void k_add_entries(int n, const int* __restrict__ off, const double* 
                               double* __restrict__ val) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) atomicAdd(&val[off[k]], v[k]);
+}
+
+// Checked build: a failed index check of the last kernels becomes
+// TF_CUDA_ERROR (with the site) and the word is cleared; a no-op otherwise.
+tf_status take_check(tf_handle* h) {
+#ifdef TF_CHECKED
+    int code = 0;
+    TF_CUDA(cudaMemcpyAsync(&code, h->d.check, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    TF_CUDA(cudaStreamSynchronize(h->stream));
+    if (code == 0) return TF_OK;
+    TF_CUDA(cudaMemset(h->d.check, 0, sizeof(int)));
+    static const char* site[] = {"", "prism node id", "element scatter offset", "Krylov product column",
+                                 "extra block column", "level-0 smoother column", "restriction row",
+                                 "prolongation column", "packing couple node", "packing extra block"};
+    set_error(std::string("index check failed: ") + (code > 0 && code < 10 ? site[code] : "unknown site"));
+    return TF_CUDA_ERROR;
+#else
+    (void)h;
+    return TF_OK;
+#endif
 }
 
 // The extra-block values of the current assembly back to the host copy
@@ -1233,7 +1256,7 @@ tf_status tf_begin_step(tf_handle* h, double dt) {
                             h->stream));
     h->assembled = false;
     if (h->pk) TF_TRY(packing_detect(h));  // runOneStep: detectPacingNodes after growth (Simulation.cpp:5920)
-    return TF_OK;
+    return take_check(h);
 }
 
 tf_status tf_assemble(tf_handle* h) {
@@ -1250,6 +1273,7 @@ tf_status tf_assemble(tf_handle* h) {
     TF_TRY(launch_element(h));
     if (h->opt.deterministic) TF_TRY(launch_deterministic_gather(h));
     if (h->pk) TF_TRY(packing_assemble(h));  // after addImplicitKViscousExternalToJacobian (Simulation.cpp:6489-6493)
+    TF_TRY(take_check(h));
     h->assembled = true;
     return TF_OK;
 }
@@ -1275,6 +1299,7 @@ tf_status tf_solve(tf_handle* h, int32_t* iters, double* relres) {
     int it = 0;
     double rr = 0.0;
     tf_status s = krylov_solve(h, &it, &rr);
+    TF_TRY(take_check(h));
     if (!h->bind_slave.empty() && (s == TF_OK || s == TF_KRYLOV_NOT_CONVERGED)) {
         int* ds = nullptr;
         int* dm = nullptr;

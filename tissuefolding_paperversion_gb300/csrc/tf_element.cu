@@ -68,6 +68,10 @@ struct ElemArgs {
     double* __restrict__ Kv;
     double* __restrict__ fe;
     double* __restrict__ fv;
+    // checked build
+    int nn;
+    int64_t nval;
+    int* check;
 };
 
 // Per-Gauss-point values in registers.
@@ -94,7 +98,10 @@ __device__ __forceinline__ void gauss_point(const ElemArgs& A, int e, int gp, bo
     const int ne = A.ne;
     int nd[6];
 #pragma unroll
-    for (int a = 0; a < 6; ++a) nd[a] = __ldg(&A.conn[a * ne + e]);
+    for (int a = 0; a < 6; ++a) {
+        nd[a] = __ldg(&A.conn[a * ne + e]);
+        if (!TF_IN(A.check, nd[a], A.nn, CK_ELEM_NODE)) nd[a] = 0;
+    }
     double gX[18];
     const size_t q = 6 * (size_t)e + gp;
 #pragma unroll
@@ -313,6 +320,7 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
         }
         const int a = k / 3, d = k - 3 * (k / 3);
         const int node = __ldg(&A.conn[a * A.ne + e]);
+        if (!TF_IN(A.check, node, A.nn, CK_ELEM_NODE)) continue;
         const bool fx = A.fixed[3 * node + d] != 0;
         if (MODE == kStore) A.ef[(size_t)k * A.ne + e] = fx ? 0.0 : f;
         else if (!fx) atomicAdd(&A.g[3 * node + d], f);
@@ -367,6 +375,7 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
         }
         const int na = __ldg(&A.conn[a * A.ne + e]);
         const int nb = __ldg(&A.conn[bq * A.ne + e]);
+        if (!TF_IN(A.check, na, A.nn, CK_ELEM_NODE) || !TF_IN(A.check, nb, A.nn, CK_ELEM_NODE)) continue;
         bool fr[3], fc[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
@@ -387,14 +396,18 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
                     if (mirror) A.eblk[(3 * k + i) * stride + baseT] = v;
                 }
         } else {
-            double* dst = A.val + __ldg(&A.slot[(6 * a + bq) * A.ne + e]);
+            const int off = __ldg(&A.slot[(6 * a + bq) * A.ne + e]);
+            if (!TF_IN(A.check, off, A.nval - 8 * kSlice, CK_ELEM_SLOT)) continue;
+            double* dst = A.val + off;
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int k = 0; k < 3; ++k)
                     if (!fr[i] && !fc[k]) atomicAdd(dst + kSlice * (3 * i + k), acc[3 * i + k]);
             if (mirror) {
-                double* dt = A.val + __ldg(&A.slot[(6 * bq + a) * A.ne + e]);
+                const int offT = __ldg(&A.slot[(6 * bq + a) * A.ne + e]);
+                if (!TF_IN(A.check, offT, A.nval - 8 * kSlice, CK_ELEM_SLOT)) continue;
+                double* dt = A.val + offT;
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -656,6 +669,9 @@ ElemArgs make_args(tf_handle* h) {
     A.elem_seg = d.elem_seg;
     A.seg_active = d.seg_active;
     A.masked = d.nseg > 1 ? 1 : 0;
+    A.nn = d.nn;
+    A.nval = d.nval;
+    A.check = d.check;
     return A;
 }
 

@@ -22,6 +22,34 @@ struct NvtxRange {
     NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
+// Checked build (-DTF_CHECKED, libtfgpu_checked.so): the indexed accesses of
+// the main kernels test their index first; an index outside its array
+// records the site's code in the handle's device word `check` (the first
+// failing site wins) and the access is skipped, so nothing reads or writes
+// out of bounds.  The host turns a recorded code into TF_CUDA_ERROR after
+// the call.  In the normal build the tests compile away.
+enum CheckSite {
+    CK_ELEM_NODE = 1,    // prism node id < n_nodes (element kernels)
+    CK_ELEM_SLOT,        // scatter offset inside the block values
+    CK_SPMV_COL,         // column of the Krylov product < n_nodes
+    CK_EXTRA_COL,        // column of an extra block < n_nodes
+    CK_V0_COL,           // column of the level-0 smoother product < n_nodes
+    CK_RESTRICT_ROW,     // fine node of a restriction block < fine level size
+    CK_PROLONG_COL,      // coarse node of a prolongation block < coarse level size
+    CK_PACK_NODE,        // node of a packing couple < n_nodes
+    CK_PACK_BLOCK,       // extra block of a packing couple < extra blocks
+};
+#ifdef TF_CHECKED
+__device__ __forceinline__ bool check_in(int* flag, long long i, long long n, int code) {
+    if (i >= 0 && i < n) return true;
+    if (flag) atomicCAS(flag, 0, code);
+    return false;
+}
+#define TF_IN(flag, i, n, code) ::tf::check_in((flag), (long long)(i), (long long)(n), (code))
+#else
+#define TF_IN(flag, i, n, code) true
+#endif
+
 // Sliced block storage: a slot holds one 3x3 block for each of 32 rows.
 constexpr int kSlice = 32;
 constexpr int kSlotDoubles = 9 * kSlice;
@@ -119,6 +147,7 @@ struct Device {
     double* ge = nullptr;       // [ne] dL/d log E
     double* nu = nullptr;       // [ne] Poisson ratios (clamped to [0, 0.5])
     int* apical = nullptr;      // [nn] 1 for apical nodes
+    int* check = nullptr;       // checked build: code of the first failed index check (0: none)
 };
 
 // Indices into Device::scal (device-resident Krylov scalars).
@@ -174,7 +203,8 @@ inline void launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream
 // coalesced access.
 template <class T>
 __device__ __forceinline__ void sliced_row(const int* __restrict__ wslot0, const int* __restrict__ scol,
-                                           const T* __restrict__ val, const double* __restrict__ x, double y[3]) {
+                                           const T* __restrict__ val, const double* __restrict__ x, double y[3],
+                                           int nn = 0, int* check = nullptr) {
     const int lane = threadIdx.x & 31;
     const int wg = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const int s0 = __ldg(&wslot0[wg]), s1 = __ldg(&wslot0[wg + 1]);
@@ -184,6 +214,7 @@ __device__ __forceinline__ void sliced_row(const int* __restrict__ wslot0, const
 #pragma unroll 2
     for (int s = s0; s < s1; ++s) {
         const int j = __ldg(&col[(size_t)s * kSlice]);
+        if (!TF_IN(check, j, nn, CK_SPMV_COL)) continue;
         const T* __restrict__ v = a + (size_t)s * kSlotDoubles;
         const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
         y0 = fma((double)__ldg(&v[0]), x0, fma((double)__ldg(&v[32]), x1, fma((double)__ldg(&v[64]), x2, y0)));
@@ -283,6 +314,7 @@ bool use_multigrid(const tf_handle* h);
 void packing_free(Packing* p);
 tf_status upload_extra(tf_handle* h, bool pattern_changed);
 tf_status sync_extra_to_host(tf_handle* h);      // device extra-block values -> h_xval
+tf_status take_check(tf_handle* h);              // checked build: report and clear a failed index check
 bool amg_reused(const tf_handle* h);
 tf_status launch_adjoint_element(tf_handle* h, const double* lamv, double* carry, double* gr, double* ge, double ndt);
 void destroy_graphs(tf_handle* h);

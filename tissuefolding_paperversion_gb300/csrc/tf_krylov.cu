@@ -52,6 +52,8 @@ struct Ctx {
     const int* __restrict__ xrow;     // extra blocks (tf_add_K_triplets), null: none
     const int* __restrict__ xcol;
     const double* __restrict__ xval;
+    int nn;
+    int* check;                       // checked build: failed index checks
 };
 
 struct Where {
@@ -133,10 +135,11 @@ __device__ __forceinline__ void apply_dinv(const double* __restrict__ D, const d
 }
 
 __device__ __forceinline__ void bsr_row(const Ctx& c, int i, const double* __restrict__ x, double y[3]) {
-    sliced_row(c.wslot0, c.scol, c.val, x, y);
+    sliced_row(c.wslot0, c.scol, c.val, x, y, c.nn, c.check);
     if (c.xrow) {
         for (int p = c.xrow[i]; p < c.xrow[i + 1]; ++p) {
             const int j = c.xcol[p];
+            if (!TF_IN(c.check, j, c.nn, CK_EXTRA_COL)) continue;
             const double* __restrict__ a = c.xval + 9 * (size_t)p;
             const double x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
             y[0] = fma(a[0], x0, fma(a[1], x1, fma(a[2], x2, y[0])));
@@ -601,6 +604,8 @@ Ctx make_ctx(tf_handle* h) {
     c.xrow = d.nxb > 0 ? d.xrow : nullptr;
     c.xcol = d.xcol;
     c.xval = d.xval;
+    c.nn = d.nn;
+    c.check = d.check;
     return c;
 }
 

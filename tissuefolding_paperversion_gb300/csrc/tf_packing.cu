@@ -511,6 +511,9 @@ struct Asm {
     const double* mbar;
     const double* par;
     const uint8_t* fixed;
+    int nn;
+    int64_t nxb;
+    int* check;  // checked build: failed index checks
 };
 
 // Forces and diagonal K entries, node by node in couple order.
@@ -528,6 +531,7 @@ __global__ void k_pk_nodes(Asm A, int nnodes, const int* __restrict__ pnode, con
     for (int q = pptr[t]; q < pptr[t + 1]; ++q) {
         const int c = plist[q] >> 1, role = plist[q] & 1;
         const int n0 = A.c0[c], n1 = A.c1[c];
+        if (!TF_IN(A.check, n0, A.nn, CK_PACK_NODE) || !TF_IN(A.check, n1, A.nn, CK_PACK_NODE)) continue;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const Axis x = axis_terms(A.uk, n0, n1, A.w[3 * (size_t)c + a], A.mbar[c], k, a);
@@ -551,6 +555,9 @@ __global__ void k_pk_pairs(Asm A, int n, const int* __restrict__ x01, const int*
     if (c >= n) return;
     const double k = __ddiv_rn(kSaturation, A.par[P_THR]);
     const int n0 = A.c0[c], n1 = A.c1[c];
+    if (!TF_IN(A.check, n0, A.nn, CK_PACK_NODE) || !TF_IN(A.check, n1, A.nn, CK_PACK_NODE) ||
+        !TF_IN(A.check, x01[c], A.nxb, CK_PACK_BLOCK) || !TF_IN(A.check, x10[c], A.nxb, CK_PACK_BLOCK))
+        return;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const Axis x = axis_terms(A.uk, n0, n1, A.w[3 * (size_t)c + a], A.mbar[c], k, a);
@@ -749,7 +756,7 @@ tf_status packing_assemble(tf_handle* h) {
     Packing* p = h->pk;
     if (!p || p->n == 0) return TF_OK;
     Device& d = h->d;
-    Asm A{d.uk, p->c0, p->c1, p->w, p->mbar, p->par, d.fixed};
+    Asm A{d.uk, p->c0, p->c1, p->w, p->mbar, p->par, d.fixed, d.nn, d.nxb, d.check};
     k_pk_nodes<<<cdiv(p->nnodes, 128), 128, 0, h->stream>>>(A, p->nnodes, p->pnode, p->pptr, p->plist, d.diag, d.val,
                                                             d.g);
     TF_LAUNCH_CHECK(h);
