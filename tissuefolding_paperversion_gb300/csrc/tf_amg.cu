@@ -1578,6 +1578,8 @@ void amg_mark_stale(tf_handle* h, int level) {
 
 bool amg_reused(const tf_handle* h) { return h->amg && h->amg->reused; }
 
+bool use_multigrid(const tf_handle* h) { return h->amg != nullptr; }
+
 // Numeric phase for the current matrix.  Within a time step the matrix of
 // a later Newton iteration differs little from the first one's, so a new
 // assembly only refreshes the FP32 copies the level-0 smoother reads; the

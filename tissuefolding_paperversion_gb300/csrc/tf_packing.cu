@@ -750,8 +750,6 @@ tf_status packing_relink(tf_handle* h) {
     return TF_OK;
 }
 
-bool use_multigrid(const tf_handle* h) { return h->amg != nullptr; }
-
 tf_status packing_assemble(tf_handle* h) {
     Packing* p = h->pk;
     if (!p || p->n == 0) return TF_OK;
