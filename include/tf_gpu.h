@@ -173,6 +173,42 @@ TF_API tf_status tf_get_packing(tf_handle* h, int64_t* n, int32_t* nodes, double
                                 double* threshold, double* detect_distance);
 /* Node masses of the last detection (Node::mass), n_nodes values. */
 TF_API tf_status tf_packing_masses(tf_handle* h, double* mass);
+
+/* --- grid-based growth functions (growth type 3) ------------------------- */
+/* Adds a GridBasedGrowthFunction (GrowthFunctionTypes.h:266-609, read by
+ * ModelInputObject::readGrowthOptions): an nx x ny grid of growth rates in 1/s,
+ * rates[3*(i*ny + j) + k] for grid point (i, j) and axis k (x, y, z), and xy
+ * angles in degrees, angles_deg[i*ny + j] (NULL: all 0).  Active while
+ * init_time <= t < end_time (both kept as float, as GrowthFunctionBase does)
+ * on prisms whose initial relative z (0 apical, 1 basal) is within
+ * [zmin, zmax].  Every tf_begin_step at time t applies the active functions
+ * after the per-element rates: Simulation::calculateGrowthGridBased
+ * (Simulation.cpp:10065-10114) with ShapeBase::calculateFgFromGridCorners
+ * (ShapeBase.cpp:432-562), positions from Simulation.cpp:5833-5843.  The
+ * handle's initial relative z, columns and pinned positions come from the mesh
+ * given to tf_create.  Columnar prisms only; single-mesh handles only. */
+TF_API tf_status tf_add_grid_growth(tf_handle* h, int32_t nx, int32_t ny, const double* rates,
+                                    const double* angles_deg, double init_time, double end_time, double zmin,
+                                    double zmax);
+/* Removes every grid growth function. */
+TF_API tf_status tf_clear_grid_growth(tf_handle* h);
+/* gridGrowthsInterpolationType (0 nearest grid point, 1 bilinear; default 1)
+ * and GridGrowthsPinnedOnInitialMesh (default 0: the positions of each step's
+ * start shape), Simulation.cpp:144-146. */
+TF_API tf_status tf_set_grid_growth_mode(tf_handle* h, int32_t interpolation, int32_t pinned_on_initial_mesh);
+/* Simulation::updatePinningPositions (Simulation.cpp:6018-6023): the current
+ * shape's bounding-box positions become the pinned ones. */
+TF_API tf_status tf_repin_grid_growth(tf_handle* h);
+/* Per prism: initial relative z [n_elems], pinned positions [2*n_elems] and
+ * the current shape's positions [2*n_elems] (x block, then y block) in the
+ * bounding box, after the column rule of
+ * Simulation::updateRelativePositionsToApicalPositioning (:5987-6003).
+ * Any argument may be NULL. */
+TF_API tf_status tf_grid_growth_positions(tf_handle* h, double* rel_z, double* rel_pinned, double* rel_current);
+/* Simulation time in seconds (currSimTimeSec, starts at 0); tf_end_step
+ * advances it by the step's dt (Simulation.cpp:5969). */
+TF_API tf_status tf_set_time(tf_handle* h, double time_sec);
+TF_API tf_status tf_get_time(tf_handle* h, double* time_sec);
 /* solveForDeltaU (NewtonRaphsonSolver.cpp:382-404): solves K^T du = g, the
  * transposed system Pardiso is asked for (iparm[11] = 1, :639). */
 TF_API tf_status tf_solve(tf_handle* h, int32_t* iters, double* relres);

@@ -1,0 +1,355 @@
+"""Grid-based growth functions: numpy restatement of the reference's growth
+type 3, for checking the GPU kernels.  TEST INFRASTRUCTURE ONLY: imported by
+tests/, never by the library.
+
+Follows, in TissueFolding/TissueFolding/SourceCode/:
+  * GridBasedGrowthFunction (GrowthFunctionTypes.h:266-609): the aspect-ratio
+    test of its constructor (:336-349, threshold 1.1) and
+    preCalculateAnglesForCompatibleAveraging (:427-579): corner angles brought
+    to [0, pi] and next to the first corner that carries one, x/y rates
+    swapped where a corner turns by about 90 or 270 degrees;
+  * Simulation::calculateTissueHeight (Simulation.cpp:3280-3330) with
+    Prism::IsThisNodeMyBasal / getCorrecpondingApical / getElementHeight
+    (Prism.cpp:1497-1531);
+  * Simulation::calculateBoundingBox (Simulation.cpp:9148-9185), its running
+    "else if" included: a node that lowers the minimum is not a candidate for
+    the maximum;
+  * ShapeBase::setInitialZPosition (ShapeBase.cpp:612-627),
+    calculateRelativePosInBoundingBox (:1842-1848) with getCentre (:240-250);
+  * ShapeBase::setTissuePlacement (ShapeBase.cpp:705-770),
+    Simulation::fillInElementColumnLists (Simulation.cpp:7612-7624) with
+    Prism::constructElementStackList (Prism.cpp:2542-2584) and
+    Simulation::updateRelativePositionsToApicalPositioning (:5987-6003);
+  * ShapeBase::convertRelativePosToGridIndex (ShapeBase.cpp:633-660) and
+    calculateFgFromGridCorners (:432-562) for columnar prisms (tissue weight
+    1), Simulation::calculateGrowthGridBased (Simulation.cpp:10065-10114),
+    ShapeBase::updateGrowthIncrement (:567-586) and growShapeByFg
+    (:1215-1251).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from tissuefolding_paperversion_gb300 import mesh
+
+BOX_INIT = 100000.0   # calculateBoundingBox's starting corners
+
+
+def element_placement(conn, node_placement):
+    """(E,) 3 lateral, 1 apical, 0 basal, 2 mid-line or spanning."""
+    c = np.asarray(conn).reshape(-1, 6)
+    p = np.asarray(node_placement)[c]
+    ap = (p == 1).any(axis=1)
+    ba = (p == 0).any(axis=1)
+    la = (p == 3).any(axis=1)
+    out = np.full(c.shape[0], 2, dtype=np.int32)
+    out[ba & ~ap] = 0
+    out[ap & ~ba] = 1
+    out[la] = 3
+    return out
+
+
+def bounding_box(pos):
+    """(lo (3,), size (3,)) as calculateBoundingBox computes them."""
+    p = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
+    lo = np.minimum(BOX_INIT, p.min(axis=0)) if len(p) else np.full(3, BOX_INIT)
+    hi = np.full(3, -BOX_INIT)
+    for k in range(3):
+        x = p[:, k]
+        before = np.minimum.accumulate(np.concatenate([[BOX_INIT], x[:-1]]))
+        before = np.minimum(before, BOX_INIT)
+        cand = x[~(x < before)]
+        if cand.size:
+            hi[k] = max(-BOX_INIT, cand.max())
+    return lo, hi - lo
+
+
+def centres(pos, conn):
+    """Prism centres, summed node by node in connectivity order, then / 6."""
+    p = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
+    c = np.asarray(conn).reshape(-1, 6)
+    s = np.zeros((c.shape[0], 3))
+    for a in range(6):
+        s = s + p[c[:, a]]
+    return s / 6
+
+
+def tissue_height(pos, conn, node_placement):
+    """(layers, height) from the first basal node up its column."""
+    p = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
+    c = np.asarray(conn).reshape(-1, 6)
+    pl = np.asarray(node_placement)
+    basal = np.nonzero(pl == 0)[0]
+    if basal.size == 0:
+        return 0, 0.0
+    cur = int(basal[0])
+    layers, height = 0, 0.0
+    for _ in range(c.shape[0] + 1):
+        if pl[cur] == 1:
+            break
+        hit = np.nonzero((c[:, :3] == cur).any(axis=1))[0]
+        if hit.size == 0:
+            break
+        e = int(hit[0])
+        d = p[c[e, 0]] - p[c[e, 3]]
+        height += math.pow(float(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]), 0.5)
+        layers += 1
+        cur = int(c[e, 3 + int(np.nonzero(c[e, :3] == cur)[0][0])])
+    return layers, height
+
+
+def columns(conn, node_placement, layers):
+    """(E,) the prism whose bounding-box position each prism takes."""
+    c = np.asarray(conn).reshape(-1, 6)
+    ne = c.shape[0]
+    place = element_placement(c, node_placement)
+    by_basal = {}
+    for e in range(ne):
+        by_basal.setdefault(tuple(sorted(c[e, :3])), e)
+    src = np.arange(ne)
+    if layers < 3:
+        return src
+    for e in np.nonzero(place == 0)[0]:
+        col = [int(e)]
+        for _ in range(1, layers):
+            nxt = by_basal.get(tuple(sorted(c[col[-1], 3:])))
+            if nxt is None or nxt == col[-1]:
+                break
+            col.append(nxt)
+        if len(col) != layers or place[col[-1]] != 1:
+            continue
+        for i in range(layers - 2):
+            src[col[i]] = col[-1]
+    return src
+
+
+def relative_positions(pos, conn, src):
+    """(E, 2) positions in the bounding box after the column rule."""
+    lo, size = bounding_box(pos)
+    cen = centres(pos, conn)
+    rel = np.stack([(cen[:, 0] - lo[0]) / size[0], (cen[:, 1] - lo[1]) / size[1]], axis=1)
+    return rel[src]
+
+
+def initial_state(pos0, conn, node_placement):
+    """Tissue height, initial relative z, columns and pinned positions."""
+    layers, height = tissue_height(pos0, conn, node_placement)
+    lo, _ = bounding_box(pos0)
+    cz = centres(pos0, conn)[:, 2]
+    relz = np.clip(1.0 - (cz - lo[2]) / height, 0.0, 1.0)
+    src = columns(conn, node_placement, layers)
+    return {"layers": layers, "height": height, "relz": relz, "src": src,
+            "rel0": relative_positions(pos0, conn, src)}
+
+
+def compatible_corners(rates, angles_deg=None):
+    """rates (nx, ny, 3), angles (nx, ny) degrees -> per cell (nx-1, ny-1):
+    corner rates (4, 3), corner angles (4,), corners without an angle (4,)."""
+    r = np.asarray(rates, dtype=np.float64)
+    nx, ny = r.shape[:2]
+    ang = np.zeros((nx, ny)) if angles_deg is None else np.asarray(angles_deg, dtype=np.float64) * math.pi / 180.0
+    cg = np.zeros((nx - 1, ny - 1, 4, 3))
+    ca = np.zeros((nx - 1, ny - 1, 4))
+    ce = np.zeros((nx - 1, ny - 1, 4), dtype=bool)
+
+    def over(i, j):
+        ar = r[i, j, 0] / r[i, j, 1]
+        if ar < 0:
+            ar *= -1.0
+        if ar < 1.0:
+            ar = 1 / ar
+        return not ar < 1.1
+
+    pi = math.pi
+    for ix in range(nx - 1):
+        for iy in range(ny - 1):
+            pts = [(ix, iy), (ix + 1, iy), (ix, iy + 1), (ix + 1, iy + 1)]
+            g = [list(r[i, j]) for i, j in pts]
+            a = [0.0] * 4
+            el = [False] * 4
+            for c, (i, j) in enumerate(pts):
+                if over(i, j):
+                    a[c] = float(ang[i, j])
+                else:
+                    el[c] = True
+            for c in range(4):
+                while a[c] < 0:
+                    a[c] += pi
+                while a[c] > pi:
+                    a[c] -= pi
+            base, tet = 3, 0.0
+            for c in range(4):
+                if not el[c]:
+                    base, tet = c, a[c]
+                    break
+            flip = [False] * 4
+            for c in range(base, 4):
+                d = a[c] - tet
+                if d > 0:
+                    if pi / 4.0 <= d < 3.0 * pi / 4.0:
+                        a[c], flip[c] = a[c] - pi / 2.0, True
+                    elif 3.0 * pi / 4.0 <= d < 5.0 * pi / 4.0:
+                        a[c] = a[c] - pi
+                    elif 5.0 * pi / 4.0 <= d < 7.0 * pi / 4.0:
+                        a[c], flip[c] = a[c] - 6.0 * pi / 4.0, True
+                    elif d >= 7.0 * pi / 4.0:
+                        a[c] = a[c] - 2.0 * pi
+                elif d < 0:
+                    if -3.0 * pi / 4.0 < d <= -pi / 4.0:
+                        a[c], flip[c] = a[c] + pi / 2.0, True
+                    elif -5.0 * pi / 4.0 < d <= -3.0 * pi / 4.0:
+                        a[c] = a[c] + pi
+                    elif -7.0 * pi / 4.0 < d <= -5.0 * pi / 4.0:
+                        a[c], flip[c] = a[c] + 6.0 * pi / 4.0, True
+                    elif d <= -7.0 * pi / 4.0:
+                        a[c] = a[c] + 2.0 * pi
+            for c in range(4):
+                if flip[c]:
+                    g[c][0], g[c][1] = g[c][1], g[c][0]
+            cg[ix, iy] = g
+            ca[ix, iy] = a
+            ce[ix, iy] = el
+    return cg, ca, ce
+
+
+def grid_index(rel, nx, ny):
+    """convertRelativePosToGridIndex: (ix, iy, fx, fy) per prism."""
+    rx = rel[:, 0] * float(np.float32(nx - 1))
+    ry = rel[:, 1] * float(np.float32(ny - 1))
+    ix = np.floor(rx).astype(np.int64)
+    iy = np.floor(ry).astype(np.int64)
+    fx = rx - ix
+    fy = ry - iy
+    hi = ix >= nx - 1
+    lo = ~hi & (ix < 0)
+    ix = np.where(hi, nx - 2, np.where(lo, 0, ix))
+    fx = np.where(hi, 1.0, np.where(lo, 0.0, fx))
+    hi = iy >= ny - 1
+    lo = ~hi & (iy < 0)
+    iy = np.where(hi, ny - 2, np.where(lo, 0, iy))
+    fy = np.where(hi, 1.0, np.where(lo, 0.0, fy))
+    return ix, iy, fx, fy
+
+
+def dgemm3(A, B, trans_b=False):
+    """Stacked 3x3 products C = A B (or A B^T) summed over k from 0 as the
+    reference's gsl_blas_dgemm stand-in does: ((0 + a0 b0) + a1 b1) + a2 b2."""
+    Bt = np.transpose(B, (0, 2, 1)) if trans_b else B
+    C = np.zeros(np.broadcast_shapes(A.shape, Bt.shape))
+    for i in range(3):
+        for j in range(3):
+            acc = np.zeros(C.shape[0])
+            for k in range(3):
+                acc = acc + A[:, i, k] * Bt[:, k, j]
+            C[:, i, j] = acc
+    return C
+
+
+def grid_increments(rel, relz, corners, dt, interp=1, zmin=0.0, zmax=1.0):
+    """(E, 3, 3) growth increments of one grid function
+    (calculateFgFromGridCorners, operations in the reference's order)."""
+    cg, ca, ce = corners
+    nx, ny = cg.shape[0] + 1, cg.shape[1] + 1
+    ne = rel.shape[0]
+    ix, iy, fx, fy = grid_index(rel, nx, ny)
+    g = cg[ix, iy]          # (E, 4, 3)
+    an = ca[ix, iy]         # (E, 4)
+    el = ce[ix, iy]         # (E, 4)
+    ux, uy = 1.0 - fx, 1.0 - fy
+    if interp == 0:
+        corner = np.where(fx > 0.5, np.where(fy > 0.5, 3, 1), np.where(fy > 0.5, 2, 0))
+        growth = g[np.arange(ne), corner]
+        angle = np.zeros(ne)
+    else:
+        fe = np.zeros(ne)
+        for c, w in enumerate((ux * uy, fx * uy, ux * fy, fx * fy)):
+            fe = np.where(el[:, c], fe + w, fe)
+        angle = an[:, 0] * ux * uy + an[:, 1] * fx * uy + an[:, 2] * ux * fy + an[:, 3] * fx * fy
+        safe = np.where(fe < 1.0, 1.0 - fe, 1.0)
+        angle = np.where(fe > 0, np.where(fe >= 0.9999999, 0.0, angle / safe), angle)
+        growth = (g[:, 0] * ux[:, None] * uy[:, None] + g[:, 1] * fx[:, None] * uy[:, None]
+                  + g[:, 2] * ux[:, None] * fy[:, None] + g[:, 3] * fx[:, None] * fy[:, None])
+    inc = np.zeros((ne, 3, 3))
+    for k in range(3):
+        inc[:, k, k] = np.exp(growth[:, k] * dt)
+    rot = angle != 0.0
+    if rot.any():
+        c, s = np.cos(angle[rot]), np.sin(angle[rot])
+        R = np.zeros((int(rot.sum()), 3, 3))
+        R[:, 0, 0], R[:, 0, 1], R[:, 1, 0], R[:, 1, 1], R[:, 2, 2] = c, -1.0 * s, s, c, 1.0
+        inc[rot] = dgemm3(dgemm3(R, inc[rot]), R, trans_b=True)
+    off = (relz < zmin) | (relz > zmax)
+    inc[off] = np.eye(3)
+    return inc
+
+
+class GridGrowthOracle:
+    """Grid functions on one tissue: the state the reference keeps for them."""
+
+    def __init__(self, pos0, conn, node_placement):
+        self.conn = np.asarray(conn).reshape(-1, 6)
+        self.state = initial_state(pos0, self.conn, node_placement)
+        self.fns = []
+        self.interp = 1
+        self.pinned = False
+
+    def add(self, rates, angles_deg=None, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0):
+        self.fns.append({"corners": compatible_corners(rates, angles_deg),
+                         "t0": float(np.float32(init_time)), "t1": float(np.float32(end_time)),
+                         "zmin": zmin, "zmax": zmax})
+
+    def repin(self, pos):
+        self.state["rel0"] = relative_positions(pos, self.conn, self.state["src"])
+
+    def increment(self, pos, time, dt, rates=None):
+        """The step's growth increment (E, 3, 3): the per-element rates'
+        diag(exp(rate dt)), then each active function's increment multiplied
+        on the left (updateGrowthIncrement)."""
+        ne = self.conn.shape[0]
+        total = np.broadcast_to(np.eye(3), (ne, 3, 3)).copy()
+        if rates is not None:
+            r = np.asarray(rates, dtype=np.float64).reshape(-1, 3)
+            for k in range(3):
+                total[:, k, k] = np.exp(r[:, k] * 1.0 * dt)
+        active = [f for f in self.fns if f["t0"] <= time < f["t1"]]
+        if not active:
+            return total
+        rel = self.state["rel0"] if self.pinned else relative_positions(pos, self.conn, self.state["src"])
+        for f in active:
+            total = dgemm3(grid_increments(rel, self.state["relz"], f["corners"], dt, self.interp, f["zmin"],
+                                           f["zmax"]), total)
+        return total
+
+    def grow(self, Fg, pos, time, dt, rates=None):
+        """Fg (E, 3, 3) after one step's growth (growShapeByFg)."""
+        Fg = np.broadcast_to(np.asarray(Fg, dtype=np.float64), (self.conn.shape[0], 3, 3))
+        return dgemm3(self.increment(pos, time, dt, rates), Fg)
+
+
+FIXTURES = ["steps_grid_growth", "steps_grid_growth_pinned"]
+
+
+def fixture_case(name):
+    """Tissue, grid functions, interpolation and pinning of a grid growth
+    fixture (tests/golden/make_golden.py --only-grid).  steps_grid_growth: a
+    4-layer sheet renumbered so that node 0 alone holds the largest x (the
+    reference's bounding box then misses the true maximum), two functions,
+    the second only in the basal half and from t = 60 s, bilinear, current
+    positions.  steps_grid_growth_pinned: a 3-layer sheet, one function,
+    nearest grid point, positions pinned on the initial mesh."""
+    if name == "steps_grid_growth":
+        t = mesh.config_tiny(seed=21, n=6, n_layers=4, eta=50.0)
+        t = mesh.swap_nodes(t, 0, int(np.argmax(t.pos.reshape(-1, 3)[:, 0])))
+        t.pos[0] += 0.4
+        ra, aa = mesh.grid_growth_inputs(31, 5, 4)
+        rb, ab = mesh.grid_growth_inputs(32, 3, 3, scale=5e-5)
+        fns = [dict(rates=ra, angles_deg=aa, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0),
+               dict(rates=rb, angles_deg=ab, init_time=60.0, end_time=1e30, zmin=0.5, zmax=1.0)]
+        return t, fns, 1, False
+    if name == "steps_grid_growth_pinned":
+        t = mesh.config_tiny(seed=22, n=5, n_layers=3, eta=0.0)
+        ra, aa = mesh.grid_growth_inputs(33, 4, 4)
+        return t, [dict(rates=ra, angles_deg=aa, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0)], 0, True
+    raise KeyError(name)

@@ -294,6 +294,14 @@ class Ref:
             L.tfr_pack_get.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
             L.tfr_node_masses.argtypes = [C.c_void_p, _dp]
             L.tfr_pack_forces.argtypes = [C.c_void_p, _dp]
+            L.tfr_add_grid_growth.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, C.c_void_p, C.c_double,
+                                              C.c_double, C.c_double, C.c_double]
+            L.tfr_set_grid_mode.argtypes = [C.c_void_p, C.c_int, C.c_int]
+            L.tfr_repin_grid_growth.argtypes = [C.c_void_p]
+            L.tfr_set_time.argtypes = [C.c_void_p, C.c_double]
+            L.tfr_get_time.restype = C.c_double
+            L.tfr_get_time.argtypes = [C.c_void_p]
+            L.tfr_grid_positions.argtypes = [C.c_void_p, _dp, _dp, _dp]
             cls._lib = L
         return cls._lib
 
@@ -417,6 +425,38 @@ class Ref:
         f = np.zeros(3 * self.nn)
         self.lib().tfr_pack_forces(self.h, f)
         return f
+
+    def add_grid_growth(self, rates, angles_deg=None, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0):
+        """The reference's GridBasedGrowthFunction: rates (nx, ny, 3) in 1/s,
+        angles_deg (nx, ny)."""
+        r = _f64(rates)
+        a = None if angles_deg is None else _f64(angles_deg)
+        self._grid_keep = getattr(self, "_grid_keep", []) + [r, a]
+        self.lib().tfr_add_grid_growth(self.h, r.shape[0], r.shape[1], r.reshape(-1),
+                                       None if a is None else a.ctypes.data_as(C.c_void_p),
+                                       init_time, end_time, zmin, zmax)
+
+    def set_grid_mode(self, interpolation=1, pinned=False):
+        self.lib().tfr_set_grid_mode(self.h, int(interpolation), 1 if pinned else 0)
+
+    def repin_grid_growth(self):
+        self.lib().tfr_repin_grid_growth(self.h)
+
+    @property
+    def time(self):
+        return self.lib().tfr_get_time(self.h)
+
+    @time.setter
+    def time(self, value):
+        self.lib().tfr_set_time(self.h, float(value))
+
+    def grid_positions(self):
+        """(relz (ne,), pinned (ne, 2), current (ne, 2))."""
+        z = np.zeros(self.ne)
+        p0 = np.zeros(2 * self.ne)
+        p = np.zeros(2 * self.ne)
+        self.lib().tfr_grid_positions(self.h, z, p0, p)
+        return z, p0.reshape(2, -1).T.copy(), p.reshape(2, -1).T.copy()
 
     def step(self, dt, rates=None):
         it = C.c_int(0)

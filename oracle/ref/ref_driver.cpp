@@ -23,16 +23,26 @@
 //     peripodial adhesion, and with no collapsed nodes),
 //     calculatePackingForcesImplicit3D :7149-7203,
 //     calculatePackingJacobian3D :7205-7300 and addPackingForces :8869-8900,
-//     in the order runOneStep / updateStepNR call them.  The reference's
-//     tissue alignment (alignTissueDVToXPositive), a rigid rotation outside
-//     the step, is not applied.
+//     in the order runOneStep / updateStepNR call them;
+//   * grid-based growth functions (tfr_add_grid_growth): the reference's own
+//     GridBasedGrowthFunction (GrowthFunctionTypes.h) applied by
+//     ShapeBase::calculateFgFromGridCorners as calculateGrowthGridBased
+//     does (Simulation.cpp:10065-10114), with calculateTissueHeight
+//     :3280-3330, assignInitialZPositions :3367-3371, fillInElementColumnLists
+//     :7612-7624, the bounding-box positions of initiateSystem :630-645 and of
+//     runOneStep :5833-5843, and updateRelativePositionsToApicalPositioning
+//     :5987-6003.
+//   The reference's tissue alignment (alignTissueDVToXPositive), a rigid
+//   rotation outside the step, is not applied.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <fstream>  // GrowthFunctionTypes.h writes summaries to std::ofstream without including it
 #include <iostream>
 #include <sstream>
 #include <vector>
 
+#include "GrowthFunctionTypes.h"
 #include "NewtonRaphsonSolver.h"
 #include "Node.h"
 #include "Prism.h"
@@ -49,6 +59,21 @@ public:
     void exposeSurfaces(std::vector<Node*>& nodes) { assignExposedSurfaceAreaIndices(nodes); }
     double lambdaValue() const { return lambda; }
     double muValue() const { return mu; }
+    double relZ() const { return initialRelativePositionInZ; }
+};
+
+// Grid-based growth functions and the simulation time (Simulation's
+// GrowthFunctions of type 3, gridGrowthsInterpolationType,
+// GridGrowthsPinnedOnInitialMesh, TissueHeight(DiscretisationLayers),
+// currSimTimeSec).
+struct GridRef {
+    std::vector<GridBasedGrowthFunction*> fns;
+    int interp = 1;
+    bool pinned = false;
+    bool setUp = false;
+    int layers = 0;
+    double height = 0.0;
+    double time = 0.0;
 };
 
 // State of the packing restatement (Simulation's packing members).
@@ -68,6 +93,7 @@ struct PackingRef {
 
 struct RefSim {
     PackingRef pk;
+    GridRef grid;
     std::vector<Node*> nodes;
     std::vector<ShapeBase*> elements;
     NewtonRaphsonSolver* nr = nullptr;
@@ -273,6 +299,98 @@ void refPackingStepStart(RefSim* s) {
     refDetectPacking(s);
 }
 
+// Simulation::updateRelativePositionsToApicalPositioning (Simulation.cpp:5987-6003)
+void refApicalPositioning(RefSim* s) {
+    for (ShapeBase* e : s->elements) {
+        if (e->tissuePlacement != 1 || e->tissueType != 0 || !e->elementsIdsOnSameColumn) continue;
+        double rel[2];
+        e->getRelativePosInBoundingBox(rel);
+        for (int i = 0; i < s->grid.layers - 2; ++i)
+            s->elements[e->elementsIdsOnSameColumn[i]]->setRelativePosInBoundingBox(rel[0], rel[1]);
+    }
+}
+
+// Once, at the first grid function, from the current (initial) shape:
+// Simulation::calculateTissueHeight (Simulation.cpp:3280-3330),
+// calculateBoundingBox + assignInitialZPositions (:573-576),
+// fillInElementColumnLists (:7612-7624), then the element positions in the
+// bounding box, moved to the apical ones and kept as the pinned positions
+// (:631-645).
+void refGridSetup(RefSim* s) {
+    GridRef& g = s->grid;
+    g.setUp = true;
+    int cur = -1;
+    for (Node* n : s->nodes)
+        if (n->tissueType == 0 && n->tissuePlacement == 0) {
+            cur = n->Id;
+            break;
+        }
+    for (int guard = 0; cur >= 0 && s->nodes[cur]->tissuePlacement != 1 && guard <= s->nElems; ++guard) {
+        ShapeBase* owner = nullptr;
+        for (ShapeBase* e : s->elements)
+            if (e->IsThisNodeMyBasal(cur)) {
+                owner = e;
+                break;
+            }
+        if (!owner) break;
+        g.height += owner->getElementHeight();
+        g.layers++;
+        cur = owner->getCorrecpondingApical(cur);
+    }
+    refBoundingBox(s);
+    for (ShapeBase* e : s->elements) e->setInitialZPosition(s->pk.bb[0][2], g.height);
+    if (g.layers > 0)
+        for (ShapeBase* e : s->elements)
+            if (!e->IsAblated && e->tissueType == 0 && e->tissuePlacement == 0)
+                e->constructElementStackList(g.layers, s->elements);
+    refApicalPositioning(s);
+    for (ShapeBase* e : s->elements) e->setInitialRelativePosInBoundingBox();
+}
+
+// The growth of one step: cleanUpGrowthRates, the per-element rates as a
+// uniform function, then (with_grid) the grid functions active at the
+// current time (calculateGrowth, Simulation.cpp:9651-9666, after the
+// bounding-box positions of :5833-5843), and growShapeByFg.
+void refGrow(RefSim* s, double dt, const double* rates, bool with_grid) {
+    QuietCout q;
+    GridRef& g = s->grid;
+    std::vector<GridBasedGrowthFunction*> active;
+    if (with_grid)
+        for (GridBasedGrowthFunction* f : g.fns)
+            if (g.time >= f->initTime && g.time < f->endTime) active.push_back(f);
+    if (!active.empty()) {
+        refBoundingBox(s);
+        refApicalPositioning(s);
+    }
+    gsl_matrix* rot = gsl_matrix_alloc(3, 3);
+    gsl_matrix* inc = gsl_matrix_alloc(3, 3);
+    gsl_matrix* peri = gsl_matrix_alloc(3, 3);
+    gsl_matrix_set_identity(rot);
+    for (int e = 0; e < s->nElems; ++e) {
+        ShapeBase* el = s->elements[e];
+        el->setGrowthRate(dt, 0.0, 0.0, 0.0);
+        el->updateGrowthIncrementFromRate();
+        gsl_matrix_set_identity(inc);
+        gsl_matrix_set_identity(peri);
+        el->calculateFgFromRates(dt, rates[3 * e], rates[3 * e + 1], rates[3 * e + 2], rot, inc, 0, 0.0, 1.0);
+        el->updateGrowthIncrement(inc, peri);
+        for (GridBasedGrowthFunction* f : active) {
+            int ix = 0, iy = 0;
+            double fx = 1.0, fy = 1.0;
+            if (g.pinned) el->getInitialRelativePositionInTissueInGridIndex(f->getGridX(), f->getGridY(), ix, iy, fx, fy);
+            else el->getRelativePositionInTissueInGridIndex(f->getGridX(), f->getGridY(), ix, iy, fx, fy);
+            gsl_matrix_set_identity(inc);
+            gsl_matrix_set_identity(peri);
+            el->calculateFgFromGridCorners(g.interp, dt, f, inc, 0, ix, iy, fx, fy);
+            el->updateGrowthIncrement(inc, peri);
+        }
+        el->growShapeByFg();
+    }
+    gsl_matrix_free(rot);
+    gsl_matrix_free(inc);
+    gsl_matrix_free(peri);
+}
+
 }  // namespace
 
 extern "C" {
@@ -400,29 +518,10 @@ void tfr_get_positions(void* h, double* pos) {
         for (int d = 0; d < 3; ++d) pos[3 * i + d] = s->nodes[i]->Position[d];
 }
 
-// Per-element growth for one step from per-element rates (1/s), as a single
-// uniform-type growth function applied with the identity rotation.
-void tfr_grow(void* h, double dt, const double* rates) {
-    QuietCout q;
-    RefSim* s = static_cast<RefSim*>(h);
-    gsl_matrix* rot = gsl_matrix_alloc(3, 3);
-    gsl_matrix* inc = gsl_matrix_alloc(3, 3);
-    gsl_matrix* peri = gsl_matrix_alloc(3, 3);
-    gsl_matrix_set_identity(rot);
-    for (int e = 0; e < s->nElems; ++e) {
-        ShapeBase* el = s->elements[e];
-        el->setGrowthRate(dt, 0.0, 0.0, 0.0);
-        el->updateGrowthIncrementFromRate();
-        gsl_matrix_set_identity(inc);
-        gsl_matrix_set_identity(peri);
-        el->calculateFgFromRates(dt, rates[3 * e], rates[3 * e + 1], rates[3 * e + 2], rot, inc, 0, 0.0, 1.0);
-        el->updateGrowthIncrement(inc, peri);
-        el->growShapeByFg();
-    }
-    gsl_matrix_free(rot);
-    gsl_matrix_free(inc);
-    gsl_matrix_free(peri);
-}
+// The growth of one step: per-element rates (1/s) as a single uniform-type
+// growth function with the identity rotation, then the grid functions active
+// at the current time.
+void tfr_grow(void* h, double dt, const double* rates) { refGrow(static_cast<RefSim*>(h), dt, rates, true); }
 
 void tfr_update_viscosity_surfaces(void* h, double* area_out) {
     RefSim* s = static_cast<RefSim*>(h);
@@ -537,7 +636,7 @@ int tfr_step(void* h, double dt, const double* rates, int* iters, double* dunorm
     RefSim* s = static_cast<RefSim*>(h);
     if (rates) {
         tfr_grow(h, dt, rates);
-    } else if (s->pk.on) {
+    } else if (s->pk.on || !s->grid.fns.empty()) {
         // runOneStep calls growShapeByFg on every element at every step
         // (Simulation.cpp:5901-5906), which sets the volumes the node masses
         // are made of (the Prism constructor leaves them 0, Prism.cpp:218)
@@ -588,6 +687,7 @@ int tfr_step(void* h, double dt, const double* rates, int* iters, double* dunorm
     copyUkToPositions(s);
     std::cerr.rdbuf(oldErr);
     *iters = iteratorK;
+    s->grid.time += dt;  // runOneStep: currSimTimeSec += dt (Simulation.cpp:5969)
     return notConverged;
 }
 
@@ -605,7 +705,7 @@ void tfr_set_packing(void* h, int on, int drop_last_segment) {
 void tfr_pack_detect(void* h) {
     RefSim* s = static_cast<RefSim*>(h);
     std::vector<double> zero(3 * (size_t)s->nElems, 0.0);
-    tfr_grow(h, 1.0, zero.data());
+    refGrow(s, 1.0, zero.data(), false);
     QuietCout q;
     refPackingStepStart(s);
 }
@@ -642,6 +742,81 @@ void tfr_node_masses(void* h, double* mass) {
 void tfr_pack_forces(void* h, double* f) {
     RefSim* s = static_cast<RefSim*>(h);
     std::copy(s->pk.force.begin(), s->pk.force.end(), f);
+}
+
+// A GridBasedGrowthFunction over the columnar layer: rates[3*(i*ny + j) + k]
+// (1/s), angles_deg[i*ny + j] (NULL: 0), its time window and z range.
+void tfr_add_grid_growth(void* h, int nx, int ny, const double* rates, const double* angles_deg, double t0,
+                         double t1, double zmin, double zmax) {
+    RefSim* s = static_cast<RefSim*>(h);
+    QuietCout q;
+    if (!s->grid.setUp) refGridSetup(s);
+    double*** G = new double**[nx];
+    double** A = new double*[nx];
+    for (int i = 0; i < nx; ++i) {
+        G[i] = new double*[ny];
+        A[i] = new double[ny];
+        for (int j = 0; j < ny; ++j) {
+            G[i][j] = new double[3];
+            for (int k = 0; k < 3; ++k) G[i][j][k] = rates[3 * ((size_t)i * ny + j) + k];
+            A[i][j] = angles_deg ? angles_deg[(size_t)i * ny + j] : 0.0;
+        }
+    }
+    GridBasedGrowthFunction* f = new GridBasedGrowthFunction(static_cast<int>(s->grid.fns.size()), 3, t0, t1, true,
+                                                             false, false, false, nx, ny, G, A);
+    f->zMin = zmin;
+    f->zMax = zmax;
+    s->grid.fns.push_back(f);
+    for (int i = 0; i < nx; ++i) {
+        for (int j = 0; j < ny; ++j) delete[] G[i][j];
+        delete[] G[i];
+        delete[] A[i];
+    }
+    delete[] G;
+    delete[] A;
+}
+
+void tfr_set_grid_mode(void* h, int interp, int pinned) {
+    RefSim* s = static_cast<RefSim*>(h);
+    s->grid.interp = interp;
+    s->grid.pinned = pinned != 0;
+}
+
+// Simulation::updatePinningPositions (Simulation.cpp:6018-6023) at the
+// current shape.
+void tfr_repin_grid_growth(void* h) {
+    RefSim* s = static_cast<RefSim*>(h);
+    QuietCout q;
+    refBoundingBox(s);
+    refApicalPositioning(s);
+    for (ShapeBase* e : s->elements) e->setInitialRelativePosInBoundingBox();
+}
+
+void tfr_set_time(void* h, double t) { static_cast<RefSim*>(h)->grid.time = t; }
+double tfr_get_time(void* h) { return static_cast<RefSim*>(h)->grid.time; }
+
+// Initial relative z, pinned positions and the current shape's positions
+// ([2][n_elems] each, x block then y block).
+void tfr_grid_positions(void* h, double* relz, double* rel0, double* rel) {
+    RefSim* s = static_cast<RefSim*>(h);
+    QuietCout q;
+    refBoundingBox(s);
+    refApicalPositioning(s);
+    const int ne = s->nElems;
+    for (int e = 0; e < ne; ++e) {
+        double r[2], r0[2];
+        s->elements[e]->getRelativePosInBoundingBox(r);
+        s->elements[e]->getInitialRelativePosInBoundingBox(r0);
+        if (relz) relz[e] = static_cast<PrismRef*>(s->elements[e])->relZ();
+        if (rel0) {
+            rel0[e] = r0[0];
+            rel0[ne + e] = r0[1];
+        }
+        if (rel) {
+            rel[e] = r[0];
+            rel[ne + e] = r[1];
+        }
+    }
 }
 
 }  // extern "C"

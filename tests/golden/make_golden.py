@@ -4,7 +4,7 @@ Run where the reference checkout is present (it builds oracle/_ref from the
 reference's own sources with the project-written GSL/uBLAS/Pardiso
 stand-ins):
 
-    python tests/golden/make_golden.py [--only-bound | --only-packing]
+    python tests/golden/make_golden.py [--only-bound | --only-packing | --only-grid]
 
 Every fixture records the seeded inputs that produced it, so tests rebuild
 the same inputs with tissuefolding_paperversion_gb300.mesh and compare.
@@ -21,6 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
+from oracle import growth as og  # noqa: E402
 from oracle.oracle import Ref  # noqa: E402
 from tissuefolding_paperversion_gb300 import mesh  # noqa: E402
 
@@ -141,7 +142,48 @@ def packing_fixtures():
                           "config_facing_sheets(seed=13, gap=1.5, E=1e5, eta=100), packing on, every segment kept")
 
 
+def grid_growth_fixture(name, n_steps):
+    """Bounding-box positions and one growth update at the initial shape,
+    then Newton steps with the grid functions and the per-element rates."""
+    t, fns, interp, pinned = og.fixture_case(name)
+    r = Ref(t)
+    for f in fns:
+        r.add_grid_growth(**f)
+    r.set_grid_mode(interp, pinned)
+    relz, rel0, rel = r.grid_positions()
+    r.grow(t.dt, t.rates)
+    Fg_grow = r.get_Fg()[0]
+    r.close()
+    r = Ref(t)
+    for f in fns:
+        r.add_grid_growth(**f)
+    r.set_grid_mode(interp, pinned)
+    pos, iters, Fg = [], [], []
+    for _ in range(n_steps):
+        out = r.step(t.dt, t.rates)
+        pos.append(r.positions())
+        iters.append(out["iters"])
+        Fg.append(r.get_Fg()[0])
+    r.close()
+    extra = {}
+    for i, f in enumerate(fns):
+        extra[f"fn{i}_rates"] = f["rates"]
+        extra[f"fn{i}_angles"] = f["angles_deg"]
+        extra[f"fn{i}_window"] = np.array([f["init_time"], f["end_time"], f["zmin"], f["zmax"]])
+    np.savez_compressed(os.path.join(HERE, f"{name}.npz"), relz=relz, rel0=rel0, rel=rel, Fg_grow=Fg_grow,
+                        positions=np.array(pos), iters=np.array(iters), Fg=np.array(Fg), interp=interp,
+                        pinned=pinned, n_fns=len(fns), note=og.fixture_case.__doc__, **extra)
+
+
+def grid_fixtures():
+    for name in og.FIXTURES:
+        grid_growth_fixture(name, 3)
+
+
 def main():
+    if "--only-grid" in sys.argv:
+        grid_fixtures()
+        return
     if "--only-packing" in sys.argv:
         packing_fixtures()
         return
@@ -160,6 +202,7 @@ def main():
     t = mesh.config_tiny(seed=15, n=5, n_layers=2, eta=100.0)
     bound_steps_fixture("steps_tiny_bound", t, 4, "config_tiny(seed=15,n=5,n_layers=2,eta=100), bound_dofs(t)")
     packing_fixtures()
+    grid_fixtures()
 
 
 if __name__ == "__main__":

@@ -1,0 +1,180 @@
+"""Grid-based growth functions on the GPU (tf_add_grid_growth) against
+fixtures the reference's own GridBasedGrowthFunction and
+ShapeBase::calculateFgFromGridCorners produced (tests/golden/make_golden.py
+--only-grid) and against the restatement in oracle/growth.py: bounding-box
+positions bit for bit (the reference's box included), the growth update,
+Newton steps with the grid functions on, the time window, re-pinning, and
+larger sheets where the device box must replay the reference's running
+minimum over 100,000+ nodes."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import growth as G
+from tissuefolding_paperversion_gb300 import api, mesh
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+TOL_POS = 1e-8      # positions after Newton steps, relative to the largest coordinate
+TOL_FG = 1e-14      # growth tensors after one update (FMA contraction on the device)
+
+
+def _solver(t, fns, interp, pinned, **kw):
+    s = api.Solver(t, **kw)
+    for f in fns:
+        s.add_grid_growth(**f)
+    s.set_grid_growth_mode(interp, pinned)
+    return s
+
+
+@pytest.mark.parametrize("name", G.FIXTURES)
+def test_positions_match_the_reference_bit_for_bit(name):
+    f = np.load(os.path.join(GOLD, name + ".npz"))
+    t, fns, interp, pinned = G.fixture_case(name)
+    with _solver(t, fns, interp, pinned) as s:
+        relz, rel0, rel = s.grid_growth_positions()
+    np.testing.assert_array_equal(relz, f["relz"])
+    np.testing.assert_array_equal(rel0, f["rel0"])
+    np.testing.assert_array_equal(rel, f["rel"])
+
+
+@pytest.mark.parametrize("name", G.FIXTURES)
+def test_growth_update_matches_the_reference(name):
+    f = np.load(os.path.join(GOLD, name + ".npz"))
+    t, fns, interp, pinned = G.fixture_case(name)
+    with _solver(t, fns, interp, pinned) as s:
+        s.set_growth_rates(t.rates)
+        s.begin_step(t.dt)
+        Fg, invFg = s.get_Fg()
+    assert np.abs(Fg - f["Fg_grow"]).max() <= TOL_FG
+    inv = np.linalg.inv(Fg.reshape(-1, 3, 3))
+    assert np.abs(invFg.reshape(-1, 3, 3) - inv).max() <= 1e-13
+
+
+@pytest.mark.parametrize("name", G.FIXTURES)
+def test_newton_steps_match_the_reference(name):
+    f = np.load(os.path.join(GOLD, name + ".npz"))
+    t, fns, interp, pinned = G.fixture_case(name)
+    with _solver(t, fns, interp, pinned) as s:
+        s.set_growth_rates(t.rates)
+        for k in range(f["positions"].shape[0]):
+            out = s.newton_step(t.dt, allow_not_converged=False)
+            ref = f["positions"][k]
+            pos = s.positions()
+            assert np.abs(pos - ref).max() <= TOL_POS * np.abs(ref).max(), (k, np.abs(pos - ref).max())
+            assert out["iters"] == f["iters"][k], (k, out["iters"])
+            Fg, _ = s.get_Fg()
+            assert np.abs(Fg - f["Fg"][k]).max() <= 1e-12, k
+        assert s.time == pytest.approx(t.dt * f["positions"].shape[0])
+
+
+def _big_sheet(node0_max):
+    """A 120 x 120-cell, 4-layer sheet (about 72,600 nodes, 115,200 prisms)."""
+    rng = np.random.default_rng(5)
+    pos, conn, pl = mesh.rect_sheet(121, 121, 5.0, 4, 20.0, 0.5, rng)
+    ne = conn.size // 6
+    t = mesh.Tissue(pos=pos, conn=conn, fixed=np.zeros(pos.size, dtype=np.uint8), ext_visc=np.full(pos.size, 10.0),
+                    node_placement=pl, E=np.full(ne, 1000.0), nu=np.full(ne, 0.3), eta=np.zeros(ne),
+                    rates=np.zeros(3 * ne))
+    if node0_max:
+        t = mesh.swap_nodes(t, 0, int(np.argmax(t.pos.reshape(-1, 3)[:, 0])))
+        t.pos[0] += 0.3
+    return t
+
+
+@pytest.mark.parametrize("node0_max", [False, True])
+def test_device_box_replays_the_reference_on_a_large_sheet(node0_max):
+    t = _big_sheet(node0_max)
+    rates, ang = mesh.grid_growth_inputs(7, 9, 7)
+    moved = t.pos + np.random.default_rng(8).uniform(-0.2, 0.2, size=t.pos.shape)
+    o = G.GridGrowthOracle(t.pos, t.conn, t.node_placement)
+    with _solver(t, [dict(rates=rates, angles_deg=ang)], 1, False) as s:
+        relz, rel0, rel = s.grid_growth_positions()
+        np.testing.assert_array_equal(relz, o.state["relz"])
+        np.testing.assert_array_equal(rel0, o.state["rel0"])
+        np.testing.assert_array_equal(rel, G.relative_positions(t.pos, t.conn, o.state["src"]))
+        s.set_positions(moved)
+        _, _, rel = s.grid_growth_positions()
+        np.testing.assert_array_equal(rel, G.relative_positions(moved, t.conn, o.state["src"]))
+        # one growth update at the moved shape against the oracle
+        s.begin_step(60.0)
+        Fg, _ = s.get_Fg()
+    o.add(rates, ang)
+    ref = o.grow(np.broadcast_to(np.eye(3), (t.n_elems, 3, 3)), moved, 0.0, 60.0)
+    assert np.abs(Fg.reshape(-1, 3, 3) - ref).max() <= TOL_FG
+
+
+def test_uniform_isotropic_grid_equals_per_element_rates():
+    """A grid whose points all carry the same isotropic rates grows every
+    prism as the same per-element rates do (no angle: aspect ratio 1)."""
+    t = _big_sheet(False)
+    r = np.array([2e-5, 2e-5, -5e-6])
+    grid = np.broadcast_to(r, (6, 5, 3)).copy()
+    with _solver(t, [dict(rates=grid, angles_deg=np.full((6, 5), 37.0))], 1, False) as s:
+        s.begin_step(60.0)
+        Fa, _ = s.get_Fg()
+    with api.Solver(t) as s:
+        s.set_growth_rates(np.tile(r, t.n_elems))
+        s.begin_step(60.0)
+        Fb, _ = s.get_Fg()
+    assert np.abs(Fa - Fb).max() <= 1e-15
+
+
+def test_time_window_clear_and_set_time():
+    t = mesh.config_tiny(seed=30, n=5, n_layers=3)
+    rates, ang = mesh.grid_growth_inputs(9, 4, 3)
+    eye = np.tile(np.eye(3).reshape(-1), t.n_elems)
+    with _solver(t, [dict(rates=rates, angles_deg=ang, init_time=120.0, end_time=180.0)], 1, False) as s:
+        s.begin_step(60.0)                       # t = 0: before the window
+        assert np.array_equal(s.get_Fg()[0], eye)
+        s.end_step()
+        assert s.time == 60.0
+        s.time = 120.0
+        s.begin_step(60.0)                       # t = 120: inside
+        F1 = s.get_Fg()[0]
+        assert np.abs(F1 - eye).max() > 1e-4
+        s.end_step()
+        s.begin_step(60.0)                       # t = 180: end of the window is excluded
+        assert np.array_equal(s.get_Fg()[0], F1)
+        s.end_step()
+        s.time = 150.0
+        s.clear_grid_growth()
+        s.begin_step(60.0)
+        assert np.array_equal(s.get_Fg()[0], F1)
+
+
+def test_repin_takes_the_current_shape():
+    t = mesh.config_tiny(seed=31, n=5, n_layers=3)
+    rates, ang = mesh.grid_growth_inputs(10, 4, 4)
+    moved = t.pos + np.random.default_rng(2).uniform(-0.5, 0.5, size=t.pos.shape)
+    o = G.GridGrowthOracle(t.pos, t.conn, t.node_placement)
+    with _solver(t, [dict(rates=rates, angles_deg=ang)], 0, True) as s:
+        s.set_positions(moved)
+        s.repin_grid_growth()
+        _, rel0, rel = s.grid_growth_positions()
+    o.repin(moved)
+    np.testing.assert_array_equal(rel0, o.state["rel0"])
+    np.testing.assert_array_equal(rel0, rel)
+
+
+def test_refusals():
+    t = mesh.config_tiny(seed=32, n=4, n_layers=2)
+    rates, ang = mesh.grid_growth_inputs(11, 3, 3)
+    with api.Solver(t) as s:
+        with pytest.raises(api.TfError):
+            s.set_grid_growth_mode(1, False)                      # nothing added yet
+        with pytest.raises(api.TfError):
+            s.add_grid_growth(rates[:1])                          # a 1 x 3 grid
+        bad = rates.copy()
+        bad[1, 1, 0] = np.nan
+        with pytest.raises(api.TfError):
+            s.add_grid_growth(bad)
+        s.add_grid_growth(rates, ang)
+        with pytest.raises(api.TfError):
+            s.set_grid_growth_mode(2, False)
+        with pytest.raises(api.TfError):
+            s.adjoint_forward(np.zeros(t.n_elems), np.zeros(t.n_elems), 1, 60.0, 1, np.array([0, 0, 0, 1.0]))
+    with api.Batch([t, mesh.config_tiny(seed=33, n=4, n_layers=2)]) as b:
+        with pytest.raises(api.TfError):
+            b.add_grid_growth(rates, ang)

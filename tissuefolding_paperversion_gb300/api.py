@@ -32,7 +32,8 @@ EXPORTED = [
     "tf_solve_bsr_static", "tf_batch_create", "tf_batch_step", "tf_get_instances", "tf_elements_per_cta",
     "tf_adj_forward", "tf_adj_backward", "tf_adj_free", "tf_multigrid_info", "tf_read_mesh_file",
     "tf_write_frame", "tf_add_K_triplets", "tf_set_dof_bindings", "tf_set_packing", "tf_get_packing",
-    "tf_packing_masses",
+    "tf_packing_masses", "tf_add_grid_growth", "tf_clear_grid_growth", "tf_set_grid_growth_mode",
+    "tf_repin_grid_growth", "tf_grid_growth_positions", "tf_set_time", "tf_get_time",
 ]
 
 
@@ -140,6 +141,20 @@ def load(build_if_missing: bool = True):
                                  C.POINTER(C.c_double)]
     L.tf_packing_masses.restype = C.c_int
     L.tf_packing_masses.argtypes = [vp, vp]
+    L.tf_add_grid_growth.restype = C.c_int
+    L.tf_add_grid_growth.argtypes = [vp, i32, i32, vp, vp, C.c_double, C.c_double, C.c_double, C.c_double]
+    L.tf_clear_grid_growth.restype = C.c_int
+    L.tf_clear_grid_growth.argtypes = [vp]
+    L.tf_set_grid_growth_mode.restype = C.c_int
+    L.tf_set_grid_growth_mode.argtypes = [vp, i32, i32]
+    L.tf_repin_grid_growth.restype = C.c_int
+    L.tf_repin_grid_growth.argtypes = [vp]
+    L.tf_grid_growth_positions.restype = C.c_int
+    L.tf_grid_growth_positions.argtypes = [vp, vp, vp, vp]
+    L.tf_set_time.restype = C.c_int
+    L.tf_set_time.argtypes = [vp, C.c_double]
+    L.tf_get_time.restype = C.c_int
+    L.tf_get_time.argtypes = [vp, C.POINTER(C.c_double)]
     L.tf_read_mesh_file.restype = C.c_int
     L.tf_read_mesh_file.argtypes = [C.c_char_p, ip, ip, vp, vp, vp, vp, vp, vp]
     L.tf_write_frame.restype = C.c_int
@@ -303,6 +318,50 @@ class Solver:
         m = np.zeros(self.nn)
         self._check(self.L.tf_packing_masses(self.h, _ptr(m)), "tf_packing_masses")
         return m
+
+    def add_grid_growth(self, rates, angles_deg=None, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0):
+        """Grid-based growth function (growth type 3): rates (nx, ny, 3) in
+        1/s at the grid points over the tissue's bounding box, angles_deg
+        (nx, ny) their xy orientation; active for init_time <= t < end_time
+        on prisms whose initial relative z is within [zmin, zmax]."""
+        r = np.ascontiguousarray(rates, dtype=np.float64)
+        if r.ndim != 3 or r.shape[2] != 3:
+            raise ValueError("rates must have shape (nx, ny, 3)")
+        a = None if angles_deg is None else np.ascontiguousarray(angles_deg, dtype=np.float64)
+        if a is not None and a.shape != r.shape[:2]:
+            raise ValueError("angles_deg must have shape (nx, ny)")
+        self._check(self.L.tf_add_grid_growth(self.h, r.shape[0], r.shape[1], _ptr(r), _ptr(a) if a is not None
+                                              else None, init_time, end_time, zmin, zmax), "tf_add_grid_growth")
+
+    def clear_grid_growth(self):
+        self._check(self.L.tf_clear_grid_growth(self.h), "tf_clear_grid_growth")
+
+    def set_grid_growth_mode(self, interpolation=1, pinned_on_initial_mesh=False):
+        """interpolation 0: nearest grid point, 1: bilinear (the default);
+        pinned: positions of the initial mesh instead of each step's start."""
+        self._check(self.L.tf_set_grid_growth_mode(self.h, int(interpolation), 1 if pinned_on_initial_mesh else 0),
+                    "tf_set_grid_growth_mode")
+
+    def repin_grid_growth(self):
+        self._check(self.L.tf_repin_grid_growth(self.h), "tf_repin_grid_growth")
+
+    def grid_growth_positions(self):
+        """(relz (ne,), pinned (ne, 2), current (ne, 2)) bounding-box positions."""
+        z = np.zeros(self.ne)
+        p0 = np.zeros(2 * self.ne)
+        p = np.zeros(2 * self.ne)
+        self._check(self.L.tf_grid_growth_positions(self.h, _ptr(z), _ptr(p0), _ptr(p)), "tf_grid_growth_positions")
+        return z, p0.reshape(2, -1).T.copy(), p.reshape(2, -1).T.copy()
+
+    @property
+    def time(self):
+        t = C.c_double(0.0)
+        self._check(self.L.tf_get_time(self.h, C.byref(t)), "tf_get_time")
+        return t.value
+
+    @time.setter
+    def time(self, value):
+        self._check(self.L.tf_set_time(self.h, float(value)), "tf_set_time")
 
     def add_K_triplets(self, rows, cols, vals):
         """K(rows[k], cols[k]) += vals[k] after assemble() (packing/myosin-type writers)."""

@@ -123,6 +123,10 @@ void free_all(tf_handle* h) {
         packing_free(h->pk);
         h->pk = nullptr;
     }
+    if (h->growth) {
+        growth_free(h->growth);
+        h->growth = nullptr;
+    }
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (d.host_scal) cudaFreeHost(d.host_scal);
@@ -261,6 +265,7 @@ tf_status build(tf_handle* h, const tf_mesh* m, const tf_material* mat, const st
     h->h_apical.resize(nn);
     for (int i = 0; i < nn; ++i) h->h_apical[i] = m->node_placement[i] == 1 ? 1 : 0;
     h->h_place.assign(m->node_placement, m->node_placement + nn);
+    h->h_pos0.assign(m->node_pos, m->node_pos + 3 * (size_t)nn);
     for (int e = 0; e < ne; ++e) {
         double v = mat->nu[e];
         if (v > 0.5) v = 0.5;
@@ -963,6 +968,80 @@ tf_status tf_packing_masses(tf_handle* h, double* mass) {
     return packing_masses(h, mass);
 }
 
+tf_status tf_add_grid_growth(tf_handle* h, int32_t nx, int32_t ny, const double* rates, const double* angles_deg,
+                             double init_time, double end_time, double zmin, double zmax) {
+    TF_TRY(check_handle(h));
+    if (h->d.nseg != 1) return set_error("tf_add_grid_growth: grid growth works on single-mesh handles"), TF_BAD_INPUT;
+    if (nx < 2 || ny < 2 || !rates || (int64_t)nx * ny > (1 << 24))
+        return set_error("tf_add_grid_growth: needs a grid of at least 2 x 2 points and its rates"), TF_BAD_INPUT;
+    for (int64_t k = 0; k < 3 * (int64_t)nx * ny; ++k)
+        if (!std::isfinite(rates[k])) return set_error("tf_add_grid_growth: non-finite rate"), TF_BAD_INPUT;
+    if (angles_deg)
+        for (int64_t k = 0; k < (int64_t)nx * ny; ++k)
+            if (!std::isfinite(angles_deg[k])) return set_error("tf_add_grid_growth: non-finite angle"), TF_BAD_INPUT;
+    if (std::isnan(init_time) || std::isnan(end_time) || !std::isfinite(zmin) || !std::isfinite(zmax))
+        return set_error("tf_add_grid_growth: bad time window or z range"), TF_BAD_INPUT;
+    TF_CUDA(cudaSetDevice(h->device));
+    TF_CUDA(cudaStreamSynchronize(h->stream));
+    if (growth_grid_count(h) >= kMaxGridGrowthFunctions)
+        return set_error("tf_add_grid_growth: at most 8 grid growth functions per handle"), TF_BAD_INPUT;
+    if (!h->growth) {
+        const tf_status s = growth_setup(h);
+        if (s != TF_OK) {
+            growth_free(h->growth);
+            h->growth = nullptr;
+            return s;
+        }
+    }
+    return growth_add_grid(h, nx, ny, rates, angles_deg, init_time, end_time, zmin, zmax);
+}
+
+tf_status tf_clear_grid_growth(tf_handle* h) {
+    TF_TRY(check_handle(h));
+    TF_CUDA(cudaSetDevice(h->device));
+    TF_CUDA(cudaStreamSynchronize(h->stream));
+    growth_clear_grids(h);
+    return TF_OK;
+}
+
+tf_status tf_set_grid_growth_mode(tf_handle* h, int32_t interpolation, int32_t pinned_on_initial_mesh) {
+    TF_TRY(check_handle(h));
+    if ((interpolation != 0 && interpolation != 1) || (pinned_on_initial_mesh != 0 && pinned_on_initial_mesh != 1))
+        return set_error("tf_set_grid_growth_mode: interpolation and pinning are 0 or 1"), TF_BAD_INPUT;
+    if (!h->growth) return set_error("tf_set_grid_growth_mode: no grid growth function added"), TF_BAD_INPUT;
+    growth_set_mode(h, interpolation, pinned_on_initial_mesh);
+    return TF_OK;
+}
+
+tf_status tf_repin_grid_growth(tf_handle* h) {
+    TF_TRY(check_handle(h));
+    if (!h->growth) return set_error("tf_repin_grid_growth: no grid growth function added"), TF_BAD_INPUT;
+    TF_CUDA(cudaSetDevice(h->device));
+    TF_TRY(growth_repin(h));
+    return sync(h);
+}
+
+tf_status tf_grid_growth_positions(tf_handle* h, double* rel_z, double* rel_pinned, double* rel_current) {
+    TF_TRY(check_handle(h));
+    if (!h->growth) return set_error("tf_grid_growth_positions: no grid growth function added"), TF_BAD_INPUT;
+    TF_CUDA(cudaSetDevice(h->device));
+    return growth_positions(h, rel_z, rel_pinned, rel_current);
+}
+
+tf_status tf_set_time(tf_handle* h, double time_sec) {
+    TF_TRY(check_handle(h));
+    if (std::isnan(time_sec)) return set_error("tf_set_time: NaN time"), TF_BAD_INPUT;
+    h->time = time_sec;
+    return TF_OK;
+}
+
+tf_status tf_get_time(tf_handle* h, double* time_sec) {
+    TF_TRY(check_handle(h));
+    if (!time_sec) return set_error("tf_get_time: null output"), TF_BAD_INPUT;
+    *time_sec = h->time;
+    return TF_OK;
+}
+
 tf_status tf_set_dof_bindings(tf_handle* h, int32_t n, const int32_t* slave_dofs, const int32_t* master_dofs) {
     TF_TRY(check_handle(h));
     if (n < 0 || (n > 0 && (!slave_dofs || !master_dofs))) return set_error("tf_set_dof_bindings: bad arguments"), TF_BAD_INPUT;
@@ -1250,7 +1329,12 @@ tf_status tf_begin_step(tf_handle* h, double dt) {
     if (!(dt > 0.0) || !std::isfinite(dt)) return set_error("dt must be positive"), TF_BAD_INPUT;
     h->dt = dt;
     amg_mark_stale(h, 2);  // a new time step: rebuild the multigrid hierarchy at its first solve
-    if (h->have_rates) TF_TRY(launch_growth(h));
+    // calculateGrowth (Simulation.cpp:9651-9666): the per-element rates, then
+    // the grid functions active at this time, in one increment per prism
+    bool grown = false;
+    TF_TRY(launch_grid_growth(h, &grown));
+    if (!grown && h->have_rates) TF_TRY(launch_growth(h));
+    h->in_step = true;
     TF_TRY(launch_viscosity_surfaces(h));
     TF_CUDA(cudaMemcpyAsync(h->d.un, h->d.uk, sizeof(double) * 3 * (size_t)h->d.nn, cudaMemcpyDeviceToDevice,
                             h->stream));
@@ -1338,6 +1422,8 @@ tf_status tf_update(tf_handle* h, int32_t* converged, double* dunorm) {
 
 tf_status tf_end_step(tf_handle* h) {
     TF_TRY(check_handle(h));
+    if (h->in_step) h->time += h->dt;  // runOneStep: currSimTimeSec += dt (Simulation.cpp:5969)
+    h->in_step = false;
     return sync(h);
 }
 

@@ -96,23 +96,6 @@ __global__ void k_gather_forces(int nn, int ne, const int* __restrict__ fptr, co
     }
 }
 
-__device__ __forceinline__ void inv3_cof(const double* M, double* inv) {
-    const double c0 = M[4] * M[8] - M[5] * M[7];
-    const double c1 = M[5] * M[6] - M[3] * M[8];
-    const double c2 = M[3] * M[7] - M[4] * M[6];
-    const double det = M[0] * c0 + M[1] * c1 + M[2] * c2;
-    const double r = 1.0 / det;
-    inv[0] = c0 * r;
-    inv[1] = (M[2] * M[7] - M[1] * M[8]) * r;
-    inv[2] = (M[1] * M[5] - M[2] * M[4]) * r;
-    inv[3] = c1 * r;
-    inv[4] = (M[0] * M[8] - M[2] * M[6]) * r;
-    inv[5] = (M[2] * M[3] - M[0] * M[5]) * r;
-    inv[6] = c2 * r;
-    inv[7] = (M[1] * M[6] - M[0] * M[7]) * r;
-    inv[8] = (M[0] * M[4] - M[1] * M[3]) * r;
-}
-
 __global__ void k_growth(int ne, double dt, const double* __restrict__ rates, double* __restrict__ Fg,
                          double* __restrict__ invFg) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;

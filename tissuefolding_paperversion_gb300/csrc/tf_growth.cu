@@ -1,0 +1,626 @@
+// Grid-based growth functions on the device: the reference's growth type 3
+// (GridBasedGrowthFunction, GrowthFunctionTypes.h:266-609), applied every
+// step by Simulation::calculateGrowthGridBased (Simulation.cpp:10065-10114)
+// through ShapeBase::calculateFgFromGridCorners (ShapeBase.cpp:432-562).
+//
+// A function holds an nx x ny grid of growth rates (x, y, z; 1/s) and xy
+// angles (degrees).  Once, on the host (the GridBasedGrowthFunction
+// constructor and preCalculateAnglesForCompatibleAveraging): grid points whose
+// in-plane aspect ratio |rx/ry| (or its inverse) is below 1.1 carry no angle;
+// in each grid cell the angles of the 4 corners are brought to [0, pi] and
+// next to the first corner that carries one, a corner turned by about 90 (or
+// 270) degrees from it swapping its x and y rates.  Every step, per prism in
+// the function's time window whose initial relative z is within [zmin, zmax]:
+// its position in the tissue's bounding box -- pinned on the initial mesh or
+// the current one -- gives a cell and fractions
+// (ShapeBase::convertRelativePosToGridIndex, ShapeBase.cpp:633-660); the rates
+// are the nearest corner's (interpolation 0) or the bilinear mean of the 4
+// (interpolation 1, the angle averaged over the corners that carry one); the
+// increment diag(exp(rate dt)), turned by that angle about z, multiplies Fg
+// from the left after the per-element rates' increment
+// (ShapeBase::updateGrowthIncrement :567-586, growShapeByFg :1215-1251).
+//
+// Bounding-box positions (Simulation.cpp:5833-5843, 630-645): prism centres
+// relative to the nodes' box (Simulation::calculateBoundingBox :9148-9185,
+// whose running "else if" never tests a node that lowers the minimum for the
+// maximum -- reproduced exactly); the prisms of a column take the apical
+// prism's position except the two top ones
+// (Simulation::updateRelativePositionsToApicalPositioning :5987-6003, columns
+// of Prism::constructElementStackList, Prism.cpp:2542-2584).
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <map>
+#include <vector>
+
+#include "tf_internal.cuh"
+
+namespace tf {
+
+namespace {
+
+constexpr int kT = 256;
+constexpr int kBoxThreads = 1024;        // k_box: one CTA, 32 warps
+constexpr int kMaxGridFns = kMaxGridGrowthFunctions;
+constexpr double kBoxInit = 100000.0;    // calculateBoundingBox's starting corners (+-1e5)
+constexpr double kPi = 3.14159265358979323846;
+
+#define GR_TRY(expr)                \
+    do {                            \
+        tf_status _s = (expr);      \
+        if (_s != TF_OK) return _s; \
+    } while (0)
+
+template <class T>
+tf_status put(T** p, const std::vector<T>& v) {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), std::max<size_t>(v.size(), 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        set_error("device allocation failed for a growth function");
+        return TF_OUT_OF_MEMORY;
+    }
+    if (!v.empty()) TF_CUDA(cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return TF_OK;
+}
+
+}  // namespace
+
+struct GridGrowth {
+    int nx = 0, ny = 0;
+    double t0 = 0, t1 = 0, zmin = 0, zmax = 1;
+    double* cg = nullptr;    // [(nx-1)*(ny-1)][4][3] compatible corner rates
+    double* ca = nullptr;    // [(nx-1)*(ny-1)][4] compatible corner angles (rad)
+    uint8_t* ce = nullptr;   // [(nx-1)*(ny-1)][4] 1: the corner carries no angle
+};
+
+struct Growth {
+    std::vector<GridGrowth> grids;
+    int interp = 1;           // gridGrowthsInterpolationType (Simulation.cpp:146)
+    int pinned = 0;           // GridGrowthsPinnedOnInitialMesh (Simulation.cpp:144)
+    int layers = 0;           // TissueHeightDiscretisationLayers
+    double height = 0;        // TissueHeight
+    double* relz = nullptr;   // [ne] initial relative z (0 apical, 1 basal)
+    double* rel0 = nullptr;   // [2][ne] pinned bounding-box positions
+    double* rel = nullptr;    // [2][ne] positions at the current step's start
+    int* colsrc = nullptr;    // [ne] the prism whose position a prism takes
+    double* box = nullptr;    // [4] min x, min y, size x, size y
+};
+
+namespace {
+
+void free_grid(GridGrowth& f) {
+    cudaFree(f.cg);
+    cudaFree(f.ca);
+    cudaFree(f.ce);
+    f.cg = f.ca = nullptr;
+    f.ce = nullptr;
+}
+
+// ShapeBase::setTissuePlacement (ShapeBase.cpp:705-770): 3 lateral, 1 apical,
+// 0 basal, 2 mid-line or spanning the tissue.
+int element_placement(const tf_handle* h, int e) {
+    bool ap = false, ba = false, la = false;
+    for (int a = 0; a < 6; ++a) {
+        const int p = h->h_place[h->h_conn[6 * (size_t)e + a]];
+        if (p == 1) ap = true;
+        else if (p == 0) ba = true;
+        else if (p == 3) la = true;
+    }
+    if (la) return 3;
+    if (ap) return ba ? 2 : 1;
+    return ba ? 0 : 2;
+}
+
+// Simulation::calculateBoundingBox over every node, no y symmetry.
+void host_box(const double* pos, int nn, double lo[3], double size[3]) {
+    double hi[3];
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = kBoxInit;
+        hi[k] = -kBoxInit;
+    }
+    for (int i = 0; i < nn; ++i)
+        for (int k = 0; k < 3; ++k) {
+            const double p = pos[3 * (size_t)i + k];
+            if (p < lo[k]) lo[k] = p;
+            else if (p > hi[k]) hi[k] = p;
+        }
+    for (int k = 0; k < 3; ++k) size[k] = hi[k] - lo[k];
+}
+
+// Simulation::calculateTissueHeight (Simulation.cpp:3280-3330) for a
+// columnar tissue: from the first basal node, prism by prism up to an apical
+// node, summing Prism::getElementHeight (Prism.cpp:1526-1531).
+void tissue_height(const tf_handle* h, const double* pos, int* layers, double* height) {
+    const int nn = h->d.nn, ne = h->d.ne;
+    *layers = 0;
+    *height = 0.0;
+    int cur = -1;
+    for (int i = 0; i < nn && cur < 0; ++i)
+        if (h->h_place[i] == 0) cur = i;
+    if (cur < 0) return;
+    for (int guard = 0; h->h_place[cur] != 1 && guard <= ne; ++guard) {
+        int found = -1, slot = -1;
+        for (int e = 0; e < ne && found < 0; ++e)
+            for (int a = 0; a < 3; ++a)
+                if (h->h_conn[6 * (size_t)e + a] == cur) {
+                    found = e;
+                    slot = a;
+                    break;
+                }
+        if (found < 0) return;
+        const int* c = &h->h_conn[6 * (size_t)found];
+        double s = 0.0;
+        for (int k = 0; k < 3; ++k) {
+            const double dd = pos[3 * (size_t)c[0] + k] - pos[3 * (size_t)c[3] + k];
+            s += dd * dd;
+        }
+        *height += std::pow(s, 0.5);
+        ++*layers;
+        cur = c[slot + 3];
+    }
+}
+
+// Corner values of every cell, made compatible (GridBasedGrowthFunction's
+// constructor, GrowthFunctionTypes.h:281-351, and
+// preCalculateAnglesForCompatibleAveraging, :427-579).
+void compatible_corners(int nx, int ny, const double* rates, const double* angles_deg, std::vector<double>& cg,
+                        std::vector<double>& ca, std::vector<uint8_t>& ce) {
+    const size_t ncell = (size_t)(nx - 1) * (ny - 1);
+    cg.assign(12 * ncell, 0.0);
+    ca.assign(4 * ncell, 0.0);
+    ce.assign(4 * ncell, 0);
+    auto rate = [&](int i, int j, int k) { return rates[3 * ((size_t)i * ny + j) + k]; };
+    auto angle = [&](int i, int j) { return angles_deg ? angles_deg[(size_t)i * ny + j] * kPi / 180.0 : 0.0; };
+    auto carries_angle = [&](int i, int j) {
+        double ar = rate(i, j, 0) / rate(i, j, 1);
+        if (ar < 0) ar *= -1.0;
+        if (ar < 1.0) ar = 1 / ar;
+        return !(ar < 1.1);
+    };
+    for (int ix = 0; ix < nx - 1; ++ix)
+        for (int iy = 0; iy < ny - 1; ++iy) {
+            const int ci[4] = {ix, ix + 1, ix, ix + 1}, cj[4] = {iy, iy, iy + 1, iy + 1};
+            double g[4][3], a[4] = {0.0, 0.0, 0.0, 0.0};
+            bool elim[4] = {false, false, false, false};
+            for (int c = 0; c < 4; ++c) {
+                for (int k = 0; k < 3; ++k) g[c][k] = rate(ci[c], cj[c], k);
+                if (carries_angle(ci[c], cj[c])) a[c] = angle(ci[c], cj[c]);
+                else elim[c] = true;
+            }
+            for (int c = 0; c < 4; ++c) {
+                while (a[c] < 0) a[c] += kPi;
+                while (a[c] > kPi) a[c] -= kPi;
+            }
+            // the base angle: the first corner that carries one (else corner 3, angle 0)
+            int base = 3;
+            double tet = 0;
+            for (int c = 0; c < 4; ++c)
+                if (!elim[c]) {
+                    tet = a[c];
+                    base = c;
+                    break;
+                }
+            bool flip[4] = {false, false, false, false};
+            for (int c = base; c < 4; ++c) {
+                const double dt = a[c] - tet;
+                if (dt > 0) {
+                    if (dt >= kPi / 4.0 && dt < 3.0 * kPi / 4.0) {
+                        a[c] = a[c] - kPi / 2.0;
+                        flip[c] = true;
+                    } else if (dt >= 3.0 * kPi / 4.0 && dt < 5.0 * kPi / 4.0) {
+                        a[c] = a[c] - kPi;
+                    } else if (dt >= 5.0 * kPi / 4.0 && dt < 7.0 * kPi / 4.0) {
+                        a[c] = a[c] - 6.0 * kPi / 4.0;
+                        flip[c] = true;
+                    } else if (dt >= 7.0 * kPi / 4.0) {
+                        a[c] = a[c] - 2.0 * kPi;
+                    }
+                } else if (dt < 0) {
+                    if (dt <= -kPi / 4.0 && dt > -3.0 * kPi / 4.0) {
+                        a[c] = a[c] + kPi / 2.0;
+                        flip[c] = true;
+                    } else if (dt <= -3.0 * kPi / 4.0 && dt > -5.0 * kPi / 4.0) {
+                        a[c] = a[c] + kPi;
+                    } else if (dt <= -5.0 * kPi / 4.0 && dt > -7.0 * kPi / 4.0) {
+                        a[c] = a[c] + 6.0 * kPi / 4.0;
+                        flip[c] = true;
+                    } else if (dt <= -7.0 * kPi / 4.0) {
+                        a[c] = a[c] + 2.0 * kPi;
+                    }
+                }
+            }
+            const size_t cell = (size_t)ix * (ny - 1) + iy;
+            for (int c = 0; c < 4; ++c) {
+                if (flip[c]) std::swap(g[c][0], g[c][1]);
+                for (int k = 0; k < 3; ++k) cg[12 * cell + 3 * c + k] = g[c][k];
+                ca[4 * cell + c] = a[c];
+                ce[4 * cell + c] = elim[c] ? 1 : 0;
+            }
+        }
+}
+
+// ---- device ---------------------------------------------------------------
+
+// Min (or max) over the CTA's 1024 threads, returned to every thread.
+__device__ double cta_reduce(double v, bool take_max, double* red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double w = __shfl_down_sync(0xffffffffu, v, o);
+        v = take_max ? fmax(v, w) : fmin(v, w);
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        v = red[threadIdx.x];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double w = __shfl_down_sync(0xffffffffu, v, o);
+            v = take_max ? fmax(v, w) : fmin(v, w);
+        }
+        if (threadIdx.x == 0) red[32] = v;
+    }
+    __syncthreads();
+    const double r = red[32];
+    __syncthreads();
+    return r;
+}
+
+// calculateBoundingBox in x and y on the device, bit for bit.  The minimum is
+// min(1e5, all nodes).  The maximum is that of the nodes that did not lower
+// the running minimum: whenever the largest coordinate is reached by a node
+// other than node 0 that is the plain maximum (such a node cannot have
+// lowered the minimum below node 0's); only when node 0 alone holds it does a
+// second pass replay the running minimum (per-thread chunks in node order,
+// an exclusive min-scan over the chunks, then the chunks walked in order).
+__global__ void __launch_bounds__(kBoxThreads) k_box(int nn, const double* __restrict__ pos, double* __restrict__ box) {
+    __shared__ double red[33];
+    __shared__ double scan[kBoxThreads];
+    double lo[2], hi[2];
+    const int t = threadIdx.x;
+    for (int k = 0; k < 2; ++k) {
+        double mn = kBoxInit, mx = -kBoxInit;
+        for (int i = t; i < nn; i += kBoxThreads) {
+            const double p = pos[3 * (size_t)i + k];
+            mn = fmin(mn, p);
+            if (i > 0) mx = fmax(mx, p);
+        }
+        lo[k] = cta_reduce(mn, false, red);
+        hi[k] = cta_reduce(mx, true, red);
+        if (nn > 0 && pos[k] > hi[k]) {  // node 0 alone holds the largest coordinate (uniform branch)
+            const int chunk = (nn + kBoxThreads - 1) / kBoxThreads;
+            const int i0 = min(nn, t * chunk), i1 = min(nn, i0 + chunk);
+            double cm = INFINITY;
+            for (int i = i0; i < i1; ++i) cm = fmin(cm, pos[3 * (size_t)i + k]);
+            scan[t] = cm;
+            __syncthreads();
+            for (int o = 1; o < kBoxThreads; o <<= 1) {
+                const double v = t >= o ? scan[t - o] : INFINITY;
+                __syncthreads();
+                scan[t] = fmin(scan[t], v);
+                __syncthreads();
+            }
+            double run = t > 0 ? fmin(kBoxInit, scan[t - 1]) : kBoxInit;
+            double up = -kBoxInit;
+            for (int i = i0; i < i1; ++i) {
+                const double p = pos[3 * (size_t)i + k];
+                if (p < run) run = p;
+                else if (p > up) up = p;
+            }
+            hi[k] = cta_reduce(up, true, red);
+        }
+    }
+    if (t == 0) {
+        box[0] = lo[0];
+        box[1] = lo[1];
+        box[2] = hi[0] - lo[0];
+        box[3] = hi[1] - lo[1];
+    }
+}
+
+// ShapeBase::calculateRelativePosInBoundingBox (ShapeBase.cpp:1842-1848) of
+// the prism colsrc[e], whose position prism e takes.
+__global__ void k_relpos(int ne, const int* __restrict__ conn, const double* __restrict__ pos,
+                         const double* __restrict__ box, const int* __restrict__ colsrc, double* __restrict__ rel) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    const int s = colsrc[e];
+    double c[2] = {0.0, 0.0};
+    for (int a = 0; a < 6; ++a) {
+        const int n = conn[(size_t)a * ne + s];
+        c[0] += pos[3 * (size_t)n];
+        c[1] += pos[3 * (size_t)n + 1];
+    }
+    rel[e] = (c[0] / 6 - box[0]) / box[2];
+    rel[ne + e] = (c[1] / 6 - box[1]) / box[3];
+}
+
+struct GridFn {
+    int nx, ny;
+    double zmin, zmax;
+    const double* cg;
+    const double* ca;
+    const uint8_t* ce;
+};
+
+struct GridArgs {
+    int ne, nfn, interp;
+    double dt;
+    const double* rates;  // [3][ne] per-element rates, or null
+    const double* relz;
+    const double* rel;    // [2][ne]
+    GridFn fn[kMaxGridFns];
+};
+
+// Products and sums written out with explicit rounding, in the reference's
+// order of operations (left to right; gsl_blas_dgemm accumulating over k from
+// 0), so that no multiply-add is contracted into an FMA.  Where almost all of
+// a cell's corners carry no angle the interpolated angle is divided by a
+// small 1 - fe, which magnifies any rounding difference.
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+
+__device__ __forceinline__ void mat3_mul(const double* A, const double* B, double* C, bool transB) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double acc = 0.0;
+            for (int k = 0; k < 3; ++k) acc = add(acc, mul(A[3 * i + k], transB ? B[3 * j + k] : B[3 * k + j]));
+            C[3 * i + j] = acc;
+        }
+}
+
+// Per prism: the growth increment of the step -- diag(exp(rate dt)) of the
+// per-element rates, then each active grid function's increment
+// (ShapeBase::calculateFgFromGridCorners, columnar prism, tissue weight 1)
+// multiplied on the left (updateGrowthIncrement) -- and Fg <- increment Fg
+// (growShapeByFg).
+__global__ void k_grid_growth(GridArgs G, double* __restrict__ Fg, double* __restrict__ invFg) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= G.ne) return;
+    const int ne = G.ne;
+    double M[9] = {1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
+    if (G.rates)
+        for (int k = 0; k < 3; ++k) M[4 * k] = exp(G.rates[(size_t)k * ne + e] * 1.0 * G.dt);
+    const double rz = G.relz[e];
+    const double rel_x = G.rel[e], rel_y = G.rel[ne + e];
+    for (int f = 0; f < G.nfn; ++f) {
+        const GridFn& F = G.fn[f];
+        if (rz < F.zmin || rz > F.zmax) continue;  // isGrowthRateApplicable (ShapeBase.cpp:277-300): identity
+        // ShapeBase::convertRelativePosToGridIndex
+        const double rx = rel_x * (float)(F.nx - 1), ry = rel_y * (float)(F.ny - 1);
+        int ix = (int)floor(rx), iy = (int)floor(ry);
+        double fx = rx - ix, fy = ry - iy;
+        if (ix >= F.nx - 1) {
+            ix = F.nx - 2;
+            fx = 1.0;
+        } else if (ix < 0) {
+            ix = 0;
+            fx = 0.0;
+        }
+        if (iy >= F.ny - 1) {
+            iy = F.ny - 2;
+            fy = 1.0;
+        } else if (iy < 0) {
+            iy = 0;
+            fy = 0.0;
+        }
+        const size_t cell = (size_t)ix * (F.ny - 1) + iy;
+        const double* g = F.cg + 12 * cell;  // corner c, axis k at g[3c + k]
+        const double* an = F.ca + 4 * cell;
+        const uint8_t* el = F.ce + 4 * cell;
+        const double ux = 1.0 - fx, uy = 1.0 - fy;
+        double growth[3];
+        double angle = 0;
+        if (G.interp == 0) {
+            const int c = fx > 0.5 ? (fy > 0.5 ? 3 : 1) : (fy > 0.5 ? 2 : 0);
+            for (int k = 0; k < 3; ++k) growth[k] = g[3 * c + k];
+        } else {
+            double fe = 0.0;
+            if (el[0]) fe = add(fe, mul(ux, uy));
+            if (el[1]) fe = add(fe, mul(fx, uy));
+            if (el[2]) fe = add(fe, mul(ux, fy));
+            if (el[3]) fe = add(fe, mul(fx, fy));
+            angle = add(add(add(mul(mul(an[0], ux), uy), mul(mul(an[1], fx), uy)), mul(mul(an[2], ux), fy)),
+                        mul(mul(an[3], fx), fy));
+            if (fe > 0) {
+                if (fe >= 0.9999999) angle = 0.0;
+                else angle /= (1.0 - fe);
+            }
+            for (int k = 0; k < 3; ++k)
+                growth[k] = add(add(add(mul(mul(g[k], ux), uy), mul(mul(g[3 + k], fx), uy)), mul(mul(g[6 + k], ux), fy)),
+                                mul(mul(g[9 + k], fx), fy));
+        }
+        double inc[9] = {exp(growth[0] * G.dt), 0.0, 0.0, 0.0, exp(growth[1] * G.dt), 0.0, 0.0, 0.0,
+                         exp(growth[2] * G.dt)};
+        if (angle != 0.0) {  // R inc R^T, R the rotation by the angle about z
+            const double c = cos(angle), s = sin(angle);
+            const double R[9] = {c, -1.0 * s, 0.0, s, c, 0.0, 0.0, 0.0, 1.0};
+            double t[9];
+            mat3_mul(R, inc, t, false);
+            mat3_mul(t, R, inc, true);
+        }
+        double P[9];
+        mat3_mul(inc, M, P, false);
+        for (int k = 0; k < 9; ++k) M[k] = P[k];
+    }
+    double F0[9], out[9], inv[9];
+    for (int k = 0; k < 9; ++k) F0[k] = Fg[(size_t)k * ne + e];
+    mat3_mul(M, F0, out, false);
+    inv3_cof(out, inv);
+    for (int k = 0; k < 9; ++k) {
+        Fg[(size_t)k * ne + e] = out[k];
+        invFg[(size_t)k * ne + e] = inv[k];
+    }
+}
+
+// Box and bounding-box positions of the current positions into rel_out.
+tf_status launch_relpos(tf_handle* h, double* rel_out) {
+    Growth* g = h->growth;
+    Device& d = h->d;
+    k_box<<<1, kBoxThreads, 0, h->stream>>>(d.nn, d.uk, g->box);
+    TF_LAUNCH_CHECK(h);
+    k_relpos<<<cdiv(d.ne, kT), kT, 0, h->stream>>>(d.ne, d.conn, d.uk, g->box, g->colsrc, rel_out);
+    TF_LAUNCH_CHECK(h);
+    return TF_OK;
+}
+
+}  // namespace
+
+void growth_free(Growth* g) {
+    if (!g) return;
+    for (auto& f : g->grids) free_grid(f);
+    void* ptrs[] = {g->relz, g->rel0, g->rel, g->colsrc, g->box};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete g;
+}
+
+// Tissue height, initial relative z (assignInitialZPositions, Simulation.cpp
+// :3367-3371, after calculateBoundingBox), the columns and the pinned
+// positions (Simulation.cpp:630-645), from the mesh's positions at creation.
+tf_status growth_setup(tf_handle* h) {
+    Growth* g = new Growth;
+    h->growth = g;
+    const int ne = h->d.ne, nn = h->d.nn;
+    const double* pos0 = h->h_pos0.data();
+    tissue_height(h, pos0, &g->layers, &g->height);
+    double lo[3], size[3];
+    host_box(pos0, nn, lo, size);
+    // ShapeBase::setInitialZPosition (ShapeBase.cpp:612-627)
+    std::vector<double> relz(ne), rel(2 * (size_t)ne), rel0(2 * (size_t)ne);
+    for (int e = 0; e < ne; ++e) {
+        double c[3] = {0.0, 0.0, 0.0};
+        for (int a = 0; a < 6; ++a)
+            for (int k = 0; k < 3; ++k) c[k] += pos0[3 * (size_t)h->h_conn[6 * (size_t)e + a] + k];
+        for (int k = 0; k < 3; ++k) c[k] /= 6;
+        double r = 1.0 - ((c[2] - lo[2]) / g->height);
+        if (r < 0) r = 0;
+        if (r > 1.0) r = 1.0;
+        relz[e] = r;
+        rel[e] = (c[0] - lo[0]) / size[0];
+        rel[ne + e] = (c[1] - lo[1]) / size[1];
+    }
+    // Columns: from each basal prism up, the first prism (in element order)
+    // whose basal triangle is the current apical one.
+    std::map<std::array<int, 3>, int> by_basal;
+    auto tri = [&](int e, int o) {
+        std::array<int, 3> k = {h->h_conn[6 * (size_t)e + o], h->h_conn[6 * (size_t)e + o + 1],
+                                h->h_conn[6 * (size_t)e + o + 2]};
+        std::sort(k.begin(), k.end());
+        return k;
+    };
+    for (int e = 0; e < ne; ++e) by_basal.emplace(tri(e, 0), e);
+    std::vector<int> colsrc(ne);
+    for (int e = 0; e < ne; ++e) colsrc[e] = e;
+    const int L = g->layers;
+    std::vector<int> col;
+    for (int e = 0; e < ne; ++e) {
+        if (element_placement(h, e) != 0 || L < 3) continue;
+        col.assign(1, e);
+        for (int i = 1; i < L; ++i) {
+            auto it = by_basal.find(tri(col.back(), 3));
+            if (it == by_basal.end() || it->second == col.back()) break;
+            col.push_back(it->second);
+        }
+        if ((int)col.size() != L) continue;
+        const int top = col.back();
+        if (element_placement(h, top) != 1) continue;
+        for (int i = 0; i < L - 2; ++i) colsrc[col[i]] = top;
+    }
+    for (int e = 0; e < ne; ++e) {
+        rel0[e] = rel[colsrc[e]];
+        rel0[ne + e] = rel[ne + colsrc[e]];
+    }
+    GR_TRY(put(&g->relz, relz));
+    GR_TRY(put(&g->rel0, rel0));
+    GR_TRY(put(&g->rel, std::vector<double>(2 * (size_t)ne, 0.0)));
+    GR_TRY(put(&g->colsrc, colsrc));
+    GR_TRY(put(&g->box, std::vector<double>(4, 0.0)));
+    return TF_OK;
+}
+
+tf_status growth_add_grid(tf_handle* h, int nx, int ny, const double* rates, const double* angles_deg, double t0,
+                          double t1, double zmin, double zmax) {
+    GridGrowth f;
+    f.nx = nx;
+    f.ny = ny;
+    f.t0 = static_cast<float>(t0);  // GrowthFunctionBase keeps its times as float
+    f.t1 = static_cast<float>(t1);
+    f.zmin = zmin;
+    f.zmax = zmax;
+    std::vector<double> cg, ca;
+    std::vector<uint8_t> ce;
+    compatible_corners(nx, ny, rates, angles_deg, cg, ca, ce);
+    tf_status s = put(&f.cg, cg);
+    if (s == TF_OK) s = put(&f.ca, ca);
+    if (s == TF_OK) s = put(&f.ce, ce);
+    if (s != TF_OK) {
+        free_grid(f);
+        return s;
+    }
+    h->growth->grids.push_back(f);
+    return TF_OK;
+}
+
+void growth_clear_grids(tf_handle* h) {
+    if (!h->growth) return;
+    for (auto& f : h->growth->grids) free_grid(f);
+    h->growth->grids.clear();
+}
+
+void growth_set_mode(tf_handle* h, int interp, int pinned) {
+    h->growth->interp = interp;
+    h->growth->pinned = pinned;
+}
+
+// Simulation::updatePinningPositions (Simulation.cpp:6018-6023): the current
+// bounding-box positions become the pinned ones.
+tf_status growth_repin(tf_handle* h) { return launch_relpos(h, h->growth->rel0); }
+
+int growth_grid_count(const tf_handle* h) { return h->growth ? static_cast<int>(h->growth->grids.size()) : 0; }
+
+// The growth of a step when grid functions are active at the handle's time
+// (Simulation.cpp:10068): per-element rates and grid functions in one
+// increment per prism.  *done = false: no grid function is active, the
+// per-element rates alone apply.
+tf_status launch_grid_growth(tf_handle* h, bool* done) {
+    *done = false;
+    Growth* g = h->growth;
+    if (!g || g->grids.empty()) return TF_OK;
+    Device& d = h->d;
+    const double t = h->time;
+    GridArgs A{};
+    A.ne = d.ne;
+    A.interp = g->interp;
+    A.dt = h->dt;
+    A.rates = h->have_rates ? d.rates : nullptr;
+    A.relz = g->relz;
+    A.rel = g->pinned ? g->rel0 : g->rel;
+    for (const auto& f : g->grids) {
+        if (!(t >= f.t0 && t < f.t1)) continue;
+        A.fn[A.nfn++] = GridFn{f.nx, f.ny, f.zmin, f.zmax, f.cg, f.ca, f.ce};
+    }
+    if (A.nfn == 0) return TF_OK;
+    if (!g->pinned) GR_TRY(launch_relpos(h, g->rel));
+    k_grid_growth<<<cdiv(d.ne, kT), kT, 0, h->stream>>>(A, d.Fg, d.invFg);
+    TF_LAUNCH_CHECK(h);
+    *done = true;
+    return TF_OK;
+}
+
+// Host copies for the tests: relative z, pinned positions, and the positions
+// of the current shape.
+tf_status growth_positions(tf_handle* h, double* relz, double* rel0, double* rel) {
+    Growth* g = h->growth;
+    const size_t ne = h->d.ne;
+    if (relz) TF_CUDA(cudaMemcpyAsync(relz, g->relz, ne * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (rel0) TF_CUDA(cudaMemcpyAsync(rel0, g->rel0, 2 * ne * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (rel) {
+        GR_TRY(launch_relpos(h, g->rel));
+        TF_CUDA(cudaMemcpyAsync(rel, g->rel, 2 * ne * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    }
+    TF_CUDA(cudaStreamSynchronize(h->stream));
+    return TF_OK;
+}
+
+}  // namespace tf

@@ -162,6 +162,25 @@ constexpr int kAmgMaxLevels = 10;
 
 struct Amg;      // multigrid hierarchy (tf_amg.cu)
 struct Packing;  // packing between tissue surfaces (tf_packing.cu)
+struct Growth;   // grid-based growth functions (tf_growth.cu)
+
+// Inverse of a 3x3 matrix (row-major) by cofactors.
+__device__ __forceinline__ void inv3_cof(const double* M, double* inv) {
+    const double c0 = M[4] * M[8] - M[5] * M[7];
+    const double c1 = M[5] * M[6] - M[3] * M[8];
+    const double c2 = M[3] * M[7] - M[4] * M[6];
+    const double det = M[0] * c0 + M[1] * c1 + M[2] * c2;
+    const double r = 1.0 / det;
+    inv[0] = c0 * r;
+    inv[1] = (M[2] * M[7] - M[1] * M[8]) * r;
+    inv[2] = (M[1] * M[5] - M[2] * M[4]) * r;
+    inv[3] = c1 * r;
+    inv[4] = (M[0] * M[8] - M[2] * M[6]) * r;
+    inv[5] = (M[2] * M[3] - M[0] * M[5]) * r;
+    inv[6] = c2 * r;
+    inv[7] = (M[1] * M[6] - M[0] * M[7]) * r;
+    inv[8] = (M[0] * M[4] - M[1] * M[3]) * r;
+}
 
 // Programmatic dependent launch for the chains of short kernels of the
 // linear solve: a kernel launched with launch_pdl may be scheduled as its
@@ -263,6 +282,10 @@ struct tf_handle {
     int last_iters[2] = {0, 0};                 // iterations of the last solve per method (chunk planning)
     tf::Amg* amg = nullptr;                     // multigrid preconditioner (null: block-Jacobi)
     tf::Packing* pk = nullptr;                  // packing between tissue surfaces (null: off)
+    tf::Growth* growth = nullptr;               // grid-based growth functions (null: none added yet)
+    double time = 0.0;                          // simulation time (currSimTimeSec), advanced by tf_end_step
+    bool in_step = false;                       // between tf_begin_step and tf_end_step
+    std::vector<double> h_pos0;                 // node positions of the mesh at creation
 };
 
 namespace tf {
@@ -312,6 +335,17 @@ tf_status packing_relink(tf_handle* h);          // couple blocks in the current
 // as X_{l+1} = P^T X_l P).
 bool use_multigrid(const tf_handle* h);
 void packing_free(Packing* p);
+tf_status growth_setup(tf_handle* h);           // grid growth tables from the mesh at creation
+tf_status growth_add_grid(tf_handle* h, int nx, int ny, const double* rates, const double* angles_deg, double t0,
+                          double t1, double zmin, double zmax);
+void growth_clear_grids(tf_handle* h);
+void growth_set_mode(tf_handle* h, int interp, int pinned);
+tf_status growth_repin(tf_handle* h);
+int growth_grid_count(const tf_handle* h);
+constexpr int kMaxGridGrowthFunctions = 8;      // grid growth functions per handle
+tf_status launch_grid_growth(tf_handle* h, bool* done);  // rates + the grid functions active at h->time
+tf_status growth_positions(tf_handle* h, double* relz, double* rel0, double* rel);
+void growth_free(Growth* g);
 tf_status upload_extra(tf_handle* h, bool pattern_changed);
 tf_status sync_extra_to_host(tf_handle* h);      // device extra-block values -> h_xval
 tf_status take_check(tf_handle* h);              // checked build: report and clear a failed index check

@@ -355,6 +355,33 @@ def perturbed_state(t: Tissue, seed: int = 1, amp: float = 0.05):
     return uk, un
 
 
+def swap_nodes(t: Tissue, a: int, b: int) -> Tissue:
+    """The same tissue with node ids a and b exchanged: positions, placement,
+    boundary conditions and connectivity follow the nodes."""
+    perm = np.arange(t.n_nodes)
+    perm[a], perm[b] = b, a
+    pos = t.pos.reshape(-1, 3)[perm].reshape(-1).copy()
+    fixed = t.fixed.reshape(-1, 3)[perm].reshape(-1).copy()
+    ev = t.ext_visc.reshape(-1, 3)[perm].reshape(-1).copy()
+    return dataclasses.replace(t, pos=pos, conn=perm[t.conn].astype(np.int32), fixed=fixed, ext_visc=ev,
+                               node_placement=t.node_placement[perm].copy())
+
+
+def grid_growth_inputs(seed: int, nx: int = 5, ny: int = 4, scale: float = 1e-4):
+    """Seeded rates (nx, ny, 3) in 1/s and xy angles (nx, ny) in degrees for a
+    grid-based growth function: anisotropic in-plane rates, some grid points
+    nearly isotropic (aspect ratio below 1.1, so their angle is not used) and
+    angles over (-200, 200) degrees, so that neighbouring corners are turned
+    by about 90 and 180 degrees from each other."""
+    rng = np.random.default_rng(seed)
+    r = np.empty((nx, ny, 3))
+    r[:, :, 0] = rng.uniform(0.2, 1.0, size=(nx, ny)) * scale
+    r[:, :, 1] = r[:, :, 0] * rng.choice([0.3, 0.5, 1.02, 2.5], size=(nx, ny))
+    r[:, :, 2] = rng.uniform(-0.2, 0.2, size=(nx, ny)) * scale
+    ang = rng.uniform(-200.0, 200.0, size=(nx, ny))
+    return r, ang
+
+
 def growth_Fg(t: Tissue, seed: int = 2, amp: float = 0.02) -> np.ndarray:
     """A seeded non-trivial growth tensor per element (near identity)."""
     rng = np.random.default_rng(seed)
