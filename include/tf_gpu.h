@@ -174,24 +174,45 @@ TF_API tf_status tf_get_packing(tf_handle* h, int64_t* n, int32_t* nodes, double
 /* Node masses of the last detection (Node::mass), n_nodes values. */
 TF_API tf_status tf_packing_masses(tf_handle* h, double* mass);
 
-/* --- grid-based growth functions (growth type 3) ------------------------- */
-/* Adds a GridBasedGrowthFunction (GrowthFunctionTypes.h:266-609, read by
- * ModelInputObject::readGrowthOptions): an nx x ny grid of growth rates in 1/s,
- * rates[3*(i*ny + j) + k] for grid point (i, j) and axis k (x, y, z), and xy
- * angles in degrees, angles_deg[i*ny + j] (NULL: all 0).  Active while
- * init_time <= t < end_time (both kept as float, as GrowthFunctionBase does)
- * on prisms whose initial relative z (0 apical, 1 basal) is within
- * [zmin, zmax].  Every tf_begin_step at time t applies the active functions
- * after the per-element rates: Simulation::calculateGrowthGridBased
- * (Simulation.cpp:10065-10114) with ShapeBase::calculateFgFromGridCorners
- * (ShapeBase.cpp:432-562), positions from Simulation.cpp:5833-5843.  The
- * handle's initial relative z, columns and pinned positions come from the mesh
- * given to tf_create.  Columnar prisms only; single-mesh handles only. */
+/* --- growth functions (GrowthFunctionBase types 1-3) --------------------- */
+/* Growth functions of the reference (GrowthFunctionTypes.h), applied at every
+ * tf_begin_step at simulation time t, in the order they were added, after the
+ * per-element rates of tf_set_growth_rates: Simulation::calculateGrowth
+ * (Simulation.cpp:9651-9666) -- each active function (init_time <= t <
+ * end_time, both kept as float as GrowthFunctionBase does) multiplies the
+ * growth increment of every prism whose initial relative z (0 apical,
+ * 1 basal; assignInitialZPositions, Simulation.cpp:3367-3371) is within
+ * [zmin, zmax] (ShapeBase::isGrowthRateApplicable, ShapeBase.cpp:277-300),
+ * and Fg <- increment Fg (growShapeByFg, ShapeBase.cpp:1215-1251).  Rates in
+ * 1/s (x, y, z).  Columnar prisms; single-mesh handles; at most 16 functions.
+ * The initial relative z, the prism columns and the pinned grid positions come
+ * from the mesh given to tf_create. */
+/* Type 1, UniformGrowthFunction (GrowthFunctionTypes.h:14-100) applied by
+ * calculateGrowthUniform (Simulation.cpp:9757-9799): R diag(exp(rate dt)) R^T,
+ * R the rotation by angle_rad about z (ShapeBase::calculateFgFromRates,
+ * ShapeBase.cpp:396-421). */
+TF_API tf_status tf_add_uniform_growth(tf_handle* h, const double* rates, double angle_rad, double init_time,
+                                       double end_time, double zmin, double zmax);
+/* Type 2, RingGrowthFunction (GrowthFunctionTypes.h:150-264) applied by
+ * calculateGrowthRing (Simulation.cpp:9801-9885): for prisms whose centre lies
+ * at an xy distance d from (centre_x, centre_y) with r_in^2 < d^2 < r_out^2,
+ * the uniform increment of rates x (1 - (d - r_in)/(r_out - r_in)); centre,
+ * radii and d in single precision as the reference reads them. */
+TF_API tf_status tf_add_ring_growth(tf_handle* h, double centre_x, double centre_y, double inner_radius,
+                                    double outer_radius, const double* rates, double angle_rad, double init_time,
+                                    double end_time, double zmin, double zmax);
+/* Type 3, GridBasedGrowthFunction (GrowthFunctionTypes.h:266-609, read by
+ * ModelInputObject::readGrowthOptions): an nx x ny grid of rates,
+ * rates[3*(i*ny + j) + k] for grid point (i, j) and axis k, and xy angles in
+ * degrees, angles_deg[i*ny + j] (NULL: all 0), over the tissue's bounding box;
+ * Simulation::calculateGrowthGridBased (Simulation.cpp:10065-10114) with
+ * ShapeBase::calculateFgFromGridCorners (ShapeBase.cpp:432-562), positions
+ * from Simulation.cpp:5833-5843. */
 TF_API tf_status tf_add_grid_growth(tf_handle* h, int32_t nx, int32_t ny, const double* rates,
                                     const double* angles_deg, double init_time, double end_time, double zmin,
                                     double zmax);
-/* Removes every grid growth function. */
-TF_API tf_status tf_clear_grid_growth(tf_handle* h);
+/* Removes every growth function (the per-element rates stay). */
+TF_API tf_status tf_clear_growth_functions(tf_handle* h);
 /* gridGrowthsInterpolationType (0 nearest grid point, 1 bilinear; default 1)
  * and GridGrowthsPinnedOnInitialMesh (default 0: the positions of each step's
  * start shape), Simulation.cpp:144-146. */

@@ -1,8 +1,14 @@
-"""Grid-based growth functions: numpy restatement of the reference's growth
-type 3, for checking the GPU kernels.  TEST INFRASTRUCTURE ONLY: imported by
-tests/, never by the library.
+"""Growth functions: numpy restatement of the reference's growth types 1
+(uniform), 2 (ring) and 3 (grid-based), for checking the GPU kernels.  TEST
+INFRASTRUCTURE ONLY: imported by tests/, never by the library.
 
 Follows, in TissueFolding/TissueFolding/SourceCode/:
+  * Simulation::calculateGrowth (Simulation.cpp:9651-9666) with
+    calculateGrowthUniform (:9757-9799) and calculateGrowthRing (:9801-9885):
+    ShapeBase::calculateFgFromRates (ShapeBase.cpp:396-421), R diag(exp(r dt))
+    R^T with the function's xy rotation, the ring's rates scaled by
+    1 - (d - r_in)/(r_out - r_in) with centre, radii and d in single
+    precision;
   * GridBasedGrowthFunction (GrowthFunctionTypes.h:266-609): the aspect-ratio
     test of its constructor (:336-349, threshold 1.1) and
     preCalculateAnglesForCompatibleAveraging (:427-579): corner angles brought
@@ -285,8 +291,38 @@ def grid_increments(rel, relz, corners, dt, interp=1, zmin=0.0, zmax=1.0):
     return inc
 
 
-class GridGrowthOracle:
-    """Grid functions on one tissue: the state the reference keeps for them."""
+def rotation(angle):
+    c, s = math.cos(angle), math.sin(angle)
+    return np.array([[c, -1.0 * s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]])
+
+
+def rates_increment(r, R, dt):
+    """calculateFgFromRates, tissue weight 1: r (E, 3) -> (E, 3, 3)."""
+    ne = r.shape[0]
+    d = np.zeros((ne, 3, 3))
+    for k in range(3):
+        d[:, k, k] = np.exp(r[:, k] * 1.0 * dt)
+    Rs = np.broadcast_to(R, (ne, 3, 3))
+    return dgemm3(dgemm3(Rs, d), Rs, trans_b=True)
+
+
+def ring_scale(pos, conn, fn):
+    """(E,) the ring's rate scale per prism, NaN outside the ring."""
+    cen = centres(pos, conn)
+    f32 = np.float32
+    cx, cy, rin, rout = f32(fn["cx"]), f32(fn["cy"]), f32(fn["rin"]), f32(fn["rout"])
+    dx = float(cx) - cen[:, 0]
+    dy = float(cy) - cen[:, 1]
+    d2 = dx * dx + dy * dy
+    rin2, rout2 = float(rin * rin), float(rout * rout)
+    inside = (d2 > rin2) & (d2 < rout2)
+    dist = np.sqrt(d2).astype(np.float32)
+    frac = ((dist - rin) / (rout - rin)).astype(np.float32)
+    return np.where(inside, 1.0 - frac.astype(np.float64), np.nan)
+
+
+class GrowthOracle:
+    """Growth functions on one tissue: the state the reference keeps for them."""
 
     def __init__(self, pos0, conn, node_placement):
         self.conn = np.asarray(conn).reshape(-1, 6)
@@ -295,10 +331,26 @@ class GridGrowthOracle:
         self.interp = 1
         self.pinned = False
 
-    def add(self, rates, angles_deg=None, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0):
-        self.fns.append({"corners": compatible_corners(rates, angles_deg),
-                         "t0": float(np.float32(init_time)), "t1": float(np.float32(end_time)),
-                         "zmin": zmin, "zmax": zmax})
+    @staticmethod
+    def _window(init_time, end_time, zmin, zmax):
+        return {"t0": float(np.float32(init_time)), "t1": float(np.float32(end_time)), "zmin": zmin, "zmax": zmax}
+
+    def add_grid_growth(self, rates, angles_deg=None, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0):
+        """A grid-based function (type 3)."""
+        self.fns.append({"type": 3, "corners": compatible_corners(rates, angles_deg),
+                         **self._window(init_time, end_time, zmin, zmax)})
+
+    add = add_grid_growth
+
+    def add_uniform_growth(self, rates, angle_rad=0.0, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0):
+        self.fns.append({"type": 1, "rate": np.asarray(rates, dtype=np.float64), "R": rotation(angle_rad),
+                         **self._window(init_time, end_time, zmin, zmax)})
+
+    def add_ring_growth(self, centre, inner_radius, outer_radius, rates, angle_rad=0.0, init_time=-1e30, end_time=1e30,
+                 zmin=0.0, zmax=1.0):
+        self.fns.append({"type": 2, "rate": np.asarray(rates, dtype=np.float64), "R": rotation(angle_rad),
+                         "cx": centre[0], "cy": centre[1], "rin": inner_radius, "rout": outer_radius,
+                         **self._window(init_time, end_time, zmin, zmax)})
 
     def repin(self, pos):
         self.state["rel0"] = relative_positions(pos, self.conn, self.state["src"])
@@ -317,9 +369,20 @@ class GridGrowthOracle:
         if not active:
             return total
         rel = self.state["rel0"] if self.pinned else relative_positions(pos, self.conn, self.state["src"])
+        relz = self.state["relz"]
         for f in active:
-            total = dgemm3(grid_increments(rel, self.state["relz"], f["corners"], dt, self.interp, f["zmin"],
-                                           f["zmax"]), total)
+            if f["type"] == 3:
+                inc = grid_increments(rel, relz, f["corners"], dt, self.interp, f["zmin"], f["zmax"])
+            else:
+                r = np.broadcast_to(f["rate"], (ne, 3)).copy()
+                keep = (relz >= f["zmin"]) & (relz <= f["zmax"])
+                if f["type"] == 2:
+                    sf = ring_scale(pos, self.conn, f)
+                    keep &= ~np.isnan(sf)
+                    r = r * np.where(np.isnan(sf), 0.0, sf)[:, None]
+                inc = rates_increment(r, f["R"], dt)
+                inc[~keep] = np.eye(3)
+            total = dgemm3(inc, total)
         return total
 
     def grow(self, Fg, pos, time, dt, rates=None):
@@ -329,6 +392,33 @@ class GridGrowthOracle:
 
 
 FIXTURES = ["steps_grid_growth", "steps_grid_growth_pinned"]
+MIXED_FIXTURE = "steps_growth_functions"
+
+
+def add_functions(obj, fns):
+    """Adds function descriptors ({"kind": "uniform" | "ring" | "grid", ...
+    arguments}) to a solver, the reference driver or a GrowthOracle -- all
+    three name the calls add_uniform_growth / add_ring_growth /
+    add_grid_growth."""
+    for f in fns:
+        kw = {k: v for k, v in f.items() if k != "kind"}
+        getattr(obj, "add_" + f.get("kind", "grid") + "_growth")(**kw)
+
+
+def mixed_case():
+    """Tissue and functions of the steps_growth_functions fixture: a 3-layer
+    sheet with a uniform function turned by 0.7 rad in the apical 60 %, a
+    ring, a grid function, and a second ring from t = 60 s in the basal 70 %,
+    applied in this order after the per-element rates."""
+    t = mesh.config_tiny(seed=23, n=7, n_layers=3, eta=20.0)
+    ra, aa = mesh.grid_growth_inputs(34, 4, 4)
+    fns = [dict(kind="uniform", rates=[3e-5, 1e-5, -2e-6], angle_rad=0.7, zmin=0.0, zmax=0.6),
+           dict(kind="ring", centre=(14.3, 12.1), inner_radius=4.0, outer_radius=19.0, rates=[5e-5, 2e-5, 0.0],
+                angle_rad=-0.4),
+           dict(kind="grid", rates=ra, angles_deg=aa),
+           dict(kind="ring", centre=(2.0, 30.0), inner_radius=0.0, outer_radius=25.0, rates=[1e-5, 4e-5, 1e-6],
+                init_time=60.0, zmin=0.3, zmax=1.0)]
+    return t, fns
 
 
 def fixture_case(name):
@@ -353,3 +443,6 @@ def fixture_case(name):
         ra, aa = mesh.grid_growth_inputs(33, 4, 4)
         return t, [dict(rates=ra, angles_deg=aa, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0)], 0, True
     raise KeyError(name)
+
+
+GridGrowthOracle = GrowthOracle

@@ -296,6 +296,11 @@ class Ref:
             L.tfr_pack_forces.argtypes = [C.c_void_p, _dp]
             L.tfr_add_grid_growth.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, C.c_void_p, C.c_double,
                                               C.c_double, C.c_double, C.c_double]
+            L.tfr_add_uniform_growth.argtypes = [C.c_void_p, _dp, C.c_double, C.c_double, C.c_double, C.c_double,
+                                                 C.c_double]
+            L.tfr_add_ring_growth.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double, _dp,
+                                              C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]
+            L.tfr_clear_growth_functions.argtypes = [C.c_void_p]
             L.tfr_set_grid_mode.argtypes = [C.c_void_p, C.c_int, C.c_int]
             L.tfr_repin_grid_growth.argtypes = [C.c_void_p]
             L.tfr_set_time.argtypes = [C.c_void_p, C.c_double]
@@ -435,6 +440,18 @@ class Ref:
         self.lib().tfr_add_grid_growth(self.h, r.shape[0], r.shape[1], r.reshape(-1),
                                        None if a is None else a.ctypes.data_as(C.c_void_p),
                                        init_time, end_time, zmin, zmax)
+
+    def add_uniform_growth(self, rates, angle_rad=0.0, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0):
+        self.lib().tfr_add_uniform_growth(self.h, _f64(rates).reshape(3), angle_rad, init_time, end_time, zmin,
+                                          zmax)
+
+    def add_ring_growth(self, centre, inner_radius, outer_radius, rates, angle_rad=0.0, init_time=-1e30,
+                        end_time=1e30, zmin=0.0, zmax=1.0):
+        self.lib().tfr_add_ring_growth(self.h, float(centre[0]), float(centre[1]), inner_radius, outer_radius,
+                                       _f64(rates).reshape(3), angle_rad, init_time, end_time, zmin, zmax)
+
+    def clear_growth_functions(self):
+        self.lib().tfr_clear_growth_functions(self.h)
 
     def set_grid_mode(self, interpolation=1, pinned=False):
         self.lib().tfr_set_grid_mode(self.h, int(interpolation), 1 if pinned else 0)

@@ -24,10 +24,13 @@
 //     calculatePackingForcesImplicit3D :7149-7203,
 //     calculatePackingJacobian3D :7205-7300 and addPackingForces :8869-8900,
 //     in the order runOneStep / updateStepNR call them;
-//   * grid-based growth functions (tfr_add_grid_growth): the reference's own
-//     GridBasedGrowthFunction (GrowthFunctionTypes.h) applied by
-//     ShapeBase::calculateFgFromGridCorners as calculateGrowthGridBased
-//     does (Simulation.cpp:10065-10114), with calculateTissueHeight
+//   * growth functions (tfr_add_*_growth): the reference's own
+//     UniformGrowthFunction, RingGrowthFunction and GridBasedGrowthFunction
+//     (GrowthFunctionTypes.h) applied as calculateGrowth does
+//     (Simulation.cpp:9651-9666): calculateGrowthUniform :9757-9799,
+//     calculateGrowthRing :9801-9885 and calculateGrowthGridBased
+//     :10065-10114 (ShapeBase::calculateFgFromRates /
+//     calculateFgFromGridCorners), with calculateTissueHeight
 //     :3280-3330, assignInitialZPositions :3367-3371, fillInElementColumnLists
 //     :7612-7624, the bounding-box positions of initiateSystem :630-645 and of
 //     runOneStep :5833-5843, and updateRelativePositionsToApicalPositioning
@@ -62,12 +65,12 @@ public:
     double relZ() const { return initialRelativePositionInZ; }
 };
 
-// Grid-based growth functions and the simulation time (Simulation's
-// GrowthFunctions of type 3, gridGrowthsInterpolationType,
+// Growth functions and the simulation time (Simulation's GrowthFunctions,
+// gridGrowthsInterpolationType,
 // GridGrowthsPinnedOnInitialMesh, TissueHeight(DiscretisationLayers),
 // currSimTimeSec).
 struct GridRef {
-    std::vector<GridBasedGrowthFunction*> fns;
+    std::vector<GrowthFunctionBase*> fns;
     int interp = 1;
     bool pinned = false;
     bool setUp = false;
@@ -347,18 +350,47 @@ void refGridSetup(RefSim* s) {
     for (ShapeBase* e : s->elements) e->setInitialRelativePosInBoundingBox();
 }
 
+// Simulation::calculateGrowthRing (Simulation.cpp:9801-9885) for one
+// element: false when its centre is outside the ring, else the increment of
+// the scaled rates.
+bool refRingIncrement(ShapeBase* el, GrowthFunctionBase* f, double dt, gsl_matrix* inc) {
+    float centre[2];
+    f->getCentre(centre[0], centre[1]);
+    float innerRadius = f->getInnerRadius();
+    float outerRadius = f->getOuterRadius();
+    double maxValues[3];
+    f->getGrowthRate(maxValues);
+    float innerRadius2 = innerRadius * innerRadius;
+    float outerRadius2 = outerRadius * outerRadius;
+    double* c = el->getCentre();
+    double d[2] = {centre[0] - c[0], centre[1] - c[1]};
+    delete[] c;
+    double dmag2 = d[0] * d[0] + d[1] * d[1];
+    if (!(dmag2 > innerRadius2 && dmag2 < outerRadius2)) return false;
+    float distance = pow(dmag2, 0.5);
+    double sf = (1.0 - (distance - innerRadius) / (outerRadius - innerRadius));
+    double growthscale[3] = {maxValues[0] * sf, maxValues[1] * sf, maxValues[2] * sf};
+    el->calculateFgFromRates(dt, growthscale[0], growthscale[1], growthscale[2], f->getShearAngleRotationMatrix(),
+                             inc, 0, f->zMin, f->zMax);
+    return true;
+}
+
 // The growth of one step: cleanUpGrowthRates, the per-element rates as a
-// uniform function, then (with_grid) the grid functions active at the
-// current time (calculateGrowth, Simulation.cpp:9651-9666, after the
-// bounding-box positions of :5833-5843), and growShapeByFg.
-void refGrow(RefSim* s, double dt, const double* rates, bool with_grid) {
+// uniform function, then (with_functions) the growth functions active at the
+// current time in their order (calculateGrowth, Simulation.cpp:9651-9666,
+// after the bounding-box positions of :5833-5843), and growShapeByFg.
+void refGrow(RefSim* s, double dt, const double* rates, bool with_functions) {
     QuietCout q;
     GridRef& g = s->grid;
-    std::vector<GridBasedGrowthFunction*> active;
-    if (with_grid)
-        for (GridBasedGrowthFunction* f : g.fns)
-            if (g.time >= f->initTime && g.time < f->endTime) active.push_back(f);
-    if (!active.empty()) {
+    std::vector<GrowthFunctionBase*> active;
+    bool grid = false;
+    if (with_functions)
+        for (GrowthFunctionBase* f : g.fns)
+            if (g.time >= f->initTime && g.time < f->endTime) {
+                active.push_back(f);
+                grid |= f->Type == 3;
+            }
+    if (grid) {
         refBoundingBox(s);
         refApicalPositioning(s);
     }
@@ -374,14 +406,26 @@ void refGrow(RefSim* s, double dt, const double* rates, bool with_grid) {
         gsl_matrix_set_identity(peri);
         el->calculateFgFromRates(dt, rates[3 * e], rates[3 * e + 1], rates[3 * e + 2], rot, inc, 0, 0.0, 1.0);
         el->updateGrowthIncrement(inc, peri);
-        for (GridBasedGrowthFunction* f : active) {
-            int ix = 0, iy = 0;
-            double fx = 1.0, fy = 1.0;
-            if (g.pinned) el->getInitialRelativePositionInTissueInGridIndex(f->getGridX(), f->getGridY(), ix, iy, fx, fy);
-            else el->getRelativePositionInTissueInGridIndex(f->getGridX(), f->getGridY(), ix, iy, fx, fy);
+        for (GrowthFunctionBase* f : active) {
             gsl_matrix_set_identity(inc);
             gsl_matrix_set_identity(peri);
-            el->calculateFgFromGridCorners(g.interp, dt, f, inc, 0, ix, iy, fx, fy);
+            if (f->Type == 1) {
+                double r[3];
+                f->getGrowthRate(r);
+                el->calculateFgFromRates(dt, r[0], r[1], r[2], f->getShearAngleRotationMatrix(), inc, 0, f->zMin,
+                                         f->zMax);
+            } else if (f->Type == 2) {
+                if (!refRingIncrement(el, f, dt, inc)) continue;
+            } else {
+                GridBasedGrowthFunction* gf = static_cast<GridBasedGrowthFunction*>(f);
+                int ix = 0, iy = 0;
+                double fx = 1.0, fy = 1.0;
+                if (g.pinned)
+                    el->getInitialRelativePositionInTissueInGridIndex(gf->getGridX(), gf->getGridY(), ix, iy, fx, fy);
+                else
+                    el->getRelativePositionInTissueInGridIndex(gf->getGridX(), gf->getGridY(), ix, iy, fx, fy);
+                el->calculateFgFromGridCorners(g.interp, dt, gf, inc, 0, ix, iy, fx, fy);
+            }
             el->updateGrowthIncrement(inc, peri);
         }
         el->growShapeByFg();
@@ -743,6 +787,35 @@ void tfr_pack_forces(void* h, double* f) {
     RefSim* s = static_cast<RefSim*>(h);
     std::copy(s->pk.force.begin(), s->pk.force.end(), f);
 }
+
+// A UniformGrowthFunction over the columnar layer: rates (1/s), xy angle (rad).
+void tfr_add_uniform_growth(void* h, const double* rates, double angle, double t0, double t1, double zmin,
+                            double zmax) {
+    RefSim* s = static_cast<RefSim*>(h);
+    QuietCout q;
+    if (!s->grid.setUp) refGridSetup(s);
+    UniformGrowthFunction* f = new UniformGrowthFunction(static_cast<int>(s->grid.fns.size()), 1, t0, t1, true,
+                                                         false, false, false, rates[0], rates[1], rates[2], angle);
+    f->zMin = zmin;
+    f->zMax = zmax;
+    s->grid.fns.push_back(f);
+}
+
+// A RingGrowthFunction over the columnar layer.
+void tfr_add_ring_growth(void* h, double cx, double cy, double r_in, double r_out, const double* rates,
+                         double angle, double t0, double t1, double zmin, double zmax) {
+    RefSim* s = static_cast<RefSim*>(h);
+    QuietCout q;
+    if (!s->grid.setUp) refGridSetup(s);
+    RingGrowthFunction* f = new RingGrowthFunction(static_cast<int>(s->grid.fns.size()), 2, t0, t1, true, false,
+                                                   false, false, cx, cy, r_in, r_out, rates[0], rates[1], rates[2],
+                                                   angle);
+    f->zMin = zmin;
+    f->zMax = zmax;
+    s->grid.fns.push_back(f);
+}
+
+void tfr_clear_growth_functions(void* h) { static_cast<RefSim*>(h)->grid.fns.clear(); }
 
 // A GridBasedGrowthFunction over the columnar layer: rates[3*(i*ny + j) + k]
 // (1/s), angles_deg[i*ny + j] (NULL: 0), its time window and z range.

@@ -147,16 +147,14 @@ def grid_growth_fixture(name, n_steps):
     then Newton steps with the grid functions and the per-element rates."""
     t, fns, interp, pinned = og.fixture_case(name)
     r = Ref(t)
-    for f in fns:
-        r.add_grid_growth(**f)
+    og.add_functions(r, fns)
     r.set_grid_mode(interp, pinned)
     relz, rel0, rel = r.grid_positions()
     r.grow(t.dt, t.rates)
     Fg_grow = r.get_Fg()[0]
     r.close()
     r = Ref(t)
-    for f in fns:
-        r.add_grid_growth(**f)
+    og.add_functions(r, fns)
     r.set_grid_mode(interp, pinned)
     pos, iters, Fg = [], [], []
     for _ in range(n_steps):
@@ -175,9 +173,33 @@ def grid_growth_fixture(name, n_steps):
                         pinned=pinned, n_fns=len(fns), note=og.fixture_case.__doc__, **extra)
 
 
+def growth_functions_fixture(n_steps):
+    """Newton steps with uniform, ring and grid functions mixed (in their
+    order) after the per-element rates, and one growth update at the initial
+    shape."""
+    t, fns = og.mixed_case()
+    r = Ref(t)
+    og.add_functions(r, fns)
+    r.grow(t.dt, t.rates)
+    Fg_grow = r.get_Fg()[0]
+    r.close()
+    r = Ref(t)
+    og.add_functions(r, fns)
+    pos, iters, Fg = [], [], []
+    for _ in range(n_steps):
+        out = r.step(t.dt, t.rates)
+        pos.append(r.positions())
+        iters.append(out["iters"])
+        Fg.append(r.get_Fg()[0])
+    r.close()
+    np.savez_compressed(os.path.join(HERE, og.MIXED_FIXTURE + ".npz"), Fg_grow=Fg_grow, positions=np.array(pos),
+                        iters=np.array(iters), Fg=np.array(Fg), note=og.mixed_case.__doc__)
+
+
 def grid_fixtures():
     for name in og.FIXTURES:
         grid_growth_fixture(name, 3)
+    growth_functions_fixture(3)
 
 
 def main():

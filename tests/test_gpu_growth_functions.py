@@ -1,11 +1,10 @@
-"""Grid-based growth functions on the GPU (tf_add_grid_growth) against
-fixtures the reference's own GridBasedGrowthFunction and
-ShapeBase::calculateFgFromGridCorners produced (tests/golden/make_golden.py
---only-grid) and against the restatement in oracle/growth.py: bounding-box
-positions bit for bit (the reference's box included), the growth update,
-Newton steps with the grid functions on, the time window, re-pinning, and
-larger sheets where the device box must replay the reference's running
-minimum over 100,000+ nodes."""
+"""Growth functions on the GPU (tf_add_uniform_growth, tf_add_ring_growth,
+tf_add_grid_growth) against fixtures the reference's own growth-function
+classes produced (tests/golden/make_golden.py --only-grid) and against the
+restatement in oracle/growth.py: grid bounding-box positions bit for bit (the
+reference's box included), the growth update, Newton steps with the
+functions on, the time window, re-pinning, and larger sheets where the device
+box must replay the reference's running minimum over 70,000+ nodes."""
 import os
 
 import numpy as np
@@ -17,7 +16,7 @@ from tissuefolding_paperversion_gb300 import api, mesh
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 TOL_POS = 1e-8      # positions after Newton steps, relative to the largest coordinate
-TOL_FG = 1e-14      # growth tensors after one update (FMA contraction on the device)
+TOL_FG = 1e-14      # growth tensors after one update (CUDA exp, sin and cos against the host libm)
 
 
 def _solver(t, fns, interp, pinned, **kw):
@@ -139,7 +138,7 @@ def test_time_window_clear_and_set_time():
         assert np.array_equal(s.get_Fg()[0], F1)
         s.end_step()
         s.time = 150.0
-        s.clear_grid_growth()
+        s.clear_growth_functions()
         s.begin_step(60.0)
         assert np.array_equal(s.get_Fg()[0], F1)
 
@@ -178,3 +177,81 @@ def test_refusals():
     with api.Batch([t, mesh.config_tiny(seed=33, n=4, n_layers=2)]) as b:
         with pytest.raises(api.TfError):
             b.add_grid_growth(rates, ang)
+
+
+def test_mixed_functions_growth_update_matches_the_reference():
+    f = np.load(os.path.join(GOLD, G.MIXED_FIXTURE + ".npz"))
+    t, fns = G.mixed_case()
+    with api.Solver(t) as s:
+        G.add_functions(s, fns)
+        s.set_growth_rates(t.rates)
+        s.begin_step(t.dt)
+        Fg, _ = s.get_Fg()
+    assert np.abs(Fg - f["Fg_grow"]).max() <= TOL_FG
+
+
+def test_mixed_functions_newton_steps_match_the_reference():
+    f = np.load(os.path.join(GOLD, G.MIXED_FIXTURE + ".npz"))
+    t, fns = G.mixed_case()
+    with api.Solver(t) as s:
+        G.add_functions(s, fns)
+        s.set_growth_rates(t.rates)
+        for k in range(f["positions"].shape[0]):
+            out = s.newton_step(t.dt, allow_not_converged=False)
+            ref = f["positions"][k]
+            pos = s.positions()
+            assert np.abs(pos - ref).max() <= TOL_POS * np.abs(ref).max(), (k, np.abs(pos - ref).max())
+            assert out["iters"] == f["iters"][k], (k, out["iters"])
+            assert np.abs(s.get_Fg()[0] - f["Fg"][k]).max() <= 1e-12, k
+
+
+def test_uniform_function_without_angle_equals_per_element_rates():
+    t = _big_sheet(False)
+    r = np.array([2e-5, -1e-5, 3e-6])
+    with api.Solver(t) as s:
+        s.add_uniform_growth(r)
+        s.begin_step(60.0)
+        Fa, Ia = s.get_Fg()
+    with api.Solver(t) as s:
+        s.set_growth_rates(np.tile(r, t.n_elems))
+        s.begin_step(60.0)
+        Fb, Ib = s.get_Fg()
+    assert np.array_equal(Fa, Fb) and np.array_equal(Ia, Ib)
+
+
+def test_mixed_functions_on_a_large_sheet_match_the_oracle():
+    t = _big_sheet(True)
+    ra, aa = mesh.grid_growth_inputs(12, 7, 9)
+    fns = [dict(kind="ring", centre=(300.0, 250.0), inner_radius=40.0, outer_radius=260.0, rates=[4e-5, 1e-5, 0.0],
+                angle_rad=0.3),
+           dict(kind="grid", rates=ra, angles_deg=aa, zmin=0.25, zmax=1.0),
+           dict(kind="uniform", rates=[1e-5, 2e-5, -3e-6], angle_rad=-1.1, zmin=0.0, zmax=0.5)]
+    rates = np.random.default_rng(4).uniform(0, 1e-5, size=3 * t.n_elems)
+    moved = t.pos + np.random.default_rng(9).uniform(-0.3, 0.3, size=t.pos.shape)
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(o, fns)
+    with api.Solver(t) as s:
+        G.add_functions(s, fns)
+        s.set_growth_rates(rates)
+        s.set_positions(moved)
+        s.begin_step(60.0)
+        Fg, _ = s.get_Fg()
+    ref = o.grow(np.eye(3), moved, 0.0, 60.0, rates)
+    assert np.abs(Fg.reshape(-1, 3, 3) - ref).max() <= TOL_FG
+    sf = G.ring_scale(moved, t.conn, o.fns[0])
+    assert 0 < np.isnan(sf).sum() < t.n_elems
+
+
+def test_function_refusals():
+    t = mesh.config_tiny(seed=34, n=4, n_layers=2)
+    with api.Solver(t) as s:
+        with pytest.raises(api.TfError):
+            s.add_ring_growth((0.0, 0.0), 5.0, 5.0, [1e-5, 1e-5, 0.0])          # r_out must exceed r_in
+        with pytest.raises(api.TfError):
+            s.add_uniform_growth([np.inf, 0.0, 0.0])
+        for _ in range(16):
+            s.add_uniform_growth([1e-6, 1e-6, 0.0])
+        with pytest.raises(api.TfError):
+            s.add_uniform_growth([1e-6, 1e-6, 0.0])                          # at most 16 functions
+        s.clear_growth_functions()
+        s.add_uniform_growth([1e-6, 1e-6, 0.0])

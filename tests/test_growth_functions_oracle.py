@@ -1,7 +1,8 @@
-"""The grid-based growth oracle (oracle/growth.py) pinned against the
+"""The growth-function oracle (oracle/growth.py) pinned against the
 reference: the committed fixtures (made by the reference's own
-GridBasedGrowthFunction and ShapeBase::calculateFgFromGridCorners) and, where
-the reference builds here, the reference driver directly."""
+UniformGrowthFunction, RingGrowthFunction, GridBasedGrowthFunction and
+ShapeBase::calculateFgFromRates / calculateFgFromGridCorners) and, where the
+reference builds here, the reference driver directly."""
 from __future__ import annotations
 
 import math
@@ -147,4 +148,53 @@ def test_repin_matches_the_reference_driver():
     o = G.GridGrowthOracle(t.pos, t.conn, t.node_placement)
     o.repin(moved)
     np.testing.assert_array_equal(rel0, o.state["rel0"])
+    R.close()
+
+
+def test_mixed_functions_match_the_reference():
+    f = np.load(os.path.join(GOLD, G.MIXED_FIXTURE + ".npz"))
+    t, fns = G.mixed_case()
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(o, fns)
+    Fg = o.grow(np.eye(3), t.pos, 0.0, t.dt, t.rates)
+    assert np.abs(Fg.reshape(-1) - f["Fg_grow"]).max() <= 1e-15
+    # every function reaches some prisms and leaves others
+    sf = G.ring_scale(t.pos, t.conn, o.fns[1])
+    assert 0 < np.isnan(sf).sum() < t.n_elems
+    relz = o.state["relz"]
+    assert 0 < (relz <= 0.6).sum() < t.n_elems
+
+
+def test_ring_scale_in_single_precision():
+    t = mesh.config_tiny(seed=5, n=6, n_layers=2)
+    fn = dict(cx=12.3, cy=7.7, rin=3.0, rout=11.0)
+    sf = G.ring_scale(t.pos, t.conn, fn)
+    c = G.centres(t.pos, t.conn)
+    d = np.hypot(c[:, 0] - 12.3, c[:, 1] - 7.7)
+    inside = ~np.isnan(sf)
+    assert ((d > 3.0) & (d < 11.0) == inside).all()
+    # linear from 1 at the inner radius to 0 at the outer one, to float precision
+    assert np.abs(sf[inside] - (1.0 - (d[inside] - 3.0) / 8.0)).max() < 1e-6
+
+
+@ref_only
+def test_mixed_functions_match_the_reference_driver():
+    t, fns = G.mixed_case()
+    R = Ref(t)
+    G.add_functions(R, fns)
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(o, fns)
+    moved = t.pos + np.random.default_rng(3).uniform(-0.3, 0.3, size=t.pos.shape)
+    R.set_positions(moved)
+    for time in (0.0, 60.0):
+        R.time = time
+        F0 = R.get_Fg()[0]
+        R.grow(60.0, t.rates)
+        F1 = R.get_Fg()[0]
+        Fo = o.grow(F0.reshape(-1, 3, 3), moved, time, 60.0, t.rates)
+        assert np.abs(F1.reshape(-1, 3, 3) - Fo).max() <= 1e-15
+    R.clear_growth_functions()
+    F0 = R.get_Fg()[0]
+    R.grow(60.0, np.zeros(3 * t.n_elems))
+    assert np.array_equal(R.get_Fg()[0], F0)
     R.close()

@@ -32,7 +32,8 @@ EXPORTED = [
     "tf_solve_bsr_static", "tf_batch_create", "tf_batch_step", "tf_get_instances", "tf_elements_per_cta",
     "tf_adj_forward", "tf_adj_backward", "tf_adj_free", "tf_multigrid_info", "tf_read_mesh_file",
     "tf_write_frame", "tf_add_K_triplets", "tf_set_dof_bindings", "tf_set_packing", "tf_get_packing",
-    "tf_packing_masses", "tf_add_grid_growth", "tf_clear_grid_growth", "tf_set_grid_growth_mode",
+    "tf_packing_masses", "tf_add_uniform_growth", "tf_add_ring_growth", "tf_add_grid_growth",
+    "tf_clear_growth_functions", "tf_set_grid_growth_mode",
     "tf_repin_grid_growth", "tf_grid_growth_positions", "tf_set_time", "tf_get_time",
 ]
 
@@ -143,8 +144,13 @@ def load(build_if_missing: bool = True):
     L.tf_packing_masses.argtypes = [vp, vp]
     L.tf_add_grid_growth.restype = C.c_int
     L.tf_add_grid_growth.argtypes = [vp, i32, i32, vp, vp, C.c_double, C.c_double, C.c_double, C.c_double]
-    L.tf_clear_grid_growth.restype = C.c_int
-    L.tf_clear_grid_growth.argtypes = [vp]
+    L.tf_add_uniform_growth.restype = C.c_int
+    L.tf_add_uniform_growth.argtypes = [vp, vp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double]
+    L.tf_add_ring_growth.restype = C.c_int
+    L.tf_add_ring_growth.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double, vp, C.c_double,
+                                     C.c_double, C.c_double, C.c_double, C.c_double]
+    L.tf_clear_growth_functions.restype = C.c_int
+    L.tf_clear_growth_functions.argtypes = [vp]
     L.tf_set_grid_growth_mode.restype = C.c_int
     L.tf_set_grid_growth_mode.argtypes = [vp, i32, i32]
     L.tf_repin_grid_growth.restype = C.c_int
@@ -319,6 +325,22 @@ class Solver:
         self._check(self.L.tf_packing_masses(self.h, _ptr(m)), "tf_packing_masses")
         return m
 
+    def add_uniform_growth(self, rates, angle_rad=0.0, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0):
+        """Uniform growth function (type 1): rates (3,) in 1/s oriented by
+        angle_rad in the xy plane."""
+        r = np.ascontiguousarray(rates, dtype=np.float64).reshape(3)
+        self._check(self.L.tf_add_uniform_growth(self.h, _ptr(r), angle_rad, init_time, end_time, zmin, zmax),
+                    "tf_add_uniform_growth")
+
+    def add_ring_growth(self, centre, inner_radius, outer_radius, rates, angle_rad=0.0, init_time=-1e30,
+                        end_time=1e30, zmin=0.0, zmax=1.0):
+        """Ring growth function (type 2): rates (3,) at the inner radius,
+        falling linearly to 0 at the outer radius."""
+        r = np.ascontiguousarray(rates, dtype=np.float64).reshape(3)
+        self._check(self.L.tf_add_ring_growth(self.h, float(centre[0]), float(centre[1]), inner_radius,
+                                              outer_radius, _ptr(r), angle_rad, init_time, end_time, zmin, zmax),
+                    "tf_add_ring_growth")
+
     def add_grid_growth(self, rates, angles_deg=None, init_time=-1e30, end_time=1e30, zmin=0.0, zmax=1.0):
         """Grid-based growth function (growth type 3): rates (nx, ny, 3) in
         1/s at the grid points over the tissue's bounding box, angles_deg
@@ -333,8 +355,8 @@ class Solver:
         self._check(self.L.tf_add_grid_growth(self.h, r.shape[0], r.shape[1], _ptr(r), _ptr(a) if a is not None
                                               else None, init_time, end_time, zmin, zmax), "tf_add_grid_growth")
 
-    def clear_grid_growth(self):
-        self._check(self.L.tf_clear_grid_growth(self.h), "tf_clear_grid_growth")
+    def clear_growth_functions(self):
+        self._check(self.L.tf_clear_growth_functions(self.h), "tf_clear_growth_functions")
 
     def set_grid_growth_mode(self, interpolation=1, pinned_on_initial_mesh=False):
         """interpolation 0: nearest grid point, 1: bilinear (the default);

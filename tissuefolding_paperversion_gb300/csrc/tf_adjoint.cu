@@ -447,8 +447,8 @@ TF_API tf_status tf_adj_forward(tf_handle* h, const double* rate, const double* 
         set_error("tf_adj_forward: the adjoint works on single-mesh handles");
         return TF_BAD_INPUT;
     }
-    if (h->d.nxb > 0 || !h->bind_slave.empty() || h->pk || growth_grid_count(h) > 0) {
-        set_error("tf_adj_forward: added K entries, packing, bound DOFs and grid growth are not differentiated");
+    if (h->d.nxb > 0 || !h->bind_slave.empty() || h->pk || growth_count(h) > 0) {
+        set_error("tf_adj_forward: added K entries, packing, bound DOFs and growth functions are not differentiated");
         return TF_BAD_INPUT;
     }
     if (!(loss_params[3] > 0.0)) {

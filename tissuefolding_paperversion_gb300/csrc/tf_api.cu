@@ -968,23 +968,21 @@ tf_status tf_packing_masses(tf_handle* h, double* mass) {
     return packing_masses(h, mass);
 }
 
-tf_status tf_add_grid_growth(tf_handle* h, int32_t nx, int32_t ny, const double* rates, const double* angles_deg,
-                             double init_time, double end_time, double zmin, double zmax) {
+namespace {
+
+// Common checks of the tf_add_*_growth calls; sets the growth tables up at
+// the first function.
+tf_status growth_prologue(tf_handle* h, const char* what, const double* rates, double t0, double t1, double zmin,
+                          double zmax) {
     TF_TRY(check_handle(h));
-    if (h->d.nseg != 1) return set_error("tf_add_grid_growth: grid growth works on single-mesh handles"), TF_BAD_INPUT;
-    if (nx < 2 || ny < 2 || !rates || (int64_t)nx * ny > (1 << 24))
-        return set_error("tf_add_grid_growth: needs a grid of at least 2 x 2 points and its rates"), TF_BAD_INPUT;
-    for (int64_t k = 0; k < 3 * (int64_t)nx * ny; ++k)
-        if (!std::isfinite(rates[k])) return set_error("tf_add_grid_growth: non-finite rate"), TF_BAD_INPUT;
-    if (angles_deg)
-        for (int64_t k = 0; k < (int64_t)nx * ny; ++k)
-            if (!std::isfinite(angles_deg[k])) return set_error("tf_add_grid_growth: non-finite angle"), TF_BAD_INPUT;
-    if (std::isnan(init_time) || std::isnan(end_time) || !std::isfinite(zmin) || !std::isfinite(zmax))
-        return set_error("tf_add_grid_growth: bad time window or z range"), TF_BAD_INPUT;
-    TF_CUDA(cudaSetDevice(h->device));
+    const std::string w(what);
+    if (h->d.nseg != 1) return set_error(w + ": growth functions work on single-mesh handles"), TF_BAD_INPUT;
+    if (!rates) return set_error(w + ": null rates"), TF_BAD_INPUT;
+    if (std::isnan(t0) || std::isnan(t1) || !std::isfinite(zmin) || !std::isfinite(zmax))
+        return set_error(w + ": bad time window or z range"), TF_BAD_INPUT;
+    if (growth_count(h) >= kMaxGrowthFunctions)
+        return set_error(w + ": at most 16 growth functions per handle"), TF_BAD_INPUT;
     TF_CUDA(cudaStreamSynchronize(h->stream));
-    if (growth_grid_count(h) >= kMaxGridGrowthFunctions)
-        return set_error("tf_add_grid_growth: at most 8 grid growth functions per handle"), TF_BAD_INPUT;
     if (!h->growth) {
         const tf_status s = growth_setup(h);
         if (s != TF_OK) {
@@ -993,14 +991,53 @@ tf_status tf_add_grid_growth(tf_handle* h, int32_t nx, int32_t ny, const double*
             return s;
         }
     }
+    return TF_OK;
+}
+
+bool all_finite(const double* v, int64_t n) {
+    for (int64_t k = 0; k < n; ++k)
+        if (!std::isfinite(v[k])) return false;
+    return true;
+}
+
+}  // namespace
+
+tf_status tf_add_uniform_growth(tf_handle* h, const double* rates, double angle_rad, double init_time,
+                                double end_time, double zmin, double zmax) {
+    TF_TRY(growth_prologue(h, "tf_add_uniform_growth", rates, init_time, end_time, zmin, zmax));
+    if (!all_finite(rates, 3) || !std::isfinite(angle_rad))
+        return set_error("tf_add_uniform_growth: non-finite rate or angle"), TF_BAD_INPUT;
+    return growth_add_uniform(h, rates, angle_rad, init_time, end_time, zmin, zmax);
+}
+
+tf_status tf_add_ring_growth(tf_handle* h, double centre_x, double centre_y, double inner_radius,
+                             double outer_radius, const double* rates, double angle_rad, double init_time,
+                             double end_time, double zmin, double zmax) {
+    TF_TRY(growth_prologue(h, "tf_add_ring_growth", rates, init_time, end_time, zmin, zmax));
+    if (!all_finite(rates, 3) || !std::isfinite(angle_rad) || !std::isfinite(centre_x) || !std::isfinite(centre_y) ||
+        !(inner_radius >= 0.0) || !(outer_radius > inner_radius) || !std::isfinite(outer_radius))
+        return set_error("tf_add_ring_growth: needs finite values and 0 <= inner radius < outer radius"),
+               TF_BAD_INPUT;
+    return growth_add_ring(h, centre_x, centre_y, inner_radius, outer_radius, rates, angle_rad, init_time, end_time,
+                           zmin, zmax);
+}
+
+tf_status tf_add_grid_growth(tf_handle* h, int32_t nx, int32_t ny, const double* rates, const double* angles_deg,
+                             double init_time, double end_time, double zmin, double zmax) {
+    if (nx < 2 || ny < 2 || (int64_t)nx * ny > (1 << 24))
+        return set_error("tf_add_grid_growth: needs a grid of at least 2 x 2 points"), TF_BAD_INPUT;
+    if (rates && !all_finite(rates, 3 * (int64_t)nx * ny))
+        return set_error("tf_add_grid_growth: non-finite rate"), TF_BAD_INPUT;
+    if (angles_deg && !all_finite(angles_deg, (int64_t)nx * ny))
+        return set_error("tf_add_grid_growth: non-finite angle"), TF_BAD_INPUT;
+    TF_TRY(growth_prologue(h, "tf_add_grid_growth", rates, init_time, end_time, zmin, zmax));
     return growth_add_grid(h, nx, ny, rates, angles_deg, init_time, end_time, zmin, zmax);
 }
 
-tf_status tf_clear_grid_growth(tf_handle* h) {
+tf_status tf_clear_growth_functions(tf_handle* h) {
     TF_TRY(check_handle(h));
-    TF_CUDA(cudaSetDevice(h->device));
     TF_CUDA(cudaStreamSynchronize(h->stream));
-    growth_clear_grids(h);
+    growth_clear(h);
     return TF_OK;
 }
 
@@ -1008,14 +1045,14 @@ tf_status tf_set_grid_growth_mode(tf_handle* h, int32_t interpolation, int32_t p
     TF_TRY(check_handle(h));
     if ((interpolation != 0 && interpolation != 1) || (pinned_on_initial_mesh != 0 && pinned_on_initial_mesh != 1))
         return set_error("tf_set_grid_growth_mode: interpolation and pinning are 0 or 1"), TF_BAD_INPUT;
-    if (!h->growth) return set_error("tf_set_grid_growth_mode: no grid growth function added"), TF_BAD_INPUT;
+    if (!h->growth) return set_error("tf_set_grid_growth_mode: no growth function added"), TF_BAD_INPUT;
     growth_set_mode(h, interpolation, pinned_on_initial_mesh);
     return TF_OK;
 }
 
 tf_status tf_repin_grid_growth(tf_handle* h) {
     TF_TRY(check_handle(h));
-    if (!h->growth) return set_error("tf_repin_grid_growth: no grid growth function added"), TF_BAD_INPUT;
+    if (!h->growth) return set_error("tf_repin_grid_growth: no growth function added"), TF_BAD_INPUT;
     TF_CUDA(cudaSetDevice(h->device));
     TF_TRY(growth_repin(h));
     return sync(h);
@@ -1023,7 +1060,7 @@ tf_status tf_repin_grid_growth(tf_handle* h) {
 
 tf_status tf_grid_growth_positions(tf_handle* h, double* rel_z, double* rel_pinned, double* rel_current) {
     TF_TRY(check_handle(h));
-    if (!h->growth) return set_error("tf_grid_growth_positions: no grid growth function added"), TF_BAD_INPUT;
+    if (!h->growth) return set_error("tf_grid_growth_positions: no growth function added"), TF_BAD_INPUT;
     TF_CUDA(cudaSetDevice(h->device));
     return growth_positions(h, rel_z, rel_pinned, rel_current);
 }
@@ -1330,9 +1367,9 @@ tf_status tf_begin_step(tf_handle* h, double dt) {
     h->dt = dt;
     amg_mark_stale(h, 2);  // a new time step: rebuild the multigrid hierarchy at its first solve
     // calculateGrowth (Simulation.cpp:9651-9666): the per-element rates, then
-    // the grid functions active at this time, in one increment per prism
+    // the growth functions active at this time, in one increment per prism
     bool grown = false;
-    TF_TRY(launch_grid_growth(h, &grown));
+    TF_TRY(launch_growth_functions(h, &grown));
     if (!grown && h->have_rates) TF_TRY(launch_growth(h));
     h->in_step = true;
     TF_TRY(launch_viscosity_surfaces(h));

@@ -1,9 +1,20 @@
-// Grid-based growth functions on the device: the reference's growth type 3
-// (GridBasedGrowthFunction, GrowthFunctionTypes.h:266-609), applied every
-// step by Simulation::calculateGrowthGridBased (Simulation.cpp:10065-10114)
-// through ShapeBase::calculateFgFromGridCorners (ShapeBase.cpp:432-562).
+// Growth functions on the device: the reference's GrowthFunctionBase types
+// 1 (uniform), 2 (ring) and 3 (grid-based), GrowthFunctionTypes.h, applied in
+// the order they were added, each in its time window and z range, by one
+// kernel per step that multiplies every prism's growth increment by theirs
+// (Simulation::calculateGrowth, Simulation.cpp:9651-9666, with
+// calculateGrowthUniform :9757-9799, calculateGrowthRing :9801-9885 and
+// calculateGrowthGridBased :10065-10114; ShapeBase::calculateFgFromRates
+// ShapeBase.cpp:396-421, calculateFgFromGridCorners :432-562,
+// updateGrowthIncrement :567-586, growShapeByFg :1215-1251).  The handle's
+// per-element rates (tf_set_growth_rates) act as a uniform function first in
+// the list.
 //
-// A function holds an nx x ny grid of growth rates (x, y, z; 1/s) and xy
+// Uniform: diag(exp(rate dt)) turned by the function's xy angle.  Ring: the
+// same with the rates scaled by 1 - (d - r_in)/(r_out - r_in) for prisms
+// whose centre lies at a distance d in (r_in, r_out) from the ring's centre
+// (the reference keeps centre, radii and d in single precision).  Grid:
+// a function holds an nx x ny grid of growth rates (x, y, z; 1/s) and xy
 // angles (degrees).  Once, on the host (the GridBasedGrowthFunction
 // constructor and preCalculateAnglesForCompatibleAveraging): grid points whose
 // in-plane aspect ratio |rx/ry| (or its inverse) is below 1.1 carry no angle;
@@ -41,7 +52,7 @@ namespace {
 
 constexpr int kT = 256;
 constexpr int kBoxThreads = 1024;        // k_box: one CTA, 32 warps
-constexpr int kMaxGridFns = kMaxGridGrowthFunctions;
+constexpr int kMaxFns = kMaxGrowthFunctions;
 constexpr double kBoxInit = 100000.0;    // calculateBoundingBox's starting corners (+-1e5)
 constexpr double kPi = 3.14159265358979323846;
 
@@ -66,16 +77,26 @@ tf_status put(T** p, const std::vector<T>& v) {
 
 }  // namespace
 
-struct GridGrowth {
-    int nx = 0, ny = 0;
+enum GrowthType { kUniform = 1, kRing = 2, kGrid = 3 };  // GrowthFunctionBase::Type
+
+struct GrowthFn {
+    int type = kGrid;
     double t0 = 0, t1 = 0, zmin = 0, zmax = 1;
+    // uniform and ring: maximum rates (1/s) and the rotation of the xy angle
+    double rate[3] = {0.0, 0.0, 0.0};
+    double R[9] = {1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
+    // ring, in single precision as Simulation::calculateGrowthRing reads them
+    float cx = 0.f, cy = 0.f, rin = 0.f, rout = 0.f;
+    // grid
+    int nx = 0, ny = 0;
     double* cg = nullptr;    // [(nx-1)*(ny-1)][4][3] compatible corner rates
     double* ca = nullptr;    // [(nx-1)*(ny-1)][4] compatible corner angles (rad)
     uint8_t* ce = nullptr;   // [(nx-1)*(ny-1)][4] 1: the corner carries no angle
 };
 
 struct Growth {
-    std::vector<GridGrowth> grids;
+    std::vector<GrowthFn> fns;
+    bool setup = false;       // grid positions set up (first grid function)
     int interp = 1;           // gridGrowthsInterpolationType (Simulation.cpp:146)
     int pinned = 0;           // GridGrowthsPinnedOnInitialMesh (Simulation.cpp:144)
     int layers = 0;           // TissueHeightDiscretisationLayers
@@ -89,7 +110,7 @@ struct Growth {
 
 namespace {
 
-void free_grid(GridGrowth& f) {
+void free_fn(GrowthFn& f) {
     cudaFree(f.cg);
     cudaFree(f.ca);
     cudaFree(f.ce);
@@ -335,21 +356,26 @@ __global__ void k_relpos(int ne, const int* __restrict__ conn, const double* __r
     rel[ne + e] = (c[1] / 6 - box[1]) / box[3];
 }
 
-struct GridFn {
-    int nx, ny;
+struct FnArgs {
+    int type, nx, ny;
     double zmin, zmax;
+    double rate[3];
+    double R[9];
+    float cx, cy, rin, rout;
     const double* cg;
     const double* ca;
     const uint8_t* ce;
 };
 
-struct GridArgs {
+struct GrowArgs {
     int ne, nfn, interp;
     double dt;
     const double* rates;  // [3][ne] per-element rates, or null
-    const double* relz;
-    const double* rel;    // [2][ne]
-    GridFn fn[kMaxGridFns];
+    const int* conn;      // [6][ne]
+    const double* pos;    // node positions of the step's start shape
+    const double* relz;   // [ne] initial relative z
+    const double* rel;    // [2][ne] bounding-box positions (grid functions)
+    FnArgs fn[kMaxFns];
 };
 
 // Products and sums written out with explicit rounding, in the reference's
@@ -369,75 +395,117 @@ __device__ __forceinline__ void mat3_mul(const double* A, const double* B, doubl
         }
 }
 
+// ShapeBase::calculateFgFromRates with tissue weight 1: R diag(exp(r dt)) R^T.
+__device__ __forceinline__ void rates_increment(const double* r, const double* R, double dt, double* inc) {
+    const double d[9] = {exp(r[0] * 1.0 * dt), 0.0, 0.0, 0.0, exp(r[1] * 1.0 * dt), 0.0, 0.0, 0.0,
+                         exp(r[2] * 1.0 * dt)};
+    double t[9];
+    mat3_mul(R, d, t, false);
+    mat3_mul(t, R, inc, true);
+}
+
+// ShapeBase::calculateFgFromGridCorners for a columnar prism (tissue weight 1).
+__device__ void grid_increment(const FnArgs& F, int interp, double rel_x, double rel_y, double dt, double* inc) {
+    // ShapeBase::convertRelativePosToGridIndex
+    const double rx = rel_x * (float)(F.nx - 1), ry = rel_y * (float)(F.ny - 1);
+    int ix = (int)floor(rx), iy = (int)floor(ry);
+    double fx = rx - ix, fy = ry - iy;
+    if (ix >= F.nx - 1) {
+        ix = F.nx - 2;
+        fx = 1.0;
+    } else if (ix < 0) {
+        ix = 0;
+        fx = 0.0;
+    }
+    if (iy >= F.ny - 1) {
+        iy = F.ny - 2;
+        fy = 1.0;
+    } else if (iy < 0) {
+        iy = 0;
+        fy = 0.0;
+    }
+    const size_t cell = (size_t)ix * (F.ny - 1) + iy;
+    const double* g = F.cg + 12 * cell;  // corner c, axis k at g[3c + k]
+    const double* an = F.ca + 4 * cell;
+    const uint8_t* el = F.ce + 4 * cell;
+    const double ux = 1.0 - fx, uy = 1.0 - fy;
+    double growth[3];
+    double angle = 0;
+    if (interp == 0) {
+        const int c = fx > 0.5 ? (fy > 0.5 ? 3 : 1) : (fy > 0.5 ? 2 : 0);
+        for (int k = 0; k < 3; ++k) growth[k] = g[3 * c + k];
+    } else {
+        double fe = 0.0;
+        if (el[0]) fe = add(fe, mul(ux, uy));
+        if (el[1]) fe = add(fe, mul(fx, uy));
+        if (el[2]) fe = add(fe, mul(ux, fy));
+        if (el[3]) fe = add(fe, mul(fx, fy));
+        angle = add(add(add(mul(mul(an[0], ux), uy), mul(mul(an[1], fx), uy)), mul(mul(an[2], ux), fy)),
+                    mul(mul(an[3], fx), fy));
+        if (fe > 0) {
+            if (fe >= 0.9999999) angle = 0.0;
+            else angle /= (1.0 - fe);
+        }
+        for (int k = 0; k < 3; ++k)
+            growth[k] = add(add(add(mul(mul(g[k], ux), uy), mul(mul(g[3 + k], fx), uy)), mul(mul(g[6 + k], ux), fy)),
+                            mul(mul(g[9 + k], fx), fy));
+    }
+    const double d[9] = {exp(growth[0] * dt), 0.0, 0.0, 0.0, exp(growth[1] * dt), 0.0, 0.0, 0.0,
+                         exp(growth[2] * dt)};
+    if (angle != 0.0) {  // R inc R^T, R the rotation by the angle about z
+        const double c = cos(angle), s = sin(angle);
+        const double R[9] = {c, -1.0 * s, 0.0, s, c, 0.0, 0.0, 0.0, 1.0};
+        double t[9];
+        mat3_mul(R, d, t, false);
+        mat3_mul(t, R, inc, true);
+    } else {
+        for (int k = 0; k < 9; ++k) inc[k] = d[k];
+    }
+}
+
 // Per prism: the growth increment of the step -- diag(exp(rate dt)) of the
-// per-element rates, then each active grid function's increment
-// (ShapeBase::calculateFgFromGridCorners, columnar prism, tissue weight 1)
-// multiplied on the left (updateGrowthIncrement) -- and Fg <- increment Fg
-// (growShapeByFg).
-__global__ void k_grid_growth(GridArgs G, double* __restrict__ Fg, double* __restrict__ invFg) {
+// per-element rates, then each active function's increment multiplied on
+// the left (updateGrowthIncrement) -- and Fg <- increment Fg (growShapeByFg).
+__global__ void k_grow(GrowArgs G, double* __restrict__ Fg, double* __restrict__ invFg) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= G.ne) return;
     const int ne = G.ne;
     double M[9] = {1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
     if (G.rates)
         for (int k = 0; k < 3; ++k) M[4 * k] = exp(G.rates[(size_t)k * ne + e] * 1.0 * G.dt);
-    const double rz = G.relz[e];
-    const double rel_x = G.rel[e], rel_y = G.rel[ne + e];
+    bool centred = false;
+    double cx = 0.0, cy = 0.0;
     for (int f = 0; f < G.nfn; ++f) {
-        const GridFn& F = G.fn[f];
-        if (rz < F.zmin || rz > F.zmax) continue;  // isGrowthRateApplicable (ShapeBase.cpp:277-300): identity
-        // ShapeBase::convertRelativePosToGridIndex
-        const double rx = rel_x * (float)(F.nx - 1), ry = rel_y * (float)(F.ny - 1);
-        int ix = (int)floor(rx), iy = (int)floor(ry);
-        double fx = rx - ix, fy = ry - iy;
-        if (ix >= F.nx - 1) {
-            ix = F.nx - 2;
-            fx = 1.0;
-        } else if (ix < 0) {
-            ix = 0;
-            fx = 0.0;
-        }
-        if (iy >= F.ny - 1) {
-            iy = F.ny - 2;
-            fy = 1.0;
-        } else if (iy < 0) {
-            iy = 0;
-            fy = 0.0;
-        }
-        const size_t cell = (size_t)ix * (F.ny - 1) + iy;
-        const double* g = F.cg + 12 * cell;  // corner c, axis k at g[3c + k]
-        const double* an = F.ca + 4 * cell;
-        const uint8_t* el = F.ce + 4 * cell;
-        const double ux = 1.0 - fx, uy = 1.0 - fy;
-        double growth[3];
-        double angle = 0;
-        if (G.interp == 0) {
-            const int c = fx > 0.5 ? (fy > 0.5 ? 3 : 1) : (fy > 0.5 ? 2 : 0);
-            for (int k = 0; k < 3; ++k) growth[k] = g[3 * c + k];
+        const FnArgs& F = G.fn[f];
+        double inc[9];
+        if (F.type == kGrid) {
+            const double rz = G.relz[e];
+            if (rz < F.zmin || rz > F.zmax) continue;  // isGrowthRateApplicable (ShapeBase.cpp:277-300): identity
+            grid_increment(F, G.interp, G.rel[e], G.rel[ne + e], G.dt, inc);
         } else {
-            double fe = 0.0;
-            if (el[0]) fe = add(fe, mul(ux, uy));
-            if (el[1]) fe = add(fe, mul(fx, uy));
-            if (el[2]) fe = add(fe, mul(ux, fy));
-            if (el[3]) fe = add(fe, mul(fx, fy));
-            angle = add(add(add(mul(mul(an[0], ux), uy), mul(mul(an[1], fx), uy)), mul(mul(an[2], ux), fy)),
-                        mul(mul(an[3], fx), fy));
-            if (fe > 0) {
-                if (fe >= 0.9999999) angle = 0.0;
-                else angle /= (1.0 - fe);
+            const double rz = G.relz[e];
+            if (rz < F.zmin || rz > F.zmax) continue;
+            double r[3] = {F.rate[0], F.rate[1], F.rate[2]};
+            if (F.type == kRing) {
+                if (!centred) {  // ShapeBase::getCentre (ShapeBase.cpp:240-250)
+                    for (int a = 0; a < 6; ++a) {
+                        const int n = G.conn[(size_t)a * ne + e];
+                        cx = add(cx, G.pos[3 * (size_t)n]);
+                        cy = add(cy, G.pos[3 * (size_t)n + 1]);
+                    }
+                    cx /= 6;
+                    cy /= 6;
+                    centred = true;
+                }
+                const double dx = (double)F.cx - cx, dy = (double)F.cy - cy;
+                const double d2 = add(mul(dx, dx), mul(dy, dy));
+                const float rin2 = __fmul_rn(F.rin, F.rin), rout2 = __fmul_rn(F.rout, F.rout);
+                if (!(d2 > (double)rin2 && d2 < (double)rout2)) continue;
+                const float dist = __double2float_rn(sqrt(d2));
+                const double sf = 1.0 - (double)__fdiv_rn(__fsub_rn(dist, F.rin), __fsub_rn(F.rout, F.rin));
+                for (int k = 0; k < 3; ++k) r[k] = mul(r[k], sf);
             }
-            for (int k = 0; k < 3; ++k)
-                growth[k] = add(add(add(mul(mul(g[k], ux), uy), mul(mul(g[3 + k], fx), uy)), mul(mul(g[6 + k], ux), fy)),
-                                mul(mul(g[9 + k], fx), fy));
-        }
-        double inc[9] = {exp(growth[0] * G.dt), 0.0, 0.0, 0.0, exp(growth[1] * G.dt), 0.0, 0.0, 0.0,
-                         exp(growth[2] * G.dt)};
-        if (angle != 0.0) {  // R inc R^T, R the rotation by the angle about z
-            const double c = cos(angle), s = sin(angle);
-            const double R[9] = {c, -1.0 * s, 0.0, s, c, 0.0, 0.0, 0.0, 1.0};
-            double t[9];
-            mat3_mul(R, inc, t, false);
-            mat3_mul(t, R, inc, true);
+            rates_increment(r, F.R, G.dt, inc);
         }
         double P[9];
         mat3_mul(inc, M, P, false);
@@ -468,7 +536,7 @@ tf_status launch_relpos(tf_handle* h, double* rel_out) {
 
 void growth_free(Growth* g) {
     if (!g) return;
-    for (auto& f : g->grids) free_grid(f);
+    for (auto& f : g->fns) free_fn(f);
     void* ptrs[] = {g->relz, g->rel0, g->rel, g->colsrc, g->box};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -539,15 +607,57 @@ tf_status growth_setup(tf_handle* h) {
     return TF_OK;
 }
 
-tf_status growth_add_grid(tf_handle* h, int nx, int ny, const double* rates, const double* angles_deg, double t0,
-                          double t1, double zmin, double zmax) {
-    GridGrowth f;
-    f.nx = nx;
-    f.ny = ny;
+namespace {
+
+// The rotation of GrowthFunctionBase's xy angle (UniformGrowthFunction /
+// RingGrowthFunction constructors, GrowthFunctionTypes.h:37-52, :196-211).
+void angle_rotation(double angle, double* R) {
+    const double c = std::cos(angle), s = std::sin(angle);
+    const double r[9] = {c, -1.0 * s, 0.0, s, c, 0.0, 0.0, 0.0, 1.0};
+    for (int k = 0; k < 9; ++k) R[k] = r[k];
+}
+
+GrowthFn window(double t0, double t1, double zmin, double zmax) {
+    GrowthFn f;
     f.t0 = static_cast<float>(t0);  // GrowthFunctionBase keeps its times as float
     f.t1 = static_cast<float>(t1);
     f.zmin = zmin;
     f.zmax = zmax;
+    return f;
+}
+
+}  // namespace
+
+tf_status growth_add_uniform(tf_handle* h, const double* rates, double angle, double t0, double t1, double zmin,
+                             double zmax) {
+    GrowthFn f = window(t0, t1, zmin, zmax);
+    f.type = kUniform;
+    for (int k = 0; k < 3; ++k) f.rate[k] = rates[k];
+    angle_rotation(angle, f.R);
+    h->growth->fns.push_back(f);
+    return TF_OK;
+}
+
+tf_status growth_add_ring(tf_handle* h, double cx, double cy, double r_in, double r_out, const double* rates,
+                          double angle, double t0, double t1, double zmin, double zmax) {
+    GrowthFn f = window(t0, t1, zmin, zmax);
+    f.type = kRing;
+    for (int k = 0; k < 3; ++k) f.rate[k] = rates[k];
+    angle_rotation(angle, f.R);
+    f.cx = static_cast<float>(cx);  // RingGrowthFunction::getCentre / getInnerRadius / getOuterRadius
+    f.cy = static_cast<float>(cy);
+    f.rin = static_cast<float>(r_in);
+    f.rout = static_cast<float>(r_out);
+    h->growth->fns.push_back(f);
+    return TF_OK;
+}
+
+tf_status growth_add_grid(tf_handle* h, int nx, int ny, const double* rates, const double* angles_deg, double t0,
+                          double t1, double zmin, double zmax) {
+    GrowthFn f = window(t0, t1, zmin, zmax);
+    f.type = kGrid;
+    f.nx = nx;
+    f.ny = ny;
     std::vector<double> cg, ca;
     std::vector<uint8_t> ce;
     compatible_corners(nx, ny, rates, angles_deg, cg, ca, ce);
@@ -555,17 +665,17 @@ tf_status growth_add_grid(tf_handle* h, int nx, int ny, const double* rates, con
     if (s == TF_OK) s = put(&f.ca, ca);
     if (s == TF_OK) s = put(&f.ce, ce);
     if (s != TF_OK) {
-        free_grid(f);
+        free_fn(f);
         return s;
     }
-    h->growth->grids.push_back(f);
+    h->growth->fns.push_back(f);
     return TF_OK;
 }
 
-void growth_clear_grids(tf_handle* h) {
+void growth_clear(tf_handle* h) {
     if (!h->growth) return;
-    for (auto& f : h->growth->grids) free_grid(f);
-    h->growth->grids.clear();
+    for (auto& f : h->growth->fns) free_fn(f);
+    h->growth->fns.clear();
 }
 
 void growth_set_mode(tf_handle* h, int interp, int pinned) {
@@ -577,32 +687,50 @@ void growth_set_mode(tf_handle* h, int interp, int pinned) {
 // bounding-box positions become the pinned ones.
 tf_status growth_repin(tf_handle* h) { return launch_relpos(h, h->growth->rel0); }
 
-int growth_grid_count(const tf_handle* h) { return h->growth ? static_cast<int>(h->growth->grids.size()) : 0; }
+int growth_count(const tf_handle* h) { return h->growth ? static_cast<int>(h->growth->fns.size()) : 0; }
 
-// The growth of a step when grid functions are active at the handle's time
-// (Simulation.cpp:10068): per-element rates and grid functions in one
-// increment per prism.  *done = false: no grid function is active, the
+// The growth of a step when growth functions are active at the handle's time
+// (each in init_time <= t < end_time): the per-element rates and the active
+// functions in one increment per prism.  *done = false: none is active, the
 // per-element rates alone apply.
-tf_status launch_grid_growth(tf_handle* h, bool* done) {
+tf_status launch_growth_functions(tf_handle* h, bool* done) {
     *done = false;
     Growth* g = h->growth;
-    if (!g || g->grids.empty()) return TF_OK;
+    if (!g || g->fns.empty()) return TF_OK;
     Device& d = h->d;
     const double t = h->time;
-    GridArgs A{};
+    GrowArgs A{};
     A.ne = d.ne;
     A.interp = g->interp;
     A.dt = h->dt;
     A.rates = h->have_rates ? d.rates : nullptr;
+    A.conn = d.conn;
+    A.pos = d.uk;
     A.relz = g->relz;
     A.rel = g->pinned ? g->rel0 : g->rel;
-    for (const auto& f : g->grids) {
+    bool grid = false;
+    for (const auto& f : g->fns) {
         if (!(t >= f.t0 && t < f.t1)) continue;
-        A.fn[A.nfn++] = GridFn{f.nx, f.ny, f.zmin, f.zmax, f.cg, f.ca, f.ce};
+        FnArgs& F = A.fn[A.nfn++];
+        F.type = f.type;
+        F.nx = f.nx;
+        F.ny = f.ny;
+        F.zmin = f.zmin;
+        F.zmax = f.zmax;
+        for (int k = 0; k < 3; ++k) F.rate[k] = f.rate[k];
+        for (int k = 0; k < 9; ++k) F.R[k] = f.R[k];
+        F.cx = f.cx;
+        F.cy = f.cy;
+        F.rin = f.rin;
+        F.rout = f.rout;
+        F.cg = f.cg;
+        F.ca = f.ca;
+        F.ce = f.ce;
+        grid |= f.type == kGrid;
     }
     if (A.nfn == 0) return TF_OK;
-    if (!g->pinned) GR_TRY(launch_relpos(h, g->rel));
-    k_grid_growth<<<cdiv(d.ne, kT), kT, 0, h->stream>>>(A, d.Fg, d.invFg);
+    if (grid && !g->pinned) GR_TRY(launch_relpos(h, g->rel));
+    k_grow<<<cdiv(d.ne, kT), kT, 0, h->stream>>>(A, d.Fg, d.invFg);
     TF_LAUNCH_CHECK(h);
     *done = true;
     return TF_OK;

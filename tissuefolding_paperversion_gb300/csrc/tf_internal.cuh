@@ -162,7 +162,7 @@ constexpr int kAmgMaxLevels = 10;
 
 struct Amg;      // multigrid hierarchy (tf_amg.cu)
 struct Packing;  // packing between tissue surfaces (tf_packing.cu)
-struct Growth;   // grid-based growth functions (tf_growth.cu)
+struct Growth;   // growth functions (tf_growth.cu)
 
 // Inverse of a 3x3 matrix (row-major) by cofactors.
 __device__ __forceinline__ void inv3_cof(const double* M, double* inv) {
@@ -282,7 +282,7 @@ struct tf_handle {
     int last_iters[2] = {0, 0};                 // iterations of the last solve per method (chunk planning)
     tf::Amg* amg = nullptr;                     // multigrid preconditioner (null: block-Jacobi)
     tf::Packing* pk = nullptr;                  // packing between tissue surfaces (null: off)
-    tf::Growth* growth = nullptr;               // grid-based growth functions (null: none added yet)
+    tf::Growth* growth = nullptr;               // growth functions (null: none added yet)
     double time = 0.0;                          // simulation time (currSimTimeSec), advanced by tf_end_step
     bool in_step = false;                       // between tf_begin_step and tf_end_step
     std::vector<double> h_pos0;                 // node positions of the mesh at creation
@@ -335,15 +335,19 @@ tf_status packing_relink(tf_handle* h);          // couple blocks in the current
 // as X_{l+1} = P^T X_l P).
 bool use_multigrid(const tf_handle* h);
 void packing_free(Packing* p);
-tf_status growth_setup(tf_handle* h);           // grid growth tables from the mesh at creation
+tf_status growth_setup(tf_handle* h);           // growth-function tables from the mesh at creation
+constexpr int kMaxGrowthFunctions = 16;         // growth functions per handle
+tf_status growth_add_uniform(tf_handle* h, const double* rates, double angle, double t0, double t1, double zmin,
+                             double zmax);
+tf_status growth_add_ring(tf_handle* h, double cx, double cy, double r_in, double r_out, const double* rates,
+                          double angle, double t0, double t1, double zmin, double zmax);
 tf_status growth_add_grid(tf_handle* h, int nx, int ny, const double* rates, const double* angles_deg, double t0,
                           double t1, double zmin, double zmax);
-void growth_clear_grids(tf_handle* h);
+void growth_clear(tf_handle* h);
 void growth_set_mode(tf_handle* h, int interp, int pinned);
 tf_status growth_repin(tf_handle* h);
-int growth_grid_count(const tf_handle* h);
-constexpr int kMaxGridGrowthFunctions = 8;      // grid growth functions per handle
-tf_status launch_grid_growth(tf_handle* h, bool* done);  // rates + the grid functions active at h->time
+int growth_count(const tf_handle* h);
+tf_status launch_growth_functions(tf_handle* h, bool* done);  // rates + the functions active at h->time
 tf_status growth_positions(tf_handle* h, double* relz, double* rel0, double* rel);
 void growth_free(Growth* g);
 tf_status upload_extra(tf_handle* h, bool pattern_changed);
