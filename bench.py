@@ -527,6 +527,75 @@ def run_packing(args):
     }))
 
 
+def growth_functions_for(t):
+    """A uniform function turned in the xy plane in the apical half, a ring
+    and a grid function over the sheet, as a model file would set them."""
+    from tissuefolding_paperversion_gb300 import mesh
+
+    p = t.pos.reshape(-1, 3)
+    lo, hi = p.min(axis=0), p.max(axis=0)
+    ra, aa = mesh.grid_growth_inputs(1, 12, 9, scale=2e-5)
+    return [dict(kind="uniform", rates=[1e-5, 5e-6, 0.0], angle_rad=0.6, zmin=0.0, zmax=0.5),
+            dict(kind="ring", centre=((lo[0] + hi[0]) / 2, (lo[1] + hi[1]) / 2), inner_radius=0.1 * (hi[0] - lo[0]),
+                 outer_radius=0.45 * (hi[0] - lo[0]), rates=[2e-5, 2e-5, 0.0], angle_rad=0.0),
+            dict(kind="grid", rates=ra, angles_deg=aa)]
+
+
+def run_growth(args, t):
+    """The per-step growth update with growth functions of the three reference
+    types (uniform, ring, grid on the current shape) against the per-element
+    rates alone; the CPU baseline is the numpy restatement of the reference's
+    calculateGrowth on the same sheet."""
+    from tissuefolding_paperversion_gb300 import api
+
+    fns = growth_functions_for(t)
+    times = {}
+    with api.Solver(t) as s:
+        s.set_growth_rates(t.rates)
+        for with_fns in (False, True):
+            if with_fns:
+                for f in fns:
+                    kw = {k: v for k, v in f.items() if k != "kind"}
+                    getattr(s, "add_" + f["kind"] + "_growth")(**kw)
+            for _ in range(args.warmup):
+                s.begin_step(t.dt)
+                s.end_step()
+            w = []
+            for _ in range(max(args.steps, 5)):
+                w0 = time.perf_counter()
+                s.begin_step(t.dt)
+                s.end_step()                   # synchronises the stream
+                w.append(time.perf_counter() - w0)
+            times[with_fns] = float(np.median(w))
+        l0 = s.launch_count()
+        s.begin_step(t.dt)
+        s.end_step()
+        launches = s.launch_count() - l0
+    extra_s = max(times[True] - times[False], 1e-9)
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import growth as og
+        o = og.GrowthOracle(t.pos, t.conn, t.node_placement)
+        og.add_functions(o, fns)
+        w0 = time.perf_counter()
+        o.grow(np.eye(3), t.pos, 0.0, t.dt, t.rates)
+        cpu_s = time.perf_counter() - w0
+        cpu = {"value": t.n_elems / cpu_s, "unit": "prisms/s", "cores": 1, "kind": "port",
+               "sample": f"numpy restatement of calculateGrowth on all {t.n_elems} prisms, {cpu_s:.2f} s"}
+    print(json.dumps({
+        "metric": "growth update with uniform + ring + grid functions, prisms/s", "value": t.n_elems / times[True],
+        "unit": "prisms/s", "n_gpus": 1, "steps": max(args.steps, 5), "warmup": args.warmup,
+        "ms_per_step": times[True] * 1e3, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"growth-functions-{t.n_elems}", "prisms": t.n_elems, "nodes": t.n_nodes,
+                   "functions": [f["kind"] for f in fns]},
+        "begin_step_ms": {"rates_only": times[False] * 1e3, "with_functions": times[True] * 1e3},
+        "functions_extra_ms": extra_s * 1e3,
+        "timing": "host wall clock around begin_step + end_step (synchronous), median of the timed steps",
+        "gpu_launches": launches,
+        "cpu_baseline": cpu,
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -534,10 +603,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="large", choices=["large", "medium", "small", "wing"])
-    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint", "packing"],
+    ap.add_argument("--workload", default="plain", choices=["plain", "batch", "adjoint", "packing", "growth"],
                     help="plain: the 320k-prism Newton step; batch: the 256-instance sweep; "
                          "adjoint: gradient of an apical shape loss through n steps; "
-                         "packing: couple detection between two facing sheets")
+                         "packing: couple detection between two facing sheets; "
+                         "growth: the per-step growth update with uniform, ring and grid functions")
     ap.add_argument("--pack-n", type=int, default=200, help="nodes per side of each sheet (packing workload)")
     ap.add_argument("--adj-steps", type=int, default=50)
     ap.add_argument("--adj-every", type=int, default=10)
@@ -572,6 +642,9 @@ def main():
         return
     if args.workload == "adjoint":
         run_adjoint(args, t)
+        return
+    if args.workload == "growth":
+        run_growth(args, t)
         return
     if args.impl == "reference":
         run_reference(args, t)

@@ -14,7 +14,8 @@ Follows, in TissueFolding/TissueFolding/SourceCode/:
     apical (and, for prisms with a basal node, basal) side length, and the
     detection grid, whose only populated cell is [0][0] (prism centres lie
     inside the bounding box, at fractions in [0, 1));
-  * Simulation::calculateBoundingBox (Simulation.cpp:9148-9185);
+  * Simulation::calculateBoundingBox (Simulation.cpp:9148-9185), with its
+    running "else if" (oracle/growth.py bounding_box);
   * Simulation::detectPacingNodes (Simulation.cpp:8167-8440): couples of
     packing-eligible nodes (Node::checkIfNodeHasPacking, Node.cpp:133-150:
     mass > 0, apical or basal) on the same surface, not neighbours, closer
@@ -27,6 +28,8 @@ Follows, in TissueFolding/TissueFolding/SourceCode/:
 from __future__ import annotations
 
 import numpy as np
+
+from oracle.growth import bounding_box
 
 MULTIPLIER = 5000.0      # packingMultiplier (Simulation.cpp:8187)
 SATURATION = 5.0         # sigmoidSaturationForPacking (:8188)
@@ -130,8 +133,7 @@ def detect(pos, conn, placement, masses, drop_last_segment=True, masters=None, n
     col, g00 = side_lengths(pos, conn, placement)
     r = 0.4 * g00
     t2_00 = r * r
-    bb0 = P.min(axis=0)
-    bbs = P.max(axis=0) - bb0
+    bb0, bbs = bounding_box(P)
     eligible = (masses != 0) & ((pl == 0) | (pl == 1))
     if nb is None:
         nb = neighbours(conn, nn)

@@ -97,6 +97,25 @@ def test_cell_list_finds_the_couples_of_the_full_scan(seed, n, merge):
     assert abs(got["threshold"] - want["threshold"]) <= 1e-13 * want["threshold"]
 
 
+@pytest.mark.parametrize("seed,n", [(8, 9), (9, 40)])
+def test_reference_box_when_node_0_holds_the_maximum(seed, n):
+    """Node 0 alone at the largest x: the device box replays the reference's
+    running minimum, so the couples are the reference's."""
+    t = mesh.config_facing_sheets(seed=seed, n=n, gap=1.5, E=100000.0, offset=(0.4, 0.2))
+    t = mesh.swap_nodes(t, 0, int(np.argmax(t.pos.reshape(-1, 3)[:, 0])))
+    t.pos[0] += 0.3
+    vref = op.reference_volumes(t.pos.reshape(-1, 3)[t.conn.reshape(-1, 6)])
+    m = op.node_masses(t.conn, t.n_nodes, vref, np.tile(np.eye(3), (t.n_elems, 1, 1)))
+    want = op.detect(t.pos, t.conn, t.node_placement, m, True)
+    with api.Solver(t) as s:
+        s.set_packing(True, reference_merge=True)
+        s.begin_step(t.dt)
+        got = s.packing()
+    assert len(want["nodes"]) > 0
+    np.testing.assert_array_equal(got["nodes"], want["nodes"])
+    np.testing.assert_allclose(got["w"], want["w"], rtol=0, atol=1e-15)
+
+
 def test_multigrid_sees_the_couples():
     # without the couples' coarse images the V-cycle's coarse correction misses
     # the stiff coupling between the sheets and the solve diverges; with them

@@ -98,3 +98,35 @@ def test_restatement_matches_the_reference_driver_when_present():
                 np.testing.assert_array_equal(r.node_masses(), _masses(t))
         finally:
             r.close()
+
+
+def _node0_at_max_x(t):
+    """The same sheets renumbered so that node 0 alone holds the largest x."""
+    t = mesh.swap_nodes(t, 0, int(np.argmax(t.pos.reshape(-1, 3)[:, 0])))
+    t.pos[0] += 0.3
+    return t
+
+
+def test_reference_box_when_node_0_holds_the_maximum():
+    """The reference's bounding box never tests node 0 for the maximum; the
+    restatement keeps that, and it changes which first nodes find couples."""
+    from oracle.oracle import Ref
+    from oracle.growth import bounding_box
+
+    t = _node0_at_max_x(mesh.config_facing_sheets(seed=8, n=9, gap=1.5, E=100000.0, offset=(0.4, 0.2)))
+    p = t.pos.reshape(-1, 3)
+    lo, size = bounding_box(p)
+    assert lo[0] + size[0] < p[:, 0].max()
+    want = op.detect(t.pos, t.conn, t.node_placement, _masses(t), True)
+    assert len(want["nodes"]) > 0 and 0 not in want["nodes"][:, 0]
+    if not Ref.available():
+        pytest.skip("reference checkout not present")
+    r = Ref(t)
+    try:
+        r.set_packing(True, True)
+        r.pack_detect()
+        got = r.packing()
+        np.testing.assert_array_equal(got["nodes"], want["nodes"])
+        np.testing.assert_array_equal(got["w"], want["w"])
+    finally:
+        r.close()

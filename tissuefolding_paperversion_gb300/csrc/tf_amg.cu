@@ -723,28 +723,26 @@ __device__ __forceinline__ bool seg_stopped(const double* scal, int seg) {
 }
 
 // Sum of one value over the grid: partials per CTA, the last CTA to arrive
-// adds them in CTA order (no waiting).  True in thread 0 of that CTA.
+// folds them in a fixed order, all its threads at once (no waiting).  True in
+// thread 0 of that CTA.
 __device__ bool grid_sum(double v, double* part, unsigned* ticket, double* total) {
-    __shared__ double sm[kT / 32];
+    __shared__ double sm[1][kT / 32 + 1];
     __shared__ bool last;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) sm[warp] = v;
-    __syncthreads();
+    double x[1] = {v};
+    cta_sum<kT, 1>(x, sm);
     if (threadIdx.x == 0) {
-        double b = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += sm[w];
-        part[blockIdx.x] = b;
+        part[blockIdx.x] = x[0];
         __threadfence();
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (!last || threadIdx.x != 0) return false;
+    if (!last) return false;
     __threadfence();
-    double t = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) t += __ldcg(&part[b]);
-    *total = t;
+    double t[1] = {0.0};
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) t[0] += __ldcg(&part[b]);
+    cta_sum<kT, 1>(t, sm);
+    if (threadIdx.x != 0) return false;
+    *total = t[0];
     *ticket = 0u;
     return true;
 }

@@ -51,9 +51,8 @@ namespace tf {
 namespace {
 
 constexpr int kT = 256;
-constexpr int kBoxThreads = 1024;        // k_box: one CTA, 32 warps
+constexpr int kBoxCtas = 2 * 152;        // k_box: two CTAs per SM
 constexpr int kMaxFns = kMaxGrowthFunctions;
-constexpr double kBoxInit = 100000.0;    // calculateBoundingBox's starting corners (+-1e5)
 constexpr double kPi = 3.14159265358979323846;
 
 #define GR_TRY(expr)                \
@@ -106,6 +105,8 @@ struct Growth {
     double* rel = nullptr;    // [2][ne] positions at the current step's start
     int* colsrc = nullptr;    // [ne] the prism whose position a prism takes
     double* box = nullptr;    // [4] min x, min y, size x, size y
+    double* part = nullptr;   // [kBoxCtas][4] k_box's per-CTA partials
+    unsigned* ticket = nullptr;  // k_box's arrival counter (0 between launches)
 };
 
 namespace {
@@ -137,8 +138,8 @@ int element_placement(const tf_handle* h, int e) {
 void host_box(const double* pos, int nn, double lo[3], double size[3]) {
     double hi[3];
     for (int k = 0; k < 3; ++k) {
-        lo[k] = kBoxInit;
-        hi[k] = -kBoxInit;
+        lo[k] = kBoxCorner;
+        hi[k] = -kBoxCorner;
     }
     for (int i = 0; i < nn; ++i)
         for (int k = 0; k < 3; ++k) {
@@ -263,79 +264,49 @@ void compatible_corners(int nx, int ny, const double* rates, const double* angle
 
 // ---- device ---------------------------------------------------------------
 
-// Min (or max) over the CTA's 1024 threads, returned to every thread.
-__device__ double cta_reduce(double v, bool take_max, double* red) {
+// calculateBoundingBox in x and y on the device, bit for bit: per-CTA
+// minima over all nodes and maxima over nodes 1.., folded in CTA order by the
+// last CTA to arrive (no waiting), which settles node 0
+// (reference_box_max) and writes min x, min y, size x, size y.
+__global__ void __launch_bounds__(kT) k_box(int nn, const double* __restrict__ pos, double* __restrict__ part,
+                                            unsigned* __restrict__ ticket, double* __restrict__ box) {
+    constexpr int kind[4] = {1, 1, 2, 2};
+    __shared__ double sm[4][kT / 32 + 1];
+    __shared__ double scan[kT];
+    __shared__ bool last;
+    double v[4] = {INFINITY, INFINITY, -INFINITY, -INFINITY};  // min x, min y, max x, max y (nodes 1..)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += gridDim.x * blockDim.x) {
+        const double x = pos[3 * (size_t)i], y = pos[3 * (size_t)i + 1];
+        v[0] = fmin(v[0], x);
+        v[1] = fmin(v[1], y);
+        if (i > 0) {
+            v[2] = fmax(v[2], x);
+            v[3] = fmax(v[3], y);
+        }
+    }
+    cta_combine<kT, 4>(v, kind, sm);
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 4; ++q) part[4 * (size_t)blockIdx.x + q] = v[q];
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double f[4] = {INFINITY, INFINITY, -INFINITY, -INFINITY};
+    for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x)
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double w = __shfl_down_sync(0xffffffffu, v, o);
-        v = take_max ? fmax(v, w) : fmin(v, w);
-    }
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        v = red[threadIdx.x];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double w = __shfl_down_sync(0xffffffffu, v, o);
-            v = take_max ? fmax(v, w) : fmin(v, w);
-        }
-        if (threadIdx.x == 0) red[32] = v;
-    }
-    __syncthreads();
-    const double r = red[32];
-    __syncthreads();
-    return r;
-}
-
-// calculateBoundingBox in x and y on the device, bit for bit.  The minimum is
-// min(1e5, all nodes).  The maximum is that of the nodes that did not lower
-// the running minimum: whenever the largest coordinate is reached by a node
-// other than node 0 that is the plain maximum (such a node cannot have
-// lowered the minimum below node 0's); only when node 0 alone holds it does a
-// second pass replay the running minimum (per-thread chunks in node order,
-// an exclusive min-scan over the chunks, then the chunks walked in order).
-__global__ void __launch_bounds__(kBoxThreads) k_box(int nn, const double* __restrict__ pos, double* __restrict__ box) {
-    __shared__ double red[33];
-    __shared__ double scan[kBoxThreads];
-    double lo[2], hi[2];
-    const int t = threadIdx.x;
-    for (int k = 0; k < 2; ++k) {
-        double mn = kBoxInit, mx = -kBoxInit;
-        for (int i = t; i < nn; i += kBoxThreads) {
-            const double p = pos[3 * (size_t)i + k];
-            mn = fmin(mn, p);
-            if (i > 0) mx = fmax(mx, p);
-        }
-        lo[k] = cta_reduce(mn, false, red);
-        hi[k] = cta_reduce(mx, true, red);
-        if (nn > 0 && pos[k] > hi[k]) {  // node 0 alone holds the largest coordinate (uniform branch)
-            const int chunk = (nn + kBoxThreads - 1) / kBoxThreads;
-            const int i0 = min(nn, t * chunk), i1 = min(nn, i0 + chunk);
-            double cm = INFINITY;
-            for (int i = i0; i < i1; ++i) cm = fmin(cm, pos[3 * (size_t)i + k]);
-            scan[t] = cm;
-            __syncthreads();
-            for (int o = 1; o < kBoxThreads; o <<= 1) {
-                const double v = t >= o ? scan[t - o] : INFINITY;
-                __syncthreads();
-                scan[t] = fmin(scan[t], v);
-                __syncthreads();
-            }
-            double run = t > 0 ? fmin(kBoxInit, scan[t - 1]) : kBoxInit;
-            double up = -kBoxInit;
-            for (int i = i0; i < i1; ++i) {
-                const double p = pos[3 * (size_t)i + k];
-                if (p < run) run = p;
-                else if (p > up) up = p;
-            }
-            hi[k] = cta_reduce(up, true, red);
-        }
-    }
-    if (t == 0) {
-        box[0] = lo[0];
-        box[1] = lo[1];
-        box[2] = hi[0] - lo[0];
-        box[3] = hi[1] - lo[1];
+        for (int q = 0; q < 4; ++q) f[q] = combine_as(kind[q], f[q], __ldcg(&part[4 * (size_t)c + q]));
+    cta_combine<kT, 4>(f, kind, sm);
+    if (threadIdx.x == 0) *ticket = 0u;
+    const double lox = fmin(f[0], kBoxCorner), loy = fmin(f[1], kBoxCorner);  // calculateBoundingBox's corners
+    const double hx = reference_box_max<kT>(nn, pos, 0, f[2], scan);
+    const double hy = reference_box_max<kT>(nn, pos, 1, f[3], scan);
+    if (threadIdx.x == 0) {
+        box[0] = lox;
+        box[1] = loy;
+        box[2] = hx - lox;
+        box[3] = hy - loy;
     }
 }
 
@@ -374,34 +345,60 @@ struct GrowArgs {
     const int* conn;      // [6][ne]
     const double* pos;    // node positions of the step's start shape
     const double* relz;   // [ne] initial relative z
-    const double* rel;    // [2][ne] bounding-box positions (grid functions)
+    const double* rel;    // [2][ne] pinned bounding-box positions, or null: from box and colsrc
+    const double* box;    // [4] this step's box (grid functions, current positions)
+    const int* colsrc;    // [ne] the prism whose position a prism takes
     FnArgs fn[kMaxFns];
 };
 
 // Products and sums written out with explicit rounding, in the reference's
-// order of operations (left to right; gsl_blas_dgemm accumulating over k from
-// 0), so that no multiply-add is contracted into an FMA.  Where almost all of
+// order of operations (left to right; its 3x3 products accumulating over k
+// from 0), so that no multiply-add is contracted into an FMA.  Where almost all of
 // a cell's corners carry no angle the interpolated angle is divided by a
 // small 1 - fe, which magnifies any rounding difference.
 __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 
-__device__ __forceinline__ void mat3_mul(const double* A, const double* B, double* C, bool transB) {
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) {
-            double acc = 0.0;
-            for (int k = 0; k < 3; ++k) acc = add(acc, mul(A[3 * i + k], transB ? B[3 * j + k] : B[3 * k + j]));
-            C[3 * i + j] = acc;
-        }
+// Every growth increment here turns about z only, so increments and their
+// products keep the form [[a, b, 0], [c, d, 0], [0, 0, e]]; the reference's
+// 3x3 products of such matrices add exact zero products, left out here.
+__device__ __forceinline__ void mul_xy_z(const double* A, const double* B, double* C) {
+    C[0] = add(mul(A[0], B[0]), mul(A[1], B[3]));
+    C[1] = add(mul(A[0], B[1]), mul(A[1], B[4]));
+    C[3] = add(mul(A[3], B[0]), mul(A[4], B[3]));
+    C[4] = add(mul(A[3], B[1]), mul(A[4], B[4]));
+    C[8] = mul(A[8], B[8]);
+    C[2] = C[5] = C[6] = C[7] = 0.0;
 }
 
-// ShapeBase::calculateFgFromRates with tissue weight 1: R diag(exp(r dt)) R^T.
+// M Fg for an increment M of that form and a general Fg.
+__device__ __forceinline__ void mul_xy_z_full(const double* M, const double* F, double* C) {
+    for (int j = 0; j < 3; ++j) {
+        C[j] = add(mul(M[0], F[j]), mul(M[1], F[3 + j]));
+        C[3 + j] = add(mul(M[3], F[j]), mul(M[4], F[3 + j]));
+        C[6 + j] = mul(M[8], F[6 + j]);
+    }
+}
+
+// R diag(d0, d1, d2) R^T for R = [[c, -s, 0], [s, c, 0], [0, 0, 1]], the two
+// 3x3 products of the reference with their exact zero terms left out (adding
+// a zero product changes no sum): T = R D has one product per entry, and each
+// in-plane entry of T R^T is one sum of two products.
+__device__ __forceinline__ void rotate_diag(double c, double s, double d0, double d1, double d2, double* inc) {
+    const double ms = -1.0 * s;
+    const double t00 = mul(c, d0), t01 = mul(ms, d1), t10 = mul(s, d0), t11 = mul(c, d1);
+    inc[0] = add(mul(t00, c), mul(t01, ms));
+    inc[1] = add(mul(t00, s), mul(t01, c));
+    inc[3] = add(mul(t10, c), mul(t11, ms));
+    inc[4] = add(mul(t10, s), mul(t11, c));
+    inc[2] = inc[5] = inc[6] = inc[7] = 0.0;
+    inc[8] = d2;
+}
+
+// ShapeBase::calculateFgFromRates with tissue weight 1: R diag(exp(r dt)) R^T,
+// R the function's rotation about z (R[0] = cos, R[3] = sin).
 __device__ __forceinline__ void rates_increment(const double* r, const double* R, double dt, double* inc) {
-    const double d[9] = {exp(r[0] * 1.0 * dt), 0.0, 0.0, 0.0, exp(r[1] * 1.0 * dt), 0.0, 0.0, 0.0,
-                         exp(r[2] * 1.0 * dt)};
-    double t[9];
-    mat3_mul(R, d, t, false);
-    mat3_mul(t, R, inc, true);
+    rotate_diag(R[0], R[3], exp(r[0] * 1.0 * dt), exp(r[1] * 1.0 * dt), exp(r[2] * 1.0 * dt), inc);
 }
 
 // ShapeBase::calculateFgFromGridCorners for a columnar prism (tissue weight 1).
@@ -450,16 +447,14 @@ __device__ void grid_increment(const FnArgs& F, int interp, double rel_x, double
             growth[k] = add(add(add(mul(mul(g[k], ux), uy), mul(mul(g[3 + k], fx), uy)), mul(mul(g[6 + k], ux), fy)),
                             mul(mul(g[9 + k], fx), fy));
     }
-    const double d[9] = {exp(growth[0] * dt), 0.0, 0.0, 0.0, exp(growth[1] * dt), 0.0, 0.0, 0.0,
-                         exp(growth[2] * dt)};
+    const double d0 = exp(growth[0] * dt), d1 = exp(growth[1] * dt), d2 = exp(growth[2] * dt);
     if (angle != 0.0) {  // R inc R^T, R the rotation by the angle about z
-        const double c = cos(angle), s = sin(angle);
-        const double R[9] = {c, -1.0 * s, 0.0, s, c, 0.0, 0.0, 0.0, 1.0};
-        double t[9];
-        mat3_mul(R, d, t, false);
-        mat3_mul(t, R, inc, true);
+        rotate_diag(cos(angle), sin(angle), d0, d1, d2, inc);
     } else {
-        for (int k = 0; k < 9; ++k) inc[k] = d[k];
+        for (int k = 0; k < 9; ++k) inc[k] = 0.0;
+        inc[0] = d0;
+        inc[4] = d1;
+        inc[8] = d2;
     }
 }
 
@@ -473,15 +468,32 @@ __global__ void k_grow(GrowArgs G, double* __restrict__ Fg, double* __restrict__
     double M[9] = {1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0};
     if (G.rates)
         for (int k = 0; k < 3; ++k) M[4 * k] = exp(G.rates[(size_t)k * ne + e] * 1.0 * G.dt);
-    bool centred = false;
-    double cx = 0.0, cy = 0.0;
+    bool centred = false, have_rel = false;
+    double cx = 0.0, cy = 0.0, rel_x = 0.0, rel_y = 0.0;
     for (int f = 0; f < G.nfn; ++f) {
         const FnArgs& F = G.fn[f];
         double inc[9];
         if (F.type == kGrid) {
             const double rz = G.relz[e];
             if (rz < F.zmin || rz > F.zmax) continue;  // isGrowthRateApplicable (ShapeBase.cpp:277-300): identity
-            grid_increment(F, G.interp, G.rel[e], G.rel[ne + e], G.dt, inc);
+            if (!have_rel) {
+                if (G.rel) {
+                    rel_x = G.rel[e];
+                    rel_y = G.rel[ne + e];
+                } else {  // as k_relpos computes it
+                    const int sp = G.colsrc[e];
+                    double c[2] = {0.0, 0.0};
+                    for (int a = 0; a < 6; ++a) {
+                        const int n = G.conn[(size_t)a * ne + sp];
+                        c[0] += G.pos[3 * (size_t)n];
+                        c[1] += G.pos[3 * (size_t)n + 1];
+                    }
+                    rel_x = (c[0] / 6 - G.box[0]) / G.box[2];
+                    rel_y = (c[1] / 6 - G.box[1]) / G.box[3];
+                }
+                have_rel = true;
+            }
+            grid_increment(F, G.interp, rel_x, rel_y, G.dt, inc);
         } else {
             const double rz = G.relz[e];
             if (rz < F.zmin || rz > F.zmax) continue;
@@ -508,12 +520,12 @@ __global__ void k_grow(GrowArgs G, double* __restrict__ Fg, double* __restrict__
             rates_increment(r, F.R, G.dt, inc);
         }
         double P[9];
-        mat3_mul(inc, M, P, false);
+        mul_xy_z(inc, M, P);
         for (int k = 0; k < 9; ++k) M[k] = P[k];
     }
     double F0[9], out[9], inv[9];
     for (int k = 0; k < 9; ++k) F0[k] = Fg[(size_t)k * ne + e];
-    mat3_mul(M, F0, out, false);
+    mul_xy_z_full(M, F0, out);
     inv3_cof(out, inv);
     for (int k = 0; k < 9; ++k) {
         Fg[(size_t)k * ne + e] = out[k];
@@ -525,7 +537,7 @@ __global__ void k_grow(GrowArgs G, double* __restrict__ Fg, double* __restrict__
 tf_status launch_relpos(tf_handle* h, double* rel_out) {
     Growth* g = h->growth;
     Device& d = h->d;
-    k_box<<<1, kBoxThreads, 0, h->stream>>>(d.nn, d.uk, g->box);
+    k_box<<<kBoxCtas, kT, 0, h->stream>>>(d.nn, d.uk, g->part, g->ticket, g->box);
     TF_LAUNCH_CHECK(h);
     k_relpos<<<cdiv(d.ne, kT), kT, 0, h->stream>>>(d.ne, d.conn, d.uk, g->box, g->colsrc, rel_out);
     TF_LAUNCH_CHECK(h);
@@ -537,7 +549,7 @@ tf_status launch_relpos(tf_handle* h, double* rel_out) {
 void growth_free(Growth* g) {
     if (!g) return;
     for (auto& f : g->fns) free_fn(f);
-    void* ptrs[] = {g->relz, g->rel0, g->rel, g->colsrc, g->box};
+    void* ptrs[] = {g->relz, g->rel0, g->rel, g->colsrc, g->box, g->part, g->ticket};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete g;
@@ -604,6 +616,8 @@ tf_status growth_setup(tf_handle* h) {
     GR_TRY(put(&g->rel, std::vector<double>(2 * (size_t)ne, 0.0)));
     GR_TRY(put(&g->colsrc, colsrc));
     GR_TRY(put(&g->box, std::vector<double>(4, 0.0)));
+    GR_TRY(put(&g->part, std::vector<double>(4 * (size_t)kBoxCtas, 0.0)));
+    GR_TRY(put(&g->ticket, std::vector<unsigned>(1, 0u)));
     return TF_OK;
 }
 
@@ -707,7 +721,9 @@ tf_status launch_growth_functions(tf_handle* h, bool* done) {
     A.conn = d.conn;
     A.pos = d.uk;
     A.relz = g->relz;
-    A.rel = g->pinned ? g->rel0 : g->rel;
+    A.rel = g->pinned ? g->rel0 : nullptr;
+    A.box = g->box;
+    A.colsrc = g->colsrc;
     bool grid = false;
     for (const auto& f : g->fns) {
         if (!(t >= f.t0 && t < f.t1)) continue;
@@ -729,7 +745,10 @@ tf_status launch_growth_functions(tf_handle* h, bool* done) {
         grid |= f.type == kGrid;
     }
     if (A.nfn == 0) return TF_OK;
-    if (grid && !g->pinned) GR_TRY(launch_relpos(h, g->rel));
+    if (grid && !g->pinned) {  // this step's box; k_grow forms the positions
+        k_box<<<kBoxCtas, kT, 0, h->stream>>>(d.nn, d.uk, g->part, g->ticket, g->box);
+        TF_LAUNCH_CHECK(h);
+    }
     k_grow<<<cdiv(d.ne, kT), kT, 0, h->stream>>>(A, d.Fg, d.invFg);
     TF_LAUNCH_CHECK(h);
     *done = true;

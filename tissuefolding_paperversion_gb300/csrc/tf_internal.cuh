@@ -182,6 +182,99 @@ __device__ __forceinline__ void inv3_cof(const double* M, double* inv) {
     inv[8] = (M[0] * M[4] - M[1] * M[3]) * r;
 }
 
+// Values combined over a CTA of NT threads: kind[q] 0 sum, 1 min, 2 max; warp
+// shuffles, then warp 0 over the warps' values (fixed order: deterministic);
+// every thread gets the results in v.  A dependent chain of FP64 operations
+// costs on the order of 100 cycles per step on this part, so no fold here
+// runs on one thread alone.  sm: shared scratch of N x (NT/32 + 1) doubles.
+__device__ __forceinline__ double combine_as(int kind, double a, double b) {
+    return kind == 0 ? a + b : (kind == 1 ? fmin(a, b) : fmax(a, b));
+}
+__device__ __forceinline__ double identity_of(int kind) {
+    return kind == 0 ? 0.0 : (kind == 1 ? INFINITY : -INFINITY);
+}
+template <int NT, int N>
+__device__ __forceinline__ void cta_combine(double (&v)[N], const int (&kind)[N], double (*sm)[NT / 32 + 1]) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+        double x = v[q];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x = combine_as(kind[q], x, __shfl_down_sync(0xffffffffu, x, o));
+        if (lane == 0) sm[q][warp] = x;
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int q = 0; q < N; ++q) {
+            double x = lane < NT / 32 ? sm[q][lane] : identity_of(kind[q]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x = combine_as(kind[q], x, __shfl_down_sync(0xffffffffu, x, o));
+            if (lane == 0) sm[q][NT / 32] = x;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < N; ++q) v[q] = sm[q][NT / 32];
+    __syncthreads();
+}
+
+// Sums over the CTA (cta_combine with every kind a sum).
+template <int NT, int N>
+__device__ __forceinline__ void cta_sum(double (&v)[N], double (*sm)[NT / 32 + 1]) {
+    int kind[N];
+#pragma unroll
+    for (int q = 0; q < N; ++q) kind[q] = 0;
+    cta_combine<NT, N>(v, kind, sm);
+}
+
+// Simulation::calculateBoundingBox (Simulation.cpp:9148-9185) starts its
+// corners at +-1e5 and tests a node for the maximum only when the node did
+// not lower the running minimum (a running "else if").  A node other than 0
+// that holds the largest coordinate never lowers it, so given hi1, the
+// maximum over nodes 1.., the reference's maximum on axis k is hi1 -- unless
+// node 0 alone holds the largest coordinate; then the CTA replays the running
+// minimum: per-thread chunks in node order, an exclusive min-scan over the
+// chunks, the chunks walked in order.  Every thread of the CTA (NT threads)
+// calls it with the same hi1; scan is NT doubles of shared memory.
+constexpr double kBoxCorner = 100000.0;
+
+template <int NT>
+__device__ double reference_box_max(int nn, const double* __restrict__ pos, int k, double hi1, double* scan) {
+    if (nn <= 0 || !(pos[k] > hi1)) return fmax(hi1, -kBoxCorner);
+    const int t = threadIdx.x;
+    const int chunk = (nn + NT - 1) / NT;
+    const int i0 = min(nn, t * chunk), i1 = min(nn, i0 + chunk);
+    double cm = INFINITY;
+    for (int i = i0; i < i1; ++i) cm = fmin(cm, pos[3 * (size_t)i + k]);
+    __syncthreads();
+    scan[t] = cm;
+    __syncthreads();
+    for (int o = 1; o < NT; o <<= 1) {
+        const double v = t >= o ? scan[t - o] : INFINITY;
+        __syncthreads();
+        scan[t] = fmin(scan[t], v);
+        __syncthreads();
+    }
+    double run = t > 0 ? fmin(kBoxCorner, scan[t - 1]) : kBoxCorner;
+    double up = -kBoxCorner;
+    for (int i = i0; i < i1; ++i) {
+        const double p = pos[3 * (size_t)i + k];
+        if (p < run) run = p;
+        else if (p > up) up = p;
+    }
+    __syncthreads();
+    scan[t] = up;
+    __syncthreads();
+    for (int o = NT / 2; o > 0; o >>= 1) {
+        if (t < o) scan[t] = fmax(scan[t], scan[t + o]);
+        __syncthreads();
+    }
+    const double r = scan[0];
+    __syncthreads();
+    return r;
+}
+
 // Programmatic dependent launch for the chains of short kernels of the
 // linear solve: a kernel launched with launch_pdl may be scheduled as its
 // predecessor's blocks exit, hiding the launch gap; pdl_enter makes it wait

@@ -235,23 +235,9 @@ __device__ __forceinline__ double side_avg(const double* __restrict__ p, const i
     return c > 0 ? s / c : s;
 }
 
-// Block-wide sum (deterministic: fixed shuffle and warp order).
-__device__ double block_sum(double v, double* sm) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    __syncthreads();
-    if (lane == 0) sm[warp] = v;
-    __syncthreads();
-    double t = 0.0;
-    if (threadIdx.x == 0)
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sm[k];
-    return t;
-}
-
 // Side-length sums and the bounding box over the whole grid: per-CTA
-// partials, folded in CTA order by the last CTA to arrive (no waiting), which
-// writes the detection parameters.
+// partials, folded in a fixed order by the last CTA to arrive (no waiting),
+// which writes the detection parameters.
 constexpr int kParCtas = 2 * 152;
 constexpr int kPart = 7;  // dsum, count, grid sum, min x, min y, max x, max y
 
@@ -259,8 +245,7 @@ __global__ void __launch_bounds__(kT) k_pk_params(int nn, int ne, const double* 
                                                   const int* __restrict__ conn, const uint8_t* __restrict__ ebasal,
                                                   double* __restrict__ part, unsigned* __restrict__ ticket,
                                                   double* __restrict__ par) {
-    __shared__ double sm[kT / 32];
-    __shared__ double smn[2][kT / 32], smx[2][kT / 32];
+    __shared__ double sm[kPart][kT / 32 + 1];
     __shared__ bool last;
     double ds = 0.0, dn = 0.0, gs = 0.0;
     const int stride = gridDim.x * blockDim.x;
@@ -279,68 +264,47 @@ __global__ void __launch_bounds__(kT) k_pk_params(int nn, int ne, const double* 
         }
         gs += v;
     }
+    // the box's maximum over nodes 1.. (node 0 is settled in the fold)
     double mn[2] = {INFINITY, INFINITY}, mx[2] = {-INFINITY, -INFINITY};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += stride)
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
             mn[k] = fmin(mn[k], pos[3 * i + k]);
-            mx[k] = fmax(mx[k], pos[3 * i + k]);
+            if (i > 0) mx[k] = fmax(mx[k], pos[3 * i + k]);
         }
-    const double tds = block_sum(ds, sm), tdn = block_sum(dn, sm), tgs = block_sum(gs, sm);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 2; ++k) {
-        double a = mn[k], b = mx[k];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            a = fmin(a, __shfl_down_sync(0xffffffffu, a, o));
-            b = fmax(b, __shfl_down_sync(0xffffffffu, b, o));
-        }
-        if (lane == 0) {
-            smn[k][warp] = a;
-            smx[k][warp] = b;
-        }
-    }
-    __syncthreads();
+    constexpr int kind[kPart] = {0, 0, 0, 1, 1, 2, 2};
+    double v[kPart] = {ds, dn, gs, mn[0], mn[1], mx[0], mx[1]};
+    cta_combine<kT, kPart>(v, kind, sm);
     if (threadIdx.x == 0) {
-        double* pp = part + (size_t)kPart * blockIdx.x;
-        pp[0] = tds;
-        pp[1] = tdn;
-        pp[2] = tgs;
-        for (int k = 0; k < 2; ++k) {
-            double a = INFINITY, b = -INFINITY;
-            for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
-                a = fmin(a, smn[k][q]);
-                b = fmax(b, smx[k][q]);
-            }
-            pp[3 + k] = a;
-            pp[5 + k] = b;
-        }
+        for (int q = 0; q < kPart; ++q) part[(size_t)kPart * blockIdx.x + q] = v[q];
         __threadfence();
         last = atomicAdd(ticket, 1u) == gridDim.x - 1;
     }
     __syncthreads();
-    if (!last || threadIdx.x != 0) return;
+    if (!last) return;
+    __shared__ double scan[kT];
     __threadfence();
-    double t[kPart] = {0.0, 0.0, 0.0, INFINITY, INFINITY, -INFINITY, -INFINITY};
-    for (unsigned c = 0; c < gridDim.x; ++c) {
-        const double* pp = part + (size_t)kPart * c;
-        for (int k = 0; k < 3; ++k) t[k] += __ldcg(&pp[k]);
-        for (int k = 0; k < 2; ++k) {
-            t[3 + k] = fmin(t[3 + k], __ldcg(&pp[3 + k]));
-            t[5 + k] = fmax(t[5 + k], __ldcg(&pp[5 + k]));
-        }
-    }
-    *ticket = 0u;
-    const double col = t[0] / t[1];
-    const double g00 = 0.4 * (t[2] / ne);
+    // fold: each thread its CTAs in order, then the fixed-order CTA combine
+    double fold[kPart] = {0.0, 0.0, 0.0, INFINITY, INFINITY, -INFINITY, -INFINITY};
+    for (int c = threadIdx.x; c < (int)gridDim.x; c += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < kPart; ++q) fold[q] = combine_as(kind[q], fold[q], __ldcg(&part[(size_t)kPart * c + q]));
+    cta_combine<kT, kPart>(fold, kind, sm);
+    if (threadIdx.x == 0) *ticket = 0u;
+    fold[3] = fmin(fold[3], kBoxCorner);  // calculateBoundingBox's corners
+    fold[4] = fmin(fold[4], kBoxCorner);
+    const double hx = reference_box_max<kT>(nn, pos, 0, fold[5], scan);
+    const double hy = reference_box_max<kT>(nn, pos, 1, fold[6], scan);
+    if (threadIdx.x != 0) return;
+    const double col = fold[0] / fold[1];
+    const double g00 = 0.4 * (fold[2] / ne);
     par[P_THR] = 0.4 * col;
     par[P_DET] = g00;
     par[P_T2] = g00 * g00;
-    par[P_BB0X] = t[3];
-    par[P_BB0Y] = t[4];
-    par[P_BBSX] = t[5] - t[3];
-    par[P_BBSY] = t[6] - t[4];
+    par[P_BB0X] = fold[3];
+    par[P_BB0Y] = fold[4];
+    par[P_BBSX] = hx - fold[3];
+    par[P_BBSY] = hy - fold[4];
     par[P_CELL] = g00 * (1.0 + 1e-9);  // cells a hair wider than the distance: no pair is missed by rounding
 }
 

@@ -55,33 +55,29 @@ struct SCtx {
 
 template <int NV>
 __device__ bool s_reduce(const SCtx& c, double (&v)[NV], double (&tot)[NV]) {
-    __shared__ double sm[NV][kStaticThreads / 32];
+    __shared__ double sm[NV][kStaticThreads / 32 + 1];
     __shared__ bool last;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int k = 0; k < NV; ++k) {
-        double x = v[k];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) sm[k][warp] = x;
-    }
-    __syncthreads();
+    double x[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) x[k] = v[k];
+    cta_sum<kStaticThreads, NV>(x, sm);
     if (threadIdx.x == 0) {
-        for (int k = 0; k < NV; ++k) {
-            double x = 0.0;
-            for (int w = 0; w < kStaticThreads / 32; ++w) x += sm[k][w];
-            c.part()[k * gridDim.x + blockIdx.x] = x;
-        }
+        for (int k = 0; k < NV; ++k) c.part()[k * gridDim.x + blockIdx.x] = x[k];
         __threadfence();
         last = atomicAdd(c.ticket(), 1u) == gridDim.x - 1;
     }
     __syncthreads();
     if (!last) return false;
     __threadfence();
+    // all threads of the last CTA fold the partials (fixed order)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        x[k] = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) x[k] += __ldcg(&c.part()[k * gridDim.x + b]);
+    }
+    cta_sum<kStaticThreads, NV>(x, sm);
     if (threadIdx.x == 0) {
-        for (int k = 0; k < NV; ++k) {
-            double x = 0.0;
-            for (unsigned b = 0; b < gridDim.x; ++b) x += __ldcg(&c.part()[k * gridDim.x + b]);
-            tot[k] = x;
-        }
+        for (int k = 0; k < NV; ++k) tot[k] = x[k];
         *c.ticket() = 0u;
     }
     return true;
