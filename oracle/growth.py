@@ -3,6 +3,9 @@
 INFRASTRUCTURE ONLY: imported by tests/, never by the library.
 
 Follows, in TissueFolding/TissueFolding/SourceCode/:
+  * ShapeBase::CalculateGrowthRotationByF (ShapeBase.cpp:1656-1810), called
+    every step while growth functions exist (Simulation.cpp:5872-5876), and
+    the rotated increment of growShapeByFg (:1216-1225);
   * Simulation::calculateGrowth (Simulation.cpp:9651-9666) with
     calculateGrowthUniform (:9757-9799) and calculateGrowthRing (:9801-9885):
     ShapeBase::calculateFgFromRates (ShapeBase.cpp:396-421), R diag(exp(r dt))
@@ -321,15 +324,62 @@ def ring_scale(pos, conn, fn):
     return np.where(inside, 1.0 - frac.astype(np.float64), np.nan)
 
 
+def shape_derivatives():
+    """(6, 3, 6) derivatives of the prism's shape functions at its 6 Gauss
+    points with respect to the parametric coordinates
+    (Prism::setShapeFunctionDerivatives, Prism.cpp:655-680; Gauss points of
+    the Prism constructor, :123-148)."""
+    s = 1.0 / math.pow(3, 0.5)
+    pts = [(1 / 6, 1 / 6, s), (2 / 3, 1 / 6, s), (1 / 6, 2 / 3, s), (1 / 6, 1 / 6, -s), (2 / 3, 1 / 6, -s),
+           (1 / 6, 2 / 3, -s)]
+    out = np.zeros((6, 3, 6))
+    for p, (eta, nu, zeta) in enumerate(pts):
+        al, be, lam = (1 - zeta) / 2, (1 + zeta) / 2, 1 - eta - nu
+        out[p] = [[-al, al, 0, -be, be, 0], [-al, 0, al, -be, 0, be],
+                  [-lam / 2, -eta / 2, -nu / 2, lam / 2, eta / 2, nu / 2]]
+    return out
+
+
+def growth_rotations(pos, conn, inv_dXde):
+    """ShapeBase::CalculateGrowthRotationByF per prism: (rotated (E,), Rz (E, 3, 3)).
+    The Gauss-weighted deformation gradient of the current shape
+    (calculateTriPointFForRatation, ShapeBase.cpp:1674-1687, with
+    Prism::calculateCurrTriPointFForRotation, Prism.cpp:730-744), its rotation
+    U V^T from the singular value decomposition (calculate3DRotMatFromF,
+    ShapeBase.cpp:1731-1810: rotated if an off-diagonal entry exceeds 0.017),
+    and the angle about z (disassembleRotationMatrixForZ, :1690-1721)."""
+    x = np.asarray(pos, dtype=np.float64).reshape(-1, 3)[np.asarray(conn).reshape(-1, 6)]
+    dN = shape_derivatives()
+    F = np.zeros((x.shape[0], 3, 3))
+    for gp in range(6):
+        Jt = np.einsum("ra,eac->erc", dN[gp], x)
+        Fgp = np.transpose(Jt, (0, 2, 1)) @ inv_dXde[:, gp]
+        F = F + Fgp * (1.0 / 6.0)
+    U, _, Vt = np.linalg.svd(F)
+    R = U @ Vt
+    off = np.abs(R - np.eye(3) * np.diagonal(R, axis1=1, axis2=2)[:, :, None]).max(axis=(1, 2)) > 0.017
+    tz = np.arctan2(R[:, 0, 1], R[:, 0, 0])
+    rot = off & (np.abs(tz) > 0.017)
+    c, s = np.cos(tz), np.sin(tz)
+    Rz = np.zeros((x.shape[0], 3, 3))
+    Rz[:, 0, 0], Rz[:, 0, 1], Rz[:, 1, 0], Rz[:, 1, 1], Rz[:, 2, 2] = c, -1.0 * s, s, c, 1.0
+    return rot, Rz
+
+
 class GrowthOracle:
     """Growth functions on one tissue: the state the reference keeps for them."""
 
-    def __init__(self, pos0, conn, node_placement):
+    def __init__(self, pos0, conn, node_placement, ref_pos=None):
         self.conn = np.asarray(conn).reshape(-1, 6)
         self.state = initial_state(pos0, self.conn, node_placement)
         self.fns = []
         self.interp = 1
         self.pinned = False
+        X = (np.asarray(pos0, dtype=np.float64).reshape(-1, 3)[self.conn] if ref_pos is None
+             else np.asarray(ref_pos, dtype=np.float64).reshape(-1, 6, 3))
+        dN = shape_derivatives()
+        self.inv_dXde = np.stack([np.linalg.inv(np.transpose(np.einsum("ra,eac->erc", dN[gp], X), (0, 2, 1)))
+                                  for gp in range(6)], axis=1)
 
     @staticmethod
     def _window(init_time, end_time, zmin, zmax):
@@ -365,9 +415,9 @@ class GrowthOracle:
             r = np.asarray(rates, dtype=np.float64).reshape(-1, 3)
             for k in range(3):
                 total[:, k, k] = np.exp(r[:, k] * 1.0 * dt)
-        active = [f for f in self.fns if f["t0"] <= time < f["t1"]]
-        if not active:
+        if not self.fns:
             return total
+        active = [f for f in self.fns if f["t0"] <= time < f["t1"]]
         rel = self.state["rel0"] if self.pinned else relative_positions(pos, self.conn, self.state["src"])
         relz = self.state["relz"]
         for f in active:
@@ -383,6 +433,10 @@ class GrowthOracle:
                 inc = rates_increment(r, f["R"], dt)
                 inc[~keep] = np.eye(3)
             total = dgemm3(inc, total)
+        # growShapeByFg with rotatedGrowth (ShapeBase.cpp:1216-1225): Rz G Rz^T
+        rot, Rz = growth_rotations(pos, self.conn, self.inv_dXde)
+        if rot.any():
+            total[rot] = dgemm3(dgemm3(Rz[rot], total[rot]), Rz[rot], trans_b=True)
         return total
 
     def grow(self, Fg, pos, time, dt, rates=None):
@@ -393,6 +447,7 @@ class GrowthOracle:
 
 FIXTURES = ["steps_grid_growth", "steps_grid_growth_pinned"]
 MIXED_FIXTURE = "steps_growth_functions"
+ROTATED_FIXTURE = "steps_growth_rotated"
 
 
 def add_functions(obj, fns):
@@ -446,3 +501,24 @@ def fixture_case(name):
 
 
 GridGrowthOracle = GrowthOracle
+
+
+def turned(pos, degrees):
+    """Positions turned by `degrees` about the z axis."""
+    a = math.radians(degrees)
+    p = np.asarray(pos, dtype=np.float64).reshape(-1, 3)
+    q = p.copy()
+    q[:, 0] = math.cos(a) * p[:, 0] - math.sin(a) * p[:, 1]
+    q[:, 1] = math.sin(a) * p[:, 0] + math.cos(a) * p[:, 1]
+    return q.reshape(-1)
+
+
+def rotated_case():
+    """Tissue, start positions and functions of the steps_growth_rotated
+    fixture: a 2-layer sheet whose start shape is its mesh turned by 20
+    degrees about z (a rigid turn: no strain), an anisotropic uniform function
+    and a grid function; every prism's growth increment is turned with it."""
+    t = mesh.config_tiny(seed=24, n=6, n_layers=2, eta=30.0)
+    ra, aa = mesh.grid_growth_inputs(35, 4, 5)
+    fns = [dict(kind="uniform", rates=[5e-5, 1e-5, 0.0], angle_rad=0.2), dict(kind="grid", rates=ra, angles_deg=aa)]
+    return t, turned(t.pos, 20.0), fns

@@ -30,7 +30,8 @@
 //     (Simulation.cpp:9651-9666): calculateGrowthUniform :9757-9799,
 //     calculateGrowthRing :9801-9885 and calculateGrowthGridBased
 //     :10065-10114 (ShapeBase::calculateFgFromRates /
-//     calculateFgFromGridCorners), with calculateTissueHeight
+//     calculateFgFromGridCorners), the growth turned with each prism's
+//     rotation (updateGrowthRotationMatrices :4459-4466), with calculateTissueHeight
 //     :3280-3330, assignInitialZPositions :3367-3371, fillInElementColumnLists
 //     :7612-7624, the bounding-box positions of initiateSystem :630-645 and of
 //     runOneStep :5833-5843, and updateRelativePositionsToApicalPositioning
@@ -394,6 +395,11 @@ void refGrow(RefSim* s, double dt, const double* rates, bool with_functions) {
         refBoundingBox(s);
         refApicalPositioning(s);
     }
+    // Simulation::updateGrowthRotationMatrices (Simulation.cpp:4459-4466),
+    // called by runOneStep whenever growth functions exist (:5872-5876)
+    if (with_functions && !g.fns.empty())
+        for (ShapeBase* el : s->elements)
+            if (!el->IsAblated) el->CalculateGrowthRotationByF();
     gsl_matrix* rot = gsl_matrix_alloc(3, 3);
     gsl_matrix* inc = gsl_matrix_alloc(3, 3);
     gsl_matrix* peri = gsl_matrix_alloc(3, 3);

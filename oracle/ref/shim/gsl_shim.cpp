@@ -8,6 +8,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
+#include <cmath>
+#include <vector>
 
 extern "C" {
 
@@ -227,9 +230,63 @@ int gsl_linalg_LU_invert(const gsl_matrix* LU, const gsl_permutation* p, gsl_mat
     return 0;
 }
 
-int gsl_linalg_SV_decomp(gsl_matrix*, gsl_matrix*, gsl_vector*, gsl_vector*) {
-    shim_fatal("gsl_linalg_SV_decomp");
-    return -1;
+// A = U S V^T by one-sided (Hestenes) Jacobi rotations: pairs of columns of
+// A are rotated until orthogonal, the rotations accumulated in V; the
+// singular values are the final column norms, U the normalised columns.
+// Singular values descending, as GSL returns them.  On return A holds U.
+int gsl_linalg_SV_decomp(gsl_matrix* A, gsl_matrix* V, gsl_vector* S, gsl_vector*) {
+    const size_t M = A->size1, N = A->size2;
+    auto a = [&](size_t i, size_t j) -> double& { return A->data[i * A->tda + j]; };
+    auto v = [&](size_t i, size_t j) -> double& { return V->data[i * V->tda + j]; };
+    for (size_t i = 0; i < N; ++i)
+        for (size_t j = 0; j < N; ++j) v(i, j) = i == j ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        bool rotated = false;
+        for (size_t p = 0; p + 1 < N; ++p)
+            for (size_t q = p + 1; q < N; ++q) {
+                double alpha = 0.0, beta = 0.0, gamma = 0.0;
+                for (size_t i = 0; i < M; ++i) {
+                    alpha += a(i, p) * a(i, p);
+                    beta += a(i, q) * a(i, q);
+                    gamma += a(i, p) * a(i, q);
+                }
+                if (gamma == 0.0 || std::fabs(gamma) <= 1e-17 * std::sqrt(alpha * beta)) continue;
+                rotated = true;
+                const double zeta = (beta - alpha) / (2.0 * gamma);
+                const double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
+                const double c = 1.0 / std::sqrt(1.0 + t * t), sn = c * t;
+                for (size_t i = 0; i < M; ++i) {
+                    const double x = a(i, p), y = a(i, q);
+                    a(i, p) = c * x - sn * y;
+                    a(i, q) = sn * x + c * y;
+                }
+                for (size_t i = 0; i < N; ++i) {
+                    const double x = v(i, p), y = v(i, q);
+                    v(i, p) = c * x - sn * y;
+                    v(i, q) = sn * x + c * y;
+                }
+            }
+        if (!rotated) break;
+    }
+    std::vector<double> sig(N);
+    for (size_t j = 0; j < N; ++j) {
+        double n2 = 0.0;
+        for (size_t i = 0; i < M; ++i) n2 += a(i, j) * a(i, j);
+        sig[j] = std::sqrt(n2);
+        if (sig[j] > 0)
+            for (size_t i = 0; i < M; ++i) a(i, j) /= sig[j];
+    }
+    for (size_t j = 0; j < N; ++j) {  // descending order
+        size_t best = j;
+        for (size_t k = j + 1; k < N; ++k)
+            if (sig[k] > sig[best]) best = k;
+        if (best == j) continue;
+        std::swap(sig[j], sig[best]);
+        for (size_t i = 0; i < M; ++i) std::swap(a(i, j), a(i, best));
+        for (size_t i = 0; i < N; ++i) std::swap(v(i, j), v(i, best));
+    }
+    for (size_t j = 0; j < N; ++j) S->data[j * S->stride] = sig[j];
+    return 0;
 }
 
 gsl_eigen_symmv_workspace* gsl_eigen_symmv_alloc(size_t) {

@@ -196,10 +196,35 @@ def growth_functions_fixture(n_steps):
                         iters=np.array(iters), Fg=np.array(Fg), note=og.mixed_case.__doc__)
 
 
+def growth_rotated_fixture(n_steps):
+    """Newton steps from a start shape turned by 20 degrees: the growth of
+    every prism is turned with it (CalculateGrowthRotationByF)."""
+    t, start, fns = og.rotated_case()
+    r = Ref(t)
+    og.add_functions(r, fns)
+    r.set_positions(start)
+    r.grow(t.dt, t.rates)
+    Fg_grow = r.get_Fg()[0]
+    r.close()
+    r = Ref(t)
+    og.add_functions(r, fns)
+    r.set_positions(start)
+    pos, iters, Fg = [], [], []
+    for _ in range(n_steps):
+        out = r.step(t.dt, t.rates)
+        pos.append(r.positions())
+        iters.append(out["iters"])
+        Fg.append(r.get_Fg()[0])
+    r.close()
+    np.savez_compressed(os.path.join(HERE, og.ROTATED_FIXTURE + ".npz"), Fg_grow=Fg_grow, positions=np.array(pos),
+                        iters=np.array(iters), Fg=np.array(Fg), note=og.rotated_case.__doc__)
+
+
 def grid_fixtures():
     for name in og.FIXTURES:
         grid_growth_fixture(name, 3)
     growth_functions_fixture(3)
+    growth_rotated_fixture(3)
 
 
 def main():

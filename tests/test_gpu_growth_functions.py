@@ -255,3 +255,41 @@ def test_function_refusals():
             s.add_uniform_growth([1e-6, 1e-6, 0.0])                          # at most 16 functions
         s.clear_growth_functions()
         s.add_uniform_growth([1e-6, 1e-6, 0.0])
+
+
+def test_growth_turns_with_the_prism_like_the_reference():
+    f = np.load(os.path.join(GOLD, G.ROTATED_FIXTURE + ".npz"))
+    t, start, fns = G.rotated_case()
+    with api.Solver(t) as s:
+        G.add_functions(s, fns)
+        s.set_growth_rates(t.rates)
+        s.set_positions(start)
+        s.begin_step(t.dt)
+        Fg, _ = s.get_Fg()
+    assert np.abs(Fg - f["Fg_grow"]).max() <= TOL_FG
+    with api.Solver(t) as s:
+        G.add_functions(s, fns)
+        s.set_growth_rates(t.rates)
+        s.set_positions(start)
+        for k in range(f["positions"].shape[0]):
+            out = s.newton_step(t.dt, allow_not_converged=False)
+            ref = f["positions"][k]
+            pos = s.positions()
+            assert np.abs(pos - ref).max() <= TOL_POS * np.abs(ref).max(), (k, np.abs(pos - ref).max())
+            assert out["iters"] == f["iters"][k], (k, out["iters"])
+            assert np.abs(s.get_Fg()[0] - f["Fg"][k]).max() <= 1e-12, k
+
+
+def test_growth_rotation_on_a_large_sheet_matches_the_oracle():
+    t = _big_sheet(False)
+    fns = [dict(kind="uniform", rates=[5e-5, 1e-5, 0.0], angle_rad=0.4)]
+    start = G.turned(t.pos, 12.0) + np.random.default_rng(3).uniform(-0.2, 0.2, size=t.pos.size)
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(o, fns)
+    with api.Solver(t) as s:
+        G.add_functions(s, fns)
+        s.set_positions(start)
+        s.begin_step(60.0)
+        Fg, _ = s.get_Fg()
+    ref = o.grow(np.eye(3), start, 0.0, 60.0)
+    assert np.abs(Fg.reshape(-1, 3, 3) - ref).max() <= TOL_FG

@@ -193,8 +193,74 @@ def test_mixed_functions_match_the_reference_driver():
         F1 = R.get_Fg()[0]
         Fo = o.grow(F0.reshape(-1, 3, 3), moved, time, 60.0, t.rates)
         assert np.abs(F1.reshape(-1, 3, 3) - Fo).max() <= 1e-15
+    # without functions nothing grows (the reference keeps each prism's last
+    # growth rotation, which turns the identity increment to within rounding)
     R.clear_growth_functions()
     F0 = R.get_Fg()[0]
     R.grow(60.0, np.zeros(3 * t.n_elems))
-    assert np.array_equal(R.get_Fg()[0], F0)
+    assert np.abs(R.get_Fg()[0] - F0).max() <= 1e-15
     R.close()
+
+
+def _rotated(t, degrees):
+    """Current positions of the tissue turned by `degrees` about z."""
+    a = math.radians(degrees)
+    p = t.pos.reshape(-1, 3)
+    q = p.copy()
+    q[:, 0] = math.cos(a) * p[:, 0] - math.sin(a) * p[:, 1]
+    q[:, 1] = math.sin(a) * p[:, 0] + math.cos(a) * p[:, 1]
+    return q.reshape(-1)
+
+
+def test_growth_turns_with_the_prism():
+    """A sheet turned by 5 degrees: every prism's growth increment is turned
+    by the angle the reference extracts (atan2(R01, R00) = -5 degrees); by
+    0.5 degrees: below the reference's 0.017 thresholds, no turn."""
+    t = mesh.config_tiny(seed=7, n=5, n_layers=2)
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    rot, Rz = G.growth_rotations(_rotated(t, 5.0), t.conn, o.inv_dXde)
+    assert rot.all()
+    np.testing.assert_allclose(np.arctan2(Rz[:, 1, 0], Rz[:, 0, 0]), math.radians(-5.0), atol=1e-12)
+    rot, _ = G.growth_rotations(_rotated(t, 0.5), t.conn, o.inv_dXde)
+    assert not rot.any()
+    o.add_uniform_growth([4e-5, 1e-5, 0.0])
+    F = o.grow(np.eye(3), _rotated(t, 5.0), 0.0, 60.0)
+    d = np.exp(np.array([4e-5, 1e-5, 0.0]) * 60.0)
+    c, s = math.cos(math.radians(-5.0)), math.sin(math.radians(-5.0))
+    Rm = np.array([[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]])
+    np.testing.assert_allclose(F, np.broadcast_to(Rm @ np.diag(d) @ Rm.T, F.shape), atol=1e-12)
+
+
+@ref_only
+@pytest.mark.parametrize("degrees", [5.0, 0.5, -30.0])
+def test_growth_rotation_matches_the_reference_driver(degrees):
+    t = mesh.config_tiny(seed=8, n=5, n_layers=2)
+    ra, aa = mesh.grid_growth_inputs(60, 4, 4)
+    fns = [dict(kind="uniform", rates=[4e-5, 1e-5, 2e-6], angle_rad=0.3), dict(kind="grid", rates=ra, angles_deg=aa)]
+    R = Ref(t)
+    G.add_functions(R, fns)
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(o, fns)
+    turned = _rotated(t, degrees)
+    R.set_positions(turned)
+    F0 = R.get_Fg()[0]
+    R.grow(60.0, t.rates)
+    F1 = R.get_Fg()[0]
+    Fo = o.grow(F0.reshape(-1, 3, 3), turned, 0.0, 60.0, t.rates)
+    assert np.abs(F1.reshape(-1, 3, 3) - Fo).max() <= 1e-15
+    R.close()
+
+
+def test_rotated_fixture_matches_the_oracle():
+    f = np.load(os.path.join(GOLD, G.ROTATED_FIXTURE + ".npz"))
+    t, start, fns = G.rotated_case()
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(o, fns)
+    rot, _ = G.growth_rotations(start, t.conn, o.inv_dXde)
+    assert rot.all()
+    Fg = o.grow(np.eye(3), start, 0.0, t.dt, t.rates)
+    assert np.abs(Fg.reshape(-1) - f["Fg_grow"]).max() <= 1e-15
+    # without the turn the increment would differ
+    Fu = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(Fu, fns)
+    assert np.abs(Fu.grow(np.eye(3), t.pos, 0.0, t.dt, t.rates).reshape(-1) - f["Fg_grow"]).max() > 1e-4

@@ -106,6 +106,7 @@ struct Growth {
     int* colsrc = nullptr;    // [ne] the prism whose position a prism takes
     double* box = nullptr;    // [4] min x, min y, size x, size y
     double* part = nullptr;   // [kBoxCtas][4] k_box's per-CTA partials
+    double* gbar = nullptr;   // [18][ne] Gauss-weighted dN/dX (growth rotation)
     unsigned* ticket = nullptr;  // k_box's arrival counter (0 between launches)
 };
 
@@ -348,6 +349,7 @@ struct GrowArgs {
     const double* rel;    // [2][ne] pinned bounding-box positions, or null: from box and colsrc
     const double* box;    // [4] this step's box (grid functions, current positions)
     const int* colsrc;    // [ne] the prism whose position a prism takes
+    const double* gbar;   // [18][ne] Gauss-weighted dN_a/dX_k (growth rotation)
     FnArgs fn[kMaxFns];
 };
 
@@ -458,6 +460,75 @@ __device__ void grid_increment(const FnArgs& F, int interp, double rel_x, double
     }
 }
 
+// The rotation factor of the polar decomposition F = R U (R = U_svd V_svd^T
+// of the reference's singular value decomposition) by Higham's scaled Newton
+// iteration X <- (z X + X^-T / z) / 2, z = |det X|^(-1/3).
+__device__ void polar_rotation(const double* F, double* R) {
+    double X[9];
+    for (int k = 0; k < 9; ++k) X[k] = F[k];
+    for (int it = 0; it < 40; ++it) {
+        double inv[9];
+        inv3_cof(X, inv);
+        const double det = X[0] * (X[4] * X[8] - X[5] * X[7]) - X[1] * (X[3] * X[8] - X[5] * X[6]) +
+                           X[2] * (X[3] * X[7] - X[4] * X[6]);
+        const double z = it < 6 ? 1.0 / cbrt(fabs(det)) : 1.0;
+        double d = 0.0;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                const double y = 0.5 * (z * X[3 * i + j] + inv[3 * j + i] / z);
+                d += (y - X[3 * i + j]) * (y - X[3 * i + j]);
+                X[3 * i + j] = y;
+            }
+        if (!(d > 1e-30)) break;
+    }
+    for (int k = 0; k < 9; ++k) R[k] = X[k];
+}
+
+// ShapeBase::CalculateGrowthRotationByF for prism e: the Gauss-weighted
+// deformation gradient of the current shape (calculateTriPointFForRatation,
+// :1674-1687), its rotation (calculate3DRotMatFromF, :1731-1810: rotated if an
+// off-diagonal entry exceeds 0.017), the rotation's angle about z
+// (disassembleRotationMatrixForZ, :1690-1721: atan2(R01, R00), used beyond
+// 0.017 rad).  True with Rz = [[c, -s, 0], [s, c, 0], [0, 0, 1]].
+__device__ bool growth_rotation(const GrowArgs& G, int e, double* Rz) {
+    if (!G.gbar) return false;
+    const int ne = G.ne;
+    double F[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int a = 0; a < 6; ++a) {
+        const int n = G.conn[(size_t)a * ne + e];
+        double x[3], g[3];
+        for (int i = 0; i < 3; ++i) x[i] = G.pos[3 * (size_t)n + i];
+        for (int k = 0; k < 3; ++k) g[k] = G.gbar[(size_t)(3 * a + k) * ne + e];
+        for (int i = 0; i < 3; ++i)
+            for (int k = 0; k < 3; ++k) F[3 * i + k] += x[i] * g[k];
+    }
+    double R[9];
+    polar_rotation(F, R);
+    bool off = false;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            if (i != j && (R[3 * i + j] > 0.017 || R[3 * i + j] < -0.017)) off = true;
+    if (!off) return false;
+    const double tz = atan2(R[1], R[0]);
+    if (!(tz > 0.017 || tz < -0.017)) return false;
+    const double c = cos(tz), s = sin(tz);
+    const double r[9] = {c, -1.0 * s, 0.0, s, c, 0.0, 0.0, 0.0, 1.0};
+    for (int k = 0; k < 9; ++k) Rz[k] = r[k];
+    return true;
+}
+
+// Gauss-weighted shape-function gradients: gbar[3a + k] = sum over the 6
+// Gauss points of (1/6) dN_a/dX_k.
+__global__ void k_gbar(int ne, const double* __restrict__ gx, double* __restrict__ gbar) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    for (int r = 0; r < 18; ++r) {
+        double s = 0.0;
+        for (int gp = 0; gp < 6; ++gp) s += gx[(size_t)r * (6 * (size_t)ne) + 6 * (size_t)e + gp] * (1.0 / 6.0);
+        gbar[(size_t)r * ne + e] = s;
+    }
+}
+
 // Per prism: the growth increment of the step -- diag(exp(rate dt)) of the
 // per-element rates, then each active function's increment multiplied on
 // the left (updateGrowthIncrement) -- and Fg <- increment Fg (growShapeByFg).
@@ -523,6 +594,15 @@ __global__ void k_grow(GrowArgs G, double* __restrict__ Fg, double* __restrict__
         mul_xy_z(inc, M, P);
         for (int k = 0; k < 9; ++k) M[k] = P[k];
     }
+    // ShapeBase::CalculateGrowthRotationByF (ShapeBase.cpp:1656-1672), then
+    // the rotated increment of growShapeByFg (:1216-1225): Rz M Rz^T
+    double Rz[9];
+    if (growth_rotation(G, e, Rz)) {
+        const double RzT[9] = {Rz[0], Rz[3], 0.0, Rz[1], Rz[4], 0.0, 0.0, 0.0, 1.0};
+        double T[9];
+        mul_xy_z(Rz, M, T);
+        mul_xy_z(T, RzT, M);
+    }
     double F0[9], out[9], inv[9];
     for (int k = 0; k < 9; ++k) F0[k] = Fg[(size_t)k * ne + e];
     mul_xy_z_full(M, F0, out);
@@ -549,7 +629,7 @@ tf_status launch_relpos(tf_handle* h, double* rel_out) {
 void growth_free(Growth* g) {
     if (!g) return;
     for (auto& f : g->fns) free_fn(f);
-    void* ptrs[] = {g->relz, g->rel0, g->rel, g->colsrc, g->box, g->part, g->ticket};
+    void* ptrs[] = {g->relz, g->rel0, g->rel, g->colsrc, g->box, g->part, g->ticket, g->gbar};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete g;
@@ -617,6 +697,18 @@ tf_status growth_setup(tf_handle* h) {
     GR_TRY(put(&g->colsrc, colsrc));
     GR_TRY(put(&g->box, std::vector<double>(4, 0.0)));
     GR_TRY(put(&g->part, std::vector<double>(4 * (size_t)kBoxCtas, 0.0)));
+    {
+        cudaError_t err = cudaMalloc(reinterpret_cast<void**>(&g->gbar), 18 * sizeof(double) * (size_t)ne);
+        if (err != cudaSuccess) {
+            cudaGetLastError();
+            g->gbar = nullptr;
+            set_error("device allocation failed for a growth function");
+            return TF_OUT_OF_MEMORY;
+        }
+        k_gbar<<<cdiv(ne, kT), kT, 0, h->stream>>>(ne, h->d.gx, g->gbar);
+        TF_LAUNCH_CHECK(h);
+        TF_CUDA(cudaStreamSynchronize(h->stream));
+    }
     GR_TRY(put(&g->ticket, std::vector<unsigned>(1, 0u)));
     return TF_OK;
 }
@@ -744,7 +836,7 @@ tf_status launch_growth_functions(tf_handle* h, bool* done) {
         F.ce = f.ce;
         grid |= f.type == kGrid;
     }
-    if (A.nfn == 0) return TF_OK;
+    A.gbar = g->gbar;  // the reference turns the growth with the prism whenever functions exist (Simulation.cpp:5872-5876)
     if (grid && !g->pinned) {  // this step's box; k_grow forms the positions
         k_box<<<kBoxCtas, kT, 0, h->stream>>>(d.nn, d.uk, g->part, g->ticket, g->box);
         TF_LAUNCH_CHECK(h);
