@@ -191,20 +191,55 @@ def packing(name, kw, precond):
             "positions_max_rel_err": err, "newton_iters_identical": bool(same), "couples_identical": couples}
 
 
+def growth(name):
+    """steps with the reference's growth functions against its
+    own growth-function classes (fixtures tests/golden/steps_grid_growth*.npz,
+    steps_growth_functions.npz, steps_growth_rotated.npz)."""
+    from oracle import growth as og
+
+    f = np.load(os.path.join(GOLD, name + ".npz"))
+    start, interp, pinned = None, 1, False
+    if name == og.MIXED_FIXTURE:
+        t, fns = og.mixed_case()
+    elif name == og.ROTATED_FIXTURE:
+        t, start, fns = og.rotated_case()
+    else:
+        t, fns, interp, pinned = og.fixture_case(name)
+    err, fg, same = 0.0, 0.0, True
+    with api.Solver(t, krylov_rtol=1e-12) as s:
+        og.add_functions(s, fns)
+        s.set_grid_growth_mode(interp, pinned)
+        s.set_growth_rates(t.rates)
+        if start is not None:
+            s.set_positions(start)
+        for k in range(f["positions"].shape[0]):
+            out = s.newton_step(t.dt)
+            err = max(err, rel(s.positions(), f["positions"][k]))
+            fg = max(fg, float(np.abs(s.get_Fg()[0] - f["Fg"][k]).max()))
+            same &= out["iters"] == f["iters"][k]
+    return {"config": f"f1 growth functions: {name} ({t.n_elems} prisms, {f['positions'].shape[0]} steps)",
+            "positions_max_rel_err": err, "Fg_max_abs_err": fg, "newton_iters_identical": bool(same)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true", help="skip the 1.0M-prism wing")
+    ap.add_argument("--only-f", action="store_true", help="only the rows of the next-step features (f1, f3)")
     args = ap.parse_args()
     build_port()
-    runs = [lambda: config1(1), lambda: config1(2),
-            lambda: full_size(mesh.config_large(seed=0), "2: 320,000 prisms, first Newton step")]
-    if not args.quick:
-        runs.append(lambda: full_size(mesh.config_wing(seed=0), "3: 995,824-prism wing, first Newton step",
-                                      csr=False))
-    runs += [config4, config5]
+    runs = []
+    if not args.only_f:
+        runs += [lambda: config1(1), lambda: config1(2),
+                 lambda: full_size(mesh.config_large(seed=0), "2: 320,000 prisms, first Newton step")]
+        if not args.quick:
+            runs.append(lambda: full_size(mesh.config_wing(seed=0), "3: 995,824-prism wing, first Newton step",
+                                          csr=False))
+        runs += [config4, config5]
     for name, kw in (("steps_facing_packing", dict(seed=12, gap=1.5, E=100000.0, eta=0.0)),
                      ("steps_facing_packing_viscous", dict(seed=13, gap=1.5, E=100000.0, eta=100.0))):
         runs += [lambda name=name, kw=kw, pc=pc: packing(name, kw, pc) for pc in (1, 2)]
+    for name in ("steps_grid_growth", "steps_grid_growth_pinned", "steps_growth_functions", "steps_growth_rotated"):
+        runs.append(lambda name=name: growth(name))
     out = []
     for r in runs:
         out.append(r())
