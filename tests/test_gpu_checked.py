@@ -1,6 +1,7 @@
 """The checked build (libtfgpu_checked.so, -DTF_CHECKED): every checked index
 of the main kernels -- prism node ids and scatter offsets, Krylov and
-smoother columns, extra-block columns, multigrid transfers, packing couples --
+smoother columns, extra-block columns, multigrid transfers, packing couples,
+growth-update gathers --
 is tested before its access and a failure is reported as TF_CUDA_ERROR
 instead of touching memory out of bounds.  The same workloads through the
 checked and the normal library must flag nothing and agree bit for bit
@@ -35,6 +36,14 @@ with api.Solver(t, precond=2, deterministic=True) as s:
     s.set_packing(True)
     its = [s.newton_step(t.dt)["krylov_total"] for _ in range(2)]
     out["packing"] = [s.positions().tolist(), its]
+from oracle import growth as og
+t, start, fns = og.rotated_case()
+with api.Solver(t, deterministic=True) as s:
+    og.add_functions(s, fns + og.mixed_case()[1][1:2])
+    s.set_growth_rates(t.rates)
+    s.set_positions(start)
+    its = [s.newton_step(t.dt)["krylov_total"] for _ in range(2)]
+    out["growth"] = [s.positions().tolist(), s.get_Fg()[0].tolist(), its]
 ts = [mesh.config_tiny(seed=301, n=9, n_layers=3, eta=100.0), mesh.config_tiny(seed=303, n=6, n_layers=2)]
 with api.Batch(ts, precond=2, deterministic=True) as b:
     b.set_growth_rates()

@@ -350,6 +350,8 @@ struct GrowArgs {
     const double* box;    // [4] this step's box (grid functions, current positions)
     const int* colsrc;    // [ne] the prism whose position a prism takes
     const double* gbar;   // [18][ne] Gauss-weighted dN_a/dX_k (growth rotation)
+    int nn;
+    int* check;           // checked build: failed index tests
     FnArgs fn[kMaxFns];
 };
 
@@ -496,6 +498,7 @@ __device__ bool growth_rotation(const GrowArgs& G, int e, double* Rz) {
     double F[9] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
     for (int a = 0; a < 6; ++a) {
         const int n = G.conn[(size_t)a * ne + e];
+        if (!TF_IN(G.check, n, G.nn, CK_GROW_NODE)) continue;
         double x[3], g[3];
         for (int i = 0; i < 3; ++i) x[i] = G.pos[3 * (size_t)n + i];
         for (int k = 0; k < 3; ++k) g[k] = G.gbar[(size_t)(3 * a + k) * ne + e];
@@ -552,10 +555,11 @@ __global__ void k_grow(GrowArgs G, double* __restrict__ Fg, double* __restrict__
                     rel_x = G.rel[e];
                     rel_y = G.rel[ne + e];
                 } else {  // as k_relpos computes it
-                    const int sp = G.colsrc[e];
+                    const int sp = TF_IN(G.check, G.colsrc[e], ne, CK_GROW_PRISM) ? G.colsrc[e] : e;
                     double c[2] = {0.0, 0.0};
                     for (int a = 0; a < 6; ++a) {
                         const int n = G.conn[(size_t)a * ne + sp];
+                        if (!TF_IN(G.check, n, G.nn, CK_GROW_NODE)) continue;
                         c[0] += G.pos[3 * (size_t)n];
                         c[1] += G.pos[3 * (size_t)n + 1];
                     }
@@ -573,6 +577,7 @@ __global__ void k_grow(GrowArgs G, double* __restrict__ Fg, double* __restrict__
                 if (!centred) {  // ShapeBase::getCentre (ShapeBase.cpp:240-250)
                     for (int a = 0; a < 6; ++a) {
                         const int n = G.conn[(size_t)a * ne + e];
+                        if (!TF_IN(G.check, n, G.nn, CK_GROW_NODE)) continue;
                         cx = add(cx, G.pos[3 * (size_t)n]);
                         cy = add(cy, G.pos[3 * (size_t)n + 1]);
                     }
@@ -836,6 +841,8 @@ tf_status launch_growth_functions(tf_handle* h, bool* done) {
         F.ce = f.ce;
         grid |= f.type == kGrid;
     }
+    A.nn = d.nn;
+    A.check = d.check;
     A.gbar = g->gbar;  // the reference turns the growth with the prism whenever functions exist (Simulation.cpp:5872-5876)
     if (grid && !g->pinned) {  // this step's box; k_grow forms the positions
         k_box<<<kBoxCtas, kT, 0, h->stream>>>(d.nn, d.uk, g->part, g->ticket, g->box);

@@ -38,6 +38,8 @@ enum CheckSite {
     CK_PROLONG_COL,      // coarse node of a prolongation block < coarse level size
     CK_PACK_NODE,        // node of a packing couple < n_nodes
     CK_PACK_BLOCK,       // extra block of a packing couple < extra blocks
+    CK_GROW_NODE,        // node of a prism in the growth update < n_nodes
+    CK_GROW_PRISM,       // prism whose position a prism takes < n_elems
 };
 #ifdef TF_CHECKED
 __device__ __forceinline__ bool check_in(int* flag, long long i, long long n, int code) {
