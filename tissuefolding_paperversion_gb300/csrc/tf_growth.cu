@@ -464,7 +464,8 @@ __device__ void grid_increment(const FnArgs& F, int interp, double rel_x, double
 
 // The rotation factor of the polar decomposition F = R U (R = U_svd V_svd^T
 // of the reference's singular value decomposition) by Higham's scaled Newton
-// iteration X <- (z X + X^-T / z) / 2, z = |det X|^(-1/3).
+// iteration X <- (z X + X^-T / z) / 2, z = |det X|^(-1/3) (scaled for the first
+// three iterations, plain Newton after).
 __device__ void polar_rotation(const double* F, double* R) {
     double X[9];
     for (int k = 0; k < 9; ++k) X[k] = F[k];
@@ -473,11 +474,12 @@ __device__ void polar_rotation(const double* F, double* R) {
         inv3_cof(X, inv);
         const double det = X[0] * (X[4] * X[8] - X[5] * X[7]) - X[1] * (X[3] * X[8] - X[5] * X[6]) +
                            X[2] * (X[3] * X[7] - X[4] * X[6]);
-        const double z = it < 6 ? 1.0 / cbrt(fabs(det)) : 1.0;
+        const double zi = it < 3 ? cbrt(fabs(det)) : 1.0;  // 1 / z
+        const double z = it < 3 ? 1.0 / zi : 1.0;
         double d = 0.0;
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) {
-                const double y = 0.5 * (z * X[3 * i + j] + inv[3 * j + i] / z);
+                const double y = 0.5 * (z * X[3 * i + j] + inv[3 * j + i] * zi);
                 d += (y - X[3 * i + j]) * (y - X[3 * i + j]);
                 X[3 * i + j] = y;
             }
