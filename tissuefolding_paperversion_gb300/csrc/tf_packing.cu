@@ -85,6 +85,7 @@ struct Packing {
     int* nptr = nullptr;       // [nn+1] prisms of each node, in prism order
     int* nelem = nullptr;
     double* mass = nullptr;    // [nn] node masses of the step
+    double* vpn = nullptr;     // [ne] volume per node of each prism
     double* par = nullptr;     // [P_COUNT] parameters of the detection
     double* part = nullptr;    // per-CTA partials of the parameter reduction
     unsigned* ticket = nullptr;
@@ -115,7 +116,7 @@ struct Packing {
 
 void packing_free(Packing* p) {
     if (!p) return;
-    void* ptrs[] = {p->place, p->vref, p->ebasal, p->nptr, p->nelem, p->mass, p->par, p->part, p->ticket,
+    void* ptrs[] = {p->place, p->vref, p->ebasal, p->nptr, p->nelem, p->mass, p->vpn, p->par, p->part, p->ticket,
                     p->hoff, p->hcur, p->hids,
                     p->ccount, p->scan_tmp, p->c0, p->c1, p->w, p->mbar, p->x01, p->x10, p->pnode, p->pptr,
                     p->plist};
@@ -199,15 +200,22 @@ __device__ __forceinline__ double det_fg(const double* __restrict__ Fg, int ne, 
 }
 
 // node masses in prism order (updateNodeMasses)
-__global__ void k_pk_mass(int nn, int ne, const double* __restrict__ Fg, const double* __restrict__ vref,
-                          const int* __restrict__ nptr, const int* __restrict__ nelem, double* __restrict__ mass) {
+// The volume per node of each prism, (det(Fg) V_ref) / 6, once per prism
+// (ShapeBase::growShapeByFg, ShapeBase.cpp:1243-1245) ...
+__global__ void k_pk_vpn(int ne, const double* __restrict__ Fg, const double* __restrict__ vref,
+                         double* __restrict__ vpn) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= ne) return;
+    vpn[e] = (det_fg(Fg, ne, e) * vref[e]) / 6;
+}
+
+// ... and each node's sum over its prisms in prism order (updateNodeMasses).
+__global__ void k_pk_mass(int nn, const double* __restrict__ vpn, const int* __restrict__ nptr,
+                          const int* __restrict__ nelem, double* __restrict__ mass) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nn) return;
     double m = 0.0;
-    for (int q = nptr[i]; q < nptr[i + 1]; ++q) {
-        const int e = nelem[q];
-        m += (det_fg(Fg, ne, e) * vref[e]) / 6;
-    }
+    for (int q = nptr[i]; q < nptr[i + 1]; ++q) m += vpn[nelem[q]];
     mass[i] = m;
 }
 
@@ -567,6 +575,7 @@ tf_status packing_setup(tf_handle* h, int flags) {
     PK_TRY(put(&p->nptr, nptr));
     PK_TRY(put(&p->nelem, nelem));
     PK_TRY(alloc(&p->mass, d.nn));
+    PK_TRY(alloc(&p->vpn, d.ne));
     PK_TRY(alloc(&p->par, P_COUNT));
     PK_TRY(alloc(&p->part, (size_t)kPart * kParCtas));
     PK_TRY(alloc(&p->ticket, 1));
@@ -587,7 +596,9 @@ tf_status packing_detect(tf_handle* h) {
     Device& d = h->d;
     cudaStream_t st = h->stream;
     const int nn = d.nn;
-    k_pk_mass<<<cdiv(nn, kT), kT, 0, st>>>(nn, d.ne, d.Fg, p->vref, p->nptr, p->nelem, p->mass);
+    k_pk_vpn<<<cdiv(d.ne, kT), kT, 0, st>>>(d.ne, d.Fg, p->vref, p->vpn);
+    TF_LAUNCH_CHECK(h);
+    k_pk_mass<<<cdiv(nn, kT), kT, 0, st>>>(nn, p->vpn, p->nptr, p->nelem, p->mass);
     TF_LAUNCH_CHECK(h);
     k_pk_params<<<kParCtas, kT, 0, st>>>(nn, d.ne, d.uk, d.conn, p->ebasal, p->part, p->ticket, p->par);
     TF_LAUNCH_CHECK(h);
