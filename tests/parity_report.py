@@ -172,7 +172,7 @@ def config5():
 
 
 def packing(name, kw, precond):
-    """steps with implicit packing against the reference's own
+    """Implicit packing: steps with packing against the reference's own
     classes (fixtures tests/golden/steps_facing_packing*.npz)."""
     f = np.load(os.path.join(GOLD, name + ".npz"))
     t = mesh.config_facing_sheets(**kw)
@@ -192,7 +192,7 @@ def packing(name, kw, precond):
 
 
 def growth(name):
-    """steps with the reference's growth functions against its
+    """Growth functions: steps with the reference's growth functions against its
     own growth-function classes (fixtures tests/golden/steps_grid_growth*.npz,
     steps_growth_functions.npz, steps_growth_rotated.npz)."""
     from oracle import growth as og
