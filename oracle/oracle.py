@@ -1,6 +1,6 @@
 """ctypes bindings for the CPU oracle.  TEST INFRASTRUCTURE ONLY.
 
-Two checkers live here:
+Two oracles live here:
 
 * ``Port`` wraps ``_build/libtforacle.so``: the plain-C restatement of the
   reference's implicit prism step (``tf_oracle.c``).  It builds on any host

@@ -14,7 +14,7 @@
 //   * updateNodeViscositySurfaces (Simulation.cpp:7563-7581);
 //   * updateStepNR (Simulation.cpp:6449-6590), restated call for call with
 //     myosin, pipette and random forces switched off as in every
-//     configuration this build targets;
+//     benchmark configuration;
 //   * implicit packing between tissue surfaces when switched on
 //     (tfr_set_packing): calculateBoundingBox :9148-9185 and the elements'
 //     bounding-box positions :5833-5843, updateNodeMasses :7552-7561,

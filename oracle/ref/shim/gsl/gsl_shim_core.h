@@ -2,7 +2,7 @@
  * Project-written stand-in for the subset of the GNU Scientific Library API
  * that the reference's element / Newton-Raphson translation units call.
  * Test infrastructure only: it lets the reference sources compile unmodified
- * into oracle/_ref so that they can serve as the parity checker.  GSL itself
+ * into oracle/_ref so that they can serve as the parity oracle.  GSL itself
  * is not in this image.  Semantics follow GSL's published API documentation
  * (row-major gsl_matrix with a row stride `tda`, CBLAS transpose flags,
  * LU with partial pivoting); every routine is written here from that

@@ -1,6 +1,6 @@
 /*
  * tf_oracle: CPU restatement, in plain C, of the reference's implicit prism
- * time step.  TEST INFRASTRUCTURE ONLY.  It is the parity checker for the
+ * time step.  TEST INFRASTRUCTURE ONLY.  It is the test oracle for the
  * CUDA path (tests, __graft_entry__.smoke) and the timed CPU baseline of
  * bench.py; the product never links, loads or calls it.  Each routine follows
  * the reference function named beside it, in the reference's operation order

@@ -478,7 +478,7 @@ tf_status validate(const tf_mesh* m, const tf_material* mat) {
         return TF_BAD_INPUT;
     }
     if ((int64_t)m->n_nodes * 3 > INT32_MAX / 2 || (int64_t)m->n_elems * 36 > INT32_MAX) {
-        set_error("mesh exceeds the 32-bit index range of this build");
+        set_error("mesh exceeds the 32-bit index range of the library");
         return TF_BAD_INPUT;
     }
     for (int64_t k = 0; k < 6 * (int64_t)m->n_elems; ++k)
@@ -1232,7 +1232,7 @@ tf_status tf_batch_create(const tf_mesh* meshes, const tf_material* mats, int32_
         ne += meshes[i].n_elems;
     }
     if (nn * 3 > INT32_MAX / 2 || ne * 36 > INT32_MAX) {
-        set_error("tf_batch_create: the batch exceeds the 32-bit index range of this build");
+        set_error("tf_batch_create: the batch exceeds the 32-bit index range of the library");
         return TF_BAD_INPUT;
     }
     std::vector<double> pos, ev, E, nu, eta, ref;
