@@ -121,8 +121,10 @@ TF_API tf_status tf_set_growth_rates(tf_handle* h, const double* rates);
 
 /* --- the NewtonRaphsonSolver call sequence ------------------------------ */
 
-/* Start of a time step: growth update (if rates are set), node viscosity
- * surfaces (Simulation::updateNodeViscositySurfaces :7563-7581), then
+/* Start of a time step: growth update (per-element rates and the growth
+ * functions active at the handle's time, see tf_add_uniform_growth), node
+ * viscosity surfaces (Simulation::updateNodeViscositySurfaces :7563-7581),
+ * packing detection when on, then
  * setMatricesToZeroAtTheBeginningOfIteration + constructUnMatrix +
  * initialteUkMatrix (NewtonRaphsonSolver.cpp:102-146). */
 TF_API tf_status tf_begin_step(tf_handle* h, double dt);
