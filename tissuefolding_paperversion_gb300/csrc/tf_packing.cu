@@ -86,6 +86,8 @@ struct Packing {
     int* nelem = nullptr;
     double* mass = nullptr;    // [nn] node masses of the step
     double* vpn = nullptr;     // [ne] volume per node of each prism
+    float* posf = nullptr;     // [3 nn] positions rounded to FP32 (the scan's cheap rejection)
+    unsigned* posmax = nullptr;  // bits of the largest |FP32 coordinate|
     double* par = nullptr;     // [P_COUNT] parameters of the detection
     double* part = nullptr;    // per-CTA partials of the parameter reduction
     unsigned* ticket = nullptr;
@@ -116,7 +118,7 @@ struct Packing {
 
 void packing_free(Packing* p) {
     if (!p) return;
-    void* ptrs[] = {p->place, p->vref, p->ebasal, p->nptr, p->nelem, p->mass, p->vpn, p->par, p->part, p->ticket,
+    void* ptrs[] = {p->place, p->vref, p->ebasal, p->nptr, p->nelem, p->mass, p->vpn, p->posf, p->posmax, p->par, p->part, p->ticket,
                     p->hoff, p->hcur, p->hids,
                     p->ccount, p->scan_tmp, p->c0, p->c1, p->w, p->mbar, p->x01, p->x10, p->pnode, p->pptr,
                     p->plist};
@@ -355,6 +357,8 @@ __global__ void k_pk_hfill(int nn, const double* __restrict__ pos, const double*
 struct Scan {
     int nn, T, last_start;
     const double* pos;
+    const float* posf;
+    const unsigned* posmax;
     const double* mass;
     const int8_t* place;
     const double* par;
@@ -376,6 +380,22 @@ __device__ __forceinline__ bool neighbours(const Scan& S, int i, int j) {
     return false;
 }
 
+// FP32 copies of the positions and the largest |coordinate| among them.
+__global__ void k_pk_posf(int nn, const double* __restrict__ pos, float* __restrict__ posf,
+                          unsigned* __restrict__ posmax) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    float m = 0.f;
+    if (i < nn)
+        for (int k = 0; k < 3; ++k) {
+            const float v = (float)pos[3 * (size_t)i + k];
+            posf[3 * (size_t)i + k] = v;
+            m = fmaxf(m, fabsf(v));
+        }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(posmax, __float_as_uint(m));  // non-negative floats order as their bits
+}
+
 // Calls f(j, d2) for every couple (i, j) of first node i, in bucket order.
 template <class F>
 __device__ void for_each_partner(const Scan& S, int i, F f) {
@@ -389,6 +409,16 @@ __device__ void for_each_partner(const Scan& S, int i, F f) {
     if (!(t2 > 0)) return;
     const long long cx = cell_of(p[3 * i], h), cy = cell_of(p[3 * i + 1], h), cz = cell_of(p[3 * i + 2], h);
     const int8_t pl = S.place[i];
+    // Cheap rejection in FP32: with M the largest |coordinate| and u = 2^-24,
+    // each FP32 difference is within 2.1 u M + 1.1 u r of the exact one for a
+    // pair closer than r, so a pair whose FP32 squared distance exceeds
+    // (r + sqrt(3)(2.1 u M + 1.1 u r))^2 (1 + 5u) is farther than r; only the
+    // others take the exact FP64 test below.
+    const double u = 5.9604644775390625e-08;
+    const double r = sqrt(t2), M = (double)__uint_as_float(*S.posmax) * (1.0 + 4.0 * u);
+    const double del = 1.7320508075688772 * (2.1 * u * M + 1.1 * u * r);
+    const float t2f = __double2float_ru((r + del) * (r + del) * (1.0 + 5.0 * u));
+    const float xi = S.posf[3 * (size_t)i], yi = S.posf[3 * (size_t)i + 1], zi = S.posf[3 * (size_t)i + 2];
     unsigned seen[27];
     int nseen = 0;
     for (int a = -1; a <= 1; ++a)
@@ -402,6 +432,9 @@ __device__ void for_each_partner(const Scan& S, int i, F f) {
                 for (int q = S.hoff[bk]; q < S.hoff[bk + 1]; ++q) {
                     const int j = S.hids[q];
                     if (j <= i || S.place[j] != pl) continue;
+                    const float dxf = xi - S.posf[3 * (size_t)j], dyf = yi - S.posf[3 * (size_t)j + 1],
+                                dzf = zi - S.posf[3 * (size_t)j + 2];
+                    if (dxf * dxf + dyf * dyf + dzf * dzf > t2f) continue;
                     const double d2 = dist2(p, i, j);
                     if (!(d2 < t2) || neighbours(S, i, j)) continue;
                     f(j, d2);
@@ -576,6 +609,8 @@ tf_status packing_setup(tf_handle* h, int flags) {
     PK_TRY(put(&p->nelem, nelem));
     PK_TRY(alloc(&p->mass, d.nn));
     PK_TRY(alloc(&p->vpn, d.ne));
+    PK_TRY(alloc(&p->posf, 3 * (size_t)d.nn));
+    PK_TRY(alloc(&p->posmax, 1));
     PK_TRY(alloc(&p->par, P_COUNT));
     PK_TRY(alloc(&p->part, (size_t)kPart * kParCtas));
     PK_TRY(alloc(&p->ticket, 1));
@@ -602,6 +637,9 @@ tf_status packing_detect(tf_handle* h) {
     TF_LAUNCH_CHECK(h);
     k_pk_params<<<kParCtas, kT, 0, st>>>(nn, d.ne, d.uk, d.conn, p->ebasal, p->part, p->ticket, p->par);
     TF_LAUNCH_CHECK(h);
+    TF_CUDA(cudaMemsetAsync(p->posmax, 0, sizeof(unsigned), st));
+    k_pk_posf<<<cdiv(nn, kT), kT, 0, st>>>(nn, d.uk, p->posf, p->posmax);
+    TF_LAUNCH_CHECK(h);
     TF_CUDA(cudaMemsetAsync(p->hoff, 0, sizeof(int) * ((size_t)p->T + 1), st));
     k_pk_hcount<<<cdiv(nn, kT), kT, 0, st>>>(nn, d.uk, p->mass, p->place, p->par, p->T, p->hoff);
     TF_LAUNCH_CHECK(h);
@@ -612,7 +650,7 @@ tf_status packing_detect(tf_handle* h) {
     int seg = nn / 16;
     if (seg < 1) seg = 1;
     const int last = (p->flags & 1) ? (nn / seg - 1) * seg : nn;
-    Scan S{nn, p->T, last, d.uk, p->mass, p->place, p->par, p->hoff, p->hids, d.rowptr, d.colidx};
+    Scan S{nn, p->T, last, d.uk, p->posf, p->posmax, p->mass, p->place, p->par, p->hoff, p->hids, d.rowptr, d.colidx};
     k_pk_count<<<cdiv(nn, kT), kT, 0, st>>>(S, p->ccount);
     TF_LAUNCH_CHECK(h);
     PK_TRY(scan_exclusive(h, p->ccount, nn, p->scan_tmp));
