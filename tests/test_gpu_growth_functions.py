@@ -293,3 +293,27 @@ def test_growth_rotation_on_a_large_sheet_matches_the_oracle():
         Fg, _ = s.get_Fg()
     ref = o.grow(np.eye(3), start, 0.0, 60.0)
     assert np.abs(Fg.reshape(-1, 3, 3) - ref).max() <= TOL_FG
+
+
+def test_edge_cases_match_the_oracle():
+    """A 2 x 2 grid without angles, an empty z range, an empty time window and
+    a ring around the whole sheet, on a start shape turned by 3 degrees."""
+    t = mesh.config_tiny(seed=35, n=6, n_layers=3)
+    r2 = np.array([[[3e-5, 1e-5, 0.0], [1e-5, 3e-5, 0.0]], [[2e-5, 2e-5, 1e-6], [4e-5, 1e-5, 0.0]]])
+    fns = [dict(kind="grid", rates=r2),
+           dict(kind="uniform", rates=[5e-5, 0.0, 0.0], zmin=0.8, zmax=0.2),
+           dict(kind="uniform", rates=[5e-5, 5e-5, 0.0], init_time=100.0, end_time=100.0),
+           dict(kind="ring", centre=(12.0, 12.0), inner_radius=0.0, outer_radius=1e4, rates=[1e-5, 2e-5, 0.0],
+                angle_rad=1.2)]
+    start = G.turned(t.pos, 3.0)
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(o, fns)
+    with api.Solver(t) as s:
+        G.add_functions(s, fns)
+        s.set_positions(start)
+        s.time = 100.0
+        s.begin_step(60.0)
+        Fg, _ = s.get_Fg()
+    ref = o.grow(np.eye(3), start, 100.0, 60.0)
+    assert np.abs(Fg.reshape(-1, 3, 3) - ref).max() <= TOL_FG
+    assert np.abs(ref - np.eye(3)).max() > 1e-4

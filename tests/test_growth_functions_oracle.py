@@ -264,3 +264,27 @@ def test_rotated_fixture_matches_the_oracle():
     Fu = G.GrowthOracle(t.pos, t.conn, t.node_placement)
     G.add_functions(Fu, fns)
     assert np.abs(Fu.grow(np.eye(3), t.pos, 0.0, t.dt, t.rates).reshape(-1) - f["Fg_grow"]).max() > 1e-4
+
+
+@ref_only
+def test_edge_cases_match_the_reference_driver():
+    t = mesh.config_tiny(seed=35, n=6, n_layers=3)
+    r2 = np.array([[[3e-5, 1e-5, 0.0], [1e-5, 3e-5, 0.0]], [[2e-5, 2e-5, 1e-6], [4e-5, 1e-5, 0.0]]])
+    fns = [dict(kind="grid", rates=r2),
+           dict(kind="uniform", rates=[5e-5, 0.0, 0.0], zmin=0.8, zmax=0.2),
+           dict(kind="uniform", rates=[5e-5, 5e-5, 0.0], init_time=100.0, end_time=100.0),
+           dict(kind="ring", centre=(12.0, 12.0), inner_radius=0.0, outer_radius=1e4, rates=[1e-5, 2e-5, 0.0],
+                angle_rad=1.2)]
+    start = G.turned(t.pos, 3.0)
+    R = Ref(t)
+    G.add_functions(R, fns)
+    R.set_positions(start)
+    R.time = 100.0
+    F0 = R.get_Fg()[0]
+    R.grow(60.0, np.zeros(3 * t.n_elems))
+    F1 = R.get_Fg()[0]
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(o, fns)
+    Fo = o.grow(F0.reshape(-1, 3, 3), start, 100.0, 60.0, np.zeros(3 * t.n_elems))
+    assert np.abs(F1.reshape(-1, 3, 3) - Fo).max() <= 1e-15
+    R.close()
