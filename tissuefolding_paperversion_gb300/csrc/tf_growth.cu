@@ -507,6 +507,15 @@ __device__ bool growth_rotation(const GrowArgs& G, int e, double* Rz) {
         for (int i = 0; i < 3; ++i)
             for (int k = 0; k < 3; ++k) F[3 * i + k] += x[i] * g[k];
     }
+    // R is the orthogonal matrix nearest to F, so |R - I| <= |R - F| + |F - I|
+    // <= 2 |F - I| (Frobenius): within 0.017 no off-diagonal entry of R can
+    // exceed the reference's threshold and the iteration is not needed
+    double dev = 0.0;
+    for (int k = 0; k < 9; ++k) {
+        const double v = F[k] - ((k & 3) == 0 ? 1.0 : 0.0);
+        dev += v * v;
+    }
+    if (4.0 * dev <= 0.017 * 0.017 * (1.0 - 1e-9)) return false;
     double R[9];
     polar_rotation(F, R);
     bool off = false;
