@@ -544,19 +544,28 @@ def growth_functions_for(t):
 def run_growth(args, t):
     """The per-step growth update with growth functions of the three reference
     types (uniform, ring, grid on the current shape) against the per-element
-    rates alone; the CPU baseline is the numpy restatement of the reference's
-    calculateGrowth on the same sheet."""
+    rates alone, on the start shape and on the sheet turned by 20 degrees
+    (where every prism's growth is turned with it); the CPU baseline is the
+    numpy restatement of the reference's calculateGrowth on the same sheet."""
     from tissuefolding_paperversion_gb300 import api
 
     fns = growth_functions_for(t)
+    # the sheet turned by 20 degrees about z (its centre): every prism's deformation
+    # gradient is then a rotation, so every prism runs the polar iteration of the turn
+    p = t.pos.reshape(-1, 3)
+    c = 0.5 * (p.min(axis=0) + p.max(axis=0))
+    ang = np.deg2rad(20.0)
+    R = np.array([[np.cos(ang), -np.sin(ang), 0.0], [np.sin(ang), np.cos(ang), 0.0], [0.0, 0.0, 1.0]])
+    turned = ((p - c) @ R.T + c).reshape(-1)
     times = {}
     with api.Solver(t) as s:
         s.set_growth_rates(t.rates)
-        for with_fns in (False, True):
-            if with_fns:
+        for key in ("rates", "functions", "functions_turned"):
+            if key == "functions":
                 for f in fns:
                     kw = {k: v for k, v in f.items() if k != "kind"}
                     getattr(s, "add_" + f["kind"] + "_growth")(**kw)
+            s.set_positions(turned if key == "functions_turned" else t.pos)
             for _ in range(args.warmup):
                 s.begin_step(t.dt)
                 s.end_step()
@@ -566,11 +575,12 @@ def run_growth(args, t):
                 s.begin_step(t.dt)
                 s.end_step()                   # synchronises the stream
                 w.append(time.perf_counter() - w0)
-            times[with_fns] = float(np.median(w))
+            times[key] = float(np.median(w))
         l0 = s.launch_count()
         s.begin_step(t.dt)
         s.end_step()
         launches = s.launch_count() - l0
+    times[False], times[True] = times["rates"], times["functions"]
     extra_s = max(times[True] - times[False], 1e-9)
     cpu = None
     if not args.no_cpu_baseline:
@@ -588,8 +598,12 @@ def run_growth(args, t):
         "ms_per_step": times[True] * 1e3, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"growth-functions-{t.n_elems}", "prisms": t.n_elems, "nodes": t.n_nodes,
                    "functions": [f["kind"] for f in fns]},
-        "begin_step_ms": {"rates_only": times[False] * 1e3, "with_functions": times[True] * 1e3},
+        "begin_step_ms": {"rates_only": times[False] * 1e3, "with_functions": times[True] * 1e3,
+                          "with_functions_turned_sheet": times["functions_turned"] * 1e3},
         "functions_extra_ms": extra_s * 1e3,
+        "functions_extra_ms_turned_sheet": (times["functions_turned"] - times[False]) * 1e3,
+        "shapes": "with_functions: the start shape (no prism turned: the polar iteration is skipped); "
+                  "turned_sheet: the sheet turned by 20 degrees (every prism runs the polar iteration)",
         "timing": "host wall clock around begin_step + end_step (synchronous), median of the timed steps",
         "gpu_launches": launches,
         "cpu_baseline": cpu,

@@ -301,33 +301,23 @@ TF_API tf_status tf_time_assembly(tf_handle* h, int32_t iters, float* ms_per_ass
 /* --- solve without device allocation --------------------------------------
  * No counterpart in the reference: this is an addition for callers that may
  * not call cudaMalloc (a host that owns every device allocation, a fixed
- * memory budget, code that must not allocate between captured launches).
+ * memory budget).
  * Solves A x = b for a caller-owned 3x3 block-sparse matrix on the current
  * device with block-Jacobi preconditioned BiCGStab in FP64; every pointer is
  * a device pointer the caller owns (rowptr[n+1], colidx[nnzb], val[9*nnzb]
  * row-major blocks, b and x [3n]).  Work space is one static device array of
  * this library (about 4.3 MB, held by every GPU that loads it until exit),
  * so n_block_rows is limited to 16384; larger systems return TF_BAD_INPUT.
- * The first call on a device looks the array up and must come before any
- * stream capture.  Calls share the array: overlapping calls race, so
- * serialise them.  `stream` is a cudaStream_t (NULL: the default stream). */
+ * The first call on a device (and the first after its context changes, e.g.
+ * after cudaDeviceReset) looks the array up.  Every call synchronises
+ * `stream` and reads scalars back, so it must never be made on a stream that
+ * is being captured: it then returns TF_BAD_INPUT.  Calls share the array:
+ * overlapping calls race, so serialise them.  `stream` is a cudaStream_t
+ * (NULL: the default stream). */
 TF_API tf_status tf_solve_bsr_static(int32_t n_block_rows, const int32_t* rowptr, const int32_t* colidx,
                                      const double* val, const double* b, double* x, double rtol, int32_t max_iter,
                                      void* stream, int32_t* iters, double* relres);
 
-/* ---- discrete adjoint (no counterpart in the reference) ------------------
- * Gradients of a shape loss after n implicit steps with respect to per-element
- * in-plane growth rates r_e (rates (r_e, r_e, 0), Fg starting at I) and log
- * Young's moduli.  loss_params = {cx, cy, amp, w}:
- *   L = sum over apical nodes (z - amp exp(-((x-cx)^2 + (y-cy)^2) / (2 w^2)))^2.
- * tf_adj_forward overwrites the handle's Fg, growth rates and elastic
- * moduli (E_e = exp(logE_e), Poisson ratios kept), runs n_steps Newton steps
- * of length dt from the current positions and keeps the state every `every`
- * steps in *saved.  tf_adj_backward recomputes each span of `every` steps
- * from its saved state and solves A^T lambda = rhs per step (to a relative
- * residual of min(krylov_rtol, 1e-12): the errors of these solves are carried
- * through the earlier steps), scaling dL by dloss; it leaves the handle at the
- * final state.  Single-mesh handles only. */
 /* The reference's mesh input file (.mesh; Simulation.cpp:2074-2239): node
  * positions, tissue placement / type / circumference flags, prism node ids
  * (after Prism::checkRotationConsistency3D, Prism.cpp:364-410) and the 6 x 3
@@ -350,6 +340,19 @@ TF_API tf_status tf_write_frame(const char* path, int32_t append, double time_se
  * at least 10 entries, either may be NULL).  No reference counterpart. */
 TF_API tf_status tf_multigrid_info(tf_handle* h, int32_t* levels, int32_t* nodes, double* weights);
 
+/* ---- discrete adjoint (no counterpart in the reference) ------------------
+ * Gradients of a shape loss after n implicit steps with respect to per-element
+ * in-plane growth rates r_e (rates (r_e, r_e, 0), Fg starting at I) and log
+ * Young's moduli.  loss_params = {cx, cy, amp, w}:
+ *   L = sum over apical nodes (z - amp exp(-((x-cx)^2 + (y-cy)^2) / (2 w^2)))^2.
+ * tf_adj_forward overwrites the handle's Fg, growth rates and elastic
+ * moduli (E_e = exp(logE_e), Poisson ratios kept), runs n_steps Newton steps
+ * of length dt from the current positions and keeps the state every `every`
+ * steps in *saved.  tf_adj_backward recomputes each span of `every` steps
+ * from its saved state and solves A^T lambda = rhs per step (to a relative
+ * residual of min(krylov_rtol, 1e-12): the errors of these solves are carried
+ * through the earlier steps), scaling dL by dloss; it leaves the handle at the
+ * final state.  Single-mesh handles only. */
 typedef struct tf_adjoint tf_adjoint;
 TF_API tf_status tf_adj_forward(tf_handle* h, const double* rate, const double* logE, int32_t n_steps, double dt,
                                 int32_t every, const double* loss_params, double* loss, tf_adjoint** saved);

@@ -522,3 +522,35 @@ def rotated_case():
     ra, aa = mesh.grid_growth_inputs(35, 4, 5)
     fns = [dict(kind="uniform", rates=[5e-5, 1e-5, 0.0], angle_rad=0.2), dict(kind="grid", rates=ra, angles_deg=aa)]
     return t, turned(t.pos, 20.0), fns
+
+
+def stretched(pos, eps, centre=None):
+    """Positions stretched in x and y by 1 + eps about `centre` (a pure
+    stretch: the rotation of every prism's deformation gradient is I)."""
+    p = np.asarray(pos, dtype=np.float64).reshape(-1, 3).copy()
+    c = p.mean(axis=0) if centre is None else np.asarray(centre, dtype=np.float64)
+    p[:, :2] = c[:2] + (1.0 + eps) * (p[:, :2] - c[:2])
+    return p.reshape(-1)
+
+
+# Start shapes at the turn's thresholds: (label, kind, value, turned).  A rigid
+# turn by phi gives F = Rz(phi), whose distance 2|F - I| (Frobenius) crosses
+# 0.017 at phi = 0.00601 and whose off-diagonal entries (sin phi) and angle
+# cross the reference's 0.017 at phi = 0.0170; a stretch by 1 + eps in x and y
+# has 2|F - I| = 2 sqrt(2) eps (0.017 at eps = 0.00601) and no rotation.
+TURN_THRESHOLD_CASES = [
+    ("turn below the distance bound", "turn", 0.0059, False),
+    ("turn above the distance bound", "turn", 0.0061, False),
+    ("turn just below 0.017", "turn", 0.0169, False),
+    ("turn just above 0.017", "turn", 0.0171, True),
+    ("turn back just above 0.017", "turn", -0.0171, True),
+    ("stretch below the distance bound", "stretch", 0.0059, False),
+    ("stretch above the distance bound", "stretch", 0.0061, False),
+]
+
+
+def threshold_start(t, kind, value):
+    """Start positions of one TURN_THRESHOLD_CASES entry for tissue t."""
+    if kind == "turn":
+        return turned(t.pos, math.degrees(value))
+    return stretched(t.pos, value)

@@ -25,7 +25,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "_build", "libtforacle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libtfref.so")
-REF_SRC = "/root/reference/TissueFolding/TissueFolding/SourceCode"
+# root of the reference checkout (read only); TF_REFERENCE_DIR overrides it
+REF_ROOT = os.environ.get("TF_REFERENCE_DIR", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "TissueFolding", "TissueFolding", "SourceCode")
 
 LITERAL = 0
 CLOSED = 1
@@ -43,7 +45,7 @@ def build_port() -> str:
 def build_ref() -> str | None:
     if not os.path.isdir(REF_SRC):
         return None
-    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref")], check=True)
+    subprocess.run(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref"), f"REF={REF_SRC}"], check=True)
     return REF_LIB
 
 
@@ -214,6 +216,12 @@ class Port:
         g = np.zeros(3 * self.nn)
         self.lib().tfo_get_values(self.h, a.ctypes.data_as(C.c_void_p), g.ctypes.data_as(C.c_void_p))
         return a, g
+
+    def rhs(self):
+        """gSum of the last assembly with fixed DOFs zeroed (no matrix copy)."""
+        g = np.zeros(3 * self.nn)
+        self.lib().tfo_get_values(self.h, None, g.ctypes.data_as(C.c_void_p))
+        return g
 
     def export_filtered(self, drop=1e-13):
         L = self.lib()

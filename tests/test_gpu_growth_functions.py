@@ -317,3 +317,23 @@ def test_edge_cases_match_the_oracle():
     ref = o.grow(np.eye(3), start, 100.0, 60.0)
     assert np.abs(Fg.reshape(-1, 3, 3) - ref).max() <= TOL_FG
     assert np.abs(ref - np.eye(3)).max() > 1e-4
+
+
+@pytest.mark.parametrize("label,kind,value,expect", G.TURN_THRESHOLD_CASES)
+def test_turn_thresholds_match_the_oracle(label, kind, value, expect):
+    """The device skips the polar iteration where 2|F - I| <= 0.017 and turns
+    a prism where its rotation's off-diagonal entries and angle exceed 0.017:
+    start shapes just below and just above both bounds give the oracle's
+    growth tensors (whose rotation comes from a full SVD, no skip)."""
+    t = mesh.config_tiny(seed=41, n=5, n_layers=2, jitter=0.0)
+    fns = [dict(kind="uniform", rates=[5e-5, 1e-5, 0.0], angle_rad=0.3)]
+    start = G.threshold_start(t, kind, value)
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(o, fns)
+    ref = o.grow(np.eye(3), start, 0.0, 60.0)
+    with api.Solver(t) as s:
+        G.add_functions(s, fns)
+        s.set_positions(start)
+        s.begin_step(60.0)
+        Fg, _ = s.get_Fg()
+    assert np.abs(Fg.reshape(-1, 3, 3) - ref).max() <= TOL_FG, label

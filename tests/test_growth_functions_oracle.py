@@ -288,3 +288,39 @@ def test_edge_cases_match_the_reference_driver():
     Fo = o.grow(F0.reshape(-1, 3, 3), start, 100.0, 60.0, np.zeros(3 * t.n_elems))
     assert np.abs(F1.reshape(-1, 3, 3) - Fo).max() <= 1e-15
     R.close()
+
+
+@pytest.mark.parametrize("label,kind,value,expect", G.TURN_THRESHOLD_CASES)
+def test_turn_thresholds(label, kind, value, expect):
+    """Start shapes whose distance 2|F - I| and rotation entries sit just
+    below and just above the reference's 0.017: the prisms are turned exactly
+    where the rotation's off-diagonal entries and angle exceed it."""
+    t = mesh.config_tiny(seed=41, n=5, n_layers=2, jitter=0.0)
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    rot, Rz = G.growth_rotations(G.threshold_start(t, kind, value), t.conn, o.inv_dXde)
+    assert (rot == expect).all(), label
+    if expect:
+        np.testing.assert_allclose(np.arctan2(Rz[:, 1, 0], Rz[:, 0, 0]), -value, atol=1e-12)
+
+
+@ref_only
+@pytest.mark.parametrize("label,kind,value,expect", G.TURN_THRESHOLD_CASES)
+def test_turn_thresholds_match_the_reference_driver(label, kind, value, expect):
+    t = mesh.config_tiny(seed=41, n=5, n_layers=2, jitter=0.0)
+    fns = [dict(kind="uniform", rates=[5e-5, 1e-5, 0.0], angle_rad=0.3)]
+    start = G.threshold_start(t, kind, value)
+    R = Ref(t)
+    G.add_functions(R, fns)
+    R.set_positions(start)
+    R.grow(60.0, np.zeros(3 * t.n_elems))
+    F1 = R.get_Fg()[0]
+    R.close()
+    o = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(o, fns)
+    Fo = o.grow(np.eye(3), start, 0.0, 60.0)
+    assert np.abs(F1.reshape(-1, 3, 3) - Fo).max() <= 1e-15, label
+    # the turn changes the increment well above that agreement
+    Fu = G.GrowthOracle(t.pos, t.conn, t.node_placement)
+    G.add_functions(Fu, fns)
+    moved = np.abs(Fu.grow(np.eye(3), t.pos, 0.0, 60.0) - Fo).max()
+    assert (moved > 1e-7) == expect, (label, moved)

@@ -10,7 +10,8 @@ import pytest
 
 from tissuefolding_paperversion_gb300 import api, mesh, meshfile
 
-REF_MESH = "/root/reference/TissueFolding/ToolBox/MeshGeneration/2DEllipse"
+REF_MESH = os.path.join(os.environ.get("TF_REFERENCE_DIR", "/root/reference"),
+                        "TissueFolding", "ToolBox", "MeshGeneration", "2DEllipse")
 
 
 def _ccw(pos, conn):

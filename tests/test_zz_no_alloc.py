@@ -1,8 +1,9 @@
 """tf_solve_bsr_static: the linear solve for callers that cannot allocate
 device memory (their host owns every device allocation, or they run under a
 fixed memory budget).  It must agree with the solve behind tf_solve on the
-same system, on two calls in a row (the static work space is reused), and
-reject systems larger than its static limit.
+same system, on two calls in a row (the static work space is reused), leave
+the device's free memory unchanged on the second call, reject systems larger
+than its static limit and refuse a stream that is being captured.
 
 The test allocates device memory itself (through torch) to hold the
 caller-owned matrix and vectors; only the entry point under test must not.
@@ -60,18 +61,58 @@ def test_static_solve_matches_tf_solve_twice(eta):
     d_val = torch.from_numpy(val).to(dev)
     d_b = torch.from_numpy(g).to(dev)
     L = api.load()
-    for call in range(2):
-        d_x = torch.full((3 * t.n_nodes,), float("nan"), dtype=torch.float64, device=dev)
-        torch.cuda.synchronize()
+    d_xs = [torch.full((3 * t.n_nodes,), float("nan"), dtype=torch.float64, device=dev) for _ in range(2)]
+    torch.cuda.synchronize()
+    for call, d_x in enumerate(d_xs):
+        free_before = torch.cuda.mem_get_info(dev)[0]
         it, rr = C.c_int32(0), C.c_double(0.0)
         st = L.tf_solve_bsr_static(t.n_nodes, C.c_void_p(d_rowptr.data_ptr()), C.c_void_p(d_colidx.data_ptr()),
                                    C.c_void_p(d_val.data_ptr()), C.c_void_p(d_b.data_ptr()),
                                    C.c_void_p(d_x.data_ptr()), 1e-13, 20000, None, C.byref(it), C.byref(rr))
         assert st == api.TF_OK, L.tf_last_error().decode()
         torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info(dev)[0]
+        if call == 1:
+            # the first call may still page in the library's static array and the
+            # kernels' local memory; the second must not take any device memory
+            assert free_after == free_before, (free_before, free_after)
         x = d_x.cpu().numpy()
         assert rr.value <= 1e-13 and it.value > 0
         assert np.abs(x - du_ref).max() <= TOL * np.abs(du_ref).max(), call
+
+
+def test_static_solve_refuses_a_capturing_stream():
+    torch = pytest.importorskip("torch")
+    dev = torch.device("cuda:0")
+    n = 4
+    rowptr = torch.arange(n + 1, dtype=torch.int32, device=dev)
+    colidx = torch.arange(n, dtype=torch.int32, device=dev)
+    val = torch.eye(3, dtype=torch.float64, device=dev).reshape(-1).repeat(n)
+    b = torch.ones(3 * n, dtype=torch.float64, device=dev)
+    x = torch.zeros(3 * n, dtype=torch.float64, device=dev)
+    y = torch.zeros(1, device=dev)
+    L = api.load()
+    it, rr = C.c_int32(0), C.c_double(0.0)
+    side = torch.cuda.Stream(device=dev)
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=side):
+        y.add_(1.0)
+        st = L.tf_solve_bsr_static(n, C.c_void_p(rowptr.data_ptr()), C.c_void_p(colidx.data_ptr()),
+                                   C.c_void_p(val.data_ptr()), C.c_void_p(b.data_ptr()), C.c_void_p(x.data_ptr()),
+                                   1e-10, 10, C.c_void_p(side.cuda_stream), C.byref(it), C.byref(rr))
+    assert st == api.TF_BAD_INPUT
+    assert "captured" in L.tf_last_error().decode()
+    # the capture was left intact: the graph replays
+    graph.replay()
+    torch.cuda.synchronize()
+    assert float(y.item()) == 1.0
+    # and the same call outside a capture solves the identity system
+    st = L.tf_solve_bsr_static(n, C.c_void_p(rowptr.data_ptr()), C.c_void_p(colidx.data_ptr()),
+                               C.c_void_p(val.data_ptr()), C.c_void_p(b.data_ptr()), C.c_void_p(x.data_ptr()),
+                               1e-10, 10, None, C.byref(it), C.byref(rr))
+    assert st == api.TF_OK, L.tf_last_error().decode()
+    assert np.allclose(x.cpu().numpy(), 1.0)
 
 
 def test_static_solve_rejects_oversized_system():

@@ -10,12 +10,18 @@
 //
 // Host code cannot use the array's name as a device address, so the first
 // call on each device looks the address up with cudaGetSymbolAddress while
-// that device is current, and caches it.  Do that first call before any
-// stream capture.  All calls on a device share the one array: calls that
+// that device is current, and caches it together with the CUDA context it
+// came from; a call in another context (after cudaDeviceReset, say) looks it
+// up again.  Every call synchronises its stream and reads scalars back to the
+// host between chunks of iterations, so no call may be made on a stream that
+// is being captured: such a call returns TF_BAD_INPUT and leaves the capture
+// untouched.  All calls on a device share the one array: calls that
 // overlap on the GPU (two streams, two host threads) race on it and give
 // wrong results, so serialise them.  Each call clears the reduction ticket
 // and the scalars it reads before its first kernel, and writes every work
 // vector before reading it, so nothing carries over from the previous call.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "tf_internal.cuh"
@@ -263,21 +269,55 @@ __global__ void ks_x(SCtx c, double* __restrict__ x) {
 }
 
 std::mutex g_addr_mutex;
-double* g_addr[64] = {};
+struct ScratchAddr {
+    CUcontext ctx;
+    double* ptr;
+};
+ScratchAddr g_addr[64] = {};
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+CtxGetCurrentFn g_ctx_get = nullptr;
 
+// The current CUDA context, through the driver entry point the runtime hands
+// out (the library does not link the driver library itself).
+tf_status current_context(CUcontext* ctx) {
+    if (!g_ctx_get) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetDriverEntryPointByVersion(cuCtxGetCurrent)");
+        if (q != cudaDriverEntryPointSuccess || !fn) {
+            set_error("tf_solve_bsr_static: the driver offers no cuCtxGetCurrent");
+            return TF_CUDA_ERROR;
+        }
+        g_ctx_get = reinterpret_cast<CtxGetCurrentFn>(fn);
+    }
+    *ctx = nullptr;
+    if (g_ctx_get(ctx) != CUDA_SUCCESS || !*ctx) {
+        set_error("tf_solve_bsr_static: no current CUDA context");
+        return TF_CUDA_ERROR;
+    }
+    return TF_OK;
+}
+
+// Device address of g_static_scratch for `device`, looked up once per device
+// and context with that device current.
 tf_status scratch_address(int device, double** out) {
     if (device < 0 || device >= 64) {
         set_error("device ordinal out of range for the static solve");
         return TF_BAD_INPUT;
     }
     std::lock_guard<std::mutex> lock(g_addr_mutex);
-    if (!g_addr[device]) {
+    CUcontext ctx = nullptr;
+    tf_status s = current_context(&ctx);
+    if (s != TF_OK) return s;
+    if (!g_addr[device].ptr || g_addr[device].ctx != ctx) {
         void* p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
         if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_static_scratch)");
-        g_addr[device] = static_cast<double*>(p);
+        g_addr[device].ptr = static_cast<double*>(p);
+        g_addr[device].ctx = ctx;
     }
-    *out = g_addr[device];
+    *out = g_addr[device].ptr;
     return TF_OK;
 }
 
@@ -298,12 +338,19 @@ extern "C" TF_API tf_status tf_solve_bsr_static(int32_t n_block_rows, const int3
                   std::to_string(kStaticMaxNodes));
         return TF_BAD_INPUT;
     }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    TF_CUDA(cudaStreamIsCapturing(st, &cap));
+    if (cap != cudaStreamCaptureStatusNone) {
+        set_error("tf_solve_bsr_static: the stream is being captured; this call synchronises and reads back, "
+                  "so it cannot run inside a capture");
+        return TF_BAD_INPUT;
+    }
     int device = 0;
     TF_CUDA(cudaGetDevice(&device));
     double* base = nullptr;
     tf_status s = scratch_address(device, &base);
     if (s != TF_OK) return s;
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     SCtx c{n_block_rows, rowptr, colidx, val, base};
     const int grid = cdiv(n_block_rows, kStaticThreads);
     // clear the ticket and scalars, then the tolerance
