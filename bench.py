@@ -16,8 +16,21 @@ Reported (one JSON line on rank 0):
                (the kernel's binding roofline)
   cpu_baseline the reference's algorithm (oracle port, literal 3^6 tangent),
                all host threads, on a bounded sample of prisms
+  e2e_newton_step  the whole Newton step through the C ABI with host
+               positions in and out (tf_set_positions, tf_newton_step,
+               tf_get_positions), wall clock
+  config_small the 1,600-prism configuration: GPU Newton step against the
+               CPU port's whole step (banded-LU stand-in for Pardiso)
+  batch        256 seeded instances (1k-50k prisms) advanced in one handle
+               against the plain GPU step looped over a stratified subset
+  adjoint      gradient through 50 steps of the 320k-prism sheet
+               (checkpoints every 10): backward / forward cost, and the
+               gradient against central differences along seeded directions
+(`--quick` leaves the last three out.)
 
-`--impl reference` times the CPU implementation alone on the same metric.
+`--impl reference` times the CPU implementation alone on the same metric:
+each timed step is one bounded sample of the assembly; the full-assembly
+time it implies is reported under a key that says it is a projection.
 Inputs (~1.3 GB of device data per assembly) exceed the 129 MB L2, so no
 flush is needed between timed iterations.
 """
@@ -137,6 +150,60 @@ def cpu_sample(t, seconds_target=15.0, literal=True):
     return n / dt, n, dt, Port.threads()
 
 
+def cpu_newton_small(steps=2):
+    """The reference's own CPU-runnable case (1,600 prisms, 3,969 DOF): whole
+    implicit steps of the oracle port (literal 3^6 tangent, the reference's
+    scatter and CSR filter, banded-LU stand-in for Pardiso), all host
+    threads.  Returns (ms per step, Newton iterations per step, threads)."""
+    from oracle.oracle import LITERAL, Port
+    from tissuefolding_paperversion_gb300 import mesh
+
+    t = mesh.config_small(seed=0)
+    p = Port(t)
+    p.step(t.dt, t.rates, LITERAL)   # warm-up
+    its = []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        its.append(p.step(t.dt, t.rates, LITERAL)["iters"])
+    ms = (time.perf_counter() - t0) / steps * 1e3
+    p.close()
+    return ms, float(np.mean(its)), Port.threads()
+
+
+def recorded_cpu_newton_large():
+    """The CPU Newton step of the 320,000-prism sheet as recorded when its
+    20-step oracle run was made (oracle port, closed-form tangent, sparse
+    storage, SuperLU-preconditioned GMRES as the Pardiso stand-in)."""
+    f = os.path.join(ROOT, "tests", "golden", "steps_large_320k.npz")
+    if not os.path.exists(f):
+        return None
+    d = np.load(f)
+    return {"ms_per_step_median": float(np.median(d["step_seconds"])) * 1e3,
+            "ms_first_step_with_factorisation": float(d["step_seconds"][0]) * 1e3,
+            "newton_iters_per_step": float(np.mean(d["iters"])), "threads": int(d["threads"]),
+            "how": "recorded when tests/golden/steps_large_320k.npz was made (8-core x86 host), not in this run"}
+
+
+def small_config_measure(args):
+    """GPU vs CPU Newton step on the 1,600-prism configuration."""
+    from tissuefolding_paperversion_gb300 import api, mesh
+
+    t = mesh.config_small(seed=0)
+    with api.Solver(t) as s:
+        s.set_growth_rates(t.rates)
+        for _ in range(3):
+            s.newton_step(t.dt)
+        outs = [s.newton_step(t.dt) for _ in range(10)]
+    gpu_ms = float(np.mean([o["ms_total"] for o in outs]))
+    out = {"workload": t.name, "prisms": t.n_elems, "gpu_ms_per_step": gpu_ms,
+           "gpu_krylov_iters_per_step": float(np.mean([o["krylov_total"] for o in outs]))}
+    if not args.no_cpu_baseline:
+        ms, its, th = cpu_newton_small()
+        out.update({"cpu_ms_per_step": ms, "cpu_cores": th, "cpu_kind": "port",
+                    "cpu_newton_iters_per_step": its, "cpu_over_gpu": ms / gpu_ms})
+    return out
+
+
 def run_reference(args, t):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -146,24 +213,38 @@ def run_reference(args, t):
     Port.set_threads(os.cpu_count() or 1)
     rates = []
     for _ in range(args.warmup):
-        cpu_sample(t, seconds_target=2.0)
-    samples = []
+        cpu_sample(t, seconds_target=1.0)
+    samples, secs = [], []
+    w0 = time.perf_counter()
     for _ in range(args.steps):
         r, n, dt, th = cpu_sample(t, seconds_target=args.ref_seconds)
         rates.append(r)
         samples.append(n)
+        secs.append(dt)
+    wall = time.perf_counter() - w0
     value = statistics.median(rates)
+    ms_small, its_small, th_small = cpu_newton_small()
     line = {
         "impl": "reference", "metric": "prism K+f assemblies/s", "value": value, "unit": "prisms/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": t.name, "prisms": t.n_elems, "nodes": t.n_nodes, "dof": 3 * t.n_nodes,
                    "l2": "inputs larger than L2"},
-        "ms_per_step": t.n_elems / value * 1e3,
+        # each timed step is one bounded sample of the assembly (its prisms below)
+        "ms_per_step": wall / args.steps * 1e3,
+        "prisms_per_step": int(statistics.median(samples)),
+        "projected_ms_per_full_assembly": t.n_elems / value * 1e3,
+        "projection": "prisms of the workload / measured prisms/s; not timed as one piece",
         "cpu_baseline": {"value": value, "unit": "prisms/s", "cores": Port.threads(), "kind": "port",
                          "sample": f"element loop (literal 3^6 tangent, the reference's algorithm) + serial "
-                                   f"scatter over the first {samples[-1]} of {t.n_elems} prisms"},
+                                   f"scatter over the first {samples[-1]} of {t.n_elems} prisms per step"},
         "e2e": {"value": value, "unit": "prisms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "newton_step_cpu": {
+            "config_small": {"ms_per_step": ms_small, "newton_iters_per_step": its_small, "cores": th_small,
+                             "prisms": 1600,
+                             "how": "whole implicit steps of the port (literal tangent, banded-LU stand-in for "
+                                    "Pardiso), measured in this run"},
+            "config_large": recorded_cpu_newton_large()},
     }
     print(json.dumps(line))
 
@@ -242,8 +323,36 @@ def run_gpu(args, t):
         s.assemble()
         g = s.residual()
     e2e_s = (time.perf_counter() - e0) / args.steps
+    # the whole Newton step through the C ABI as the reference's caller uses it
+    # (tf_set_positions from host memory, tf_newton_step, tf_get_positions back)
+    host = s.positions()
+    for _ in range(2):
+        s.set_positions(host)
+        s.newton_step(t.dt)
+        host = s.positions()
+    e0 = time.perf_counter()
+    dev_ms = 0.0
+    for _ in range(args.steps):
+        s.set_positions(host)
+        dev_ms += s.newton_step(t.dt)["ms_total"]
+        host = s.positions()
+    e2e_step_ms = (time.perf_counter() - e0) / args.steps * 1e3
     s.close()
+    e2e_step = {"ms_per_step": e2e_step_ms, "device_ms_per_step": dev_ms / args.steps,
+                "calls": "tf_set_positions (H2D), tf_newton_step, tf_get_positions (D2H)",
+                "h2d_bytes_per_step": 8 * 3 * nn, "d2h_bytes_per_step": 8 * 3 * nn}
+    small = None if args.quick else small_config_measure(args)
+    batch = None
+    if not args.quick and world == 1:
+        from tissuefolding_paperversion_gb300 import mesh
 
+        ts = [mesh.config_batch_instance(k) for k in range(args.instances)]
+        batch = batch_measure(ts, 3, 1, loop_every=8)
+        batch["instances"] = len(ts)
+        batch["prisms"] = int(sum(x.n_elems for x in ts))
+    adjoint = None
+    if not args.quick and world == 1:
+        adjoint = adjoint_measure(t, args.adj_steps, args.adj_every, args.adj_fd_default)
     if rank != 0:
         return
     line = {
@@ -266,9 +375,16 @@ def run_gpu(args, t):
         "fp64": fp64,
         "gpu_launches": launches,
         "clocks": clk,
+        "e2e_newton_step": e2e_step,
     }
+    if small is not None:
+        line["config_small"] = small
+    if batch is not None:
+        line["batch"] = batch
+    if adjoint is not None:
+        line["adjoint"] = adjoint
     if not args.no_cpu_baseline:
-        r, n, dt, th = cpu_sample(t, seconds_target=args.ref_seconds)
+        r, n, dt, th = cpu_sample(t, seconds_target=max(args.ref_seconds, 12.0))
         line["cpu_baseline"] = {"value": r, "unit": "prisms/s", "cores": th, "kind": "port",
                                 "sample": f"element loop (literal 3^6 tangent) + serial scatter over "
                                           f"{n} of {ne} prisms, {dt:.1f} s"}
@@ -291,13 +407,78 @@ def run_assembly_only(args, t):
     s.close()
 
 
+def batch_measure(ts, steps, warmup, loop_every=1, dev=0, dist=None):
+    """The batched sweep on this rank's instances `ts`: one handle advancing
+    all of them (per-instance Newton counts and convergence masks, CUDA-graph
+    chunks, autotuned elements per CTA) against the plain GPU step looped
+    over them, one handle each.  With loop_every = k > 1 the loop is timed
+    over every k-th instance in size order (a stratified subset) and its
+    rate stands for the whole loop.  Rates are instance time steps
+    (implicit solves) per second of wall clock; under torch.distributed the
+    times are the max over ranks."""
+    from tissuefolding_paperversion_gb300 import api, shard
+
+    def slowest(x):
+        return shard.max_over_ranks(dist, x) if dist is not None else x
+
+    b = api.Batch(ts, device=dev)
+    b.set_growth_rates()
+    for _ in range(warmup):
+        b.step(ts[0].dt)
+    if dist is not None:
+        dist.barrier()
+    l0 = b.launch_count()
+    w0 = time.perf_counter()
+    outs = [b.step(ts[0].dt) for _ in range(steps)]
+    wall_b = slowest(time.perf_counter() - w0)
+    launches = b.launch_count() - l0
+    ms_b = slowest(sum(o["ms_total"] for o in outs))
+    ept = b.elements_per_cta()
+    b.close()
+    order = np.argsort([t.n_elems for t in ts], kind="stable")
+    loop_ids = [int(i) for i in order[::loop_every]]
+    solvers = []
+    for i in loop_ids:
+        s = api.Solver(ts[i], device=dev)
+        s.set_growth_rates(ts[i].rates)
+        solvers.append((s, ts[i]))
+    for s, t in solvers:
+        for _ in range(max(1, warmup)):
+            s.newton_step(t.dt)
+    loop_steps = max(1, min(steps, 2))
+    if dist is not None:
+        dist.barrier()
+    w0 = time.perf_counter()
+    ms_l = 0.0
+    for _ in range(loop_steps):
+        for s, t in solvers:
+            ms_l += s.newton_step(t.dt)["ms_total"]
+    wall_l = slowest(time.perf_counter() - w0)
+    ms_l = slowest(ms_l)
+    for s, _ in solvers:
+        s.close()
+    rate_b = len(ts) * steps / wall_b
+    rate_l = len(loop_ids) * loop_steps / wall_l
+    return {"batched": {"value": rate_b, "unit": "instance steps/s", "steps": steps,
+                        "ms_per_step": wall_b / steps * 1e3, "device_ms_per_step": ms_b / steps,
+                        "newton_iters_max": int(max(o["iters"].max() for o in outs)),
+                        "elements_per_cta": ept, "gpu_launches": launches},
+            "looped_plain": {"value": rate_l, "unit": "instance steps/s", "steps": loop_steps,
+                             "instances_timed": len(loop_ids),
+                             "subset": "all instances" if loop_every == 1 else
+                             f"every {loop_every}th instance in size order ({len(loop_ids)} of {len(ts)}); "
+                             "its rate stands for the whole loop",
+                             "device_ms_per_instance_step": ms_l / (loop_steps * len(loop_ids))},
+            "speedup_vs_looped": rate_b / rate_l}
+
+
 def run_batch(args):
     """Batched sweep: 256 tissues of 1k-50k prisms in one handle vs the plain
     GPU step looped over the instances (one handle each).  Metric: instance
     time steps (implicit solves) per second.  Under torchrun the instances are
     sharded over the ranks (balanced by prism count, no exchange; timings are
     the max over ranks), so the total work is fixed: strong scaling."""
-    from tissuefolding_paperversion_gb300 import api, mesh, shard
+    from tissuefolding_paperversion_gb300 import mesh, shard
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -312,80 +493,43 @@ def run_batch(args):
     mine = shard.shard_instances([t.n_elems for t in ts_all], world)[rank]
     ts = [ts_all[i] for i in mine]
     prisms = sum(t.n_elems for t in ts_all)
-    dev = local if world > 1 else 0
-
-    def slowest(x):
-        return shard.max_over_ranks(dist, x) if dist is not None else x
-
-    b = api.Batch(ts, device=dev)
-    b.set_growth_rates()
-    for _ in range(args.warmup):
-        b.step(ts[0].dt)
-    if dist is not None:
-        dist.barrier()
-    l0 = b.launch_count()
-    w0 = time.perf_counter()
-    outs = [b.step(ts[0].dt) for _ in range(args.steps)]
-    wall_b = slowest(time.perf_counter() - w0)
-    launches = b.launch_count() - l0
-    ms_b = slowest(sum(o["ms_total"] for o in outs))
-    ept = b.elements_per_cta()
-    b.close()
-    solvers = []
-    for t in ts:
-        s = api.Solver(t, device=dev)
-        s.set_growth_rates(t.rates)
-        solvers.append(s)
-    for s, t in zip(solvers, ts):
-        for _ in range(max(1, args.warmup)):
-            s.newton_step(t.dt)
-    loop_steps = max(1, min(args.steps, 2))
-    if dist is not None:
-        dist.barrier()
-    w0 = time.perf_counter()
-    ms_l = 0.0
-    for _ in range(loop_steps):
-        for s, t in zip(solvers, ts):
-            ms_l += s.newton_step(t.dt)["ms_total"]
-    wall_l = slowest(time.perf_counter() - w0)
-    ms_l = slowest(ms_l)
-    for s in solvers:
-        s.close()
-    rate_b = n * args.steps / wall_b
-    rate_l = n * loop_steps / wall_l
+    r = batch_measure(ts, args.steps, args.warmup, 1, local if world > 1 else 0, dist)
     if rank != 0:
         return
+    rate_b = r["batched"]["value"] * (n / len(ts))
     print(json.dumps({
         "metric": "batched implicit solves/s", "value": rate_b, "unit": "instance steps/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall_b / args.steps * 1e3, "higher_is_better": True,
-        "scaling": "strong", "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"batch-{n}", "instances": n, "prisms": prisms, "elements_per_cta": ept,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["batched"]["ms_per_step"],
+        "higher_is_better": True, "scaling": "strong", "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"batch-{n}", "instances": n, "prisms": prisms,
+                   "elements_per_cta": r["batched"]["elements_per_cta"],
                    "parallelism": f"instances sharded over {world} ranks" if world > 1 else "single"},
-        "looped_plain": {"value": rate_l, "unit": "instance steps/s", "steps": loop_steps,
-                         "device_ms_per_step": ms_l / loop_steps},
-        "speedup_vs_looped": rate_b / rate_l,
-        "batched_device_ms_per_step": ms_b / args.steps,
-        "newton_iters_max": int(max(o["iters"].max() for o in outs)),
-        "gpu_launches": launches,
+        "looped_plain": r["looped_plain"],
+        "speedup_vs_looped": r["speedup_vs_looped"],
+        "batched_device_ms_per_step": r["batched"]["device_ms_per_step"],
+        "newton_iters_max": r["batched"]["newton_iters_max"],
+        "gpu_launches": r["batched"]["gpu_launches"],
     }))
 
 
-def run_adjoint(args, t):
-    """Adjoint of n implicit steps on the 320k-prism sheet: loss = squared
-    distance of the final apical surface to z = 5 exp(-r^2 / (2 40^2)) µm
-    (r from the sheet centre), gradient with respect to the per-element
-    growth rates and log E; states saved every `every` steps and recomputed
-    in between.  Reports forward and backward device-synchronised wall time
-    and their ratio."""
+def adjoint_measure(t, n, every, fd_dirs, seed=1234):
+    """Adjoint of n implicit steps: loss = squared distance of the final
+    apical surface to z = 5 exp(-r^2 / (2 40^2)) um (r from the sheet
+    centre), gradient with respect to the per-element growth rates and log E;
+    states saved every `every` steps and recomputed in between.  Forward and
+    backward are timed (device-synchronised wall clock) at the default
+    tolerances.  With fd_dirs > 0 the gradient of a run with every solve
+    tight (Newton |du| <= 1e-11, Krylov 1e-13) is checked against central
+    differences (h = 1e-6 relative) of that run along fd_dirs seeded
+    directions, alternating growth rates and log E."""
     from tissuefolding_paperversion_gb300 import api
 
-    s = api.Solver(t)
     xy = t.pos.reshape(-1, 3)[:, :2]
     c = 0.5 * (xy.min(axis=0) + xy.max(axis=0))
     params = np.array([c[0], c[1], 5.0, 40.0])
     rate = t.rates.reshape(-1, 3)[:, 0].copy()
     logE = np.log(t.E)
-    n, every = args.adj_steps, args.adj_every
+    s = api.Solver(t)
     # warm-up: one short forward/backward (graphs, autotuner)
     s.set_positions(t.pos)
     _, sv = s.adjoint_forward(rate, logE, 1, t.dt, 1, params)
@@ -401,52 +545,56 @@ def run_adjoint(args, t):
     bwd = time.perf_counter() - w0
     launches = s.launch_count() - l0
     sv.free()
-    fd = []
-    rng = np.random.default_rng(1234)
-    for _ in range(args.adj_fd):
-        d = rng.standard_normal(t.n_elems)
-        h = 1e-3 * np.abs(rate).mean()
-        out = []
-        for sgn in (1.0, -1.0):
-            s.set_positions(t.pos)
-            lv, sp = s.adjoint_forward(rate + sgn * h * d, logE, n, t.dt, every, params)
-            sp.free()
-            out.append(lv)
-        f = (out[0] - out[1]) / (2 * h)
-        fd.append({"adjoint": float(gr @ d), "fd": f, "rel": abs(float(gr @ d) - f) / max(abs(f), 1e-300)})
     s.close()
-    if args.adj_fd:
-        # the same check with the step solved tightly (Newton |du| <= 1e-11, Krylov 1e-13): at the
-        # default tolerances the central differences carry the solver's error over n steps
+    out = {"forward_s": fwd, "backward_s": bwd, "backward_over_forward": bwd / fwd, "loss": loss,
+           "steps": n, "checkpoint_every": every, "parameters": 2 * t.n_elems,
+           "grad_norm": {"rate": float(np.linalg.norm(gr)), "logE": float(np.linalg.norm(ge))},
+           "gpu_launches": launches}
+    if fd_dirs:
         ts = api.Solver(t, newton_tol=1e-11, krylov_rtol=1e-13)
+
+        def lossf(r, e):
+            ts.set_positions(t.pos)
+            lv, sp = ts.adjoint_forward(r, e, n, t.dt, every, params)
+            sp.free()
+            return lv
+
         ts.set_positions(t.pos)
         _, sv = ts.adjoint_forward(rate, logE, n, t.dt, every, params)
-        gt, _ = ts.adjoint_backward(sv)
+        gt_r, gt_e = ts.adjoint_backward(sv)
         sv.free()
-        rng = np.random.default_rng(1234)
-        for k in range(args.adj_fd):
+        rng = np.random.default_rng(seed)
+        checks = []
+        for k in range(fd_dirs):
             d = rng.standard_normal(t.n_elems)
-            h = 1e-3 * np.abs(rate).mean()
-            out = []
-            for sgn in (1.0, -1.0):
-                ts.set_positions(t.pos)
-                lv, sp = ts.adjoint_forward(rate + sgn * h * d, logE, n, t.dt, every, params)
-                sp.free()
-                out.append(lv)
-            f = (out[0] - out[1]) / (2 * h)
-            fd[k]["tight_solve"] = {"adjoint": float(gt @ d), "fd": f,
-                                    "rel": abs(float(gt @ d) - f) / max(abs(f), 1e-300)}
+            if k % 2 == 0:
+                h = 1e-6 * np.abs(rate).max()
+                f = (lossf(rate + h * d, logE) - lossf(rate - h * d, logE)) / (2 * h)
+                adj = float(gt_r @ d)
+            else:
+                h = 1e-6
+                f = (lossf(rate, logE + h * d) - lossf(rate, logE - h * d)) / (2 * h)
+                adj = float(gt_e @ d)
+            checks.append({"parameter": "rate" if k % 2 == 0 else "logE", "adjoint": adj, "fd": f,
+                           "rel": abs(adj - f) / max(abs(f), 1e-300)})
         ts.close()
+        out["fd"] = {"directions": fd_dirs, "h": "1e-6 relative (rates: 1e-6 x the largest rate; log E: 1e-6)",
+                     "solves": "Newton |du| <= 1e-11, Krylov relative residual 1e-13",
+                     "max_rel_err": max(c["rel"] for c in checks), "checks": checks}
+    return out
+
+
+def run_adjoint(args, t):
+    """The adjoint workload on its own (see adjoint_measure)."""
+    n, every = args.adj_steps, args.adj_every
+    r = adjoint_measure(t, n, every, args.adj_fd)
     print(json.dumps({
-        "metric": "adjoint backward / forward cost", "value": bwd / fwd, "unit": "ratio", "n_gpus": 1,
-        "steps": n, "warmup": 1, "ms_per_step": (fwd + bwd) / n * 1e3, "higher_is_better": False,
-        "dtype": "f64", "data": "synthetic",
+        "metric": "adjoint backward / forward cost", "value": r["backward_over_forward"], "unit": "ratio",
+        "n_gpus": 1, "steps": n, "warmup": 1, "ms_per_step": (r["forward_s"] + r["backward_s"]) / n * 1e3,
+        "higher_is_better": False, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"adjoint-{t.name}", "prisms": t.n_elems, "steps": n, "checkpoint_every": every,
                    "loss": "sum over apical nodes (z - 5 exp(-r^2/(2 40^2)))^2", "parameters": 2 * t.n_elems},
-        "forward_s": fwd, "backward_s": bwd, "loss": loss,
-        "grad_norm": {"rate": float(np.linalg.norm(gr)), "logE": float(np.linalg.norm(ge))},
-        "fd_checks": fd,
-        "gpu_launches": launches,
+        **r,
     }))
 
 
@@ -629,7 +777,12 @@ def main():
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--mode", default="step", choices=["step", "assembly"],
                     help="step: Newton steps (the bench); assembly: back-to-back K+f assemblies only")
-    ap.add_argument("--ref-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-seconds", type=float, default=6.0,
+                    help="CPU seconds per timed reference step and per CPU-baseline sample")
+    ap.add_argument("--quick", action="store_true",
+                    help="plain workload only: leave out the 1,600-prism, batch and adjoint sub-measurements")
+    ap.add_argument("--adj-fd-default", type=int, default=2,
+                    help="central-difference directions of the adjoint sub-measurement of the plain workload")
     ap.add_argument("--precond", type=int, default=0,
                     help="0 auto (smoothed-aggregation multigrid from 20,000 nodes), 1 block-Jacobi, "
                          "2 smoothed-aggregation multigrid, 3 plain-aggregation multigrid")
