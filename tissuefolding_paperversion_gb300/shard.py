@@ -3,8 +3,8 @@
 The batched sweep has no exchange between instances, so a multi-GPU run gives
 each rank a subset of the instances and runs them as one batch on its own GPU;
 the only communication is the final gather of per-instance results and the
-max-over-ranks timing.  A single mesh does not shard without an interface halo
-per SpMV, which is not built: several ranks on one mesh run replicas.
+max-over-ranks timing.  One mesh over several ranks needs an interface halo
+per assembly and per matrix-vector product: that is partition.py.
 """
 from __future__ import annotations
 
