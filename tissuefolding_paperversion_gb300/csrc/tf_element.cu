@@ -20,9 +20,24 @@
 //     where per node c:  u_c = c1 dN_c + sigma_v' dN_c,
 //                        w_c = c2 dN_c + P^T dN_c,   v_c = sigma_v' dN_c,
 //     and Q = c2 I + P, P = 0.5 eta w dV (I/dt - grad v) (primes: times
-//     w dV).  That is 45 FP64 FMAs per block and Gauss point instead of 64;
-//     without viscosity K_ab = K_ba^T and only the 21 pairs a <= b are
+//     w dV).  That is 45 multiply-adds per block and Gauss point instead of
+//     64; without viscosity K_ab = K_ba^T and only the 21 pairs a <= b are
 //     formed.
+//
+// Precision split.  GB300 issues FP32 FMAs at about 64 times its FP64 rate,
+// and the tangent's block sums are ~85 % of the kernel's FP64 work.  Phase A
+// (deformation gradient, stress, shape gradients, forces) stays FP64.  The
+// per-Gauss-point vectors the blocks are built from are split into
+// double-float pairs x = hi + lo (two FP32 values, ~48 significant bits) and
+// the block sums run in double-float arithmetic on the FP32 pipe: products by
+// Dekker's exact product (hi*hi and its rounding error by one FMA, plus the
+// cross terms), sums by Knuth's two-sum, the low parts gathered in a second
+// FP32 accumulator and renormalised once per Gauss point (Dekker, "A
+// floating-point technique for extending the available precision", 1971;
+// Knuth, TAOCP vol. 2, 4.2.2).  A block entry carries a relative error of
+// ~1e-13 of its largest term, far inside the 1e-11 parity bound and far
+// below what moves a Newton iterate; the forces and everything the residual
+// depends on stay FP64.
 //
 // Layout: one CTA handles NE prisms.  Phase A: one thread per (prism, Gauss
 // point) builds the per-point vectors in shared memory.  Phase B: each
@@ -216,18 +231,112 @@ __device__ __forceinline__ void gauss_point(const ElemArgs& A, int e, int gp, bo
     }
 }
 
-// Shared per-Gauss-point vectors of the fast kernel.
+// ---- double-float arithmetic (phase B) ----------------------------------
+// A value is hi + lo with hi, lo FP32.  Every operation is an explicit
+// rounding intrinsic, so no instantiation of the kernel contracts or
+// reassociates differently (the order-fixed assembly stays bitwise
+// reproducible whatever tile the autotuner picks).
+
+// The FP64 <-> FP32 conversion instructions run on GB300's slow FP64 path,
+// so the split and the join work on the bit patterns (integer pipe) with one
+// FP64 subtraction or addition each.
+
+// float with x's value rounded to 24 significant bits; x must be a double
+// whose low 29 mantissa bits are zero (then the result is exact): sign,
+// exponent rebased 1023 -> 127, the top 23 mantissa bits.  Magnitudes below
+// FP32's normal range become a signed zero; NaN and infinity stay NaN and
+// infinity.
+__device__ __forceinline__ float f32_of_trunc(unsigned hi, unsigned lo) {
+    const unsigned sgn = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    const int fe = e - 896;
+    unsigned f = sgn | ((unsigned)fe << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    f = (fe > 0) ? f : sgn;
+    f = (e == 0x7ff) ? (sgn | 0x7f800000u | ((hi & 0xfffffu) ? 0x400000u : 0u)) : f;
+    return __uint_as_float(f);
+}
+
+// x rounded to 24 significant bits (round half away from zero on the bit
+// pattern; the carry runs into the exponent), as a double and as a float.
+__device__ __forceinline__ double round24(double x, float* f) {
+    const unsigned lo = __double2loint(x), hi = __double2hiint(x);
+    const unsigned lo2 = lo + (1u << 28);
+    const unsigned hi2 = hi + (lo2 < lo ? 1u : 0u);
+    const unsigned lo3 = lo2 & ~((1u << 29) - 1u);
+    const bool special = ((hi >> 20) & 0x7ffu) == 0x7ffu;
+    *f = f32_of_trunc(special ? hi : hi2, special ? lo : lo3);
+    return special ? x : __hiloint2double(hi2, lo3);
+}
+
+// x = hi + lo, hi and lo FP32 (~48 significant bits in all)
+__device__ __forceinline__ float2 df_split(double x) {
+    float h, l;
+    const double hd = round24(x, &h);
+    round24(x - hd, &l);
+    return make_float2(h, l);
+}
+
+// float -> double, exact, on the bit pattern (subnormal floats become zero)
+__device__ __forceinline__ double f64_of(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    const unsigned sgn = u & 0x80000000u;
+    unsigned hi = sgn | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+    hi = (e == 0u) ? sgn : hi;
+    hi = (e == 0xffu) ? (sgn | 0x7ff00000u | ((u & 0x7fffffu) ? 0x80000u : 0u)) : hi;
+    const unsigned lo = (e == 0u || e == 0xffu) ? 0u : (u << 29);
+    return __hiloint2double(hi, lo);
+}
+
+__device__ __forceinline__ double df_join(float h, float l) { return f64_of(h) + f64_of(l); }
+
+// (H, L) += x * y: Dekker's product (the rounding error of hi*hi by one FMA,
+// the cross terms into the low word; lo*lo is below the format's precision),
+// Knuth's two-sum of the high words, the error into the low word.
+__device__ __forceinline__ void df_mac(float& H, float& L, float2 x, float2 y) {
+    const float p = __fmul_rn(x.x, y.x);
+    float e = __fmaf_rn(x.x, y.x, -p);
+    e = __fmaf_rn(x.x, y.y, e);
+    e = __fmaf_rn(x.y, y.x, e);
+    const float s = __fadd_rn(H, p);
+    const float bb = __fsub_rn(s, H);
+    const float err = __fadd_rn(__fsub_rn(H, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    L = __fadd_rn(L, __fadd_rn(err, e));
+    H = s;
+}
+
+// (H, L) += x
+__device__ __forceinline__ void df_add(float& H, float& L, float2 x) {
+    const float s = __fadd_rn(H, x.x);
+    const float bb = __fsub_rn(s, H);
+    const float err = __fadd_rn(__fsub_rn(H, __fsub_rn(s, bb)), __fsub_rn(x.x, bb));
+    L = __fadd_rn(L, __fadd_rn(err, x.y));
+    H = s;
+}
+
+// Fast two-sum: the low word brought back under half an ulp of the high word.
+__device__ __forceinline__ void df_norm(float& H, float& L) {
+    const float s = __fadd_rn(H, L);
+    L = __fsub_rn(L, __fsub_rn(s, H));
+    H = s;
+}
+
+__device__ __forceinline__ float2 df_neg(float2 x) { return make_float2(-x.x, -x.y); }
+
+// Shared per-Gauss-point vectors of the fast kernel: the tangent's inputs as
+// double-float pairs, the force terms in FP64.
 template <bool VISC>
 struct GpFast;
 template <>
 struct GpFast<false> {
-    double dn[18], sdn[18], u[18], w[18];
-    double c2;
+    float2 dn[18], sdn[18], u[18], w[18];
+    float2 c2;
+    double fs[18];   // sigma' dN (forces)
 };
 template <>
 struct GpFast<true> {
-    double dn[18], sdn[18], u[18], w[18], v[18];
-    double Q[9];
+    float2 dn[18], sdn[18], u[18], w[18], v[18], Q[9];
+    double fs[18], fv[18];   // sigma' dN, sigma_v' dN (forces)
 };
 
 // Node pairs a <= b of the symmetric (inviscid) case.
@@ -255,51 +364,71 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
             GaussPoint G;
             gauss_point(A, e, gp, visc, G);
             Gp& S = sh[el * kGauss + gp];
+            // scalars and matrices the per-node vectors are formed from
+            const float2 c1 = df_split(G.c1), c2 = df_split(G.c2);
+            float2 Pm[9];
+            if constexpr (VISC) {
+#pragma unroll
+                for (int k = 0; k < 9; ++k) Pm[k] = df_split(visc ? G.pv[k] : 0.0);
+            }
 #pragma unroll
             for (int a = 0; a < 6; ++a) {
                 const double d0 = G.dn[3 * a], d1 = G.dn[3 * a + 1], d2 = G.dn[3 * a + 2];
                 double s3[3];
                 sym_apply(G.sg, d0, d1, d2, s3);
-                S.dn[3 * a] = d0;
-                S.dn[3 * a + 1] = d1;
-                S.dn[3 * a + 2] = d2;
-                S.sdn[3 * a] = s3[0];
-                S.sdn[3 * a + 1] = s3[1];
-                S.sdn[3 * a + 2] = s3[2];
+                const float2 dn[3] = {df_split(d0), df_split(d1), df_split(d2)};
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    S.dn[3 * a + i] = dn[i];
+                    S.fs[3 * a + i] = s3[i];
+                    S.sdn[3 * a + i] = df_split(s3[i]);
+                }
                 if constexpr (VISC) {
-                    double v3[3] = {0.0, 0.0, 0.0}, p3[3] = {0.0, 0.0, 0.0};
-                    if (visc) {
-                        sym_apply(G.sv, d0, d1, d2, v3);
-                        p3[0] = fma(G.pv[0], d0, fma(G.pv[3], d1, G.pv[6] * d2));
-                        p3[1] = fma(G.pv[1], d0, fma(G.pv[4], d1, G.pv[7] * d2));
-                        p3[2] = fma(G.pv[2], d0, fma(G.pv[5], d1, G.pv[8] * d2));
+                    double v3[3] = {0.0, 0.0, 0.0};
+                    if (visc) sym_apply(G.sv, d0, d1, d2, v3);
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        S.fv[3 * a + i] = v3[i];
+                        const float2 vv = df_split(v3[i]);
+                        S.v[3 * a + i] = vv;
+                        // u = c1 dN + sigma_v' dN
+                        float uH = 0.0f, uL = 0.0f;
+                        df_mac(uH, uL, c1, dn[i]);
+                        df_add(uH, uL, vv);
+                        df_norm(uH, uL);
+                        S.u[3 * a + i] = make_float2(uH, uL);
+                        // w = c2 dN + P^T dN
+                        float wH = 0.0f, wL = 0.0f;
+                        df_mac(wH, wL, c2, dn[i]);
+#pragma unroll
+                        for (int j = 0; j < 3; ++j) df_mac(wH, wL, Pm[3 * j + i], dn[j]);
+                        df_norm(wH, wL);
+                        S.w[3 * a + i] = make_float2(wH, wL);
                     }
-                    S.u[3 * a] = fma(G.c1, d0, v3[0]);
-                    S.u[3 * a + 1] = fma(G.c1, d1, v3[1]);
-                    S.u[3 * a + 2] = fma(G.c1, d2, v3[2]);
-                    S.w[3 * a] = fma(G.c2, d0, p3[0]);
-                    S.w[3 * a + 1] = fma(G.c2, d1, p3[1]);
-                    S.w[3 * a + 2] = fma(G.c2, d2, p3[2]);
-                    S.v[3 * a] = v3[0];
-                    S.v[3 * a + 1] = v3[1];
-                    S.v[3 * a + 2] = v3[2];
                 } else {
-                    S.u[3 * a] = G.c1 * d0;
-                    S.u[3 * a + 1] = G.c1 * d1;
-                    S.u[3 * a + 2] = G.c1 * d2;
-                    S.w[3 * a] = G.c2 * d0;
-                    S.w[3 * a + 1] = G.c2 * d1;
-                    S.w[3 * a + 2] = G.c2 * d2;
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        float uH = 0.0f, uL = 0.0f, wH = 0.0f, wL = 0.0f;
+                        df_mac(uH, uL, c1, dn[i]);
+                        df_mac(wH, wL, c2, dn[i]);
+                        S.u[3 * a + i] = make_float2(uH, uL);
+                        S.w[3 * a + i] = make_float2(wH, wL);
+                    }
                 }
             }
             if constexpr (VISC) {
+                // Q = c2 I + P
 #pragma unroll
-                for (int k = 0; k < 9; ++k) S.Q[k] = visc ? G.pv[k] : 0.0;
-                S.Q[0] += G.c2;
-                S.Q[4] += G.c2;
-                S.Q[8] += G.c2;
+                for (int k = 0; k < 9; ++k) {
+                    float qH = Pm[k].x, qL = Pm[k].y;
+                    if (k == 0 || k == 4 || k == 8) {
+                        df_add(qH, qL, c2);
+                        df_norm(qH, qL);
+                    }
+                    S.Q[k] = make_float2(qH, qL);
+                }
             } else {
-                S.c2 = G.c2;
+                S.c2 = c2;
             }
         }
     }
@@ -315,8 +444,8 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
         double f = 0.0;
 #pragma unroll
         for (int gp = 0; gp < kGauss; ++gp) {
-            f -= sh[el * kGauss + gp].sdn[k];
-            if constexpr (VISC) f -= sh[el * kGauss + gp].v[k];
+            f -= sh[el * kGauss + gp].fs[k];
+            if constexpr (VISC) f -= sh[el * kGauss + gp].fv[k];
         }
         const int a = k / 3, d = k - 3 * (k / 3);
         const int node = __ldg(&A.conn[a * A.ne + e]);
@@ -335,44 +464,59 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
         if (!element_live(A, e)) continue;
         const int a = VISC ? pr / 6 : kPairA[pr];
         const int bq = VISC ? pr - 6 * (pr / 6) : kPairB[pr];
-        double acc[9];
+        float aH[9], aL[9];
 #pragma unroll
-        for (int k = 0; k < 9; ++k) acc[k] = 0.0;
+        for (int k = 0; k < 9; ++k) aH[k] = aL[k] = 0.0f;
 #pragma unroll
         for (int gp = 0; gp < kGauss; ++gp) {
             const Gp& S = sh[el * kGauss + gp];
-            const double a3[3] = {S.dn[3 * a], S.dn[3 * a + 1], S.dn[3 * a + 2]};
-            const double b3[3] = {S.dn[3 * bq], S.dn[3 * bq + 1], S.dn[3 * bq + 2]};
-            const double s = fma(a3[0], b3[0], fma(a3[1], b3[1], a3[2] * b3[2]));
-            const double t = fma(a3[0], S.sdn[3 * bq], fma(a3[1], S.sdn[3 * bq + 1], a3[2] * S.sdn[3 * bq + 2]));
-            const double ua[3] = {S.u[3 * a], S.u[3 * a + 1], S.u[3 * a + 2]};
-            const double wa[3] = {S.w[3 * a], S.w[3 * a + 1], S.w[3 * a + 2]};
+            const float2 a3[3] = {S.dn[3 * a], S.dn[3 * a + 1], S.dn[3 * a + 2]};
+            const float2 b3[3] = {S.dn[3 * bq], S.dn[3 * bq + 1], S.dn[3 * bq + 2]};
+            float sH = 0.0f, sL = 0.0f, tH = 0.0f, tL = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                df_mac(sH, sL, a3[j], b3[j]);
+                df_mac(tH, tL, a3[j], S.sdn[3 * bq + j]);
+            }
+            const float2 ua[3] = {S.u[3 * a], S.u[3 * a + 1], S.u[3 * a + 2]};
+            const float2 wa[3] = {S.w[3 * a], S.w[3 * a + 1], S.w[3 * a + 2]};
             if constexpr (VISC) {
-                const double vb[3] = {S.v[3 * bq], S.v[3 * bq + 1], S.v[3 * bq + 2]};
+                const float2 s2 = make_float2(sH, sL), t2 = make_float2(tH, tL);
+                const float2 vb[3] = {df_neg(S.v[3 * bq]), df_neg(S.v[3 * bq + 1]), df_neg(S.v[3 * bq + 2])};
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
-                        double x = fma(ua[i], b3[k], acc[3 * i + k]);
-                        x = fma(b3[i], wa[k], x);
-                        x = fma(-vb[i], a3[k], x);
-                        x = fma(s, S.Q[3 * i + k], x);
-                        if (i == k) x += t;
-                        acc[3 * i + k] = x;
+                        float& H = aH[3 * i + k];
+                        float& L = aL[3 * i + k];
+                        df_mac(H, L, ua[i], b3[k]);
+                        df_mac(H, L, b3[i], wa[k]);
+                        df_mac(H, L, vb[i], a3[k]);
+                        df_mac(H, L, s2, S.Q[3 * i + k]);
+                        if (i == k) df_add(H, L, t2);
+                        df_norm(H, L);
                     }
             } else {
-                const double dg = fma(S.c2, s, t);
+                // c2 s + t on the diagonal
+                float dH = tH, dL = tL;
+                df_mac(dH, dL, S.c2, make_float2(sH, sL));
+                const float2 dg = make_float2(dH, dL);
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
-                        double x = fma(ua[i], b3[k], acc[3 * i + k]);
-                        x = fma(b3[i], wa[k], x);
-                        if (i == k) x += dg;
-                        acc[3 * i + k] = x;
+                        float& H = aH[3 * i + k];
+                        float& L = aL[3 * i + k];
+                        df_mac(H, L, ua[i], b3[k]);
+                        df_mac(H, L, b3[i], wa[k]);
+                        if (i == k) df_add(H, L, dg);
+                        df_norm(H, L);
                     }
             }
         }
+        double acc[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) acc[k] = df_join(aH[k], aL[k]);
         const int na = __ldg(&A.conn[a * A.ne + e]);
         const int nb = __ldg(&A.conn[bq * A.ne + e]);
         if (!TF_IN(A.check, na, A.nn, CK_ELEM_NODE) || !TF_IN(A.check, nb, A.nn, CK_ELEM_NODE)) continue;
