@@ -79,6 +79,14 @@ typedef struct tf_options {
                                 else block-Jacobi), 1 block-Jacobi, 2 smoothed-aggregation
                                 multigrid, 3 plain-aggregation multigrid (no reference
                                 counterpart for 2 and 3); other values: TF_BAD_INPUT */
+    double update_atol;      /* tf_newton_step / tf_batch_step only: absolute accuracy (um, 2-norm)
+                                each Newton update needs.  A linear solve stops at the looser of
+                                krylov_rtol and the relative residual that bounds the update's
+                                error by update_atol (through the largest |du| / |g| seen so far,
+                                relative residual at most 0.1); late Newton iterations, whose
+                                update is orders of magnitude below newton_tol, then need a few
+                                Krylov iterations instead of a full solve.  0: newton_tol x 1e-4;
+                                negative: off (every solve to krylov_rtol).  tf_solve ignores it. */
 } tf_options;
 
 /* Statistics of one time step (tf_newton_step). */

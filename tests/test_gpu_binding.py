@@ -38,3 +38,50 @@ def test_bindings_are_validated():
         with pytest.raises(api.TfError):
             s.set_dof_bindings([5], [5])
         s.set_dof_bindings([], [])
+
+
+def _csr_dense(ia, ja, a, n):
+    K = np.zeros((n, n))
+    for r in range(n):
+        K[r, ja[ia[r]:ia[r + 1]]] = a[ia[r]:ia[r + 1]]
+    return K
+
+
+def test_device_merges_equal_the_reference_rule():
+    """The merges run on the device (a plan built once per couple list and
+    extra-block layout) and give N^T K N + I and N^T g exactly as
+    NewtonRaphsonSolver::calculateBoundKWithSlavesMasterDoF
+    (NewtonRaphsonSolver.cpp:154-235) forms them on the dense K; a second
+    assembly and solve reuse the plan."""
+    f = np.load(os.path.join(GOLD, "steps_tiny_bound.npz"))
+    t = mesh.config_tiny(seed=15, n=5, n_layers=2, eta=100.0)
+    uk, un = mesh.perturbed_state(t, seed=17, amp=0.1)
+    n = 3 * t.n_nodes
+    with api.Solver(t, precond=1, krylov_rtol=1e-12) as s:
+        s.set_dof_bindings(f["slaves"], f["masters"])
+        for _ in range(2):
+            s.set_state(uk, un, t.dt)
+            s.assemble()
+            K = _csr_dense(*s.export_csr(0.0), n)
+            g = s.residual()
+            s.solve()
+            Kb = _csr_dense(*s.export_csr(0.0), n)
+            gb = s.residual()
+            du = s.delta_u()
+    for sd, md in zip(f["slaves"], f["masters"]):
+        g[md] += g[sd]
+        g[sd] = 0.0
+        K[md, :] += K[sd, :]
+        K[sd, :] = 0.0
+        K[:, md] += K[:, sd]
+        K[:, sd] = 0.0
+        K[sd, sd] = 1.0
+    assert np.abs(Kb - K).max() <= 1e-14 * np.abs(K).max()
+    assert np.abs(gb - g).max() <= 1e-14 * np.abs(g).max()
+    # the bound system is solved (A = K^T; a slave's row and column of the bound
+    # matrix are the unit vector and its g is zero, so its solved update is
+    # zero), and then the slaves follow their masters
+    du0 = du.copy()
+    du0[f["slaves"]] = 0.0
+    assert np.abs(K.T @ du0 - g).max() <= 1e-9 * np.abs(g).max()
+    np.testing.assert_array_equal(du[f["slaves"]], du[f["masters"]])

@@ -6,8 +6,11 @@
 #include <algorithm>
 #include <array>
 #include <map>
+#include <set>
 #include <tuple>
+#include <climits>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -127,6 +130,7 @@ void free_all(tf_handle* h) {
         growth_free(h->growth);
         h->growth = nullptr;
     }
+    bind_free(h);
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (d.host_scal) cudaFreeHost(d.host_scal);
@@ -524,6 +528,8 @@ tf_status create_handle(const tf_mesh* mesh, const tf_material* mat, const tf_op
     if (h->opt.newton_max_iter <= 0) h->opt.newton_max_iter = 20;
     if (h->opt.krylov_rtol <= 0) h->opt.krylov_rtol = 1e-8;
     if (h->opt.krylov_max_iter <= 0) h->opt.krylov_max_iter = 20000;
+    if (h->opt.update_atol == 0.0) h->opt.update_atol = 1e-4 * h->opt.newton_tol;
+    if (h->opt.update_atol < 0.0) h->opt.update_atol = 0.0;
     h->device = h->opt.device;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= h->device) {
@@ -581,7 +587,9 @@ tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* ite
         TF_CUDA(cudaEventRecord(h->ev[3], h->stream));
         int kit = 0;
         double rr = 0.0;
+        h->solve_atol = h->opt.update_atol;
         tf_status s = tf_solve(h, &kit, &rr);
+        h->solve_atol = 0.0;
         if (s != TF_OK && s != TF_KRYLOV_NOT_CONVERGED) return s;
         float ms = 0.f;
         TF_CUDA(cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]));
@@ -672,10 +680,10 @@ tf_status take_check(tf_handle* h) {
 }
 
 // The extra-block values of the current assembly back to the host copy
-// (needed before a host-side change when the device wrote some of them:
-// the packing Jacobian).
+// (needed before a host-side change or read when the device wrote some of
+// them: the packing Jacobian, the bound-DOF merges).
 tf_status sync_extra_to_host(tf_handle* h) {
-    if (!h->pk || h->d.nxb == 0) return TF_OK;
+    if (h->d.nxb == 0 || (!h->pk && !h->bound_applied)) return TF_OK;
     TF_CUDA(cudaMemcpyAsync(h->h_xval.data(), h->d.xval, sizeof(double) * 9 * (size_t)h->d.nxb,
                             cudaMemcpyDeviceToHost, h->stream));
     return sync(h);
@@ -719,21 +727,82 @@ tf_status upload_extra(tf_handle* h, bool pattern_changed) {
     return sync(h);
 }
 
-// out[9k + e] = val[off[k] + 32 e] (gather of sliced blocks) and back
-__global__ void k_blocks_get(int n, const int* __restrict__ off, const double* __restrict__ val,
-                             double* __restrict__ out) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-#pragma unroll
-    for (int e = 0; e < 9; ++e) out[9 * (size_t)k + e] = val[off[k] + kSlice * e];
+// ---- bound DOFs ------------------------------------------------------------
+//
+// K_bound = N^T K N + I, g_bound = N^T g couple by couple, as
+// NewtonRaphsonSolver::calculateBoundKWithSlavesMasterDoF
+// (NewtonRaphsonSolver.cpp:154-235) does on its dense K: g[m] += g[s],
+// g[s] = 0; the slave row is added to the master row and zeroed, then the
+// slave column to the master column, then K(s, s) = 1.  In A = K^T a row of
+// K is a column of A.
+//
+// Which entries move where depends only on the couples and the block
+// pattern, so the host turns the couples into a device program once (a
+// "plan"): per couple three waves -- the moves of the column merge, the
+// moves of the row merge, the unit diagonal -- each a list of entry
+// addresses.  Every entry of the blocks in the involved rows and columns is
+// moved (moving a zero adds nothing), so the blocks a merge can create
+// outside the element pattern are known up front and join the extra blocks
+// once.  One CTA runs the waves in order with a barrier between them; within
+// a wave the sources and destinations are disjoint and every destination has
+// one source, so its moves are independent.  The plan is rebuilt when the
+// couples or the extra-block layout change; a solve with bindings then does
+// no host transfer and no allocation.
+
+struct BindPlan {
+    int ncouple = 0;
+    int nwave = 0;
+    int64_t nop = 0;
+    int64_t* dst = nullptr;   // entry addresses: >= 0 pattern value offset, < 0: -(1 + extra value index)
+    int64_t* src = nullptr;   // kSetOne: the destination is set to 1
+    int* wave = nullptr;      // [nwave + 1] op ranges
+    int* slave = nullptr;     // [ncouple] DOFs
+    int* master = nullptr;
+    int64_t extra_version = -1;
+};
+
+constexpr int64_t kSetOne = INT64_MIN;
+
+void bind_free(tf_handle* h) {
+    if (!h->bind) return;
+    cudaFree(h->bind->dst);
+    cudaFree(h->bind->src);
+    cudaFree(h->bind->wave);
+    cudaFree(h->bind->slave);
+    cudaFree(h->bind->master);
+    delete h->bind;
+    h->bind = nullptr;
 }
 
-__global__ void k_blocks_set(int n, const int* __restrict__ off, const double* __restrict__ in,
-                             double* __restrict__ val) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-#pragma unroll
-    for (int e = 0; e < 9; ++e) val[off[k] + kSlice * e] = in[9 * (size_t)k + e];
+__device__ __forceinline__ double* bind_entry(int64_t a, double* val, double* xval) {
+    return a >= 0 ? val + a : xval + (-1 - a);
+}
+
+// The merges of all couples, in their order (one CTA; the first thread also
+// merges the right-hand side, couple by couple).
+__global__ void __launch_bounds__(1024) k_bind_apply(int ncouple, const int* __restrict__ slave,
+                                                     const int* __restrict__ master, int nwave,
+                                                     const int* __restrict__ wave, const int64_t* __restrict__ dst,
+                                                     const int64_t* __restrict__ src, double* val, double* xval,
+                                                     double* g) {
+    if (threadIdx.x == 0)
+        for (int k = 0; k < ncouple; ++k) {
+            g[master[k]] += g[slave[k]];
+            g[slave[k]] = 0.0;
+        }
+    for (int w = 0; w < nwave; ++w) {
+        for (int q = wave[w] + threadIdx.x; q < wave[w + 1]; q += blockDim.x) {
+            double* d = bind_entry(dst[q], val, xval);
+            if (src[q] == kSetOne) {
+                *d = 1.0;
+            } else {
+                double* sp = bind_entry(src[q], val, xval);
+                *d += *sp;
+                *sp = 0.0;
+            }
+        }
+        __syncthreads();
+    }
 }
 
 // du[slave] = du[master], couple by couple in their order
@@ -743,176 +812,144 @@ __global__ void k_equate(int n, const int* __restrict__ slave, const int* __rest
     for (int k = 0; k < n; ++k) du[slave[k]] = du[master[k]];
 }
 
-// K_bound = N^T K N + I, g_bound = N^T g couple by couple, as
-// NewtonRaphsonSolver::calculateBoundKWithSlavesMasterDoF
-// (NewtonRaphsonSolver.cpp:154-235) does on its dense K: the slave row is
-// added to the master row and zeroed, then the slave column to the master
-// column, then K(slave, slave) = 1.  The blocks of the nodes involved are
-// brought to the host, changed there and written back; blocks the merges
-// create outside the element pattern join the extra blocks.
-tf_status apply_bindings(tf_handle* h) {
+// Builds the plan for the current couples and extra-block layout.
+tf_status bind_build(tf_handle* h) {
     Device& d = h->d;
-    TF_TRY(sync_extra_to_host(h));
+    bind_free(h);
     const int nc = static_cast<int>(h->bind_slave.size());
-    std::vector<char> involved(d.nn, 0);
-    for (int k = 0; k < nc; ++k) {
-        involved[h->bind_slave[k] / 3] = 1;
-        involved[h->bind_master[k] / 3] = 1;
-    }
-    // blocks (J, I) with J or I involved: pattern blocks by offset, extras by index
-    using Key = std::pair<int, int>;
-    std::map<Key, std::array<double, 9>> blk;
-    std::vector<Key> pkeys;
-    std::vector<int> poff;
+    using Key = std::pair<int, int>;  // block (J, I) of A
     auto find_block = [&](int r, int c) -> int64_t {
         auto b = h->h_colidx.begin() + h->h_rowptr[r], en = h->h_colidx.begin() + h->h_rowptr[r + 1];
         auto it = std::lower_bound(b, en, c);
         return (it != en && *it == c) ? static_cast<int64_t>(it - h->h_colidx.begin()) : -1;
     };
+    // the blocks in the rows and columns of the involved nodes
+    std::vector<char> involved(d.nn, 0);
+    for (int k = 0; k < nc; ++k) {
+        involved[h->bind_slave[k] / 3] = 1;
+        involved[h->bind_master[k] / 3] = 1;
+    }
+    std::set<Key> keys;
     for (int X = 0; X < d.nn; ++X) {
         if (!involved[X]) continue;
         for (int p = h->h_rowptr[X]; p < h->h_rowptr[X + 1]; ++p) {
-            const int C = h->h_colidx[p];
-            for (const Key& k : {Key{X, C}, Key{C, X}}) {
-                if (blk.count(k)) continue;
-                blk[k] = {};
-                pkeys.push_back(k);
-                poff.push_back(h->h_bofs[find_block(k.first, k.second)]);
-            }
+            keys.insert({X, h->h_colidx[p]});
+            keys.insert({h->h_colidx[p], X});
         }
     }
-    // extra blocks in those rows and columns
-    std::vector<int> xrow(d.nn + 1, 0);
-    if (!h->h_xcols.empty())
-        for (int i = 0; i < d.nn; ++i) xrow[i + 1] = xrow[i] + static_cast<int>(h->h_xcols[i].size());
     if (!h->h_xcols.empty())
         for (int J = 0; J < d.nn; ++J)
-            for (size_t q = 0; q < h->h_xcols[J].size(); ++q) {
-                const int I = h->h_xcols[J][q];
-                if (!involved[J] && !involved[I]) continue;
-                std::array<double, 9> v;
-                for (int e = 0; e < 9; ++e) v[e] = h->h_xval[9 * (size_t)(xrow[J] + q) + e];
-                blk[{J, I}] = v;
-            }
-    const int npb = static_cast<int>(pkeys.size());
-    if (npb > 0) {
-        int* doff = nullptr;
-        double* dbuf = nullptr;
-        TF_TRY(upload(&doff, poff));
-        if (dev_alloc(&dbuf, 9 * (size_t)npb) != TF_OK) {
-            cudaFree(doff);
-            return TF_OUT_OF_MEMORY;
-        }
-        std::vector<double> hb(9 * (size_t)npb);
-        k_blocks_get<<<cdiv(npb, 256), 256, 0, h->stream>>>(npb, doff, d.val, dbuf);
-        cudaError_t e = cudaMemcpyAsync(hb.data(), dbuf, hb.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-        if (e != cudaSuccess) {
-            cudaFree(doff);
-            cudaFree(dbuf);
-            return cuda_fail(e, "binding: block gather");
-        }
-        for (int k = 0; k < npb; ++k)
-            for (int q = 0; q < 9; ++q) blk[pkeys[k]][q] = hb[9 * (size_t)k + q];
-        // the couples, in order (K(r, c) is entry (c%3, r%3) of block (c/3, r/3))
-        std::vector<double> g(3 * (size_t)d.nn);
-        e = cudaMemcpyAsync(g.data(), d.g, g.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-        if (e != cudaSuccess) {
-            cudaFree(doff);
-            cudaFree(dbuf);
-            return cuda_fail(e, "binding: rhs download");
-        }
-        bool changed = false;
-        for (int k = 0; k < nc; ++k) {
-            const int sd = h->bind_slave[k], md = h->bind_master[k];
-            const int S = sd / 3, M = md / 3, ds = sd % 3, dm = md % 3;
-            g[md] += g[sd];
-            g[sd] = 0.0;
-            // K row m += K row s; K row s = 0: column S of A into column M
-            std::vector<Key> colS;
-            for (auto& kv : blk)
-                if (kv.first.second == S) colS.push_back(kv.first);
-            for (const Key& key : colS)
-                for (int dc = 0; dc < 3; ++dc) {
-                    double& v = blk[key][3 * dc + ds];
-                    if (v == 0.0) continue;
-                    const Key tgt{key.first, M};
-                    if (!blk.count(tgt)) blk[tgt] = {};
-                    blk[tgt][3 * dc + dm] += v;
-                    v = 0.0;
-                }
-            // K column m += K column s; K column s = 0: row S of A into row M
-            std::vector<Key> rowS;
-            for (auto& kv : blk)
-                if (kv.first.first == S) rowS.push_back(kv.first);
-            for (const Key& key : rowS)
-                for (int dr = 0; dr < 3; ++dr) {
-                    double& v = blk[key][3 * ds + dr];
-                    if (v == 0.0) continue;
-                    const Key tgt{M, key.second};
-                    if (!blk.count(tgt)) blk[tgt] = {};
-                    blk[tgt][3 * dm + dr] += v;
-                    v = 0.0;
-                }
-            blk[{S, S}][3 * ds + ds] = 1.0;
-        }
-        // write back: pattern blocks through their offsets, the rest as extra blocks
-        for (int k = 0; k < npb; ++k)
-            for (int q = 0; q < 9; ++q) hb[9 * (size_t)k + q] = blk[pkeys[k]][q];
-        e = cudaMemcpyAsync(dbuf, hb.data(), hb.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream);
-        if (e == cudaSuccess) {
-            k_blocks_set<<<cdiv(npb, 256), 256, 0, h->stream>>>(npb, doff, dbuf, d.val);
-            e = cudaGetLastError();
-        }
-        if (e == cudaSuccess) e = cudaMemcpyAsync(d.g, g.data(), g.size() * sizeof(double), cudaMemcpyHostToDevice,
-                                                  h->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-        cudaFree(doff);
-        cudaFree(dbuf);
-        if (e != cudaSuccess) return cuda_fail(e, "binding: write back");
-        h->launches += 2;
-        if (h->h_xcols.empty()) h->h_xcols.resize(d.nn);
-        std::vector<std::tuple<int, int, std::array<double, 9>>> extra;
-        for (auto& kv : blk) {
-            if (find_block(kv.first.first, kv.first.second) >= 0) continue;
-            note_user_block(h, kv.first.first, kv.first.second);
-            std::vector<int>& xc = h->h_xcols[kv.first.first];
-            auto jt = std::lower_bound(xc.begin(), xc.end(), kv.first.second);
-            if (jt == xc.end() || *jt != kv.first.second) {
-                xc.insert(jt, kv.first.second);
-                changed = true;
-            }
-            extra.emplace_back(kv.first.first, kv.first.second, kv.second);
-        }
-        if (!extra.empty()) {
-            std::vector<int> row(d.nn + 1, 0);
-            for (int i = 0; i < d.nn; ++i) row[i + 1] = row[i] + static_cast<int>(h->h_xcols[i].size());
-            auto slot = [&](int J, int I) {
-                const auto& xc = h->h_xcols[J];
-                return row[J] + static_cast<int>(std::lower_bound(xc.begin(), xc.end(), I) - xc.begin());
-            };
-            if (changed) {  // new layout: the other extra blocks keep their values
-                std::vector<double> nv(9 * (size_t)row[d.nn], 0.0);
-                if (!h->h_xrow.empty())
-                    for (int i = 0; i < d.nn; ++i)
-                        for (int p = h->h_xrow[i]; p < h->h_xrow[i + 1]; ++p) {
-                            const int q = slot(i, h->h_xcol_prev[p]);
-                            for (int t = 0; t < 9; ++t) nv[9 * (size_t)q + t] = h->h_xval[9 * (size_t)p + t];
-                        }
-                h->h_xval.swap(nv);
-                h->h_xcol_prev.clear();
-                for (const auto& xc : h->h_xcols) h->h_xcol_prev.insert(h->h_xcol_prev.end(), xc.begin(), xc.end());
-            }
-            for (const auto& x : extra) {
-                const int p = slot(std::get<0>(x), std::get<1>(x));
-                for (int q = 0; q < 9; ++q) h->h_xval[9 * (size_t)p + q] = std::get<2>(x)[q];
-            }
-            TF_TRY(upload_extra(h, changed));
-        }
+            for (int I : h->h_xcols[J])
+                if (involved[J] || involved[I]) keys.insert({J, I});
+    // symbolic pass: the blocks the merges reach
+    struct Move {
+        Key dk, sk;
+        int de, se;  // entries 3 r + c within the blocks; se < 0: set to one
+    };
+    std::vector<std::vector<Move>> waves;
+    for (int k = 0; k < nc; ++k) {
+        const int sd = h->bind_slave[k], md = h->bind_master[k];
+        const int S = sd / 3, M = md / 3, ds = sd % 3, dm = md % 3;
+        // K row m += K row s: column S of A into column M
+        std::vector<Move> wa, wb;
+        std::vector<Key> colS, rowS;
+        for (const Key& key : keys)
+            if (key.second == S) colS.push_back(key);
+        for (const Key& key : colS)
+            for (int dc = 0; dc < 3; ++dc) wa.push_back({{key.first, M}, key, 3 * dc + dm, 3 * dc + ds});
+        for (const Move& m : wa) keys.insert(m.dk);
+        // K column m += K column s: row S of A into row M
+        for (const Key& key : keys)
+            if (key.first == S) rowS.push_back(key);
+        for (const Key& key : rowS)
+            for (int dr = 0; dr < 3; ++dr) wb.push_back({{M, key.second}, key, 3 * dm + dr, 3 * ds + dr});
+        for (const Move& m : wb) keys.insert(m.dk);
+        keys.insert({S, S});
+        waves.push_back(std::move(wa));
+        waves.push_back(std::move(wb));
+        waves.push_back({Move{{S, S}, {S, S}, 3 * ds + ds, -1}});
     }
+    // blocks outside the element pattern join the extra blocks (values kept)
+    bool changed = false;
+    for (const Key& key : keys) {
+        if (find_block(key.first, key.second) >= 0) continue;
+        if (h->h_xcols.empty()) h->h_xcols.resize(d.nn);
+        std::vector<int>& xc = h->h_xcols[key.first];
+        auto jt = std::lower_bound(xc.begin(), xc.end(), key.second);
+        if (jt != xc.end() && *jt == key.second) continue;
+        if (!changed) TF_TRY(sync_extra_to_host(h));
+        note_user_block(h, key.first, key.second);
+        xc.insert(jt, key.second);
+        changed = true;
+    }
+    if (changed) {
+        std::vector<int> row(d.nn + 1, 0);
+        for (int i = 0; i < d.nn; ++i) row[i + 1] = row[i] + static_cast<int>(h->h_xcols[i].size());
+        std::vector<double> nv(9 * (size_t)row[d.nn], 0.0);
+        if (!h->h_xrow.empty())
+            for (int i = 0; i < d.nn; ++i)
+                for (int p = h->h_xrow[i]; p < h->h_xrow[i + 1]; ++p) {
+                    const auto& xc = h->h_xcols[i];
+                    const int q = row[i] + static_cast<int>(std::lower_bound(xc.begin(), xc.end(),
+                                                                             h->h_xcol_prev[p]) - xc.begin());
+                    for (int t = 0; t < 9; ++t) nv[9 * (size_t)q + t] = h->h_xval[9 * (size_t)p + t];
+                }
+        h->h_xval.swap(nv);
+        h->h_xcol_prev.clear();
+        for (const auto& xc : h->h_xcols) h->h_xcol_prev.insert(h->h_xcol_prev.end(), xc.begin(), xc.end());
+        TF_TRY(upload_extra(h, true));
+    }
+    // entry addresses
+    auto addr = [&](const Key& key, int e) -> int64_t {
+        const int64_t b = find_block(key.first, key.second);
+        const int r = e / 3, c = e - 3 * (e / 3);
+        if (b >= 0) return static_cast<int64_t>(h->h_bofs[b]) + kSlice * (3 * r + c);
+        const auto& xc = h->h_xcols[key.first];
+        const int q = h->h_xrow[key.first] + static_cast<int>(std::lower_bound(xc.begin(), xc.end(), key.second) -
+                                                              xc.begin());
+        return -1 - (9 * static_cast<int64_t>(q) + e);
+    };
+    std::vector<int64_t> vdst, vsrc;
+    std::vector<int> vwave{0};
+    for (const auto& w : waves) {
+        for (const Move& m : w) {
+            vdst.push_back(addr(m.dk, m.de));
+            vsrc.push_back(m.se < 0 ? kSetOne : addr(m.sk, m.se));
+        }
+        vwave.push_back(static_cast<int>(vdst.size()));
+    }
+    BindPlan* P = new BindPlan;
+    h->bind = P;
+    P->ncouple = nc;
+    P->nwave = static_cast<int>(waves.size());
+    P->nop = static_cast<int64_t>(vdst.size());
+    if (P->nop > 0) {
+        TF_TRY(upload(&P->dst, vdst));
+        TF_TRY(upload(&P->src, vsrc));
+    }
+    TF_TRY(upload(&P->wave, vwave));
+    TF_TRY(upload(&P->slave, h->bind_slave));
+    TF_TRY(upload(&P->master, h->bind_master));
+    P->extra_version = h->extra_version;
+    return TF_OK;
+}
+
+tf_status apply_bindings(tf_handle* h) {
+    if (!h->bind || h->bind->extra_version != h->extra_version) TF_TRY(bind_build(h));
+    const BindPlan& P = *h->bind;
+    const Device& d = h->d;
+    k_bind_apply<<<1, 1024, 0, h->stream>>>(P.ncouple, P.slave, P.master, P.nwave, P.wave, P.dst, P.src, d.val,
+                                            d.xval, d.g);
+    TF_LAUNCH_CHECK(h);
     h->bound_applied = true;
     amg_mark_stale(h, 1);
+    return TF_OK;
+}
+
+tf_status equate_bound(tf_handle* h) {
+    const BindPlan& P = *h->bind;
+    k_equate<<<1, 1, 0, h->stream>>>(P.ncouple, P.slave, P.master, h->d.du);
+    TF_LAUNCH_CHECK(h);
     return TF_OK;
 }
 
@@ -1090,6 +1127,7 @@ tf_status tf_set_dof_bindings(tf_handle* h, int32_t n, const int32_t* slave_dofs
     h->bind_slave.assign(slave_dofs, slave_dofs + n);
     h->bind_master.assign(master_dofs, master_dofs + n);
     h->bound_applied = false;
+    bind_free(h);
     return TF_OK;
 }
 
@@ -1421,21 +1459,7 @@ tf_status tf_solve(tf_handle* h, int32_t* iters, double* relres) {
     double rr = 0.0;
     tf_status s = krylov_solve(h, &it, &rr);
     TF_TRY(take_check(h));
-    if (!h->bind_slave.empty() && (s == TF_OK || s == TF_KRYLOV_NOT_CONVERGED)) {
-        int* ds = nullptr;
-        int* dm = nullptr;
-        TF_TRY(upload(&ds, h->bind_slave));
-        if (upload(&dm, h->bind_master) != TF_OK) {
-            cudaFree(ds);
-            return TF_OUT_OF_MEMORY;
-        }
-        k_equate<<<1, 1, 0, h->stream>>>(static_cast<int>(h->bind_slave.size()), ds, dm, h->d.du);
-        const cudaError_t e = cudaStreamSynchronize(h->stream);
-        cudaFree(ds);
-        cudaFree(dm);
-        if (e != cudaSuccess) return cuda_fail(e, "k_equate");
-        h->launches++;
-    }
+    if (!h->bind_slave.empty() && (s == TF_OK || s == TF_KRYLOV_NOT_CONVERGED)) TF_TRY(equate_bound(h));
     if (iters) *iters = it;
     if (relres) *relres = rr;
     return s;

@@ -155,7 +155,9 @@ struct Device {
 // Indices into Device::scal (device-resident Krylov scalars).
 enum Scal {
     S_RZ = 0, S_RZ_OLD, S_PQ, S_ALPHA, S_BETA, S_OMEGA, S_RHO, S_RHO_OLD,
-    S_TS, S_TT, S_RR, S_BB, S_RR0, S_DU2, S_FLAG, S_ITER, S_TOL2, S_WHY, S_COUNT = 32
+    S_TS, S_TT, S_RR, S_BB, S_RR0, S_DU2, S_FLAG, S_ITER, S_TOL2, S_WHY,
+    S_SINV,  // largest |du| / |g| of the instance's solves so far (kept across solves)
+    S_COUNT = 32
 };
 
 constexpr int kNodeThreads = 256;    // nodes per CTA of the node-parallel kernels
@@ -165,6 +167,7 @@ constexpr int kAmgMaxLevels = 10;
 struct Amg;      // multigrid hierarchy (tf_amg.cu)
 struct Packing;  // packing between tissue surfaces (tf_packing.cu)
 struct Growth;   // growth functions (tf_growth.cu)
+struct BindPlan; // device program of the bound-DOF merges (tf_api.cu)
 
 // Inverse of a 3x3 matrix (row-major) by cofactors.
 __device__ __forceinline__ void inv3_cof(const double* M, double* inv) {
@@ -360,6 +363,8 @@ struct tf_handle {
     std::vector<int> h_xcol_prev;               // their columns in that layout
     std::vector<int> bind_slave, bind_master;   // bound DOF couples (NRSolver::slaveMasterList)
     bool bound_applied = false;                 // the couples are applied to the current assembly
+    double solve_atol = 0.0;                    // absolute update accuracy of the current solve (0: off)
+    tf::BindPlan* bind = nullptr;               // device program of the couples' row/column merges
     std::vector<double> h_xval;                 // their values of the current assembly
     int64_t extra_version = 0;                  // changes with every new extra-block layout
     std::vector<uint8_t> h_fixed;
@@ -447,6 +452,7 @@ tf_status growth_positions(tf_handle* h, double* relz, double* rel0, double* rel
 void growth_free(Growth* g);
 tf_status upload_extra(tf_handle* h, bool pattern_changed);
 tf_status sync_extra_to_host(tf_handle* h);      // device extra-block values -> h_xval
+void bind_free(tf_handle* h);                     // releases the bound-DOF plan
 tf_status take_check(tf_handle* h);              // checked build: report and clear a failed index check
 bool amg_reused(const tf_handle* h);
 tf_status launch_adjoint_element(tf_handle* h, const double* lamv, double* carry, double* gr, double* ge, double ndt);

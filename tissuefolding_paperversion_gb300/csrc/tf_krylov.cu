@@ -149,12 +149,21 @@ __device__ __forceinline__ void bsr_row(const Ctx& c, int i, const double* __res
     }
 }
 
-// Sets an instance's stop flag from its first scalars (bb = |b|^2).
-__device__ __forceinline__ void start_flags(double* s, double bb, double tol2) {
+// Sets an instance's stop flag from its first scalars (bb = |b|^2).  With an
+// absolute update accuracy atol > 0, the relative tolerance is loosened to
+// the residual |r| <= atol / sinv (sinv = the largest |du| / |g| of the
+// instance's earlier solves, which bounds |A^-1 r| / |r| along the
+// directions the step has produced), at most to a relative 0.1.
+__device__ __forceinline__ void start_flags(double* s, double bb, double tol2, double atol) {
     s[S_BB] = bb;
     s[S_RR] = bb;
     s[S_RR0] = bb;
     s[S_ITER] = 0.0;
+    const double sinv = s[S_SINV];
+    if (atol > 0.0 && sinv > 0.0 && bb > 0.0) {
+        const double r = atol / sinv;
+        tol2 = fmax(tol2, fmin(r * r / bb, 1e-2));
+    }
     s[S_TOL2] = tol2;
     s[S_WHY] = W_NONE;
     s[S_FLAG] = (bb == 0.0) ? F_CONVERGED : (isfinite(bb) ? F_RUNNING : F_NAN);
@@ -167,7 +176,8 @@ __device__ __forceinline__ void start_flags(double* s, double bb, double tol2) {
 // other instances) or solve with b = 0, which sets x = 0 (an instance whose
 // Newton loop has stopped); both are flagged done at once.
 __global__ void k_cg_init(Ctx c, const double* __restrict__ b, double* __restrict__ x, double* __restrict__ r,
-                          double* __restrict__ z, double* __restrict__ p, double tol2, int keep, int jac) {
+                          double* __restrict__ z, double* __restrict__ p, double tol2, double atol, int keep,
+                          int jac) {
     const Where w = where(c);
     const bool active = c.seg_solve[w.seg] != 0;
     if (!active && keep) {
@@ -200,7 +210,7 @@ __global__ void k_cg_init(Ctx c, const double* __restrict__ b, double* __restric
     double tot[2];
     if (reduce_seg<2>(c, w.seg, v, tot) && threadIdx.x == 0) {
         if (jac) w.s[S_RZ] = tot[0];
-        start_flags(w.s, tot[1], tol2);
+        start_flags(w.s, tot[1], tol2, atol);
     }
 }
 
@@ -328,7 +338,7 @@ __global__ void k_cg_direction(Ctx c, const double* __restrict__ z, double* __re
 // r = rhat = b, p = v = 0, x = 0; rho = (rhat, r)
 __global__ void k_bi_init(Ctx c, const double* __restrict__ b, double* __restrict__ x, double* __restrict__ r,
                           double* __restrict__ rhat, double* __restrict__ p, double* __restrict__ v, double tol2,
-                          int keep) {
+                          double atol, int keep) {
     const Where w = where(c);
     const bool active = c.seg_solve[w.seg] != 0;
     if (!active && keep) {
@@ -355,7 +365,7 @@ __global__ void k_bi_init(Ctx c, const double* __restrict__ b, double* __restric
         w.s[S_ALPHA] = 1.0;
         w.s[S_OMEGA] = 1.0;
         w.s[S_BETA] = 0.0;
-        start_flags(w.s, tot[0], tol2);
+        start_flags(w.s, tot[0], tol2, atol);
     }
 }
 
@@ -582,7 +592,12 @@ __global__ void k_update(Ctx c, double* __restrict__ uk, const double* __restric
         }
     }
     double tot[1];
-    if (reduce_seg<1>(c, w.seg, v, tot) && threadIdx.x == 0) w.s[S_DU2] = tot[0];
+    if (reduce_seg<1>(c, w.seg, v, tot) && threadIdx.x == 0) {
+        w.s[S_DU2] = tot[0];
+        // |du| / |g| of this solve: the scale that turns a residual into an update error
+        const double bb = w.s[S_BB];
+        if (bb > 0.0 && isfinite(tot[0])) w.s[S_SINV] = fmax(w.s[S_SINV], sqrt(tot[0] / bb));
+    }
 }
 
 Ctx make_ctx(tf_handle* h) {
@@ -682,7 +697,7 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
             if (sa != TF_OK) return sa;
         }
         if (method == 1) {
-            k_cg_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.z, d.p, tol2, keep, jac);
+            k_cg_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.z, d.p, tol2, h->solve_atol, keep, jac);
             if (!jac) {
                 TF_LAUNCH_CHECK(h);
                 amg_vcycle(h, d.r, d.z);
@@ -690,7 +705,7 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
                 k_cg_rz<<<d.ncta, kThreads, 0, st>>>(c, d.r, d.z, d.p, 1);
             }
         } else {
-            k_bi_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.rhat, d.p, d.q, tol2, keep);
+            k_bi_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.rhat, d.p, d.q, tol2, h->solve_atol, keep);
         }
     }
     TF_LAUNCH_CHECK(h);
