@@ -12,7 +12,7 @@ closed form, within 1e-12 of the literal 3^6 contraction).  The reference's
 dense K cannot exist at this size (2.94 TB), so the storage is the
 reference's value-filtered CSR and the solver is the Pardiso stand-in of
 ``oracle/sparse.py`` (sparse LU as the preconditioner of GMRES, run to a
-normwise backward error of 1e-15).
+normwise backward error of 1e-14).
 
 The fixture keeps what a GPU run can be compared with at any size: the Newton
 iteration count and ||du|| of every iteration of every step, per-step
@@ -82,7 +82,7 @@ def main():
         gmres_iters=np.array(solver.stats["gmres_iters"], dtype=np.int32),
         backward_error=solver.stats.get("backward_error", 0.0),
         note="oracle sparse mode: tf_oracle.c closed-form tangent, reference scatter order and CSR filter, "
-             "Pardiso stand-in = SuperLU (nested dissection) preconditioned GMRES to backward error 1e-15")
+             "Pardiso stand-in = SuperLU (nested dissection) preconditioned GMRES to backward error 1e-14")
     print(f"wrote {out} in {time.time() - t_all:.0f} s", flush=True)
 
 

@@ -138,8 +138,10 @@ def _oracle_loss(t, rate, logE, n, params):
 def test_adjoint_on_a_3200_prism_sheet_matches_differences_of_the_oracle():
     """The sheet of the 320k-prism configuration at 20 x 20 cells (4 layers,
     E log-normal, internal viscosity 100), 6 steps, checkpoints every 3;
-    central differences (h = 1e-6 relative) of the oracle's Newton steps
-    along one seeded direction per parameter set."""
+    central differences of the oracle's Newton steps along one seeded
+    direction per parameter set (h = 1e-3 of the largest rate, 1e-4 in
+    log E: steps that balance the difference's truncation against the FP64
+    rounding of the loss)."""
     t = mesh.config_large(seed=0, cells=20)
     n, every = 6, 3
     rate = t.rates.reshape(-1, 3)[:, 0].copy()
@@ -155,12 +157,12 @@ def test_adjoint_on_a_3200_prism_sheet_matches_differences_of_the_oracle():
     for which in ("rate", "logE"):
         d = rng.standard_normal(t.n_elems)
         if which == "rate":
-            h = 1e-6 * np.abs(rate).max()
+            h = 1e-3 * np.abs(rate).max()
             lp = _oracle_loss(t, rate + h * d, logE, n, params)
             lm = _oracle_loss(t, rate - h * d, logE, n, params)
             adj = float(gr @ d)
         else:
-            h = 1e-6
+            h = 1e-4
             lp = _oracle_loss(t, rate, logE + h * d, n, params)
             lm = _oracle_loss(t, rate, logE - h * d, n, params)
             adj = float(ge @ d)
@@ -171,7 +173,9 @@ def test_adjoint_on_a_3200_prism_sheet_matches_differences_of_the_oracle():
 def test_adjoint_at_full_size_matches_central_differences():
     """320,000 prisms, 50 steps of 60 s, checkpoints every 10: the gradient
     along one seeded direction per parameter set against central differences
-    (h = 1e-6 relative) of the GPU forward run, every solve tight."""
+    of the GPU forward run, every solve tight (h = 1e-3 of the largest rate,
+    1e-4 in log E; at h = 1e-6 the FP64 rounding of the loss, ~1.6e7 over
+    40,401 apical nodes, leaves the difference uncertain by ~2e-4)."""
     t = mesh.config_large(seed=0)
     n, every = 50, 10
     rate = t.rates.reshape(-1, 3)[:, 0].copy()
@@ -191,11 +195,11 @@ def test_adjoint_at_full_size_matches_central_differences():
         for which in ("rate", "logE"):
             d = rng.standard_normal(t.n_elems)
             if which == "rate":
-                h = 1e-6 * np.abs(rate).max()
+                h = 1e-3 * np.abs(rate).max()
                 fd = (loss(rate + h * d, logE) - loss(rate - h * d, logE)) / (2 * h)
                 adj = float(gr @ d)
             else:
-                h = 1e-6
+                h = 1e-4
                 fd = (loss(rate, logE + h * d) - loss(rate, logE - h * d)) / (2 * h)
                 adj = float(ge @ d)
             assert abs(adj - fd) <= TOL_GRAD * abs(fd), (which, adj, fd)
