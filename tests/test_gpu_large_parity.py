@@ -6,7 +6,11 @@ sparse storage and the Pardiso stand-in solve, because the reference's
 dense K would take 2.94 TB at this size).
 
 Per step: the Newton iteration count must be identical, ||du|| of every
-iteration must agree, and the positions of 2,048 seeded nodes must lie
+iteration must agree to 1e-6 of the step's first update (a later update
+corrects the error the earlier linear solves left, so its own norm carries
+that error: the GPU's Krylov solves stop at a relative residual of 1e-8,
+the oracle's at a backward error of 1e-14), and the positions of 2,048
+seeded nodes must lie
 within 1e-8 of the oracle's relative to the largest coordinate, with the
 block-Jacobi preconditioner and with the smoothed-aggregation multigrid
 (FP32 V-cycle, FP16 level-0 smoother operator)."""
@@ -20,7 +24,7 @@ from tissuefolding_paperversion_gb300 import api, mesh
 pytestmark = pytest.mark.gpu
 FIXTURE = os.path.join(os.path.dirname(__file__), "golden", "steps_large_320k.npz")
 TOL_POS = 1e-8      # positions after every step, relative to the largest coordinate
-TOL_DU = 1e-6       # ||du|| of the Newton iterations whose update is above 1e-6 um
+TOL_DU = 1e-6       # ||du|| of every Newton iteration, relative to the step's first update
 
 
 @pytest.mark.skipif(not os.path.exists(FIXTURE), reason="the 320k-prism oracle run is not committed")
@@ -41,8 +45,7 @@ def test_twenty_steps_of_the_320k_sheet_match_the_oracle(precond):
             assert out["iters"] == f["iters"][k], (k, out["iters"], f["iters"][k])
             ref_du = f["dunorm"][k][: f["iters"][k]]
             got_du = np.asarray(out["dunorm"])[: out["iters"]]
-            big = ref_du > 1e-6
-            assert np.all(np.abs(got_du[big] - ref_du[big]) <= TOL_DU * ref_du[big]), (k, got_du, ref_du)
+            assert np.all(np.abs(got_du - ref_du) <= TOL_DU * ref_du[0]), (k, got_du, ref_du)
             assert got_du[-1] <= 1e-8 and ref_du[-1] <= 1e-8
             err = np.abs(p[sample] - f["sample_positions"][k]).max() / scale
             worst = max(worst, err)
