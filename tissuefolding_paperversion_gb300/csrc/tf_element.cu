@@ -37,12 +37,14 @@
 // Knuth, TAOCP vol. 2, 4.2.2).  A block entry carries a relative error of
 // ~1e-13 of its largest term, far inside the 1e-11 parity bound and far
 // below what moves a Newton iterate; the forces and everything the residual
-// depends on stay FP64.
+// depends on stay FP64 (with viscosity the forces use one FP64 stress
+// sigma' + sigma_v', and the tangent's sigma' dN and sigma_v' dN come from
+// the double-float splits of the two stresses).
 //
-// Layout: one CTA handles NE prisms.  Phase A: one thread per (prism, Gauss
-// point) builds the per-point vectors in shared memory.  Phase B: each
-// thread owns 3x3 node-pair blocks, sums the six Gauss points and scatters
-// the block.  The matrix assembled is A = K^T, the system the reference
+// Layout: one CTA of 2 x 6 x NE threads handles NE prisms.  Phase A: one
+// thread per (prism, Gauss point) -- the first half of the CTA -- builds the
+// per-point vectors in shared memory.  Phase B: every thread owns 3x3
+// node-pair blocks, sums the six Gauss points and scatters the block.  The matrix assembled is A = K^T, the system the reference
 // solves (Pardiso iparm[11] = 1, NewtonRaphsonSolver.cpp:639); in that
 // orientation every element block (a, b) lands at block (conn[a], conn[b])
 // without a transpose.  Fixed DOFs are masked here, which is calcutateFixedK
@@ -54,6 +56,16 @@ namespace tf {
 namespace {
 
 enum Mode { kAtomic = 0, kStore = 2 };
+
+// Threads per Gauss point: phase A runs on the first NE x 6 threads of the
+// CTA, the pair phase and the force sums on all of them.  Twice the threads
+// of phase A give the pair phase (FP32 pipe) more warps to hide its latency
+// while other CTAs on the SM run phase A (FP64 pipe): 3.65 against 4.68 ms
+// per 320,000-prism assembly with the merged force stress below and the
+// Gauss loop of the pair phase kept rolled (unrolled it overflows the
+// instruction cache); three threads per Gauss point were slower (registers
+// then allow one CTA per SM).
+constexpr int kTpg = 2;
 
 struct ElemArgs {
     int ne;
@@ -336,8 +348,21 @@ struct GpFast<false> {
 template <>
 struct GpFast<true> {
     float2 dn[18], sdn[18], u[18], w[18], v[18], Q[9];
-    double fs[18], fv[18];   // sigma' dN, sigma_v' dN (forces)
+    double fs[18];           // (sigma' + sigma_v') dN (forces)
 };
+
+// o = s d for a symmetric s (00 11 22 01 02 12), in double-float
+__device__ __forceinline__ void df_sym_apply(const float2* s, const float2* d, float2* o) {
+    const int ix[9] = {0, 3, 4, 3, 1, 5, 4, 5, 2};
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float H = 0.0f, L = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) df_mac(H, L, s[ix[3 * i + j]], d[j]);
+        df_norm(H, L);
+        o[i] = make_float2(H, L);
+    }
+}
 
 // Node pairs a <= b of the symmetric (inviscid) case.
 __constant__ int8_t kPairA[21] = {0, 0, 0, 0, 0, 0, 1, 1, 1, 1, 1, 2, 2, 2, 2, 3, 3, 3, 4, 4, 5};
@@ -348,14 +373,15 @@ __device__ __forceinline__ bool element_live(const ElemArgs& A, int e) {
 }
 
 template <int NE, int MODE, bool VISC>
-__global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
+__global__ void __launch_bounds__(NE * kGauss * kTpg) k_element(ElemArgs A) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     using Gp = GpFast<VISC>;
     Gp* sh = reinterpret_cast<Gp*>(smem_raw);  // [NE][6]
     const int tid = threadIdx.x;
+    constexpr int NT = NE * kGauss * kTpg;
 
     // ---------------- phase A ----------------------------------------------
-    {
+    if (tid < NE * kGauss) {
         const int el = tid / kGauss;
         const int gp = tid - el * kGauss;
         const int e = blockIdx.x * NE + el;
@@ -371,25 +397,51 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
 #pragma unroll
                 for (int k = 0; k < 9; ++k) Pm[k] = df_split(visc ? G.pv[k] : 0.0);
             }
+            // VISC: one FP64 stress sigma' + sigma_v' for the forces; the
+            // tangent's sigma' dN and sigma_v' dN in double-float from the
+            // splits of the two stresses (54 FP64 multiply-adds and 36 splits
+            // fewer per Gauss point than forming both products in FP64)
+            double st[6];
+            float2 sgs[6], svs[6];
+            if constexpr (VISC) {
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    st[k] = visc ? G.sg[k] + G.sv[k] : G.sg[k];
+                    sgs[k] = df_split(G.sg[k]);
+                    svs[k] = df_split(visc ? G.sv[k] : 0.0);
+                }
+            }
 #pragma unroll
             for (int a = 0; a < 6; ++a) {
                 const double d0 = G.dn[3 * a], d1 = G.dn[3 * a + 1], d2 = G.dn[3 * a + 2];
-                double s3[3];
-                sym_apply(G.sg, d0, d1, d2, s3);
                 const float2 dn[3] = {df_split(d0), df_split(d1), df_split(d2)};
-#pragma unroll
-                for (int i = 0; i < 3; ++i) {
-                    S.dn[3 * a + i] = dn[i];
-                    S.fs[3 * a + i] = s3[i];
-                    S.sdn[3 * a + i] = df_split(s3[i]);
-                }
                 if constexpr (VISC) {
-                    double v3[3] = {0.0, 0.0, 0.0};
-                    if (visc) sym_apply(G.sv, d0, d1, d2, v3);
+                    double s3[3];
+                    sym_apply(st, d0, d1, d2, s3);
+                    float2 sd[3];
+                    df_sym_apply(sgs, dn, sd);
 #pragma unroll
                     for (int i = 0; i < 3; ++i) {
-                        S.fv[3 * a + i] = v3[i];
-                        const float2 vv = df_split(v3[i]);
+                        S.dn[3 * a + i] = dn[i];
+                        S.fs[3 * a + i] = s3[i];
+                        S.sdn[3 * a + i] = sd[i];
+                    }
+                } else {
+                    double s3[3];
+                    sym_apply(G.sg, d0, d1, d2, s3);
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        S.dn[3 * a + i] = dn[i];
+                        S.fs[3 * a + i] = s3[i];
+                        S.sdn[3 * a + i] = df_split(s3[i]);
+                    }
+                }
+                if constexpr (VISC) {
+                    float2 vs[3];
+                    df_sym_apply(svs, dn, vs);
+#pragma unroll
+                    for (int i = 0; i < 3; ++i) {
+                        const float2 vv = vs[i];
                         S.v[3 * a + i] = vv;
                         // u = c1 dN + sigma_v' dN
                         float uH = 0.0f, uL = 0.0f;
@@ -436,7 +488,7 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
 
     // ---------------- element forces: Gauss sum, fixed mask, scatter ------
     // f_a = - sum_g (sigma' + sigma_v') dN_a  (ShapeBase.cpp:2203-2227)
-    for (int task = tid; task < NE * 18; task += NE * kGauss) {
+    for (int task = tid; task < NE * 18; task += NT) {
         const int el = task / 18;
         const int k = task - el * 18;
         const int e = blockIdx.x * NE + el;
@@ -445,7 +497,6 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
 #pragma unroll
         for (int gp = 0; gp < kGauss; ++gp) {
             f -= sh[el * kGauss + gp].fs[k];
-            if constexpr (VISC) f -= sh[el * kGauss + gp].fv[k];
         }
         const int a = k / 3, d = k - 3 * (k / 3);
         const int node = __ldg(&A.conn[a * A.ne + e]);
@@ -457,7 +508,7 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
 
     // ---------------- phase B: 3x3 node-pair blocks ------------------------
     constexpr int kPairs = VISC ? 36 : 21;
-    for (int task = tid; task < NE * kPairs; task += NE * kGauss) {
+    for (int task = tid; task < NE * kPairs; task += NT) {
         const int el = task / kPairs;
         const int pr = task - el * kPairs;
         const int e = blockIdx.x * NE + el;
@@ -467,7 +518,7 @@ __global__ void __launch_bounds__(NE * kGauss) k_element(ElemArgs A) {
         float aH[9], aL[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) aH[k] = aL[k] = 0.0f;
-#pragma unroll
+#pragma unroll 1
         for (int gp = 0; gp < kGauss; ++gp) {
             const Gp& S = sh[el * kGauss + gp];
             const float2 a3[3] = {S.dn[3 * a], S.dn[3 * a + 1], S.dn[3 * a + 2]};
@@ -827,7 +878,7 @@ tf_status launch_fast(tf_handle* h, const ElemArgs& A) {
         TF_CUDA(cudaFuncSetAttribute(k_element<NE, MODE, VISC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         configured_device = h->device;
     }
-    k_element<NE, MODE, VISC><<<cdiv(A.ne, NE), NE * kGauss, smem, h->stream>>>(A);
+    k_element<NE, MODE, VISC><<<cdiv(A.ne, NE), NE * kGauss * kTpg, smem, h->stream>>>(A);
     TF_LAUNCH_CHECK(h);
     return TF_OK;
 }
