@@ -85,8 +85,11 @@ typedef struct tf_options {
                                 error by update_atol (through the largest |du| / |g| seen so far,
                                 relative residual at most 0.1); late Newton iterations, whose
                                 update is orders of magnitude below newton_tol, then need a few
-                                Krylov iterations instead of a full solve.  0: newton_tol x 1e-4;
-                                negative: off (every solve to krylov_rtol).  tf_solve ignores it. */
+                                Krylov iterations instead of a full solve.  Such a solve never
+                                decides the Newton test alone: when its |du| lies within a factor 2
+                                of newton_tol the system is solved again to krylov_rtol first.
+                                0: newton_tol x 1e-4; negative: off (every solve to krylov_rtol).
+                                tf_solve ignores it. */
 } tf_options;
 
 /* Statistics of one time step (tf_newton_step). */

@@ -588,19 +588,46 @@ tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* ite
         int kit = 0;
         double rr = 0.0;
         h->solve_atol = h->opt.update_atol;
+        h->newton_index = k;
         tf_status s = tf_solve(h, &kit, &rr);
         h->solve_atol = 0.0;
+        h->newton_index = -1;
         if (s != TF_OK && s != TF_KRYLOV_NOT_CONVERGED) return s;
         float ms = 0.f;
         TF_CUDA(cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]));
         ms_asm += ms;
         st.krylov_iters_total += kit;
         st.krylov_iters_max = std::max(st.krylov_iters_max, kit);
-        st.final_relres = rr;
-        TF_TRY(launch_update(h));
+        // |du| before the update is applied.  An inexact solve must not decide
+        // the Newton test: when a solve stopped at the update accuracy (a stop
+        // test looser than krylov_rtol) and |du| lands within a factor 2 of
+        // newton_tol, the active instances are solved again to krylov_rtol.
+        TF_TRY(launch_update_norm(h));
         TF_CUDA(cudaMemcpy2DAsync(du2.data(), sizeof(double), d.scal + S_DU2, sizeof(double) * S_COUNT,
                                   sizeof(double), d.nseg, cudaMemcpyDeviceToHost, h->stream));
         TF_TRY(sync(h));
+        if (h->opt.update_atol > 0.0) {
+            const double rt2 = h->opt.krylov_rtol * h->opt.krylov_rtol;
+            bool redo = false;
+            for (int g = 0; g < d.nseg && !redo; ++g) {
+                if (!h->h_active[g]) continue;
+                const double dn = std::sqrt(du2[g]);
+                redo = d.host_scal[(size_t)g * S_COUNT + S_TOL2] > rt2 && dn > 0.5 * h->opt.newton_tol &&
+                       dn < 2.0 * h->opt.newton_tol;
+            }
+            if (redo) {
+                int kit2 = 0;
+                s = tf_solve(h, &kit2, &rr);
+                if (s != TF_OK && s != TF_KRYLOV_NOT_CONVERGED) return s;
+                st.krylov_iters_total += kit2;
+                st.final_relres = rr;
+                TF_TRY(launch_update_norm(h));
+                TF_CUDA(cudaMemcpy2DAsync(du2.data(), sizeof(double), d.scal + S_DU2, sizeof(double) * S_COUNT,
+                                          sizeof(double), d.nseg, cudaMemcpyDeviceToHost, h->stream));
+                TF_TRY(sync(h));
+            }
+        }
+        TF_TRY(launch_update(h));
         double dmax = 0.0;
         bool any_active = false;
         for (int g = 0; g < d.nseg; ++g) {

@@ -377,9 +377,11 @@ struct tf_handle {
     std::vector<int> h_active;                  // host mirror of seg_active
     int elem_cta = 16;                          // prisms per CTA of the element kernel (autotuned)
     bool tuned = false;
-    cudaGraphExec_t graph[2][4] = {};           // Krylov chunks [method-1][log2(chunk/8)]
-    int64_t graph_kernels[2][4] = {};
+    cudaGraphExec_t graph[2][5] = {};           // Krylov chunks [method-1][log2(chunk/4)]
+    int64_t graph_kernels[2][5] = {};
     int last_iters[2] = {0, 0};                 // iterations of the last solve per method (chunk planning)
+    int plan_iters[2][8] = {};                  // the same per Newton iteration of a step (0-6, 7: later ones)
+    int newton_index = -1;                      // Newton iteration of the current solve (-1: outside a step)
     tf::Amg* amg = nullptr;                     // multigrid preconditioner (null: block-Jacobi)
     tf::Packing* pk = nullptr;                  // packing between tissue surfaces (null: off)
     tf::Growth* growth = nullptr;               // growth functions (null: none added yet)
@@ -416,6 +418,7 @@ tf_status launch_viscosity_surfaces(tf_handle* h);
 tf_status launch_block_inverse(tf_handle* h);
 tf_status krylov_solve(tf_handle* h, int* iters, double* relres);
 tf_status launch_update(tf_handle* h);
+tf_status launch_update_norm(tf_handle* h);   // |du|^2 into S_DU2 without applying du
 tf_status autotune_element(tf_handle* h);
 tf_status amg_build(tf_handle* h, const double* ref_pos);
 tf_status amg_numeric(tf_handle* h);

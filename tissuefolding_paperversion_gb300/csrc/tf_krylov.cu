@@ -579,6 +579,9 @@ __global__ void k_bi_restart(Ctx c, const double* __restrict__ r, double* __rest
 
 // uk += du; |du|^2 per instance  (NewtonRaphsonSolver::updateUkInIteration
 // :755-761, checkConvergenceViaDeltaU :727-740)
+// APPLY = false: |du|^2 only (the same sum, uk untouched), for the Newton
+// test before the update is applied.
+template <bool APPLY>
 __global__ void k_update(Ctx c, double* __restrict__ uk, const double* __restrict__ du) {
     const Where w = where(c);
     double v[1] = {0.0};
@@ -587,13 +590,14 @@ __global__ void k_update(Ctx c, double* __restrict__ uk, const double* __restric
         for (int d = 0; d < 3; ++d) {
             const int k = 3 * w.node + d;
             const double dk = du[k];
-            uk[k] = uk[k] + dk;
+            if (APPLY) uk[k] = uk[k] + dk;
             v[0] = fma(dk, dk, v[0]);
         }
     }
     double tot[1];
     if (reduce_seg<1>(c, w.seg, v, tot) && threadIdx.x == 0) {
         w.s[S_DU2] = tot[0];
+        if (!APPLY) return;
         // |du| / |g| of this solve: the scale that turns a residual into an update error
         const double bb = w.s[S_BB];
         if (bb > 0.0 && isfinite(tot[0])) w.s[S_SINV] = fmax(w.s[S_SINV], sqrt(tot[0] / bb));
@@ -658,9 +662,12 @@ int kernels_per_iteration(const tf_handle* h, int method) {
     return method == 1 ? 4 + v : 6 + 2 * v;
 }
 
-// A chunk of `8 << ci` iterations, captured once into a CUDA graph.
+constexpr int kChunk0 = 4;  // iterations of the smallest graph chunk
+constexpr int kChunks = 5;  // chunks of 4, 8, 16, 32 and 64 iterations
+
+// A chunk of `kChunk0 << ci` iterations, captured once into a CUDA graph.
 tf_status run_chunk(tf_handle* h, const Ctx& c, int method, int ci) {
-    const int n = 8 << ci;
+    const int n = kChunk0 << ci;
     cudaGraphExec_t& ex = h->graph[method - 1][ci];
     if (!ex) {
         cudaGraph_t g = nullptr;
@@ -711,27 +718,31 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
     TF_LAUNCH_CHECK(h);
     const int maxit = h->opt.krylov_max_iter;
     const size_t nscal = (size_t)d.nseg * S_COUNT;
-    // Iterations run in graph chunks of 8/16/32/64 with a flag check after
-    // each batch.  Consecutive solves of a handle need similar counts, so the
-    // first batch covers 7/8 of the previous solve's iterations (largest
-    // chunks first, no check in between) and the rest goes in chunks of 8:
-    // at most 8 iterations run past convergence.  Without a previous count
-    // the chunks double from 8.
-    int launched = 0, ci = 0;
-    int planned = (keep == 0) ? (h->last_iters[method - 1] * 7) / 8 : 0;
-    bool done = false, fixed8 = planned > 0;
+    // Iterations run in graph chunks of 4/8/16/32/64 with a flag check after
+    // each batch.  The solve of a step's k-th Newton iteration needs about as
+    // many iterations as the k-th one of the previous step (later Newton
+    // iterations, solved to an absolute update accuracy, need far fewer than
+    // the first), so the first batch covers 7/8 of that count (largest chunks
+    // first, no check in between) and the rest goes in chunks of 4: at most 4
+    // iterations run past convergence.  Outside a Newton step the previous
+    // solve's count is used; without a previous count the chunks double from 8.
+    const int slot = h->newton_index >= 0 ? std::min(h->newton_index, 7) : -1;
+    const int prev = slot >= 0 ? h->plan_iters[method - 1][slot] : h->last_iters[method - 1];
+    int launched = 0, ci = 1;
+    int planned = (keep == 0) ? (prev * 7) / 8 : 0;
+    bool done = false, fixed = planned > 0;
     while (launched < maxit && !done) {
-        int target = planned > 0 ? planned : (fixed8 ? 8 : (8 << ci));
+        int target = planned > 0 ? planned : (fixed ? kChunk0 : (kChunk0 << ci));
         planned = 0;
         target = std::min(target, maxit - launched);
         int issued = 0;
-        for (int cj = 3; cj >= 0 && issued < target; --cj)
-            while (target - issued >= (8 << cj)) {
+        for (int cj = kChunks - 1; cj >= 0 && issued < target; --cj)
+            while (target - issued >= (kChunk0 << cj)) {
                 const tf_status s = run_chunk(h, c, method, cj);
                 if (s != TF_OK) return s;
-                issued += 8 << cj;
+                issued += kChunk0 << cj;
             }
-        if (issued < target) {  // fewer than 8 left before maxit
+        if (issued < target) {  // fewer than 4 left before maxit or in the plan
             const int rest = target - issued;
             issue_iterations(h, c, method, rest);
             TF_LAUNCH_CHECK(h);
@@ -744,7 +755,7 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
         done = true;
         for (int g = 0; g < d.nseg && done; ++g)
             if (d.host_scal[(size_t)g * S_COUNT + S_FLAG] == F_RUNNING) done = false;
-        if (ci < 3) ++ci;
+        if (ci < kChunks - 1) ++ci;
     }
     int worst = F_CONVERGED, itmax = 0, bad = -1, bad_it = 0, why = 0;
     double rmax = 0.0, bad_rel = 0.0;
@@ -765,7 +776,10 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
     }
     *iters = itmax;
     *relres = rmax;
-    if (keep == 0) h->last_iters[method - 1] = itmax;
+    if (keep == 0) {
+        h->last_iters[method - 1] = itmax;
+        if (slot >= 0) h->plan_iters[method - 1][slot] = itmax;
+    }
     if (worst == F_CONVERGED) return TF_OK;
     char rel[32];
     std::snprintf(rel, sizeof(rel), "%.3g", bad_rel);
@@ -835,7 +849,15 @@ tf_status krylov_solve(tf_handle* h, int* iters, double* relres) {
 tf_status launch_update(tf_handle* h) {
     Device& d = h->d;
     const Ctx c = make_ctx(h);
-    k_update<<<d.ncta, kThreads, 0, h->stream>>>(c, d.uk, d.du);
+    k_update<true><<<d.ncta, kThreads, 0, h->stream>>>(c, d.uk, d.du);
+    TF_LAUNCH_CHECK(h);
+    return TF_OK;
+}
+
+tf_status launch_update_norm(tf_handle* h) {
+    Device& d = h->d;
+    const Ctx c = make_ctx(h);
+    k_update<false><<<d.ncta, kThreads, 0, h->stream>>>(c, d.uk, d.du);
     TF_LAUNCH_CHECK(h);
     return TF_OK;
 }
