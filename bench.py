@@ -365,6 +365,9 @@ def run_gpu(args, t):
                    "preconditioner": (("plain-aggregation" if args.precond == 3 else "smoothed-aggregation")
                                       + " multigrid " + "/".join(map(str, mg_nodes))) if mg_nodes else "block-Jacobi",
                    "krylov_iters_per_step": sum(x["krylov_total"] for x in stats) / len(stats),
+                   "krylov_iters_by_step": [int(x["krylov_total"]) for x in stats],
+                   "newton_iters_by_step": [int(x["iters"]) for x in stats],
+                   "ms_by_step": [round(float(x["ms_total"]), 3) for x in stats],
                    "ms_assembly": ms_asm / n_asm, "wall_s": wall},
         "e2e": {"value": ne / e2e_s, "unit": "prisms/s", "h2d_bytes_per_step": 2 * 8 * 3 * nn,
                 "d2h_bytes_per_step": 8 * 3 * nn},

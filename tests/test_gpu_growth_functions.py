@@ -53,9 +53,15 @@ def test_growth_update_matches_the_reference(name):
 
 @pytest.mark.parametrize("name", G.FIXTURES)
 def test_newton_steps_match_the_reference(name):
+    """The reference's last Newton update of the second step of
+    steps_grid_growth is 9.9965e-9 um, 3.5e-4 below newton_tol (1e-8): with
+    the default Krylov tolerance (relative residual 1e-8) the GPU's |du|
+    there scatters by ~3e-4 and can land on either side, so the Newton counts
+    are compared with linear solves to a relative residual of 1e-10 (|du|
+    then agrees with the reference's to ~1e-6)."""
     f = np.load(os.path.join(GOLD, name + ".npz"))
     t, fns, interp, pinned = G.fixture_case(name)
-    with _solver(t, fns, interp, pinned) as s:
+    with _solver(t, fns, interp, pinned, krylov_rtol=1e-10) as s:
         s.set_growth_rates(t.rates)
         for k in range(f["positions"].shape[0]):
             out = s.newton_step(t.dt, allow_not_converged=False)
