@@ -264,6 +264,7 @@ def run_gpu(args, t):
     s.set_growth_rates(t.rates)
     nn, ne, nnzb = s.sizes()
     mg_nodes, _ = s.multigrid_info()
+    mg_blocks = s.multigrid_blocks() if mg_nodes else None
 
     def barrier():
         if dist is not None:
@@ -353,6 +354,9 @@ def run_gpu(args, t):
     adjoint = None
     if not args.quick and world == 1:
         adjoint = adjoint_measure(t, args.adj_steps, args.adj_every, args.adj_fd_default)
+    # the read and copy bandwidth this GPU gives kernels of the library (the
+    # denominators of the solve's read-bound kernels)
+    hbm_probe = api.measure_bandwidth(local if world > 1 else 0)
     if rank != 0:
         return
     line = {
@@ -364,6 +368,7 @@ def run_gpu(args, t):
         "newton": {"ms_per_step": step_ms, "assemblies_per_step": n_asm / len(stats),
                    "preconditioner": (("plain-aggregation" if args.precond == 3 else "smoothed-aggregation")
                                       + " multigrid " + "/".join(map(str, mg_nodes))) if mg_nodes else "block-Jacobi",
+                   "multigrid_blocks": mg_blocks[0] if mg_blocks else None,
                    "krylov_iters_per_step": sum(x["krylov_total"] for x in stats) / len(stats),
                    "krylov_iters_by_step": [int(x["krylov_total"]) for x in stats],
                    "newton_iters_by_step": [int(x["iters"]) for x in stats],
@@ -379,6 +384,7 @@ def run_gpu(args, t):
         "gpu_launches": launches,
         "clocks": clk,
         "e2e_newton_step": e2e_step,
+        "hbm_probe": hbm_probe,
     }
     if small is not None:
         line["config_small"] = small

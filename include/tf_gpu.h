@@ -309,6 +309,17 @@ TF_API int64_t tf_launch_count(tf_handle* h);
  * handle's stream). */
 TF_API tf_status tf_time_assembly(tf_handle* h, int32_t iters, float* ms_per_assembly, float* ms_per_element_kernel);
 
+/* HBM bandwidth of three access patterns on `device`, measured with kernels of
+ * this library (no counterpart in the reference): a read stream of 16-byte
+ * loads (eight in flight per thread), a read stream of 32 KB bulk (TMA)
+ * copies into shared memory, and a copy (read + write bytes counted); best
+ * of `reps` timed runs each, in GB/s.  `bytes` per buffer (a multiple of
+ * 32 KB, at least 152 chunks); allocates two such buffers for the duration
+ * of the call.  These are the denominators of the read-dominated solve
+ * kernels' rooflines. */
+TF_API tf_status tf_measure_bandwidth(int32_t device, int64_t bytes, int32_t reps, double* read_gbs, double* bulk_gbs,
+                                      double* copy_gbs);
+
 /* --- solve without device allocation --------------------------------------
  * No counterpart in the reference: this is an addition for callers that may
  * not call cudaMalloc (a host that owns every device allocation, a fixed
@@ -350,6 +361,10 @@ TF_API tf_status tf_write_frame(const char* path, int32_t append, double time_se
  * of the last numeric set-up (4 / (3 lambda_max(D^-1 A)) per level; arrays of
  * at least 10 entries, either may be NULL).  No reference counterpart. */
 TF_API tf_status tf_multigrid_info(tf_handle* h, int32_t* levels, int32_t* nodes, double* weights);
+/* Matrix blocks (3x3 at level 0, 6x6 below) and prolongator blocks to the
+ * next level, per level of the hierarchy (arrays of at least 10 entries;
+ * nothing is written when block-Jacobi is used).  No reference counterpart. */
+TF_API tf_status tf_multigrid_blocks(tf_handle* h, int64_t* blocks, int64_t* prolongator_blocks);
 
 /* ---- discrete adjoint (no counterpart in the reference) ------------------
  * Gradients of a shape loss after n implicit steps with respect to per-element

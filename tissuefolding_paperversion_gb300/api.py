@@ -30,12 +30,23 @@ EXPORTED = [
     "tf_get_viscosity_surfaces", "tf_set_viscosity_surfaces", "tf_set_state", "tf_export_csr",
     "tf_element_eval", "tf_get_sizes", "tf_get_stream", "tf_launch_count", "tf_time_assembly",
     "tf_solve_bsr_static", "tf_batch_create", "tf_batch_step", "tf_get_instances", "tf_elements_per_cta",
-    "tf_adj_forward", "tf_adj_backward", "tf_adj_free", "tf_multigrid_info", "tf_read_mesh_file",
+    "tf_adj_forward", "tf_adj_backward", "tf_adj_free", "tf_multigrid_info", "tf_multigrid_blocks", "tf_read_mesh_file",
     "tf_write_frame", "tf_add_K_triplets", "tf_set_dof_bindings", "tf_set_packing", "tf_get_packing",
     "tf_packing_masses", "tf_add_uniform_growth", "tf_add_ring_growth", "tf_add_grid_growth",
     "tf_clear_growth_functions", "tf_set_grid_growth_mode",
-    "tf_repin_grid_growth", "tf_grid_growth_positions", "tf_set_time", "tf_get_time",
+    "tf_repin_grid_growth", "tf_grid_growth_positions", "tf_set_time", "tf_get_time", "tf_measure_bandwidth",
 ]
+
+
+def measure_bandwidth(device: int = 0, nbytes: int = 2 << 30, reps: int = 10) -> dict:
+    """HBM bandwidth of a 16-byte-load read stream, a bulk-copy (TMA) read
+    stream and a copy on `device`, in GB/s (tf_measure_bandwidth)."""
+    L = load()
+    r, b, c = C.c_double(), C.c_double(), C.c_double()
+    st = L.tf_measure_bandwidth(device, nbytes, reps, C.byref(r), C.byref(b), C.byref(c))
+    if st != 0:
+        raise TfError(f"tf_measure_bandwidth: {L.tf_status_string(st).decode()}: {L.tf_last_error().decode()}")
+    return {"read_gbs": r.value, "bulk_read_gbs": b.value, "copy_gbs": c.value, "bytes": nbytes}
 
 
 class TfError(RuntimeError):
@@ -132,6 +143,7 @@ def load(build_if_missing: bool = True):
     L.tf_adj_free.argtypes = [vp]
     L.tf_multigrid_info.restype = C.c_int
     L.tf_multigrid_info.argtypes = [vp, ip, vp, vp]
+    L.tf_multigrid_blocks.argtypes = [vp, vp, vp]
     L.tf_set_dof_bindings.restype = C.c_int
     L.tf_set_dof_bindings.argtypes = [vp, i32, vp, vp]
     L.tf_add_K_triplets.restype = C.c_int
@@ -158,6 +170,8 @@ def load(build_if_missing: bool = True):
     L.tf_repin_grid_growth.argtypes = [vp]
     L.tf_grid_growth_positions.restype = C.c_int
     L.tf_grid_growth_positions.argtypes = [vp, vp, vp, vp]
+    L.tf_measure_bandwidth.restype = C.c_int
+    L.tf_measure_bandwidth.argtypes = [i32, i64, i32, dp, dp, dp]
     L.tf_set_time.restype = C.c_int
     L.tf_set_time.argtypes = [vp, C.c_double]
     L.tf_get_time.restype = C.c_int
@@ -477,6 +491,14 @@ class Solver:
         w = np.zeros(10)
         self._check(self.L.tf_multigrid_info(self.h, C.byref(lv), _ptr(nodes), _ptr(w)), "tf_multigrid_info")
         return nodes[: lv.value].tolist(), w[: lv.value].tolist()
+
+    def multigrid_blocks(self):
+        """(matrix blocks, prolongator blocks) per level of the hierarchy."""
+        nodes, _ = self.multigrid_info()
+        b = np.zeros(10, dtype=np.int64)
+        p = np.zeros(10, dtype=np.int64)
+        self._check(self.L.tf_multigrid_blocks(self.h, _ptr(b), _ptr(p)), "tf_multigrid_blocks")
+        return b[: len(nodes)].tolist(), p[: len(nodes)].tolist()
 
     # -- adjoint --------------------------------------------------------------
     def adjoint_forward(self, rate, logE, n_steps, dt, every, loss_params):

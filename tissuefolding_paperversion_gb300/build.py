@@ -21,7 +21,7 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libtfgpu.so")
 LIB_CHECKED = os.path.join(LIBDIR, "libtfgpu_checked.so")
 SOURCES = ["tf_api.cu", "tf_element.cu", "tf_assembly.cu", "tf_krylov.cu", "tf_static_solve.cu", "tf_adjoint.cu", "tf_amg.cu",
-           "tf_packing.cu", "tf_growth.cu", "tf_meshio.cpp"]
+           "tf_packing.cu", "tf_growth.cu", "tf_probe.cu", "tf_meshio.cpp"]
 HEADERS = ["tf_internal.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",

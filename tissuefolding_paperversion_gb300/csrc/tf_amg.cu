@@ -174,6 +174,7 @@ tf_status zeros(T** dst, size_t n) {
         if (_s != TF_OK) return _s; \
     } while (0)
 
+
 }  // namespace
 
 // Device view of one level: what the V-cycle reads and writes, all FP32
@@ -246,8 +247,13 @@ struct Amg {
     double* part = nullptr;    // per-CTA partial sums
     unsigned* ticket = nullptr;
     float* val32 = nullptr;    // FP32 copy of the level-0 values (sliced layout)
-    __half* valh = nullptr;    // the smoother's level-0 operator S = D^-1 A in FP16 (sliced layout)
+    // the smoother's level-0 operator S = D^-1 A in FP16, slot by slot in the
+    // sliced order: entries 0-7 of a row's block as one 16-byte pack
+    // ([slot][lane][8]), then entry 8 of every block ([slot][lane]) -- two
+    // loads per block instead of nine
+    __half* valh = nullptr;
     float* dinv32 = nullptr;   // FP32 copy of the level-0 block inverses
+    float* diag32 = nullptr;   // FP32 copy of the level-0 diagonal blocks, [9 n] row-major
     int nseg = 1;
     int* cnode0 = nullptr;     // [nseg+1] coarsest-level node offsets per instance
     int* cinv0 = nullptr;      // [nseg+1] offsets of the dense inverses
@@ -281,7 +287,7 @@ void amg_free(Amg* a) {
             if (p) cudaFree(p);
     }
     void* ptrs[] = {a->omega, a->pscal, a->pv, a->pw, a->part, a->ticket, a->cnode0, a->cinv0, a->cinv,
-                    a->val32, a->dinv32, a->valh};
+                    a->val32, a->dinv32, a->valh, a->diag32};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete a;
@@ -611,6 +617,7 @@ tf_status amg_build(tf_handle* h, const double* pos) {
     AMG_TRY(zeros(&a->val32, (size_t)d.nval));
     AMG_TRY(zeros(&a->valh, (size_t)d.nval));
     AMG_TRY(zeros(&a->dinv32, 9 * (size_t)d.nn));
+    AMG_TRY(zeros(&a->diag32, 9 * (size_t)d.nn));
     AMG_TRY(zeros(&a->pscal, 2 * (size_t)a->nlev));
     AMG_TRY(zeros(&a->pv, maxv));
     AMG_TRY(zeros(&a->pw, maxv));
@@ -800,16 +807,27 @@ __device__ __forceinline__ void row0s(const Device& d, const __half* __restrict_
     const int s0 = __ldg(&d.wslot0[wg]), s1 = __ldg(&d.wslot0[wg + 1]);
     float y0 = 0.f, y1 = 0.f, y2 = 0.f;
     const int* __restrict__ col = d.scol + lane;
-    const __half* __restrict__ a = valh + lane;
+    const uint4* __restrict__ p8 = reinterpret_cast<const uint4*>(valh) + lane;
+    const __half* __restrict__ p1 = valh + (size_t)(d.nval / kSlotDoubles) * (kSlice * 8) + lane;
 #pragma unroll 4
     for (int s = s0; s < s1; ++s) {
         const int j = __ldg(&col[(size_t)s * kSlice]);
         if (!TF_IN(d.check, j, d.nn, CK_V0_COL)) continue;
-        const __half* __restrict__ v = a + (size_t)s * kSlotDoubles;
+        const uint4 pk = __ldg(&p8[(size_t)s * kSlice]);
+        const float a8 = __half2float(p1[(size_t)s * kSlice]);
+        // the low half of each word is the even entry
+        const float2 a01 = make_float2(__half2float(__ushort_as_half((unsigned short)(pk.x & 0xffffu))),
+                                       __half2float(__ushort_as_half((unsigned short)(pk.x >> 16))));
+        const float2 a23 = make_float2(__half2float(__ushort_as_half((unsigned short)(pk.y & 0xffffu))),
+                                       __half2float(__ushort_as_half((unsigned short)(pk.y >> 16))));
+        const float2 a45 = make_float2(__half2float(__ushort_as_half((unsigned short)(pk.z & 0xffffu))),
+                                       __half2float(__ushort_as_half((unsigned short)(pk.z >> 16))));
+        const float2 a67 = make_float2(__half2float(__ushort_as_half((unsigned short)(pk.w & 0xffffu))),
+                                       __half2float(__ushort_as_half((unsigned short)(pk.w >> 16))));
         const float x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
-        y0 = fmaf(__half2float(v[0]), x0, fmaf(__half2float(v[32]), x1, fmaf(__half2float(v[64]), x2, y0)));
-        y1 = fmaf(__half2float(v[96]), x0, fmaf(__half2float(v[128]), x1, fmaf(__half2float(v[160]), x2, y1)));
-        y2 = fmaf(__half2float(v[192]), x0, fmaf(__half2float(v[224]), x1, fmaf(__half2float(v[256]), x2, y2)));
+        y0 = fmaf(a01.x, x0, fmaf(a01.y, x1, fmaf(a23.x, x2, y0)));
+        y1 = fmaf(a23.y, x0, fmaf(a45.x, x1, fmaf(a45.y, x2, y1)));
+        y2 = fmaf(a67.x, x0, fmaf(a67.y, x1, fmaf(a8, x2, y2)));
     }
     y[0] = y0;
     y[1] = y1;
@@ -895,7 +913,7 @@ __global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restr
 // (its entries are O(1): the FP16 range and 11-bit mantissa suffice for a
 // preconditioner; the Krylov operator itself stays FP64).
 __global__ void k_to_h(Device d, const float* __restrict__ val32, const float* __restrict__ dinv32,
-                       __half* __restrict__ valh) {
+                       __half* __restrict__ valh, float* __restrict__ diag32) {
     const Node0 q = node0(d);
     const int lane = threadIdx.x & 31;
     const int wg = blockIdx.x * kWarps + (threadIdx.x >> 5);
@@ -903,17 +921,32 @@ __global__ void k_to_h(Device d, const float* __restrict__ val32, const float* _
     float D[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) D[k] = q.valid ? dinv32[9 * (size_t)q.i + k] : 0.f;
+    if (q.valid) {
+        const float* __restrict__ Dg = val32 + d.diag[q.i];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) diag32[9 * (size_t)q.i + k] = Dg[kSlice * k];
+    }
+    uint4* __restrict__ p8 = reinterpret_cast<uint4*>(valh) + lane;
+    __half* __restrict__ p1 = valh + (size_t)(d.nval / kSlotDoubles) * (kSlice * 8) + lane;
     for (int s = s0; s < s1; ++s) {
         const size_t base = (size_t)s * kSlotDoubles + lane;
         float A[9];
 #pragma unroll
         for (int k = 0; k < 9; ++k) A[k] = val32[base + 32 * k];
+        __half h[9];
 #pragma unroll
         for (int r = 0; r < 3; ++r)
 #pragma unroll
             for (int c = 0; c < 3; ++c)
-                valh[base + 32 * (3 * r + c)] =
+                h[3 * r + c] =
                     __float2half_rn(fmaf(D[3 * r], A[c], fmaf(D[3 * r + 1], A[3 + c], D[3 * r + 2] * A[6 + c])));
+        uint4 pk;
+        pk.x = (uint32_t)__half_as_ushort(h[0]) | ((uint32_t)__half_as_ushort(h[1]) << 16);
+        pk.y = (uint32_t)__half_as_ushort(h[2]) | ((uint32_t)__half_as_ushort(h[3]) << 16);
+        pk.z = (uint32_t)__half_as_ushort(h[4]) | ((uint32_t)__half_as_ushort(h[5]) << 16);
+        pk.w = (uint32_t)__half_as_ushort(h[6]) | ((uint32_t)__half_as_ushort(h[7]) << 16);
+        p8[(size_t)s * kSlice] = pk;
+        p1[(size_t)s * kSlice] = h[8];
     }
 }
 
@@ -1279,9 +1312,9 @@ __global__ void k_coarse_invert(AmgLevel L, const int* __restrict__ cnode0, cons
 struct V0 {  // level-0 operands
     Device d;
     const double* omega;
-    const float* val32;   // FP32 copy of the values (diagonal blocks for the residual)
     const float* dinv32;  // FP32 copy of the block inverses
     const __half* valh;   // S = D^-1 A, FP16
+    const float* diag32;  // diagonal blocks D, FP32 [9 n]
 };
 
 // x = omega D^-1 r  (r is the Krylov method's FP64 vector)
@@ -1305,11 +1338,11 @@ __global__ void k_v0_resid(V0 a, const double* __restrict__ r, const float* __re
     if (q.valid) row0s(a.d, a.valh, a.dinv32, x, q.i, y);
     if (!q.valid) return;
     // A x = D (S x), D the diagonal block
-    const float* __restrict__ Dg = a.val32 + __ldg(&a.d.diag[q.i]);
+    const float* __restrict__ Dg = a.diag32 + 9 * (size_t)q.i;
 #pragma unroll
     for (int k = 0; k < 3; ++k)
-        t[3 * q.i + k] = (float)r[3 * q.i + k] - fmaf(Dg[kSlice * (3 * k)], y[0],
-                                                      fmaf(Dg[kSlice * (3 * k + 1)], y[1], Dg[kSlice * (3 * k + 2)] * y[2]));
+        t[3 * q.i + k] = (float)r[3 * q.i + k] - fmaf(__ldg(&Dg[3 * k]), y[0],
+                                                      fmaf(__ldg(&Dg[3 * k + 1]), y[1], __ldg(&Dg[3 * k + 2]) * y[2]));
 }
 
 // out = x + omega D^-1 (r - A x), written back as the FP64 preconditioned vector
@@ -1597,7 +1630,7 @@ tf_status amg_numeric(tf_handle* h) {
     TF_LAUNCH_CHECK(h);
     k_to_f32<<<4 * 152, kT, 0, st>>>(9 * (int64_t)d.nn, d.dinv, a->dinv32);
     TF_LAUNCH_CHECK(h);
-    k_to_h<<<d.ncta, kNodeThreads, 0, st>>>(d, a->val32, a->dinv32, a->valh);
+    k_to_h<<<d.ncta, kNodeThreads, 0, st>>>(d, a->val32, a->dinv32, a->valh, a->diag32);
     TF_LAUNCH_CHECK(h);
     a->reused = a->stale == 1;
     if (a->reused) {
@@ -1689,7 +1722,7 @@ void amg_vcycle(tf_handle* h, const double* r, double* out) {
     cudaStream_t st = h->stream;
     const int nl = a->nlev;
     const int stop = a->tail > 0 ? a->tail : nl - 1;  // first level not handled kernel by kernel
-    V0 v0{d, a->omega, a->val32, a->dinv32, a->valh};
+    V0 v0{d, a->omega, a->dinv32, a->valh, a->diag32};
     AmgLevel& L0 = a->L[0];
     auto presmooth = [&](int l) { return (l < nl - 1 || !a->coarse_exact) ? 1 : 0; };
     launch_pdl(k_v0_pre, d.ncta, kNodeThreads, st, v0, r, L0.x);
@@ -1752,6 +1785,19 @@ void amg_vcycle(tf_handle* h, const double* r, double* out) {
 }
 
 }  // namespace tf
+
+extern "C" TF_API tf_status tf_multigrid_blocks(tf_handle* h, int64_t* blocks, int64_t* prolongator_blocks) {
+    if (!h || !blocks || !prolongator_blocks) {
+        tf::set_error("tf_multigrid_blocks: bad arguments");
+        return TF_BAD_INPUT;
+    }
+    tf::Amg* a = h->amg;
+    for (int l = 0; l < (a ? a->nlev : 0); ++l) {
+        blocks[l] = a->L[l].nnzb;
+        prolongator_blocks[l] = a->L[l].npb;
+    }
+    return TF_OK;
+}
 
 extern "C" TF_API tf_status tf_multigrid_info(tf_handle* h, int32_t* levels, int32_t* nodes, double* weights) {
     if (!h || !levels) {
