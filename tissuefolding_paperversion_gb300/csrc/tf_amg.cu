@@ -199,6 +199,9 @@ struct AmgLevel {
     int* pcptr = nullptr;    // [n_{l+1}+1] blocks of each coarse node (column order)
     int* pcrow = nullptr;    // [npb] fine node of each block, column order
     float* Pc = nullptr;     // [npb][bs*6] the blocks in column order
+    __half* Pvh = nullptr;   // level 0: FP16 copies of Pv and Pc for the V-cycle's transfers
+    __half* Pch = nullptr;
+    __half* valh = nullptr;  // levels >= 1: S = D^-1 A in FP16 [nnzb][36] for the V-cycle's sweeps
     int64_t npb = 0;
     uint8_t* dead = nullptr; // [n * bs] (levels >= 1) DOFs with a zero prolongator column
     // coarse image of the extra blocks outside the element pattern (levels >=
@@ -276,7 +279,7 @@ void amg_free(Amg* a) {
     for (int l = 0; l < a->nlev; ++l) {
         AmgLevel& L = a->L[l];
         void* ptrs[] = {L.rowptr, L.colidx, L.rowof, L.diag, L.val, L.seg, L.seg0, L.prow, L.pcol, L.Pv,
-                        L.pcptr, L.pcrow, L.Pc, L.dead, L.r, L.x, L.t, L.e};
+                        L.pcptr, L.pcrow, L.Pc, L.dead, L.r, L.x, L.t, L.e, L.Pvh, L.Pch, L.valh};
         for (void* p : ptrs)
             if (p) cudaFree(p);
         if (l > 0 && L.dinv) cudaFree(L.dinv);
@@ -532,6 +535,10 @@ tf_status amg_build(tf_handle* h, const double* pos) {
         AMG_TRY(up(&DL.pcptr, pcptr));
         AMG_TRY(up(&DL.pcrow, pcrow));
         AMG_TRY(zeros(&DL.Pc, (size_t)npb * bs * 6));
+        if (lev == 0) {
+            AMG_TRY(zeros(&DL.Pvh, (size_t)npb * bs * 6));
+            AMG_TRY(zeros(&DL.Pch, (size_t)npb * bs * 6));
+        }
         AmgSetup& DS = a->S[lev];
         DS.nT = nT;
         AMG_TRY(up(&DS.Pt, std::vector<float>(P.begin(), P.end())));
@@ -571,6 +578,7 @@ tf_status amg_build(tf_handle* h, const double* pos) {
         AMG_TRY(up(&CL.seg0, C.seg0));
         AMG_TRY(up(&CL.dead, dead));
         AMG_TRY(zeros(&CL.val, (size_t)cnnzb * 36));  // float
+        AMG_TRY(zeros(&CL.valh, (size_t)cnnzb * 36));
         AMG_TRY(zeros(&CL.dinv, (size_t)na * 36));
         H.push_back(std::move(C));
         ++lev;
@@ -773,30 +781,6 @@ __device__ __forceinline__ void mul3(const float* __restrict__ D, const float r[
     z[2] = fmaf(D[6], r[0], fmaf(D[7], r[1], D[8] * r[2]));
 }
 
-// Row of the FP32 copy of the sliced level-0 matrix times x (FP32 vectors).
-__device__ __forceinline__ void sliced_row32(const int* __restrict__ wslot0, const int* __restrict__ scol,
-                                             const float* __restrict__ val, const float* __restrict__ x,
-                                             float y[3]) {
-    const int lane = threadIdx.x & 31;
-    const int wg = blockIdx.x * kWarps + (threadIdx.x >> 5);
-    const int s0 = __ldg(&wslot0[wg]), s1 = __ldg(&wslot0[wg + 1]);
-    float y0 = 0.f, y1 = 0.f, y2 = 0.f;
-    const int* __restrict__ col = scol + lane;
-    const float* __restrict__ a = val + lane;
-#pragma unroll 4
-    for (int s = s0; s < s1; ++s) {
-        const int j = __ldg(&col[(size_t)s * kSlice]);
-        const float* __restrict__ v = a + (size_t)s * kSlotDoubles;
-        const float x0 = x[3 * j], x1 = x[3 * j + 1], x2 = x[3 * j + 2];
-        y0 = fmaf(__ldg(&v[0]), x0, fmaf(__ldg(&v[32]), x1, fmaf(__ldg(&v[64]), x2, y0)));
-        y1 = fmaf(__ldg(&v[96]), x0, fmaf(__ldg(&v[128]), x1, fmaf(__ldg(&v[160]), x2, y1)));
-        y2 = fmaf(__ldg(&v[192]), x0, fmaf(__ldg(&v[224]), x1, fmaf(__ldg(&v[256]), x2, y2)));
-    }
-    y[0] = y0;
-    y[1] = y1;
-    y[2] = y2;
-}
-
 // Row of S = D^-1 A (FP16, sliced) times x, FP32 sums; the extra blocks X
 // (FP64) enter as D^-1 (X x).
 __device__ __forceinline__ void row0s(const Device& d, const __half* __restrict__ valh,
@@ -886,6 +870,50 @@ __device__ __forceinline__ void row6_warp(const AmgLevel& L, int i, const float*
         }
 }
 
+// y = S x for row i of a 6-DOF level, S = D^-1 A stored in FP16 (the
+// element blocks only; extra6 adds the coarse image of the extra blocks).
+__device__ __forceinline__ void row6_warp_h(const AmgLevel& L, int i, const float* __restrict__ x, float y[6]) {
+    const int lane = threadIdx.x & 31;
+    const int kb = lane / 6, a = lane - 6 * kb;
+    float acc = 0.f;
+    const int p0 = L.rowptr[i], p1 = L.rowptr[i + 1];
+    if (lane < 30) {
+#pragma unroll 2
+        for (int p = p0 + kb; p < p1; p += 5) {
+            const int j = __ldg(&L.colidx[p]);
+            const __half2* __restrict__ v = reinterpret_cast<const __half2*>(L.valh + 36 * (size_t)p + 6 * a);
+            const float* __restrict__ xj = x + 6 * (size_t)j;
+#pragma unroll
+            for (int b2 = 0; b2 < 3; ++b2) {
+                const float2 f = __half22float2(__ldg(&v[b2]));
+                acc = fmaf(f.x, xj[2 * b2], fmaf(f.y, xj[2 * b2 + 1], acc));
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        float s2 = 0.f;
+#pragma unroll
+        for (int g = 0; g < 5; ++g) s2 += __shfl_sync(0xffffffffu, acc, 6 * g + k);
+        y[k] = s2;
+    }
+}
+
+// e = X x for row i: the coarse image of the extra blocks (every lane)
+__device__ __forceinline__ void extra6(const AmgLevel& L, int i, const float* __restrict__ x, float e[6]) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) e[k] = 0.f;
+    if (!L.xrow) return;
+    for (int q = L.xrow[i]; q < L.xrow[i + 1]; ++q) {
+        const float* __restrict__ v = L.xval + 36 * (size_t)q;
+        const float* __restrict__ xj = x + 6 * (size_t)L.xcol[q];
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+#pragma unroll
+            for (int m = 0; m < 6; ++m) e[k] = fmaf(v[6 * k + m], xj[m], e[k]);
+    }
+}
+
 // r[a] without dynamic register indexing (which would go to local memory).
 __device__ __forceinline__ float pick6(const float r[6], int a) {
     float v = 0.f;
@@ -907,6 +935,28 @@ __device__ __forceinline__ float lane_mul6(const float* __restrict__ D, const fl
 __global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
         b[k] = (float)a[k];
+}
+
+__global__ void k_f32_to_h(int64_t n, const float* __restrict__ a, __half* __restrict__ b) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+        b[k] = __float2half_rn(a[k]);
+}
+
+// S = D^-1 A of a 6-DOF level in FP16, one thread per block row
+__global__ void k_to_h6(AmgLevel L) {
+    const int64_t gid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gid >= L.nnzb * 6) return;
+    const int64_t p = gid / 6;
+    const int k = (int)(gid - 6 * p);
+    const float* __restrict__ Di = L.dinv + 36 * (size_t)L.rowof[p] + 6 * k;
+    const float* __restrict__ A = L.val + 36 * (size_t)p;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        float v = 0.f;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) v = fmaf(Di[m], A[6 * m + c], v);
+        L.valh[36 * (size_t)p + 6 * k + c] = __float2half_rn(v);
+    }
 }
 
 // S = D^-1 A for the smoother, block by block in the sliced layout, FP16
@@ -1375,14 +1425,17 @@ __global__ void k_v0_prolong(V0 a, AmgLevel F, const float* __restrict__ e, floa
     for (int q = threadIdx.x; q < nitem; q += blockDim.x) {
         const int bq = q / 3, k = q - 3 * bq;
         const int J = __ldg(&F.pcol[b0 + bq]);
-        const float* __restrict__ P = F.Pv + 18 * (size_t)(b0 + bq) + 6 * k;
         float s = 0.f;
         if (!TF_IN(F.check, J, F.ncoarse, CK_PROLONG_COL)) {
             part[q] = 0.f;
             continue;
         }
+        const __half2* __restrict__ P2 = reinterpret_cast<const __half2*>(F.Pvh + 18 * (size_t)(b0 + bq) + 6 * k);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) s = fmaf(__ldg(&P[c]), e[6 * J + c], s);
+        for (int c = 0; c < 3; ++c) {
+            const float2 f = __half22float2(__ldg(&P2[c]));
+            s = fmaf(f.x, e[6 * J + 2 * c], fmaf(f.y, e[6 * J + 2 * c + 1], s));
+        }
         part[q] = s;
     }
     __syncthreads();
@@ -1406,11 +1459,13 @@ __device__ __forceinline__ void restrict_node(const AmgLevel& F, const AmgLevel&
     const int lane = threadIdx.x & 31;
     float rc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     const int q0 = F.pcptr[I], np = BS * (F.pcptr[I + 1] - q0);
+    constexpr bool kHalf = BS == 3;  // level 0: the FP16 copy of the prolongator
     const float* __restrict__ Pc = F.Pc + (size_t)q0 * BS * 6;
+    const __half* __restrict__ Pch = kHalf ? F.Pch + (size_t)q0 * BS * 6 : nullptr;
     for (int qa = lane; qa < np; qa += 64) {
         // two (block, row) pairs per lane and pass: their loads overlap
         float tk[2] = {0.f, 0.f};
-        const float* __restrict__ P[2] = {Pc, Pc};
+        int qq[2] = {0, 0};
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
             const int q = qa + 32 * u;
@@ -1419,13 +1474,25 @@ __device__ __forceinline__ void restrict_node(const AmgLevel& F, const AmgLevel&
                 const int i = __ldg(&F.pcrow[q0 + m]);
                 if (!TF_IN(F.check, i, F.n, CK_RESTRICT_ROW)) continue;
                 tk[u] = t[BS * (size_t)i + k];
-                P[u] = Pc + 6 * (size_t)q;
+                qq[u] = q;
             }
         }
 #pragma unroll
-        for (int u = 0; u < 2; ++u)
+        for (int u = 0; u < 2; ++u) {
+            if constexpr (kHalf) {
+                const __half2* __restrict__ P2 = reinterpret_cast<const __half2*>(Pch + 6 * (size_t)qq[u]);
 #pragma unroll
-            for (int b = 0; b < 6; ++b) rc[b] = fmaf(__ldg(&P[u][b]), tk[u], rc[b]);
+                for (int b = 0; b < 3; ++b) {
+                    const float2 f = __half22float2(__ldg(&P2[b]));
+                    rc[2 * b] = fmaf(f.x, tk[u], rc[2 * b]);
+                    rc[2 * b + 1] = fmaf(f.y, tk[u], rc[2 * b + 1]);
+                }
+            } else {
+                const float* __restrict__ P = Pc + 6 * (size_t)qq[u];
+#pragma unroll
+                for (int b = 0; b < 6; ++b) rc[b] = fmaf(__ldg(&P[b]), tk[u], rc[b]);
+            }
+        }
     }
 #pragma unroll
     for (int b = 0; b < 6; ++b)
@@ -1471,24 +1538,34 @@ __device__ __forceinline__ void prolong_node(const AmgLevel& F, const float* __r
 // out_i = x_i + omega D_i^-1 (r - A x)_i for row i, by one warp
 __device__ __forceinline__ void post_row(const AmgLevel& L, const double* __restrict__ omega,
                                          const float* __restrict__ x, float* __restrict__ out, int i) {
+    // x + omega (D^-1 (r - X x) - S x), S = D^-1 A in FP16, X the extra blocks
     const int lane = threadIdx.x & 31;
     float y[6], rr[6];
-    row6_warp(L, i, x, y);
+    row6_warp_h(L, i, x, y);
+    extra6(L, i, x, rr);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) rr[k] = L.r[6 * i + k] - y[k];
+    for (int k = 0; k < 6; ++k) rr[k] = L.r[6 * i + k] - rr[k];
     if (lane < 6)
-        out[6 * i + lane] = fmaf((float)__ldg(omega), lane_mul6(L.dinv + 36 * (size_t)i, rr, lane), x[6 * i + lane]);
+        out[6 * i + lane] = fmaf((float)__ldg(omega), lane_mul6(L.dinv + 36 * (size_t)i, rr, lane) - pick6(y, lane),
+                                 x[6 * i + lane]);
+}
+
+// t_i = r_i - (A x)_i with A x = D (S x) + X x, lane k < 6 writing component k
+__device__ __forceinline__ void resid_row(const AmgLevel& L, const float* __restrict__ x, int i) {
+    const int lane = threadIdx.x & 31;
+    float y[6], e[6];
+    row6_warp_h(L, i, x, y);
+    extra6(L, i, x, e);
+    if (lane < 6)
+        L.t[6 * i + lane] = L.r[6 * i + lane] - lane_mul6(L.val + 36 * (size_t)L.diag[i], y, lane) - pick6(e, lane);
 }
 
 // t = r - A x  (one warp per row)
 __global__ void k_v6_resid(AmgLevel L, const double* __restrict__ scal, const float* __restrict__ x) {
     pdl_enter();
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
     if (i >= L.n || seg_stopped(scal, L.seg[i])) return;
-    float y[6];
-    row6_warp(L, i, x, y);
-    if (lane < 6) L.t[6 * i + lane] = L.r[6 * i + lane] - pick6(y, lane);
+    resid_row(L, x, i);
 }
 
 // out = x + omega D^-1 (r - A x)  (one warp per row)
@@ -1553,7 +1630,7 @@ __global__ void __launch_bounds__(kTailThreads) k_tail(Tail T) {
     pdl_enter();
     const int g = blockIdx.x;
     if (seg_stopped(T.scal, g)) return;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     float* cur[kAmgMaxLevels];
     for (int l = T.first; l < T.last; ++l) {
         const AmgLevel& F = T.L[l];
@@ -1566,11 +1643,7 @@ __global__ void __launch_bounds__(kTailThreads) k_tail(Tail T) {
             x = out;
         }
         cur[l] = x;
-        for (int i = F.seg0[g] + warp; i < F.seg0[g + 1]; i += nw) {
-            float y[6];
-            row6_warp(F, i, x, y);
-            if (lane < 6) F.t[6 * i + lane] = F.r[6 * i + lane] - pick6(y, lane);
-        }
+        for (int i = F.seg0[g] + warp; i < F.seg0[g + 1]; i += nw) resid_row(F, x, i);
         __syncthreads();
         for (int I = C.seg0[g] + warp; I < C.seg0[g + 1]; I += nw)
             restrict_node<6>(F, C, F.t, I, T.omega + l + 1, l + 1 < T.last ? 1 : 0);
@@ -1679,6 +1752,12 @@ tf_status amg_numeric(tf_handle* h) {
         TF_LAUNCH_CHECK(h);
         k_p_columns<<<cdiv(L.npb * L.bs * 6, kT), kT, 0, st>>>(L, S, L.bs * 6);
         TF_LAUNCH_CHECK(h);
+        if (l == 0) {
+            k_f32_to_h<<<4 * 152, kT, 0, st>>>(L.npb * L.bs * 6, L.Pv, L.Pvh);
+            TF_LAUNCH_CHECK(h);
+            k_f32_to_h<<<4 * 152, kT, 0, st>>>(L.npb * L.bs * 6, L.Pc, L.Pch);
+            TF_LAUNCH_CHECK(h);
+        }
         if (l == 0) k_ptap<3><<<cdiv(C.nnzb * 6, kT), kT, 0, st>>>(L, S, C);
         else k_ptap<6><<<cdiv(C.nnzb * 6, kT), kT, 0, st>>>(L, S, C);
         TF_LAUNCH_CHECK(h);
@@ -1688,6 +1767,8 @@ tf_status amg_numeric(tf_handle* h) {
             TF_LAUNCH_CHECK(h);
         }
         k_inv6<<<cdiv(C.n, kT), kT, 0, st>>>(C);
+        TF_LAUNCH_CHECK(h);
+        k_to_h6<<<cdiv(C.nnzb * 6, kT), kT, 0, st>>>(C);
         TF_LAUNCH_CHECK(h);
     }
     if (a->coarse_exact) {
