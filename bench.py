@@ -114,17 +114,19 @@ def algorithmic_bytes(nn, ne, nnz):
     return 408 * ne + 48 * nn + 24 * nn + 8 * nnz
 
 
-# FP64 flops per prism of one element-kernel launch, counted with ncu
-# (2 x DFMA + DADD + DMUL thread instructions / prisms) on the 135,200-prism
-# sheet with internal viscosity; the elastic-only count applies when every
-# eta is 0.
-FP64_FLOPS_PER_PRISM = {"viscous": 23968, "elastic": None}
+# Instruction mix of one element-kernel launch, counted with ncu on the
+# 135,200-prism sheet with internal viscosity (per prism): FP64 flops
+# (2 x DFMA + DADD + DMUL thread instructions; phase A and the joins) and
+# FP32 thread instructions (FADD + FFMA + FMUL; the double-float block sums),
+# with the FP64 pipe's busy fraction ncu reported.  The elastic-only counts
+# apply when every eta is 0 (not captured).
+FP64_FLOPS_PER_PRISM = {"viscous": 4644, "elastic": None}
+FP32_INST_PER_PRISM = {"viscous": 136492, "elastic": None}
+FP64_PIPE_PCT_NCU = {"viscous": 44.1, "elastic": None}
 # DRAM bytes (read + write) per prism of one element-kernel launch, from the
-# same ncu capture (331.4 MB at 135,200 prisms); the kernel's traffic grows
+# same ncu capture (333.1 MB at 135,200 prisms); the kernel's traffic grows
 # with the number of prisms, so a full launch is scaled from it.
-DRAM_BYTES_PER_PRISM = {"viscous": 331.4e6 / 135200, "elastic": None}
-# FP64 peak of GB300: 304 DFMA per cycle (ncu's peak_sustained for the whole
-# GPU) x 2 flop x 2.07 GHz
+DRAM_BYTES_PER_PRISM = {"viscous": 333.1e6 / 135200, "elastic": None}
 FP64_PEAK_TFLOPS = 304 * 2 * 2.07e9 / 1e12
 
 
@@ -309,7 +311,10 @@ def run_gpu(args, t):
         tf = fpp * ne / (elem_ms / 1e3) / 1e12
         fp64 = {"kernel": "k_element", "achieved": tf, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
                 "frac": tf / FP64_PEAK_TFLOPS, "flops_per_prism": fpp,
-                "peak_source": "ncu peak_sustained DFMA rate x max SM clock"}
+                "peak_source": "ncu peak_sustained DFMA rate x max SM clock",
+                "fp64_pipe_pct_ncu": FP64_PIPE_PCT_NCU[kind],
+                "fp32_inst_per_prism": FP32_INST_PER_PRISM[kind],
+                "note": "phase A and the forces in FP64; the tangent's block sums in double-float on the FP32 pipe"}
 
     # e2e through the C ABI with host buffers
     uk = s.positions()
