@@ -118,6 +118,10 @@ void free_all(tf_handle* h) {
                     d.tblk, d.valT, d.lamv, d.carry, d.dldu, d.gr, d.ge, d.nu, d.apical, d.xrow, d.xcol, d.xval,
                     d.check};
     destroy_graphs(h);
+    if (h->kloop_ctl) cudaFree(h->kloop_ctl);
+    if (h->kloop_host) cudaFreeHost(h->kloop_host);
+    h->kloop_ctl = nullptr;
+    h->kloop_host = nullptr;
     if (h->amg) {
         amg_free(h->amg);
         h->amg = nullptr;

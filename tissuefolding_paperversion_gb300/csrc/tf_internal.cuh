@@ -379,6 +379,10 @@ struct tf_handle {
     bool tuned = false;
     cudaGraphExec_t graph[2][5] = {};           // Krylov chunks [method-1][log2(chunk/4)]
     int64_t graph_kernels[2][5] = {};
+    cudaGraphExec_t kloop[2] = {};              // a whole solve as one graph (device-side while loop) [method-1]
+    bool kloop_off = false;                     // that graph could not be built here: host-checked chunks
+    int* kloop_ctl = nullptr;                   // device: [iterations run, iteration cap]
+    int* kloop_host = nullptr;                  // pinned copy of the iterations run
     int last_iters[2] = {0, 0};                 // iterations of the last solve per method (chunk planning)
     int plan_iters[2][8] = {};                  // the same per Newton iteration of a step (0-6, 7: later ones)
     int newton_index = -1;                      // Newton iteration of the current solve (-1: outside a step)

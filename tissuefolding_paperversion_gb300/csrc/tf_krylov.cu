@@ -688,6 +688,64 @@ tf_status run_chunk(tf_handle* h, const Ctx& c, int method, int ci) {
     return TF_OK;
 }
 
+// Loop control of the device-side Krylov loop (one warp): counts the
+// iteration and keeps the loop going while an instance is still running and
+// the iteration cap is not reached, so the loop always ends.
+__global__ void k_krylov_ctl(const double* __restrict__ scal, int nseg, int* __restrict__ ctl,
+                             cudaGraphConditionalHandle loop) {
+    bool running = false;
+    for (int g = threadIdx.x; g < nseg; g += 32) running |= __ldcg(&scal[(size_t)g * S_COUNT + S_FLAG]) == F_RUNNING;
+    running = __any_sync(0xffffffffu, running);
+    if (threadIdx.x == 0) {
+        const int it = ctl[0] + 1;
+        ctl[0] = it;
+        cudaGraphSetConditional(loop, (running && it < ctl[1]) ? 1u : 0u);
+    }
+}
+
+__global__ void k_krylov_arm(int* __restrict__ ctl, int cap) {
+    ctl[0] = 0;
+    ctl[1] = cap;
+}
+
+// A whole solve's iterations as one graph: a conditional while node whose
+// body is one iteration followed by k_krylov_ctl; no host round trip and no
+// iteration past convergence.  Returns false when the graph cannot be built
+// (the caller then runs host-checked chunks).
+bool build_krylov_loop(tf_handle* h, const Ctx& c, int method) {
+    cudaGraph_t g = nullptr;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) return false;
+    cudaGraphConditionalHandle hc = 0;
+    bool ok = cudaGraphConditionalHandleCreate(&hc, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+    cudaGraphNodeParams p = {};
+    cudaGraphNode_t node = nullptr;
+    if (ok) {
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = hc;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p) == cudaSuccess;
+    }
+    if (ok) {
+        cudaGraph_t body = p.conditional.phGraph_out[0];
+        ok = cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) ==
+             cudaSuccess;
+        if (ok) {
+            issue_iterations(h, c, method, 1);
+            k_krylov_ctl<<<1, 32, 0, h->stream>>>(h->d.scal, h->d.nseg, h->kloop_ctl, hc);
+            cudaGraph_t out = nullptr;
+            ok = cudaStreamEndCapture(h->stream, &out) == cudaSuccess;
+        }
+    }
+    if (ok) ok = cudaGraphInstantiate(&h->kloop[method - 1], g, 0) == cudaSuccess;
+    cudaGraphDestroy(g);
+    if (!ok) {
+        h->kloop[method - 1] = nullptr;
+        (void)cudaGetLastError();
+    }
+    return ok;
+}
+
 tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* relres) {
     Device& d = h->d;
     const Ctx c = make_ctx(h);
@@ -731,6 +789,23 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
     int launched = 0, ci = 1;
     int planned = (keep == 0) ? (prev * 7) / 8 : 0;
     bool done = false, fixed = planned > 0;
+    if (!h->kloop_off && !h->kloop_ctl) {
+        TF_CUDA(cudaMalloc(&h->kloop_ctl, 2 * sizeof(int)));
+        TF_CUDA(cudaMallocHost(&h->kloop_host, sizeof(int)));
+    }
+    if (!h->kloop_off && !h->kloop[method - 1] && !build_krylov_loop(h, c, method)) h->kloop_off = true;
+    if (!h->kloop_off) {
+        // the device-side loop: every iteration until convergence (or the cap)
+        k_krylov_arm<<<1, 1, 0, st>>>(h->kloop_ctl, maxit);
+        TF_LAUNCH_CHECK(h);
+        TF_CUDA(cudaGraphLaunch(h->kloop[method - 1], st));
+        TF_CUDA(cudaMemcpyAsync(h->kloop_host, h->kloop_ctl, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TF_CUDA(cudaMemcpyAsync(d.host_scal, d.scal, sizeof(double) * nscal, cudaMemcpyDeviceToHost, st));
+        TF_CUDA(cudaStreamSynchronize(st));
+        launched = *h->kloop_host;
+        h->launches += (int64_t)launched * (kernels_per_iteration(h, method) + 1);
+        done = true;
+    }
     while (launched < maxit && !done) {
         int target = planned > 0 ? planned : (fixed ? kChunk0 : (kChunk0 << ci));
         planned = 0;
@@ -869,6 +944,11 @@ void destroy_graphs(tf_handle* h) {
                 cudaGraphExecDestroy(g);
                 g = nullptr;
             }
+    for (auto& g : h->kloop)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
 }
 
 }  // namespace tf
