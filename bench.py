@@ -377,6 +377,7 @@ def run_gpu(args, t):
                    "krylov_iters_per_step": sum(x["krylov_total"] for x in stats) / len(stats),
                    "krylov_iters_by_step": [int(x["krylov_total"]) for x in stats],
                    "newton_iters_by_step": [int(x["iters"]) for x in stats],
+                   "device_loop_iters_by_step": [int(x.get("device_iters", 0)) for x in stats],
                    "ms_by_step": [round(float(x["ms_total"]), 3) for x in stats],
                    "ms_assembly": ms_asm / n_asm, "wall_s": wall},
         "e2e": {"value": ne / e2e_s, "unit": "prisms/s", "h2d_bytes_per_step": 2 * 8 * 3 * nn,

@@ -103,6 +103,8 @@ typedef struct tf_step_stats {
     float ms_assemble;          /* device time spent in assembly (all iterations) */
     float ms_solve;             /* device time spent in linear solves */
     float ms_total;             /* device time of the whole step */
+    int32_t device_iters;       /* Newton iterations run by the device-side loop (one graph launch for the
+                                   iterations after the step's first; the rest ran host-driven) */
 } tf_step_stats;
 
 TF_API const char* tf_status_string(tf_status s);

@@ -75,7 +75,8 @@ class tf_options(C.Structure):
 class tf_step_stats(C.Structure):
     _fields_ = [("newton_iters", C.c_int32), ("krylov_iters_total", C.c_int32), ("krylov_iters_max", C.c_int32),
                 ("converged", C.c_int32), ("dunorm", C.c_double * 32), ("final_relres", C.c_double),
-                ("ms_assemble", C.c_float), ("ms_solve", C.c_float), ("ms_total", C.c_float)]
+                ("ms_assemble", C.c_float), ("ms_solve", C.c_float), ("ms_total", C.c_float),
+                ("device_iters", C.c_int32)]
 
 
 _lib = None
@@ -431,7 +432,7 @@ class Solver:
         return {"status": s, "iters": n, "dunorm": np.array(st.dunorm[: min(n, 32)]),
                 "krylov_total": st.krylov_iters_total, "krylov_max": st.krylov_iters_max,
                 "converged": bool(st.converged), "relres": st.final_relres, "ms_assemble": st.ms_assemble,
-                "ms_solve": st.ms_solve, "ms_total": st.ms_total}
+                "ms_solve": st.ms_solve, "ms_total": st.ms_total, "device_iters": st.device_iters}
 
     # -- inspection ---------------------------------------------------------
     def residual(self):
@@ -583,7 +584,8 @@ class Batch(Solver):
         allow = (TF_NOT_CONVERGED,) if allow_not_converged else ()
         s = self._check(self.L.tf_batch_step(self.h, dt, _ptr(iters), _ptr(conv), C.byref(st)), "tf_batch_step", allow)
         return {"status": s, "iters": iters, "converged": conv.astype(bool), "krylov_total": st.krylov_iters_total,
-                "ms_total": st.ms_total, "ms_assemble": st.ms_assemble, "newton_rounds": st.newton_iters}
+                "ms_total": st.ms_total, "ms_assemble": st.ms_assemble, "newton_rounds": st.newton_iters,
+                "device_iters": st.device_iters}
 
     def instance_positions(self, i):
         p = self.positions()

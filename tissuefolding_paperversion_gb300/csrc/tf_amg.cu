@@ -1690,6 +1690,29 @@ bool use_multigrid(const tf_handle* h) { return h->amg != nullptr; }
 // coarse operators, block inverses and smoother weights are rebuilt at the
 // first solve of each time step (and whenever a solve with reused coarse
 // levels fails, see krylov_solve).
+// The level-0 copies the smoother reads, from the current assembly: FP32
+// values and block inverses, the FP16 operator S = D^-1 A and the diagonal
+// blocks (kernels only: also captured into the device Newton loop).
+void amg_refresh(tf_handle* h) {
+    Amg* a = h->amg;
+    Device& d = h->d;
+    cudaStream_t st = h->stream;
+    k_to_f32<<<4 * 152, kT, 0, st>>>(d.nval, d.val, a->val32);
+    h->launches++;
+    k_to_f32<<<4 * 152, kT, 0, st>>>(9 * (int64_t)d.nn, d.dinv, a->dinv32);
+    h->launches++;
+    k_to_h<<<d.ncta, kNodeThreads, 0, st>>>(d, a->val32, a->dinv32, a->valh, a->diag32);
+    h->launches++;
+}
+
+// The refresh above has run for the current assembly (inside the device
+// Newton loop): nothing is stale, the coarse levels are the reused ones.
+void amg_refreshed(tf_handle* h) {
+    if (!h->amg) return;
+    h->amg->stale = 0;
+    h->amg->reused = true;
+}
+
 tf_status amg_numeric(tf_handle* h) {
     NvtxRange nvtx_range("tf multigrid numeric");
     Amg* a = h->amg;
@@ -1698,13 +1721,7 @@ tf_status amg_numeric(tf_handle* h) {
         TF_CUDA(cudaFuncSetAttribute(k_v0_prolong, cudaFuncAttributeMaxDynamicSharedMemorySize, a->v0_smem));
     Device& d = h->d;
     cudaStream_t st = h->stream;
-    // FP32 copies of the level-0 values and block inverses for the smoother
-    k_to_f32<<<4 * 152, kT, 0, st>>>(d.nval, d.val, a->val32);
-    TF_LAUNCH_CHECK(h);
-    k_to_f32<<<4 * 152, kT, 0, st>>>(9 * (int64_t)d.nn, d.dinv, a->dinv32);
-    TF_LAUNCH_CHECK(h);
-    k_to_h<<<d.ncta, kNodeThreads, 0, st>>>(d, a->val32, a->dinv32, a->valh, a->diag32);
-    TF_LAUNCH_CHECK(h);
+    amg_refresh(h);
     a->reused = a->stale == 1;
     if (a->reused) {
         a->stale = 0;

@@ -122,6 +122,16 @@ void free_all(tf_handle* h) {
     if (h->kloop_host) cudaFreeHost(h->kloop_host);
     h->kloop_ctl = nullptr;
     h->kloop_host = nullptr;
+    if (h->nd) cudaFree(h->nd);
+    if (h->nd_host) cudaFreeHost(h->nd_host);
+    if (h->nd_seg) cudaFree(h->nd_seg);
+    if (h->nd_seg_host) cudaFreeHost(h->nd_seg_host);
+    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    h->nd = nullptr;
+    h->nd_host = nullptr;
+    h->nd_seg = nullptr;
+    h->nd_seg_host = nullptr;
+    h->cap_stream = nullptr;
     if (h->amg) {
         amg_free(h->amg);
         h->amg = nullptr;
@@ -585,6 +595,7 @@ tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* ite
     std::vector<double> du2(d.nseg);
     float ms_asm = 0.f;
     int k = 0;
+    bool device_tried = false;
     while (true) {
         TF_CUDA(cudaEventRecord(h->ev[2], h->stream));
         TF_TRY(tf_assemble(h));
@@ -655,6 +666,14 @@ tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* ite
         if (!any_active) break;
         TF_CUDA(cudaMemcpyAsync(d.seg_active, h->h_active.data(), sizeof(int) * (size_t)d.nseg,
                                 cudaMemcpyHostToDevice, h->stream));
+        if (!device_tried) {
+            // the rest of the step's iterations as one graph on the device; an
+            // iteration it hands back (exc) continues on this host path
+            device_tried = true;
+            bool ran = false, exc = false;
+            TF_TRY(newton_device_loop(h, it.data(), cv.data(), capped.data(), &k, &st, &ms_asm, &ran, &exc));
+            if (ran && !exc) break;
+        }
     }
     std::fill(h->h_active.begin(), h->h_active.end(), 1);
     TF_CUDA(cudaMemcpyAsync(d.seg_active, h->h_active.data(), sizeof(int) * (size_t)d.nseg, cudaMemcpyHostToDevice,

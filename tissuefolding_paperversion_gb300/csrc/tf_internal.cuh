@@ -169,6 +169,16 @@ struct Packing;  // packing between tissue surfaces (tf_packing.cu)
 struct Growth;   // growth functions (tf_growth.cu)
 struct BindPlan; // device program of the bound-DOF merges (tf_api.cu)
 
+// State of the device-side Newton loop (tf_krylov.cu), in device memory with a
+// pinned host mirror.
+struct NewtonDev {
+    int k;                     // Newton iterations of the step so far
+    int exc;                   // 1: the loop stopped for the host (solve failed, non-finite or near-threshold update)
+    int krylov_total, krylov_max;
+    unsigned long long t0, t_asm;  // assembly timing (%globaltimer, ns)
+    double dunorm[32];         // largest |du| over the instances, per Newton iteration
+};
+
 // Inverse of a 3x3 matrix (row-major) by cofactors.
 __device__ __forceinline__ void inv3_cof(const double* M, double* inv) {
     const double c0 = M[4] * M[8] - M[5] * M[7];
@@ -380,6 +390,15 @@ struct tf_handle {
     cudaGraphExec_t graph[2][5] = {};           // Krylov chunks [method-1][log2(chunk/4)]
     int64_t graph_kernels[2][5] = {};
     cudaGraphExec_t kloop[2] = {};              // a whole solve as one graph (device-side while loop) [method-1]
+    cudaGraphExec_t nloop = nullptr;            // the Newton iterations after a step's first as one graph
+    double nloop_dt = 0.0;                      // the step length that graph was captured with
+    bool nloop_off = false;                     // that graph could not be built here: host-driven iterations
+    int64_t nloop_kernels = 0;                  // kernels of one of its Newton iterations outside the Krylov loop
+    cudaStream_t cap_stream = nullptr;          // second stream for capturing nested loop bodies
+    tf::NewtonDev* nd = nullptr;                // device Newton-loop state and its pinned mirror
+    tf::NewtonDev* nd_host = nullptr;
+    int* nd_seg = nullptr;                      // device [3][nseg]: Newton iterations, converged, capped
+    int* nd_seg_host = nullptr;                 // pinned mirror
     bool kloop_off = false;                     // that graph could not be built here: host-checked chunks
     int* kloop_ctl = nullptr;                   // device: [iterations run, iteration cap]
     int* kloop_host = nullptr;                  // pinned copy of the iterations run
@@ -423,9 +442,16 @@ tf_status launch_block_inverse(tf_handle* h);
 tf_status krylov_solve(tf_handle* h, int* iters, double* relres);
 tf_status launch_update(tf_handle* h);
 tf_status launch_update_norm(tf_handle* h);   // |du|^2 into S_DU2 without applying du
+// The Newton iterations after the first of a step on the device (one graph
+// launch); io arrays per instance are the host's bookkeeping, updated.
+// *ran = false when the loop is not available here (nothing was done).
+tf_status newton_device_loop(tf_handle* h, int* it, int* cv, int* capped, int* k, tf_step_stats* st, float* ms_asm,
+                             bool* ran, bool* exc);
 tf_status autotune_element(tf_handle* h);
 tf_status amg_build(tf_handle* h, const double* ref_pos);
 tf_status amg_numeric(tf_handle* h);
+void amg_refresh(tf_handle* h);     // launches the level-0 smoother copies of the current assembly
+void amg_refreshed(tf_handle* h);   // records that amg_refresh ran for the current assembly
 void amg_vcycle(tf_handle* h, const double* r, double* out);
 int amg_vcycle_kernels(const tf_handle* h);
 void amg_free(Amg* a);

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
 #include "tf_internal.cuh"
@@ -582,7 +583,9 @@ __global__ void k_bi_restart(Ctx c, const double* __restrict__ r, double* __rest
 // APPLY = false: |du|^2 only (the same sum, uk untouched), for the Newton
 // test before the update is applied.
 template <bool APPLY>
-__global__ void k_update(Ctx c, double* __restrict__ uk, const double* __restrict__ du) {
+__global__ void k_update(Ctx c, double* __restrict__ uk, const double* __restrict__ du,
+                         const int* __restrict__ skip = nullptr) {
+    if (skip && __ldcg(skip)) return;  // the device Newton loop handed this update to the host
     const Where w = where(c);
     double v[1] = {0.0};
     if (w.valid) {
@@ -703,9 +706,12 @@ __global__ void k_krylov_ctl(const double* __restrict__ scal, int nseg, int* __r
     }
 }
 
-__global__ void k_krylov_arm(int* __restrict__ ctl, int cap) {
+// Resets the iteration count of a device-side Krylov loop (and, inside an
+// enclosing loop, opens the Krylov loop's condition again).
+__global__ void k_krylov_arm(int* __restrict__ ctl, int cap, cudaGraphConditionalHandle loop, int open) {
     ctl[0] = 0;
     ctl[1] = cap;
+    if (open) cudaGraphSetConditional(loop, 1u);
 }
 
 // A whole solve's iterations as one graph: a conditional while node whose
@@ -796,7 +802,7 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
     if (!h->kloop_off && !h->kloop[method - 1] && !build_krylov_loop(h, c, method)) h->kloop_off = true;
     if (!h->kloop_off) {
         // the device-side loop: every iteration until convergence (or the cap)
-        k_krylov_arm<<<1, 1, 0, st>>>(h->kloop_ctl, maxit);
+        k_krylov_arm<<<1, 1, 0, st>>>(h->kloop_ctl, maxit, 0, 0);
         TF_LAUNCH_CHECK(h);
         TF_CUDA(cudaGraphLaunch(h->kloop[method - 1], st));
         TF_CUDA(cudaMemcpyAsync(h->kloop_host, h->kloop_ctl, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -937,6 +943,301 @@ tf_status launch_update_norm(tf_handle* h) {
     return TF_OK;
 }
 
+// ---- the Newton loop on the device -----------------------------------------
+// Iterations 2, 3, ... of a time step (the first, with the multigrid rebuild
+// and any retries, runs host-driven) as one graph: a conditional while node
+// whose body is a whole Newton iteration -- assembly, the level-0 refresh of
+// the multigrid, the Krylov solve as a nested while node, |du|, the Newton
+// test of every instance (k_newton_ctl) and the update -- so a step needs one
+// host wait after its first iteration.  Anything the device does not decide
+// (a solve that did not converge, a non-finite update, a loosened solve whose
+// |du| lands near newton_tol) stops the loop before the update is applied and
+// hands the iteration back to the host path.
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__global__ void k_stamp_begin(NewtonDev* nd) { nd->t0 = global_ns(); }
+__global__ void k_stamp_end(NewtonDev* nd) { nd->t_asm += global_ns() - nd->t0; }
+
+// The Newton test of every instance after a solve (one CTA): the reference's
+// |du| <= tol (NewtonRaphsonSolver.cpp:727-752) and the iteration cap, the
+// instance mask of the next iteration, and the loop condition.
+__global__ void __launch_bounds__(256) k_newton_ctl(const double* __restrict__ scal, int nseg,
+                                                    int* __restrict__ active, int* __restrict__ it,
+                                                    int* __restrict__ cv, int* __restrict__ capped, NewtonDev* nd,
+                                                    double tol, double rtol2, int max_iter, int loosened,
+                                                    cudaGraphConditionalHandle loop) {
+    __shared__ int exc, any;
+    __shared__ double dmax;
+    __shared__ int kmax;
+    if (threadIdx.x == 0) {
+        exc = 0;
+        any = 0;
+        dmax = 0.0;
+        kmax = 0;
+    }
+    __syncthreads();
+    for (int g = threadIdx.x; g < nseg; g += blockDim.x) {
+        if (!active[g]) continue;
+        const double* s = scal + (size_t)g * S_COUNT;
+        const double dn = sqrt(__ldcg(&s[S_DU2]));
+        const bool near = loosened && __ldcg(&s[S_TOL2]) > rtol2 && dn > 0.5 * tol && dn < 2.0 * tol;
+        if (__ldcg(&s[S_FLAG]) != F_CONVERGED || !isfinite(dn) || near) atomicExch(&exc, 1);
+    }
+    __syncthreads();
+    if (exc) {
+        if (threadIdx.x == 0) {
+            nd->exc = 1;
+            cudaGraphSetConditional(loop, 0u);
+        }
+        return;
+    }
+    for (int g = threadIdx.x; g < nseg; g += blockDim.x) {
+        if (!active[g]) continue;
+        const double* s = scal + (size_t)g * S_COUNT;
+        const double dn = sqrt(__ldcg(&s[S_DU2]));
+        atomicMax(&kmax, (int)__ldcg(&s[S_ITER]));
+        // dn >= 0: the bit patterns of non-negative doubles order like the values
+        atomicMax(reinterpret_cast<unsigned long long*>(&dmax), (unsigned long long)__double_as_longlong(dn));
+        it[g] += 1;
+        if (!(dn > tol)) {
+            cv[g] = 1;
+            active[g] = 0;
+        } else if (it[g] > max_iter) {
+            capped[g] = 1;
+            active[g] = 0;
+        } else {
+            any = 1;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int k = nd->k;
+        if (k < 32) nd->dunorm[k] = dmax;
+        nd->k = k + 1;
+        nd->krylov_total += kmax;
+        nd->krylov_max = max(nd->krylov_max, kmax);
+        cudaGraphSetConditional(loop, any ? 1u : 0u);
+    }
+}
+
+namespace {
+
+// A conditional handle of the graph being captured on h->stream (its value is
+// set by a kernel before the node that uses it: nothing resets it when an
+// enclosing loop runs the node again).
+bool capture_handle(tf_handle* h, cudaGraphConditionalHandle* hc) {
+    cudaStreamCaptureStatus stat;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamGetCaptureInfo(h->stream, &stat, nullptr, &g, nullptr, nullptr, nullptr) != cudaSuccess ||
+        stat != cudaStreamCaptureStatusActive)
+        return false;
+    return cudaGraphConditionalHandleCreate(hc, g, 0, 0) == cudaSuccess;
+}
+
+// Adds a while node on handle hc to the graph being captured on h->stream and
+// captures its body (one call of `body` on h->stream, swapped for the capture
+// stream); later work captured on h->stream follows the node.
+template <class Body>
+bool capture_while(tf_handle* h, cudaGraphConditionalHandle hc, Body body) {
+    cudaStreamCaptureStatus stat;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edges = nullptr;
+    size_t ndeps = 0;
+    if (cudaStreamGetCaptureInfo(h->stream, &stat, nullptr, &g, &deps, &edges, &ndeps) != cudaSuccess ||
+        stat != cudaStreamCaptureStatusActive)
+        return false;
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = hc;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if (cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p) != cudaSuccess) return false;
+    if (cudaStreamUpdateCaptureDependencies(h->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies) !=
+        cudaSuccess)
+        return false;
+    cudaGraph_t bg = p.conditional.phGraph_out[0];
+    if (cudaStreamBeginCaptureToGraph(h->cap_stream, bg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+        cudaSuccess)
+        return false;
+    std::swap(h->stream, h->cap_stream);
+    body();
+    std::swap(h->stream, h->cap_stream);
+    cudaGraph_t out = nullptr;
+    return cudaStreamEndCapture(h->cap_stream, &out) == cudaSuccess;
+}
+
+// One Newton iteration on h->stream (being captured): see above.
+bool issue_newton_iteration(tf_handle* h, cudaGraphConditionalHandle newton) {
+    Device& d = h->d;
+    const Ctx c = make_ctx(h);
+    cudaStream_t st = h->stream;
+    const int method = h->method;
+    const bool mg = use_multigrid(h);
+    k_stamp_begin<<<1, 1, 0, st>>>(h->nd);
+    if (launch_prepare(h) != TF_OK || launch_element(h) != TF_OK) return false;
+    if (h->opt.deterministic && launch_deterministic_gather(h) != TF_OK) return false;
+    k_stamp_end<<<1, 1, 0, st>>>(h->nd);
+    if (cudaMemcpyAsync(d.seg_solve, d.seg_active, sizeof(int) * (size_t)d.nseg, cudaMemcpyDeviceToDevice, st) !=
+        cudaSuccess)
+        return false;
+    if (launch_block_inverse(h) != TF_OK) return false;
+    if (mg) amg_refresh(h);
+    const double tol2 = h->opt.krylov_rtol * h->opt.krylov_rtol;
+    const int jac = mg ? 0 : 1;
+    if (method == 1) {
+        k_cg_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.z, d.p, tol2, h->opt.update_atol, 0, jac);
+        if (mg) {
+            amg_vcycle(h, d.r, d.z);
+            k_cg_rz<<<d.ncta, kThreads, 0, st>>>(c, d.r, d.z, d.p, 1);
+        }
+    } else {
+        k_bi_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.rhat, d.p, d.q, tol2, h->opt.update_atol, 0);
+    }
+    cudaGraphConditionalHandle kc = 0;
+    if (!capture_handle(h, &kc)) return false;
+    k_krylov_arm<<<1, 1, 0, st>>>(h->kloop_ctl, h->opt.krylov_max_iter, kc, 1);
+    bool ok = capture_while(h, kc, [&] {
+        issue_iterations(h, c, method, 1);
+        k_krylov_ctl<<<1, 32, 0, h->stream>>>(d.scal, d.nseg, h->kloop_ctl, kc);
+    });
+    if (!ok) return false;
+    k_update<false><<<d.ncta, kThreads, 0, st>>>(c, d.uk, d.du);
+    int* seg = h->nd_seg;
+    k_newton_ctl<<<1, 256, 0, st>>>(d.scal, d.nseg, d.seg_active, seg, seg + d.nseg, seg + 2 * d.nseg, h->nd,
+                                     h->opt.newton_tol, tol2, h->opt.newton_max_iter, h->opt.update_atol > 0.0 ? 1 : 0,
+                                     newton);
+    k_update<true><<<d.ncta, kThreads, 0, st>>>(c, d.uk, d.du, &h->nd->exc);
+    return cudaGetLastError() == cudaSuccess;
+}
+
+bool build_newton_loop(tf_handle* h) {
+    cudaGraph_t g = nullptr;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) return false;
+    cudaGraphConditionalHandle hc = 0;
+    bool ok = cudaGraphConditionalHandleCreate(&hc, g, 1, cudaGraphCondAssignDefault) == cudaSuccess;
+    cudaGraphNodeParams p = {};
+    cudaGraphNode_t node = nullptr;
+    if (ok) {
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = hc;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p) == cudaSuccess;
+    }
+    if (ok) {
+        ok = cudaStreamBeginCaptureToGraph(h->stream, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            const int64_t l0 = h->launches;
+            ok = issue_newton_iteration(h, hc);
+            h->launches = l0;
+            // kernels of one iteration outside the Krylov loop: two time
+            // stamps, prepare, element (+2 order-fixed gathers), block
+            // inverse, the multigrid refresh (3), the solver's start (CG with
+            // multigrid: init, a V-cycle, rz), the loop arm, |du|, the Newton
+            // test and the update
+            const bool mg = use_multigrid(h);
+            h->nloop_kernels = 2 + 2 + (h->opt.deterministic ? 2 : 0) + 1 + (mg ? 3 : 0) +
+                               (h->method == 1 && mg ? 2 + amg_vcycle_kernels(h) : 1) + 1 + 3;
+            cudaGraph_t out = nullptr;
+            ok = (cudaStreamEndCapture(h->stream, &out) == cudaSuccess) && ok;
+        }
+    }
+    if (ok) ok = cudaGraphInstantiate(&h->nloop, g, 0) == cudaSuccess;
+    cudaGraphDestroy(g);
+    if (!ok) {
+        h->nloop = nullptr;
+        (void)cudaGetLastError();
+    }
+    return ok;
+}
+
+}  // namespace
+
+tf_status newton_device_loop(tf_handle* h, int* it, int* cv, int* capped, int* k, tf_step_stats* st, float* ms_asm,
+                             bool* ran, bool* exc) {
+    Device& d = h->d;
+    *ran = false;
+    *exc = false;
+    // the device loop covers the plain path: no packing, no bound DOFs, no
+    // checked build (those keep host work between the iterations)
+#ifdef TF_CHECKED
+    return TF_OK;
+#endif
+    if (h->nloop_off || h->pk || !h->bind_slave.empty() || h->kloop_off) return TF_OK;
+    if (!h->kloop_ctl) {
+        TF_CUDA(cudaMalloc(&h->kloop_ctl, 2 * sizeof(int)));
+        TF_CUDA(cudaMallocHost(&h->kloop_host, sizeof(int)));
+    }
+    if (!h->nd) {
+        TF_CUDA(cudaMalloc(&h->nd, sizeof(NewtonDev)));
+        TF_CUDA(cudaMallocHost(&h->nd_host, sizeof(NewtonDev)));
+        TF_CUDA(cudaMalloc(&h->nd_seg, 3 * sizeof(int) * (size_t)d.nseg));
+        TF_CUDA(cudaMallocHost(&h->nd_seg_host, 3 * sizeof(int) * (size_t)d.nseg));
+    }
+    if (!h->cap_stream) TF_CUDA(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
+    if (h->nloop && h->nloop_dt != h->dt) {
+        cudaGraphExecDestroy(h->nloop);
+        h->nloop = nullptr;
+    }
+    if (!h->nloop) {
+        if (!build_newton_loop(h)) {
+            h->nloop_off = true;
+            return TF_OK;
+        }
+        h->nloop_dt = h->dt;
+    }
+    // state in: the host's per-instance bookkeeping and mask
+    NewtonDev& nh = *h->nd_host;
+    std::memset(&nh, 0, sizeof(NewtonDev));
+    nh.k = *k;
+    int* sh = h->nd_seg_host;
+    for (int g = 0; g < d.nseg; ++g) {
+        sh[g] = it[g];
+        sh[d.nseg + g] = cv[g];
+        sh[2 * d.nseg + g] = capped[g];
+    }
+    TF_CUDA(cudaMemcpyAsync(h->nd, h->nd_host, sizeof(NewtonDev), cudaMemcpyHostToDevice, h->stream));
+    TF_CUDA(cudaMemcpyAsync(h->nd_seg, sh, 3 * sizeof(int) * (size_t)d.nseg, cudaMemcpyHostToDevice, h->stream));
+    TF_CUDA(cudaMemcpyAsync(d.seg_active, h->h_active.data(), sizeof(int) * (size_t)d.nseg, cudaMemcpyHostToDevice,
+                            h->stream));
+    TF_CUDA(cudaGraphLaunch(h->nloop, h->stream));
+    TF_CUDA(cudaMemcpyAsync(h->nd_host, h->nd, sizeof(NewtonDev), cudaMemcpyDeviceToHost, h->stream));
+    TF_CUDA(cudaMemcpyAsync(sh, h->nd_seg, 3 * sizeof(int) * (size_t)d.nseg, cudaMemcpyDeviceToHost, h->stream));
+    TF_CUDA(cudaMemcpyAsync(h->h_active.data(), d.seg_active, sizeof(int) * (size_t)d.nseg, cudaMemcpyDeviceToHost,
+                            h->stream));
+    TF_CUDA(cudaStreamSynchronize(h->stream));
+    // state out
+    *ran = true;
+    *exc = nh.exc != 0;
+    for (int g = 0; g < d.nseg; ++g) {
+        it[g] = sh[g];
+        cv[g] = sh[d.nseg + g];
+        capped[g] = sh[2 * d.nseg + g];
+    }
+    for (int j = *k; j < std::min(nh.k, 32); ++j) st->dunorm[j] = nh.dunorm[j];
+    const int done = nh.k - *k;
+    *k = nh.k;
+    st->device_iters += done;
+    st->krylov_iters_total += nh.krylov_total;
+    st->krylov_iters_max = std::max(st->krylov_iters_max, nh.krylov_max);
+    *ms_asm += (float)(nh.t_asm * 1e-6);
+    // kernels the graph ran: the fixed ones of each Newton iteration (an
+    // iteration handed back ran all but the update) and one control kernel
+    // more than the solver's own per Krylov iteration
+    h->launches += (int64_t)(done + (*exc ? 1 : 0)) * h->nloop_kernels +
+                   (int64_t)nh.krylov_total * (kernels_per_iteration(h, h->method) + 1);
+    if (use_multigrid(h)) amg_refreshed(h);
+    h->assembled = true;
+    return TF_OK;
+}
+
 void destroy_graphs(tf_handle* h) {
     for (auto& row : h->graph)
         for (auto& g : row)
@@ -949,6 +1250,10 @@ void destroy_graphs(tf_handle* h) {
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
+    if (h->nloop) {
+        cudaGraphExecDestroy(h->nloop);
+        h->nloop = nullptr;
+    }
 }
 
 }  // namespace tf
