@@ -295,6 +295,7 @@ def run_gpu(args, t):
         step_ms, per_asm = float(v[0]), float(v[1])
         asm_rate = ne * world / (per_asm / 1e3)
 
+    tiles = s.tiles()
     # element-kernel roofline (back-to-back assemblies at the converged state)
     per_asm_ms, elem_ms = s.time_assembly(max(3, args.steps))
     ia, ja, a = s.export_csr(0.0)
@@ -374,6 +375,7 @@ def run_gpu(args, t):
                    "preconditioner": (("plain-aggregation" if args.precond == 3 else "smoothed-aggregation")
                                       + " multigrid " + "/".join(map(str, mg_nodes))) if mg_nodes else "block-Jacobi",
                    "multigrid_blocks": mg_blocks[0] if mg_blocks else None,
+                   "autotuned": tiles,
                    "krylov_iters_per_step": sum(x["krylov_total"] for x in stats) / len(stats),
                    "krylov_iters_by_step": [int(x["krylov_total"]) for x in stats],
                    "newton_iters_by_step": [int(x["iters"]) for x in stats],

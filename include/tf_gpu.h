@@ -278,6 +278,11 @@ TF_API tf_status tf_batch_step(tf_handle* h, double dt, int32_t* newton_iters, i
 TF_API tf_status tf_get_instances(tf_handle* h, int32_t* n_instances, int32_t* node_offsets, int32_t* elem_offsets);
 /* Prisms per CTA of the element kernel chosen by the autotuner (8, 16, 32). */
 TF_API int32_t tf_elements_per_cta(tf_handle* h);
+/* The solve's kernel variants the autotuner chose by timing them on the
+ * handle's own matrix before its first solve: block rows' slots in flight per
+ * lane in the FP64 SpMV (1, 2, 4) and in the multigrid's level-0 smoother
+ * (2, 4, 8; 0 without multigrid).  No reference counterpart. */
+TF_API tf_status tf_solve_variants(tf_handle* h, int32_t* spmv_unroll, int32_t* smoother_unroll);
 
 /* --- inspection (parity tests) ------------------------------------------ */
 

@@ -65,3 +65,23 @@ def test_autotuner_picks_a_valid_tile():
         b.set_growth_rates()
         b.step(60.0)
         assert b.elements_per_cta() in (8, 16, 32)
+
+
+def test_solve_autotuner_picks_valid_variants():
+    """The solve's kernel variants are timed on the handle's own matrix before
+    its first solve (FP64 SpMV: 1, 2 or 4 slots in flight per lane; level-0
+    smoother: 2, 4 or 8) and the solution does not depend on the choice."""
+    t = mesh.config_large(seed=0, cells=40)
+    res = []
+    for autotune in (True, False):
+        with api.Solver(t, precond=2, autotune=autotune) as s:
+            s.set_growth_rates(t.rates)
+            its = [s.newton_step(t.dt)["iters"] for _ in range(2)]
+            v = s.tiles()
+            res.append((its, s.positions()))
+        if autotune:
+            assert v["spmv_unroll"] in (1, 2, 4) and v["smoother_unroll"] in (2, 4, 8), v
+        else:
+            assert v["spmv_unroll"] == 2 and v["smoother_unroll"] == 4, v
+    assert res[0][0] == res[1][0]
+    assert np.abs(res[0][1] - res[1][1]).max() <= 1e-12 * np.abs(res[1][1]).max()

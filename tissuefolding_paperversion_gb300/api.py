@@ -30,6 +30,7 @@ EXPORTED = [
     "tf_get_viscosity_surfaces", "tf_set_viscosity_surfaces", "tf_set_state", "tf_export_csr",
     "tf_element_eval", "tf_get_sizes", "tf_get_stream", "tf_launch_count", "tf_time_assembly",
     "tf_solve_bsr_static", "tf_batch_create", "tf_batch_step", "tf_get_instances", "tf_elements_per_cta",
+    "tf_solve_variants",
     "tf_adj_forward", "tf_adj_backward", "tf_adj_free", "tf_multigrid_info", "tf_multigrid_blocks", "tf_read_mesh_file",
     "tf_write_frame", "tf_add_K_triplets", "tf_set_dof_bindings", "tf_set_packing", "tf_get_packing",
     "tf_packing_masses", "tf_add_uniform_growth", "tf_add_ring_growth", "tf_add_grid_growth",
@@ -134,6 +135,7 @@ def load(build_if_missing: bool = True):
     L.tf_get_instances.argtypes = [vp, ip, vp, vp]
     L.tf_elements_per_cta.restype = i32
     L.tf_elements_per_cta.argtypes = [vp]
+    L.tf_solve_variants.argtypes = [vp, ip, ip]
     L.tf_solve_bsr_static.restype = C.c_int
     L.tf_solve_bsr_static.argtypes = [i32, vp, vp, vp, vp, vp, C.c_double, i32, vp, ip, dp]
     L.tf_adj_forward.restype = C.c_int
@@ -492,6 +494,15 @@ class Solver:
         w = np.zeros(10)
         self._check(self.L.tf_multigrid_info(self.h, C.byref(lv), _ptr(nodes), _ptr(w)), "tf_multigrid_info")
         return nodes[: lv.value].tolist(), w[: lv.value].tolist()
+
+    def tiles(self):
+        """The autotuner's choices: prisms per CTA of the element kernel and
+        the slots in flight per lane of the FP64 SpMV and of the level-0
+        smoother (chosen at the first solve)."""
+        su, mu = C.c_int32(0), C.c_int32(0)
+        self._check(self.L.tf_solve_variants(self.h, C.byref(su), C.byref(mu)), "tf_solve_variants")
+        return {"elements_per_cta": int(self.L.tf_elements_per_cta(self.h)), "spmv_unroll": su.value,
+                "smoother_unroll": mu.value}
 
     def multigrid_blocks(self):
         """(matrix blocks, prolongator blocks) per level of the hierarchy."""

@@ -265,6 +265,7 @@ struct Amg {
     int max_cm = 0;
     int v0_smem = 0;           // shared memory of the level-0 prolongation (3 floats per block of a CTA)
     int tail = 0;              // levels tail..nlev-1 run in one kernel (one CTA per instance); 0: none
+    int smooth_unroll = 4;     // slots in flight per lane in the level-0 smoother's row product (2, 4, 8)
     std::vector<int> h_n;      // nodes per level (host)
     std::vector<int> h_prow[kAmgMaxLevels], h_pcol[kAmgMaxLevels];  // prolongator patterns (host)
     int64_t x_version = -1;    // extra-block layout the coarse extra blocks were built for
@@ -783,6 +784,7 @@ __device__ __forceinline__ void mul3(const float* __restrict__ D, const float r[
 
 // Row of S = D^-1 A (FP16, sliced) times x, FP32 sums; the extra blocks X
 // (FP64) enter as D^-1 (X x).
+template <int U = 4>
 __device__ __forceinline__ void row0s(const Device& d, const __half* __restrict__ valh,
                                       const float* __restrict__ dinv32, const float* __restrict__ x, int i,
                                       float y[3]) {
@@ -793,7 +795,7 @@ __device__ __forceinline__ void row0s(const Device& d, const __half* __restrict_
     const int* __restrict__ col = d.scol + lane;
     const uint4* __restrict__ p8 = reinterpret_cast<const uint4*>(valh) + lane;
     const __half* __restrict__ p1 = valh + (size_t)(d.nval / kSlotDoubles) * (kSlice * 8) + lane;
-#pragma unroll 4
+#pragma unroll U
     for (int s = s0; s < s1; ++s) {
         const int j = __ldg(&col[(size_t)s * kSlice]);
         if (!TF_IN(d.check, j, d.nn, CK_V0_COL)) continue;
@@ -1380,12 +1382,13 @@ __global__ void k_v0_pre(V0 a, const double* __restrict__ r, float* __restrict__
 }
 
 // t = r - A x
+template <int U>
 __global__ void k_v0_resid(V0 a, const double* __restrict__ r, const float* __restrict__ x, float* __restrict__ t) {
     pdl_enter();
     const Node0 q = node0(a.d);
     if (seg_stopped(a.d.scal, q.seg)) return;
     float y[3];
-    if (q.valid) row0s(a.d, a.valh, a.dinv32, x, q.i, y);
+    if (q.valid) row0s<U>(a.d, a.valh, a.dinv32, x, q.i, y);
     if (!q.valid) return;
     // A x = D (S x), D the diagonal block
     const float* __restrict__ Dg = a.diag32 + 9 * (size_t)q.i;
@@ -1396,12 +1399,13 @@ __global__ void k_v0_resid(V0 a, const double* __restrict__ r, const float* __re
 }
 
 // out = x + omega D^-1 (r - A x), written back as the FP64 preconditioned vector
+template <int U>
 __global__ void k_v0_post(V0 a, const double* __restrict__ r, const float* __restrict__ x, double* __restrict__ out) {
     pdl_enter();
     const Node0 q = node0(a.d);
     if (seg_stopped(a.d.scal, q.seg)) return;
     float y[3];
-    if (q.valid) row0s(a.d, a.valh, a.dinv32, x, q.i, y);
+    if (q.valid) row0s<U>(a.d, a.valh, a.dinv32, x, q.i, y);
     if (!q.valid) return;
     // x + omega D^-1 (r - A x) = x + omega (D^-1 r - S x)
     const float om = (float)__ldg(a.omega);
@@ -1804,6 +1808,39 @@ tf_status amg_numeric(tf_handle* h) {
     return TF_OK;
 }
 
+// The level-0 smoother's row product with 2, 4 or 8 slots in flight per
+// lane, timed on the handle's own matrix (k_v0_resid: one residual of the
+// current smoother operator into the level's work vector); called once per
+// handle by the solve autotuner.
+tf_status amg_autotune(tf_handle* h) {
+    Amg* a = h->amg;
+    Device& d = h->d;
+    cudaStream_t st = h->stream;
+    AmgLevel& L0 = a->L[0];
+    V0 v0{d, a->omega, a->dinv32, a->valh, a->diag32};
+    float best = 1e30f;
+    for (int u : {2, 4, 8}) {
+        for (int r = 0; r < 4; ++r) {  // one warm-up, three timed
+            if (r == 1) TF_CUDA(cudaEventRecord(h->ev[4], st));
+            if (u == 2) k_v0_resid<2><<<d.ncta, kNodeThreads, 0, st>>>(v0, d.g, L0.x, L0.t);
+            else if (u == 4) k_v0_resid<4><<<d.ncta, kNodeThreads, 0, st>>>(v0, d.g, L0.x, L0.t);
+            else k_v0_resid<8><<<d.ncta, kNodeThreads, 0, st>>>(v0, d.g, L0.x, L0.t);
+            TF_LAUNCH_CHECK(h);
+        }
+        TF_CUDA(cudaEventRecord(h->ev[5], st));
+        TF_CUDA(cudaEventSynchronize(h->ev[5]));
+        float ms = 0.f;
+        TF_CUDA(cudaEventElapsedTime(&ms, h->ev[4], h->ev[5]));
+        if (ms < best) {
+            best = ms;
+            a->smooth_unroll = u;
+        }
+    }
+    return TF_OK;
+}
+
+int amg_smoother_unroll(const tf_handle* h) { return h->amg ? h->amg->smooth_unroll : 0; }
+
 int amg_vcycle_kernels(const tf_handle* h) {
     const Amg* a = h->amg;
     const int per = 2 * kCoarseSweeps + 2;  // kernels of a coarse level run kernel by kernel
@@ -1824,7 +1861,11 @@ void amg_vcycle(tf_handle* h, const double* r, double* out) {
     AmgLevel& L0 = a->L[0];
     auto presmooth = [&](int l) { return (l < nl - 1 || !a->coarse_exact) ? 1 : 0; };
     launch_pdl(k_v0_pre, d.ncta, kNodeThreads, st, v0, r, L0.x);
-    launch_pdl(k_v0_resid, d.ncta, kNodeThreads, st, v0, r, L0.x, L0.t);
+    switch (a->smooth_unroll) {
+        case 2: launch_pdl(k_v0_resid<2>, d.ncta, kNodeThreads, st, v0, r, L0.x, L0.t); break;
+        case 8: launch_pdl(k_v0_resid<8>, d.ncta, kNodeThreads, st, v0, r, L0.x, L0.t); break;
+        default: launch_pdl(k_v0_resid<4>, d.ncta, kNodeThreads, st, v0, r, L0.x, L0.t); break;
+    }
     launch_pdl(k_restrict<3>, cdiv(32 * (int64_t)a->L[1].n, kT), kT, st, L0, a->L[1], (const float*)L0.t,
                (const double*)d.scal, (const double*)(a->omega + 1), presmooth(1));
     float* cur[kAmgMaxLevels] = {};
@@ -1879,7 +1920,11 @@ void amg_vcycle(tf_handle* h, const double* r, double* out) {
     }
     launch_pdl_smem(k_v0_prolong, d.ncta, kNodeThreads, (size_t)a->v0_smem, st, v0, L0, (const float*)a->L[1].e,
                     L0.x);
-    launch_pdl(k_v0_post, d.ncta, kNodeThreads, st, v0, r, L0.x, out);
+    switch (a->smooth_unroll) {
+        case 2: launch_pdl(k_v0_post<2>, d.ncta, kNodeThreads, st, v0, r, L0.x, out); break;
+        case 8: launch_pdl(k_v0_post<8>, d.ncta, kNodeThreads, st, v0, r, L0.x, out); break;
+        default: launch_pdl(k_v0_post<4>, d.ncta, kNodeThreads, st, v0, r, L0.x, out); break;
+    }
 }
 
 }  // namespace tf

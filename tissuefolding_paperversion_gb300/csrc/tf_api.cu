@@ -1375,6 +1375,13 @@ tf_status tf_get_instances(tf_handle* h, int32_t* n_instances, int32_t* node_off
 
 int32_t tf_elements_per_cta(tf_handle* h) { return h ? h->elem_cta : 0; }
 
+tf_status tf_solve_variants(tf_handle* h, int32_t* spmv_unroll, int32_t* smoother_unroll) {
+    TF_TRY(check_handle(h));
+    if (spmv_unroll) *spmv_unroll = h->spmv_unroll;
+    if (smoother_unroll) *smoother_unroll = amg_smoother_unroll(h);
+    return TF_OK;
+}
+
 tf_status tf_destroy(tf_handle* h) {
     if (!h) return TF_OK;
     cudaSetDevice(h->device);

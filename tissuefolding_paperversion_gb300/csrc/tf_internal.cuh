@@ -328,7 +328,7 @@ inline void launch_pdl(void (*kernel)(KArgs...), int grid, int block, cudaStream
 // of kNodeThreads); the warp walks its slots together, each lane reading
 // its own row's block, so every load of a block entry or column is one
 // coalesced access.
-template <class T>
+template <class T, int U = 2>
 __device__ __forceinline__ void sliced_row(const int* __restrict__ wslot0, const int* __restrict__ scol,
                                            const T* __restrict__ val, const double* __restrict__ x, double y[3],
                                            int nn = 0, int* check = nullptr) {
@@ -338,7 +338,7 @@ __device__ __forceinline__ void sliced_row(const int* __restrict__ wslot0, const
     double y0 = 0.0, y1 = 0.0, y2 = 0.0;
     const int* __restrict__ col = scol + lane;
     const T* __restrict__ a = val + lane;
-#pragma unroll 2
+#pragma unroll U
     for (int s = s0; s < s1; ++s) {
         const int j = __ldg(&col[(size_t)s * kSlice]);
         if (!TF_IN(check, j, nn, CK_SPMV_COL)) continue;
@@ -403,6 +403,8 @@ struct tf_handle {
     int* kloop_ctl = nullptr;                   // device: [iterations run, iteration cap]
     int* kloop_host = nullptr;                  // pinned copy of the iterations run
     int last_iters[2] = {0, 0};                 // iterations of the last solve per method (chunk planning)
+    bool solve_tuned = false;                   // the solve's kernel variants below were chosen by timing
+    int spmv_unroll = 2;                        // slots in flight per lane in the FP64 block SpMV (1, 2, 4)
     int plan_iters[2][8] = {};                  // the same per Newton iteration of a step (0-6, 7: later ones)
     int newton_index = -1;                      // Newton iteration of the current solve (-1: outside a step)
     tf::Amg* amg = nullptr;                     // multigrid preconditioner (null: block-Jacobi)
@@ -451,6 +453,8 @@ tf_status autotune_element(tf_handle* h);
 tf_status amg_build(tf_handle* h, const double* ref_pos);
 tf_status amg_numeric(tf_handle* h);
 void amg_refresh(tf_handle* h);     // launches the level-0 smoother copies of the current assembly
+tf_status amg_autotune(tf_handle* h);  // picks the level-0 smoother's row-product variant by timing
+int amg_smoother_unroll(const tf_handle* h);
 void amg_refreshed(tf_handle* h);   // records that amg_refresh ran for the current assembly
 void amg_vcycle(tf_handle* h, const double* r, double* out);
 int amg_vcycle_kernels(const tf_handle* h);

@@ -135,8 +135,9 @@ __device__ __forceinline__ void apply_dinv(const double* __restrict__ D, const d
     z[2] = fma(D[6], r[0], fma(D[7], r[1], D[8] * r[2]));
 }
 
+template <int U = 2>
 __device__ __forceinline__ void bsr_row(const Ctx& c, int i, const double* __restrict__ x, double y[3]) {
-    sliced_row(c.wslot0, c.scol, c.val, x, y, c.nn, c.check);
+    sliced_row<double, U>(c.wslot0, c.scol, c.val, x, y, c.nn, c.check);
     if (c.xrow) {
         for (int p = c.xrow[i]; p < c.xrow[i + 1]; ++p) {
             const int j = c.xcol[p];
@@ -216,6 +217,7 @@ __global__ void k_cg_init(Ctx c, const double* __restrict__ b, double* __restric
 }
 
 // q = A p; alpha = rz / (p, q)
+template <int U>
 __global__ void k_cg_spmv(Ctx c, const double* __restrict__ p, double* __restrict__ q) {
     pdl_enter();
     const Where w = where(c);
@@ -223,7 +225,7 @@ __global__ void k_cg_spmv(Ctx c, const double* __restrict__ p, double* __restric
     double v[1] = {0.0};
     if (w.valid) {
         double y[3];
-        bsr_row(c, w.node, p, y);
+        bsr_row<U>(c, w.node, p, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             q[3 * w.node + d] = y[d];
@@ -392,6 +394,7 @@ __global__ void k_bi_dir(Ctx c, const double* __restrict__ r, const double* __re
 }
 
 // v = A phat; alpha = rho / (rhat, v)
+template <int U>
 __global__ void k_bi_spmv1(Ctx c, const double* __restrict__ phat, const double* __restrict__ rhat,
                            double* __restrict__ v) {
     pdl_enter();
@@ -400,7 +403,7 @@ __global__ void k_bi_spmv1(Ctx c, const double* __restrict__ phat, const double*
     double s[1] = {0.0};
     if (w.valid) {
         double y[3];
-        bsr_row(c, w.node, phat, y);
+        bsr_row<U>(c, w.node, phat, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             v[3 * w.node + d] = y[d];
@@ -476,6 +479,7 @@ __global__ void k_bi_half(Ctx c, double* __restrict__ x, const double* __restric
 }
 
 // t = A shat; omega = (t, s) / (t, t)
+template <int U>
 __global__ void k_bi_spmv2(Ctx c, const double* __restrict__ shat, const double* __restrict__ s,
                            double* __restrict__ t) {
     pdl_enter();
@@ -484,7 +488,7 @@ __global__ void k_bi_spmv2(Ctx c, const double* __restrict__ shat, const double*
     double acc[2] = {0.0, 0.0};
     if (w.valid) {
         double y[3];
-        bsr_row(c, w.node, shat, y);
+        bsr_row<U>(c, w.node, shat, y);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             t[3 * w.node + d] = y[d];
@@ -632,14 +636,15 @@ Ctx make_ctx(tf_handle* h) {
 }
 
 // Issues n iterations of `method` on the stream (no host interaction).
-void issue_iterations(tf_handle* h, const Ctx& c, int method, int n) {
+template <int U>
+void issue_iterations_u(tf_handle* h, const Ctx& c, int method, int n) {
     Device& d = h->d;
     cudaStream_t st = h->stream;
     const int nb = d.ncta;
     const int jac = use_multigrid(h) ? 0 : 1;
     for (int it = 0; it < n; ++it) {
         if (method == 1) {
-            launch_pdl(k_cg_spmv, nb, kThreads, st, c, d.p, d.q);
+            launch_pdl(k_cg_spmv<U>, nb, kThreads, st, c, d.p, d.q);
             launch_pdl(k_cg_update, nb, kThreads, st, c, d.du, d.r, d.z, d.p, d.q, jac);
             if (!jac) {
                 amg_vcycle(h, d.r, d.z);
@@ -649,14 +654,71 @@ void issue_iterations(tf_handle* h, const Ctx& c, int method, int n) {
         } else {
             launch_pdl(k_bi_dir, nb, kThreads, st, c, d.r, d.q, d.p, d.z, jac);
             if (!jac) amg_vcycle(h, d.p, d.z);
-            launch_pdl(k_bi_spmv1, nb, kThreads, st, c, d.z, d.rhat, d.q);
+            launch_pdl(k_bi_spmv1<U>, nb, kThreads, st, c, d.z, d.rhat, d.q);
             launch_pdl(k_bi_s, nb, kThreads, st, c, d.r, d.q, d.s, d.sh, d.du, d.z, jac);
             if (!jac) amg_vcycle(h, d.s, d.sh);
             launch_pdl(k_bi_half, nb, kThreads, st, c, d.du, d.z);
-            launch_pdl(k_bi_spmv2, nb, kThreads, st, c, d.sh, d.s, d.t);
+            launch_pdl(k_bi_spmv2<U>, nb, kThreads, st, c, d.sh, d.s, d.t);
             launch_pdl(k_bi_x, nb, kThreads, st, c, d.du, d.r, d.rhat, d.z, d.sh, d.s, d.t);
         }
     }
+}
+
+void issue_iterations(tf_handle* h, const Ctx& c, int method, int n) {
+    switch (h->spmv_unroll) {
+        case 1: issue_iterations_u<1>(h, c, method, n); break;
+        case 4: issue_iterations_u<4>(h, c, method, n); break;
+        default: issue_iterations_u<2>(h, c, method, n); break;
+    }
+}
+
+// y = A x alone (no dot, no flags): the SpMV variants the solve autotuner times
+template <int U>
+__global__ void k_spmv_probe(Ctx c, const double* __restrict__ x, double* __restrict__ y) {
+    const Where w = where(c);
+    if (!w.valid) return;
+    double v[3];
+    bsr_row<U>(c, w.node, x, v);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) y[3 * w.node + d] = v[d];
+}
+
+// Picks the solve's kernel variants by timing them on the handle's own
+// matrix, once per handle before its first solve builds any graph: the
+// FP64 block SpMV with 1, 2 or 4 slots in flight per lane, and (multigrid)
+// the level-0 smoother's row product with 2, 4 or 8.  Results do not depend
+// on the choice (the same products in the same order).
+tf_status autotune_solve(tf_handle* h) {
+    if (h->solve_tuned) return TF_OK;
+    h->solve_tuned = true;
+    if (h->opt.autotune_off) return TF_OK;
+    Device& d = h->d;
+    const Ctx c = make_ctx(h);
+    cudaStream_t st = h->stream;
+    // every instance "running" while the variants are timed (the solver's
+    // start writes all the scalars afterwards; nothing is kept across solves
+    // before the first one)
+    TF_CUDA(cudaMemsetAsync(d.scal, 0, sizeof(double) * (size_t)d.nseg * S_COUNT, st));
+    float best = 1e30f;
+    for (int u : {1, 2, 4}) {
+        for (int r = 0; r < 4; ++r) {  // one warm-up, three timed
+            if (r == 1) TF_CUDA(cudaEventRecord(h->ev[4], st));
+            if (u == 1) k_spmv_probe<1><<<d.ncta, kThreads, 0, st>>>(c, d.du, d.q);
+            else if (u == 2) k_spmv_probe<2><<<d.ncta, kThreads, 0, st>>>(c, d.du, d.q);
+            else k_spmv_probe<4><<<d.ncta, kThreads, 0, st>>>(c, d.du, d.q);
+            TF_LAUNCH_CHECK(h);
+        }
+        TF_CUDA(cudaEventRecord(h->ev[5], st));
+        TF_CUDA(cudaEventSynchronize(h->ev[5]));
+        float ms = 0.f;
+        TF_CUDA(cudaEventElapsedTime(&ms, h->ev[4], h->ev[5]));
+        if (ms < best) {
+            best = ms;
+            h->spmv_unroll = u;
+        }
+    }
+    if (use_multigrid(h)) return amg_autotune(h);
+    return TF_OK;
 }
 
 int kernels_per_iteration(const tf_handle* h, int method) {
@@ -766,6 +828,10 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
         if (use_multigrid(h)) {
             const tf_status sa = amg_numeric(h);
             if (sa != TF_OK) return sa;
+        }
+        {
+            const tf_status su = autotune_solve(h);  // once per handle, before any graph captures the choice
+            if (su != TF_OK) return su;
         }
         if (method == 1) {
             k_cg_init<<<d.ncta, kThreads, 0, st>>>(c, d.g, d.du, d.r, d.z, d.p, tol2, h->solve_atol, keep, jac);
