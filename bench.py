@@ -380,6 +380,7 @@ def run_gpu(args, t):
                    "krylov_iters_by_step": [int(x["krylov_total"]) for x in stats],
                    "newton_iters_by_step": [int(x["iters"]) for x in stats],
                    "device_loop_iters_by_step": [int(x.get("device_iters", 0)) for x in stats],
+                   "device_loop_handback_by_step": [int(x.get("device_handback", 0)) for x in stats],
                    "ms_by_step": [round(float(x["ms_total"]), 3) for x in stats],
                    "ms_assembly": ms_asm / n_asm, "wall_s": wall},
         "e2e": {"value": ne / e2e_s, "unit": "prisms/s", "h2d_bytes_per_step": 2 * 8 * 3 * nn,
@@ -529,7 +530,7 @@ def run_batch(args):
     }))
 
 
-def adjoint_measure(t, n, every, fd_dirs, seed=1234):
+def adjoint_measure(t, n, every, fd_dirs, seed=1234, fd_h6=0):
     """Adjoint of n implicit steps: loss = squared distance of the final
     apical surface to z = 5 exp(-r^2 / (2 40^2)) um (r from the sheet
     centre), gradient with respect to the per-element growth rates and log E;
@@ -596,19 +597,31 @@ def adjoint_measure(t, n, every, fd_dirs, seed=1234):
                 h = 1e-4
                 f = (lossf(rate, logE + h * d) - lossf(rate, logE - h * d)) / (2 * h)
                 adj = float(gt_e @ d)
+            c6 = {}
+            if k < fd_h6:
+                # the same direction at h = 1e-6 relative (rates: 1e-6 x the
+                # largest rate; log E: 1e-6), where the loss's rounding shows
+                h6 = (1e-6 * np.abs(rate).max()) if k % 2 == 0 else 1e-6
+                if k % 2 == 0:
+                    f6 = (lossf(rate + h6 * d, logE) - lossf(rate - h6 * d, logE)) / (2 * h6)
+                else:
+                    f6 = (lossf(rate, logE + h6 * d) - lossf(rate, logE - h6 * d)) / (2 * h6)
+                c6 = {"fd_h1e-6": f6, "rel_h1e-6": abs(adj - f6) / max(abs(f6), 1e-300)}
             checks.append({"parameter": "rate" if k % 2 == 0 else "logE", "adjoint": adj, "fd": f,
-                           "rel": abs(adj - f) / max(abs(f), 1e-300)})
+                           "rel": abs(adj - f) / max(abs(f), 1e-300), **c6})
         ts.close()
         out["fd"] = {"directions": fd_dirs, "h": "rates: 1e-3 x the largest rate; log E: 1e-4",
                      "solves": "Newton |du| <= 1e-11, Krylov relative residual 1e-13",
                      "max_rel_err": max(c["rel"] for c in checks), "checks": checks}
+        if fd_h6:
+            out["fd"]["max_rel_err_h1e-6"] = max(c["rel_h1e-6"] for c in checks if "rel_h1e-6" in c)
     return out
 
 
 def run_adjoint(args, t):
     """The adjoint workload on its own (see adjoint_measure)."""
     n, every = args.adj_steps, args.adj_every
-    r = adjoint_measure(t, n, every, args.adj_fd)
+    r = adjoint_measure(t, n, every, args.adj_fd, fd_h6=args.adj_fd_h6)
     print(json.dumps({
         "metric": "adjoint backward / forward cost", "value": r["backward_over_forward"], "unit": "ratio",
         "n_gpus": 1, "steps": n, "warmup": 1, "ms_per_step": (r["forward_s"] + r["backward_s"]) / n * 1e3,
@@ -795,6 +808,8 @@ def main():
     ap.add_argument("--adj-steps", type=int, default=50)
     ap.add_argument("--adj-every", type=int, default=10)
     ap.add_argument("--adj-fd", type=int, default=0, help="central-difference checks along random directions")
+    ap.add_argument("--adj-fd-h6", type=int, default=0,
+                    help="of those directions, how many are also differenced at h = 1e-6 relative")
     ap.add_argument("--instances", type=int, default=256)
     ap.add_argument("--mode", default="step", choices=["step", "assembly"],
                     help="step: Newton steps (the bench); assembly: back-to-back K+f assemblies only")

@@ -86,8 +86,9 @@ typedef struct tf_options {
                                 relative residual at most 0.1); late Newton iterations, whose
                                 update is orders of magnitude below newton_tol, then need a few
                                 Krylov iterations instead of a full solve.  Such a solve never
-                                decides the Newton test alone: when its |du| lies within a factor 2
-                                of newton_tol the system is solved again to krylov_rtol first.
+                                decides the Newton test alone: when its |du| lies within
+                                max(1e3 update_atol, 1e-3 newton_tol) of newton_tol the system is
+                                solved again to krylov_rtol first.
                                 0: newton_tol x 1e-4; negative: off (every solve to krylov_rtol).
                                 tf_solve ignores it. */
 } tf_options;
@@ -105,6 +106,10 @@ typedef struct tf_step_stats {
     float ms_total;             /* device time of the whole step */
     int32_t device_iters;       /* Newton iterations run by the device-side loop (one graph launch for the
                                    iterations after the step's first; the rest ran host-driven) */
+    int32_t device_handback;    /* why that loop handed an iteration back to the host: 0 it did not,
+                                   1 a loosened solve's |du| near newton_tol, 3 a non-finite update,
+                                   10 + the Krylov flag (11 converged is not used, 12 breakdown, 13 NaN,
+                                   10 still running at the iteration cap) for a solve that did not converge */
 } tf_step_stats;
 
 TF_API const char* tf_status_string(tf_status s);

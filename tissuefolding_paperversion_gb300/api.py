@@ -77,7 +77,7 @@ class tf_step_stats(C.Structure):
     _fields_ = [("newton_iters", C.c_int32), ("krylov_iters_total", C.c_int32), ("krylov_iters_max", C.c_int32),
                 ("converged", C.c_int32), ("dunorm", C.c_double * 32), ("final_relres", C.c_double),
                 ("ms_assemble", C.c_float), ("ms_solve", C.c_float), ("ms_total", C.c_float),
-                ("device_iters", C.c_int32)]
+                ("device_iters", C.c_int32), ("device_handback", C.c_int32)]
 
 
 _lib = None
@@ -434,7 +434,8 @@ class Solver:
         return {"status": s, "iters": n, "dunorm": np.array(st.dunorm[: min(n, 32)]),
                 "krylov_total": st.krylov_iters_total, "krylov_max": st.krylov_iters_max,
                 "converged": bool(st.converged), "relres": st.final_relres, "ms_assemble": st.ms_assemble,
-                "ms_solve": st.ms_solve, "ms_total": st.ms_total, "device_iters": st.device_iters}
+                "ms_solve": st.ms_solve, "ms_total": st.ms_total, "device_iters": st.device_iters,
+                "device_handback": st.device_handback}
 
     # -- inspection ---------------------------------------------------------
     def residual(self):
@@ -596,7 +597,7 @@ class Batch(Solver):
         s = self._check(self.L.tf_batch_step(self.h, dt, _ptr(iters), _ptr(conv), C.byref(st)), "tf_batch_step", allow)
         return {"status": s, "iters": iters, "converged": conv.astype(bool), "krylov_total": st.krylov_iters_total,
                 "ms_total": st.ms_total, "ms_assemble": st.ms_assemble, "newton_rounds": st.newton_iters,
-                "device_iters": st.device_iters}
+                "device_iters": st.device_iters, "device_handback": st.device_handback}
 
     def instance_positions(self, i):
         p = self.positions()

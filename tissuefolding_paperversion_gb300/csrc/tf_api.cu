@@ -615,8 +615,8 @@ tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* ite
         st.krylov_iters_max = std::max(st.krylov_iters_max, kit);
         // |du| before the update is applied.  An inexact solve must not decide
         // the Newton test: when a solve stopped at the update accuracy (a stop
-        // test looser than krylov_rtol) and |du| lands within a factor 2 of
-        // newton_tol, the active instances are solved again to krylov_rtol.
+        // test looser than krylov_rtol) and |du| lands near newton_tol
+        // (near_newton_tol), the active instances are solved again to krylov_rtol.
         TF_TRY(launch_update_norm(h));
         TF_CUDA(cudaMemcpy2DAsync(du2.data(), sizeof(double), d.scal + S_DU2, sizeof(double) * S_COUNT,
                                   sizeof(double), d.nseg, cudaMemcpyDeviceToHost, h->stream));
@@ -627,8 +627,8 @@ tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* ite
             for (int g = 0; g < d.nseg && !redo; ++g) {
                 if (!h->h_active[g]) continue;
                 const double dn = std::sqrt(du2[g]);
-                redo = d.host_scal[(size_t)g * S_COUNT + S_TOL2] > rt2 && dn > 0.5 * h->opt.newton_tol &&
-                       dn < 2.0 * h->opt.newton_tol;
+                redo = d.host_scal[(size_t)g * S_COUNT + S_TOL2] > rt2 &&
+                       near_newton_tol(dn, h->opt.newton_tol, h->opt.update_atol);
             }
             if (redo) {
                 int kit2 = 0;

@@ -179,6 +179,16 @@ struct NewtonDev {
     double dunorm[32];         // largest |du| over the instances, per Newton iteration
 };
 
+// A Newton update from a solve stopped at the update accuracy atol (looser
+// than krylov_rtol) whose norm dn lies this close to newton_tol is solved
+// again to krylov_rtol before the Newton test: the band is a thousand times
+// the accuracy asked of the update (at least 1e-3 of the tolerance), so the
+// loosening cannot move |du| across the tolerance unnoticed.
+__host__ __device__ __forceinline__ bool near_newton_tol(double dn, double tol, double atol) {
+    const double band = fmax(1e3 * atol, 1e-3 * tol);
+    return fabs(dn - tol) <= band;
+}
+
 // Inverse of a 3x3 matrix (row-major) by cofactors.
 __device__ __forceinline__ void inv3_cof(const double* M, double* inv) {
     const double c0 = M[4] * M[8] - M[5] * M[7];

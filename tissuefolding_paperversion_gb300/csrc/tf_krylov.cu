@@ -1034,7 +1034,7 @@ __global__ void k_stamp_end(NewtonDev* nd) { nd->t_asm += global_ns() - nd->t0; 
 __global__ void __launch_bounds__(256) k_newton_ctl(const double* __restrict__ scal, int nseg,
                                                     int* __restrict__ active, int* __restrict__ it,
                                                     int* __restrict__ cv, int* __restrict__ capped, NewtonDev* nd,
-                                                    double tol, double rtol2, int max_iter, int loosened,
+                                                    double tol, double rtol2, int max_iter, double atol,
                                                     cudaGraphConditionalHandle loop) {
     __shared__ int exc, any;
     __shared__ double dmax;
@@ -1050,13 +1050,17 @@ __global__ void __launch_bounds__(256) k_newton_ctl(const double* __restrict__ s
         if (!active[g]) continue;
         const double* s = scal + (size_t)g * S_COUNT;
         const double dn = sqrt(__ldcg(&s[S_DU2]));
-        const bool near = loosened && __ldcg(&s[S_TOL2]) > rtol2 && dn > 0.5 * tol && dn < 2.0 * tol;
-        if (__ldcg(&s[S_FLAG]) != F_CONVERGED || !isfinite(dn) || near) atomicExch(&exc, 1);
+        const bool near = atol > 0.0 && __ldcg(&s[S_TOL2]) > rtol2 && near_newton_tol(dn, tol, atol);
+        // reason: 1 a loosened solve near newton_tol, 2 a solve that did not
+        // converge (flag 2 + the solver's flag), 3 a non-finite update
+        const double fl = __ldcg(&s[S_FLAG]);
+        const int why = !isfinite(dn) ? 3 : (fl != F_CONVERGED ? 2 : (near ? 1 : 0));
+        if (why) atomicMax(&exc, why == 2 ? 10 + (int)fl : why);
     }
     __syncthreads();
     if (exc) {
         if (threadIdx.x == 0) {
-            nd->exc = 1;
+            nd->exc = exc;
             cudaGraphSetConditional(loop, 0u);
         }
         return;
@@ -1176,8 +1180,7 @@ bool issue_newton_iteration(tf_handle* h, cudaGraphConditionalHandle newton) {
     k_update<false><<<d.ncta, kThreads, 0, st>>>(c, d.uk, d.du);
     int* seg = h->nd_seg;
     k_newton_ctl<<<1, 256, 0, st>>>(d.scal, d.nseg, d.seg_active, seg, seg + d.nseg, seg + 2 * d.nseg, h->nd,
-                                     h->opt.newton_tol, tol2, h->opt.newton_max_iter, h->opt.update_atol > 0.0 ? 1 : 0,
-                                     newton);
+                                     h->opt.newton_tol, tol2, h->opt.newton_max_iter, h->opt.update_atol, newton);
     k_update<true><<<d.ncta, kThreads, 0, st>>>(c, d.uk, d.du, &h->nd->exc);
     return cudaGetLastError() == cudaSuccess;
 }
@@ -1282,6 +1285,7 @@ tf_status newton_device_loop(tf_handle* h, int* it, int* cv, int* capped, int* k
     // state out
     *ran = true;
     *exc = nh.exc != 0;
+    st->device_handback = nh.exc;
     for (int g = 0; g < d.nseg; ++g) {
         it[g] = sh[g];
         cv[g] = sh[d.nseg + g];
