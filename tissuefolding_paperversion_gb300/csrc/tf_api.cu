@@ -122,6 +122,9 @@ void free_all(tf_handle* h) {
     if (h->kloop_host) cudaFreeHost(h->kloop_host);
     h->kloop_ctl = nullptr;
     h->kloop_host = nullptr;
+    if (h->du0) cudaFree(h->du0);
+    h->du0 = nullptr;
+    h->have_du0 = false;
     if (h->nd) cudaFree(h->nd);
     if (h->nd_host) cudaFreeHost(h->nd_host);
     if (h->nd_seg) cudaFree(h->nd_seg);
@@ -641,6 +644,12 @@ tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* ite
                                           sizeof(double), d.nseg, cudaMemcpyDeviceToHost, h->stream));
                 TF_TRY(sync(h));
             }
+        }
+        if (k == 0) {  // the start of the next step's first solve
+            if (!h->du0) TF_CUDA(cudaMalloc(&h->du0, sizeof(double) * 3 * (size_t)d.nn));
+            TF_CUDA(cudaMemcpyAsync(h->du0, d.du, sizeof(double) * 3 * (size_t)d.nn, cudaMemcpyDeviceToDevice,
+                                    h->stream));
+            h->have_du0 = true;
         }
         TF_TRY(launch_update(h));
         double dmax = 0.0;

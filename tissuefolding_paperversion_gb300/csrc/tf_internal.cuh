@@ -417,6 +417,8 @@ struct tf_handle {
     int spmv_unroll = 2;                        // slots in flight per lane in the FP64 block SpMV (1, 2, 4)
     int plan_iters[2][8] = {};                  // the same per Newton iteration of a step (0-6, 7: later ones)
     int newton_index = -1;                      // Newton iteration of the current solve (-1: outside a step)
+    double* du0 = nullptr;                      // the first Newton update of the last step (start of the next)
+    bool have_du0 = false;
     tf::Amg* amg = nullptr;                     // multigrid preconditioner (null: block-Jacobi)
     tf::Packing* pk = nullptr;                  // packing between tissue surfaces (null: off)
     tf::Growth* growth = nullptr;               // growth functions (null: none added yet)
