@@ -599,17 +599,19 @@ tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* ite
     float ms_asm = 0.f;
     int k = 0;
     bool device_tried = false;
+    bool assembled_tight = false;  // the device loop handed back an assembled iteration to solve tightly
     while (true) {
         TF_CUDA(cudaEventRecord(h->ev[2], h->stream));
-        TF_TRY(tf_assemble(h));
+        if (!assembled_tight) TF_TRY(tf_assemble(h));
         TF_CUDA(cudaEventRecord(h->ev[3], h->stream));
         int kit = 0;
         double rr = 0.0;
-        h->solve_atol = h->opt.update_atol;
+        h->solve_atol = assembled_tight ? 0.0 : h->opt.update_atol;
         h->newton_index = k;
         tf_status s = tf_solve(h, &kit, &rr);
         h->solve_atol = 0.0;
         h->newton_index = -1;
+        assembled_tight = false;
         if (s != TF_OK && s != TF_KRYLOV_NOT_CONVERGED) return s;
         float ms = 0.f;
         TF_CUDA(cudaEventElapsedTime(&ms, h->ev[2], h->ev[3]));
@@ -682,6 +684,9 @@ tf_status newton_run(tf_handle* h, double dt, tf_step_stats* stats, int32_t* ite
             bool ran = false, exc = false;
             TF_TRY(newton_device_loop(h, it.data(), cv.data(), capped.data(), &k, &st, &ms_asm, &ran, &exc));
             if (ran && !exc) break;
+            // handed back because a loosened solve's |du| came near newton_tol:
+            // the iteration's assembly is in place, only its solve is redone
+            if (ran && st.device_handback == 1) assembled_tight = true;
         }
     }
     std::fill(h->h_active.begin(), h->h_active.end(), 1);

@@ -1068,10 +1068,13 @@ __global__ void __launch_bounds__(256) k_newton_ctl(const double* __restrict__ s
         const double fl = __ldcg(&s[S_FLAG]);
         const int why = !isfinite(dn) ? 3 : (fl != F_CONVERGED ? 2 : (near ? 1 : 0));
         if (why) atomicMax(&exc, why == 2 ? 10 + (int)fl : why);
+        atomicMax(&kmax, (int)__ldcg(&s[S_ITER]));
     }
     __syncthreads();
     if (exc) {
         if (threadIdx.x == 0) {
+            nd->krylov_total += kmax;  // the handed-back iteration's solve ran too
+            nd->krylov_max = max(nd->krylov_max, kmax);
             nd->exc = exc;
             cudaGraphSetConditional(loop, 0u);
         }
@@ -1081,7 +1084,6 @@ __global__ void __launch_bounds__(256) k_newton_ctl(const double* __restrict__ s
         if (!active[g]) continue;
         const double* s = scal + (size_t)g * S_COUNT;
         const double dn = sqrt(__ldcg(&s[S_DU2]));
-        atomicMax(&kmax, (int)__ldcg(&s[S_ITER]));
         // dn >= 0: the bit patterns of non-negative doubles order like the values
         atomicMax(reinterpret_cast<unsigned long long*>(&dmax), (unsigned long long)__double_as_longlong(dn));
         it[g] += 1;
