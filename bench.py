@@ -262,7 +262,7 @@ def run_gpu(args, t):
         import torch.distributed as dist  # noqa: F811
 
         dist.init_process_group("gloo")
-    s = api.Solver(t, device=local if world > 1 else 0, precond=args.precond)
+    s = api.Solver(t, device=local if world > 1 else 0, precond=args.precond, host_loops=args.host_loops)
     s.set_growth_rates(t.rates)
     nn, ne, nnzb = s.sizes()
     mg_nodes, _ = s.multigrid_info()
@@ -835,6 +835,9 @@ def main():
                     help="0 auto (smoothed-aggregation multigrid from 20,000 nodes), 1 block-Jacobi, "
                          "2 smoothed-aggregation multigrid, 3 plain-aggregation multigrid")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--host-loops", action="store_true",
+                    help="host-checked Krylov chunks and host-driven Newton iterations instead of the device-side "
+                         "while loops (ncu cannot see kernels inside conditional graph nodes)")
     args = ap.parse_args()
     from tissuefolding_paperversion_gb300 import mesh
 

@@ -91,6 +91,10 @@ typedef struct tf_options {
                                 solved again to krylov_rtol first.
                                 0: newton_tol x 1e-4; negative: off (every solve to krylov_rtol).
                                 tf_solve ignores it. */
+    int32_t host_loops;      /* 1: the Krylov iterations run as host-checked CUDA-graph chunks and
+                                every Newton iteration is host-driven, instead of the device-side
+                                while loops (for profilers that cannot see kernels inside conditional
+                                graph nodes); same results.  No reference counterpart. */
 } tf_options;
 
 /* Statistics of one time step (tf_newton_step). */

@@ -58,3 +58,19 @@ def test_packing_keeps_the_host_loop():
         out = s.newton_step(t.dt)
         assert out["device_iters"] == 0
         assert out["iters"] >= 2
+
+
+def test_host_loops_option_gives_the_same_steps():
+    """tf_options.host_loops (host-checked Krylov chunks, host-driven Newton
+    iterations: what a profiler that cannot see inside conditional graph nodes
+    needs) takes the same Newton steps."""
+    t = mesh.config_large(seed=0, cells=40)
+    res = []
+    for host in (False, True):
+        with api.Solver(t, precond=2, host_loops=host) as s:
+            s.set_growth_rates(t.rates)
+            outs = [s.newton_step(t.dt) for _ in range(2)]
+            res.append(([o["iters"] for o in outs], s.positions(), [o["device_iters"] for o in outs]))
+    assert res[0][0] == res[1][0]
+    assert res[1][2] == [0, 0] and all(d > 0 for d in res[0][2])
+    assert np.abs(res[0][1] - res[1][1]).max() <= 1e-12 * np.abs(res[1][1]).max()

@@ -873,6 +873,7 @@ tf_status krylov_run(tf_handle* h, int method, int keep, int* iters, double* rel
     int launched = 0, ci = 1;
     int planned = (keep == 0) ? (prev * 7) / 8 : 0;
     bool done = false, fixed = planned > 0;
+    if (h->opt.host_loops) h->kloop_off = true;
     if (!h->kloop_off && !h->kloop_ctl) {
         TF_CUDA(cudaMalloc(&h->kloop_ctl, 2 * sizeof(int)));
         TF_CUDA(cudaMallocHost(&h->kloop_host, sizeof(int)));
@@ -1255,7 +1256,7 @@ tf_status newton_device_loop(tf_handle* h, int* it, int* cv, int* capped, int* k
 #ifdef TF_CHECKED
     return TF_OK;
 #endif
-    if (h->nloop_off || h->pk || !h->bind_slave.empty() || h->kloop_off) return TF_OK;
+    if (h->nloop_off || h->pk || !h->bind_slave.empty() || h->kloop_off || h->opt.host_loops) return TF_OK;
     if (!h->kloop_ctl) {
         TF_CUDA(cudaMalloc(&h->kloop_ctl, 2 * sizeof(int)));
         TF_CUDA(cudaMallocHost(&h->kloop_host, sizeof(int)));
