@@ -25,7 +25,9 @@ Reported (one JSON line on rank 0):
                against the plain GPU step looped over a stratified subset
   adjoint      gradient through 50 steps of the 320k-prism sheet
                (checkpoints every 10): backward / forward cost, and the
-               gradient against central differences along seeded directions
+               gradient against central differences along seeded directions;
+               fd_32_directions: 32 directions, 4-point differences, on a
+               3,200-prism sheet of the same kind (50 steps)
 (`--quick` leaves the last three out.)
 
 `--impl reference` times the CPU implementation alone on the same metric:
@@ -360,6 +362,7 @@ def run_gpu(args, t):
     adjoint = None
     if not args.quick and world == 1:
         adjoint = adjoint_measure(t, args.adj_steps, args.adj_every, args.adj_fd_default)
+        adjoint["fd_32_directions"] = adjoint_fd_sheet()
     # the read and copy bandwidth this GPU gives kernels of the library (the
     # denominators of the solve's read-bound kernels)
     hbm_probe = api.measure_bandwidth(local if world > 1 else 0)
@@ -626,6 +629,58 @@ def adjoint_measure(t, n, every, fd_dirs, seed=1234, fd_h6=0, fd_order4=False):
         if fd_h6:
             out["fd"]["max_rel_err_h1e-6"] = max(c["rel_h1e-6"] for c in checks if "rel_h1e-6" in c)
     return out
+
+
+def adjoint_fd_sheet(cells=20, n=50, every=10, dirs=32, h=1e-2, seed=4321):
+    """The adjoint against central differences along `dirs` seeded
+    directions, alternating growth rates and log E, on a 20 x 20-cell sheet
+    of the 320k-prism sheet's kind (4 layers, 3,200 prisms, log-normal E,
+    internal viscosity 100, Gaussian growth bump) with the same loss, 50
+    steps and checkpoints every 10.  Every solve is tight (Newton |du| <=
+    1e-11, Krylov 1e-13, multigrid) and assembly deterministic.  A converged
+    forward run is a function of its parameters only to ~1e-12 in the
+    positions (the Newton test stops at |du| <= 1e-11), which 2-point
+    differences at h = 1e-6 amplify to up to ~1e-4 of the derivative along
+    log E; fourth-order differences at h = 1e-2 (rates: 1e-2 x the largest
+    rate) bring that noise to ~1e-8 with O(h^4) truncation."""
+    from tissuefolding_paperversion_gb300 import api, mesh
+
+    t = mesh.config_large(seed=7, cells=cells)
+    xy = t.pos.reshape(-1, 3)[:, :2]
+    c = 0.5 * (xy.min(axis=0) + xy.max(axis=0))
+    params = np.array([c[0], c[1], 5.0, 40.0])
+    rate = t.rates.reshape(-1, 3)[:, 0].copy()
+    logE = np.log(t.E)
+    w0 = time.perf_counter()
+    with api.Solver(t, newton_tol=1e-11, krylov_rtol=1e-13, deterministic=True, precond=2) as s:
+        def lossf(r, e):
+            s.set_positions(t.pos)
+            lv, sp = s.adjoint_forward(r, e, n, t.dt, every, params)
+            sp.free()
+            return lv
+
+        s.set_positions(t.pos)
+        loss, sv = s.adjoint_forward(rate, logE, n, t.dt, every, params)
+        gr, ge = s.adjoint_backward(sv)
+        sv.free()
+        rng = np.random.default_rng(seed)
+        rel = []
+        for k in range(dirs):
+            d = rng.standard_normal(t.n_elems)
+            if k % 2 == 0:
+                hr = h * np.abs(rate).max()
+                f = lambda a: lossf(rate + a * hr * d, logE)
+                scale, adj = hr, float(gr @ d)
+            else:
+                f = lambda a: lossf(rate, logE + a * h * d)
+                scale, adj = h, float(ge @ d)
+            fd = (-f(2) + 8 * f(1) - 8 * f(-1) + f(-2)) / (12 * scale)
+            rel.append(abs(adj - fd) / max(abs(fd), 1e-300))
+    return {"prisms": t.n_elems, "steps": n, "checkpoint_every": every, "directions": dirs,
+            "h": f"{h:g} (rates: {h:g} x the largest rate), 4-point central",
+            "solves": "Newton |du| <= 1e-11, Krylov relative residual 1e-13, multigrid, deterministic assembly",
+            "loss": loss, "max_rel_err": max(rel), "median_rel_err": float(np.median(rel)),
+            "rel_err_rate": rel[0::2], "rel_err_logE": rel[1::2], "wall_s": time.perf_counter() - w0}
 
 
 def run_adjoint(args, t):

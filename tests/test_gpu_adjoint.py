@@ -67,6 +67,49 @@ def test_adjoint_matches_central_differences(eta, n, every):
                 assert abs(adj - fd) <= TOL_GRAD * abs(fd), (which, adj, fd)
 
 
+def test_adjoint_matches_central_differences_32_directions():
+    """32 seeded directions (16 along the growth rates, 16 along log E) on a
+    3,200-prism sheet of the 320k-prism sheet's kind (log-normal E, internal
+    viscosity 100, Gaussian growth bump), 20 steps, checkpoints every 5,
+    multigrid solves.  Fourth-order central differences at h = 1e-2 (rates:
+    1e-2 x the largest rate): a converged forward run is a function of its
+    parameters only to ~1e-12 in the positions (Newton stops at |du| <=
+    1e-11), which 2-point differences at h = 1e-6 amplify to ~1e-4 of the
+    derivative along log E; at h = 1e-2 that noise is ~1e-8 and the
+    truncation O(h^4)."""
+    t = mesh.config_large(seed=7, cells=20)
+    xy = t.pos.reshape(-1, 3)[:, :2]
+    c = 0.5 * (xy.min(axis=0) + xy.max(axis=0))
+    params = np.array([c[0], c[1], 5.0, 40.0])
+    rate = t.rates.reshape(-1, 3)[:, 0].copy()
+    logE = np.log(t.E)
+    n, every, h = 20, 5, 1e-2
+    rng = np.random.default_rng(4321)
+    with api.Solver(t, newton_tol=1e-11, krylov_rtol=1e-13, deterministic=True, precond=2) as s:
+        _, saved = _loss(s, t, rate, logE, n, every, params)
+        gr, ge = s.adjoint_backward(saved)
+        saved.free()
+
+        def lossf(r, e):
+            lv, sp = _loss(s, t, r, e, n, every, params)
+            sp.free()
+            return lv
+
+        errs = []
+        for k in range(32):
+            d = rng.standard_normal(t.n_elems)
+            if k % 2 == 0:
+                hr = h * np.abs(rate).max()
+                f = lambda a: lossf(rate + a * hr * d, logE)
+                scale, adj = hr, gr @ d
+            else:
+                f = lambda a: lossf(rate, logE + a * h * d)
+                scale, adj = h, ge @ d
+            fd = (-f(2) + 8 * f(1) - 8 * f(-1) + f(-2)) / (12 * scale)
+            errs.append(abs(adj - fd) / abs(fd))
+    assert max(errs) <= TOL_GRAD, errs
+
+
 def test_adjoint_gradient_is_independent_of_checkpoint_spacing():
     t, rate, logE, params = _tissue(100.0, seed=9)
     out = []
