@@ -274,8 +274,7 @@ def run_gpu(args, t):
         if dist is not None:
             dist.barrier()
 
-    for _ in range(args.warmup):
-        s.newton_step(t.dt)
+    wstats = [s.newton_step(t.dt) for _ in range(args.warmup)]
     barrier()
     l0 = s.launch_count()
     clocks = Clocks(local)
@@ -385,7 +384,10 @@ def run_gpu(args, t):
                    "device_loop_iters_by_step": [int(x.get("device_iters", 0)) for x in stats],
                    "device_loop_handback_by_step": [int(x.get("device_handback", 0)) for x in stats],
                    "ms_by_step": [round(float(x["ms_total"]), 3) for x in stats],
-                   "ms_assembly": ms_asm / n_asm, "wall_s": wall},
+                   "ms_assembly": ms_asm / n_asm, "wall_s": wall,
+                   "warmup_steps": {"krylov_iters_by_step": [int(x["krylov_total"]) for x in wstats],
+                                    "newton_iters_by_step": [int(x["iters"]) for x in wstats],
+                                    "ms_by_step": [round(float(x["ms_total"]), 3) for x in wstats]}},
         "e2e": {"value": ne / e2e_s, "unit": "prisms/s", "h2d_bytes_per_step": 2 * 8 * 3 * nn,
                 "d2h_bytes_per_step": 8 * 3 * nn},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
