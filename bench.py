@@ -264,7 +264,8 @@ def run_gpu(args, t):
         import torch.distributed as dist  # noqa: F811
 
         dist.init_process_group("gloo")
-    s = api.Solver(t, device=local if world > 1 else 0, precond=args.precond, host_loops=args.host_loops)
+    s = api.Solver(t, device=local if world > 1 else 0, precond=args.precond, host_loops=args.host_loops,
+                   multigrid_reuse_steps=args.mg_reuse)
     s.set_growth_rates(t.rates)
     nn, ne, nnzb = s.sizes()
     mg_nodes, _ = s.multigrid_info()
@@ -378,6 +379,7 @@ def run_gpu(args, t):
                                       + " multigrid " + "/".join(map(str, mg_nodes))) if mg_nodes else "block-Jacobi",
                    "multigrid_blocks": mg_blocks[0] if mg_blocks else None,
                    "autotuned": tiles,
+                   "multigrid_reuse_steps": args.mg_reuse if args.mg_reuse else 4,
                    "krylov_iters_per_step": sum(x["krylov_total"] for x in stats) / len(stats),
                    "krylov_iters_by_step": [int(x["krylov_total"]) for x in stats],
                    "newton_iters_by_step": [int(x["iters"]) for x in stats],
@@ -892,6 +894,10 @@ def main():
                     help="0 auto (smoothed-aggregation multigrid from 20,000 nodes), 1 block-Jacobi, "
                          "2 smoothed-aggregation multigrid, 3 plain-aggregation multigrid")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mg-reuse", type=int, default=0,
+                    help="plain workload: keep the multigrid's coarse levels for up to this many steps "
+                         "(tf_options.multigrid_reuse_steps; 0: the library's default, 4; negative: "
+                         "rebuild at every step)")
     ap.add_argument("--host-loops", action="store_true",
                     help="host-checked Krylov chunks and host-driven Newton iterations instead of the device-side "
                          "while loops (ncu cannot see kernels inside conditional graph nodes)")

@@ -95,6 +95,16 @@ typedef struct tf_options {
                                 every Newton iteration is host-driven, instead of the device-side
                                 while loops (for profilers that cannot see kernels inside conditional
                                 graph nodes); same results.  No reference counterpart. */
+    int32_t multigrid_reuse_steps; /* multigrid only: the coarse levels (aggregates' prolongators,
+                                Galerkin operators, smoother weights) built at a time step's first
+                                solve are kept for up to k further time steps, the level-0 smoother
+                                always using the current matrix; they are rebuilt at the next step
+                                once a step's first solve needs more than 1.25 x (+2) the Krylov
+                                iterations of the first solve after the last rebuild, and at once
+                                when a solve with kept levels does not converge.  Changes Krylov
+                                counts only (every solve meets the same tolerance).  0: the default,
+                                k = 4; negative: rebuilt at every time step.  No reference
+                                counterpart. */
 } tf_options;
 
 /* Statistics of one time step (tf_newton_step). */

@@ -123,3 +123,20 @@ def test_multigrid_adjoint_matches_central_differences():
         b.free()
         fd = (lp - lm) / (2 * h)
         assert abs(ge @ d - fd) <= 1e-6 * abs(fd)
+
+
+def test_kept_coarse_levels_keep_the_newton_steps():
+    """tf_options.multigrid_reuse_steps: coarse levels kept across time steps
+    (the default, 4 steps, and 2) change the Krylov counts only -- the Newton
+    counts and the positions (1e-8 relative) are those of a rebuild at every
+    step (negative)."""
+    t = mesh.config_large(seed=3, cells=40)
+    res = []
+    for keep in (-1, 0, 2):
+        with api.Solver(t, precond=2, multigrid_reuse_steps=keep) as s:
+            s.set_growth_rates(t.rates)
+            outs = [s.newton_step(t.dt) for _ in range(7)]
+            res.append(([o["iters"] for o in outs], s.positions()))
+    for its, pos in res[1:]:
+        assert its == res[0][0]
+        assert np.abs(pos - res[0][1]).max() <= 1e-8 * np.abs(res[0][1]).max()

@@ -70,7 +70,7 @@ class tf_options(C.Structure):
     _fields_ = [("newton_tol", C.c_double), ("newton_max_iter", C.c_int32), ("krylov_rtol", C.c_double),
                 ("krylov_max_iter", C.c_int32), ("krylov_method", C.c_int32), ("deterministic", C.c_int32),
                 ("device", C.c_int32), ("autotune_off", C.c_int32), ("precond", C.c_int32),
-                ("update_atol", C.c_double), ("host_loops", C.c_int32)]
+                ("update_atol", C.c_double), ("host_loops", C.c_int32), ("multigrid_reuse_steps", C.c_int32)]
 
 
 class tf_step_stats(C.Structure):
@@ -224,7 +224,7 @@ class Solver:
 
     def __init__(self, tissue, newton_tol=1e-8, newton_max_iter=20, krylov_rtol=1e-8, krylov_max_iter=20000,
                  krylov_method=0, deterministic=False, device=0, autotune=True, precond=0, update_atol=0.0,
-                 host_loops=False):
+                 host_loops=False, multigrid_reuse_steps=0):
         self.L = load()
         t = tissue
         self.t = t
@@ -232,7 +232,7 @@ class Solver:
         self._arrays, m, mat = _mesh_structs(t)
         opt = tf_options(newton_tol, newton_max_iter, krylov_rtol, krylov_max_iter, krylov_method,
                          1 if deterministic else 0, device, 0 if autotune else 1, precond, update_atol,
-                         1 if host_loops else 0)
+                         1 if host_loops else 0, multigrid_reuse_steps)
         h = C.c_void_p()
         self._check(self.L.tf_create(C.byref(m), C.byref(mat), C.byref(opt), C.byref(h)), "tf_create")
         self.h = h
@@ -562,7 +562,7 @@ class Batch(Solver):
 
     def __init__(self, tissues, newton_tol=1e-8, newton_max_iter=20, krylov_rtol=1e-8, krylov_max_iter=20000,
                  krylov_method=0, deterministic=False, device=0, autotune=True, precond=0, update_atol=0.0,
-                 host_loops=False):
+                 host_loops=False, multigrid_reuse_steps=0):
         self.L = load()
         self.tissues = list(tissues)
         n = len(self.tissues)
@@ -575,7 +575,7 @@ class Batch(Solver):
         self._arrays = keep
         opt = tf_options(newton_tol, newton_max_iter, krylov_rtol, krylov_max_iter, krylov_method,
                          1 if deterministic else 0, device, 0 if autotune else 1, precond, update_atol,
-                         1 if host_loops else 0)
+                         1 if host_loops else 0, multigrid_reuse_steps)
         h = C.c_void_p()
         self._check(self.L.tf_batch_create(meshes, mats, n, C.byref(opt), C.byref(h)), "tf_batch_create")
         self.h = h

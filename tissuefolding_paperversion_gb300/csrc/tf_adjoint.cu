@@ -431,6 +431,18 @@ tf_status adj_backward(tf_handle* h, tf_adjoint* a, double dloss, double* grad_r
     return TF_OK;
 }
 
+// The adjoint's forward runs, and the steps its backward pass recomputes,
+// rebuild the multigrid's coarse levels at every time step (as a handle with
+// multigrid_reuse_steps < 0 does) for the scope of the call.
+struct CoarseRebuiltEachStep {
+    tf_handle* h;
+    int keep;
+    explicit CoarseRebuiltEachStep(tf_handle* hh) : h(hh), keep(hh->opt.multigrid_reuse_steps) {
+        h->opt.multigrid_reuse_steps = 0;
+    }
+    ~CoarseRebuiltEachStep() { h->opt.multigrid_reuse_steps = keep; }
+};
+
 }  // namespace
 
 extern "C" {
@@ -463,6 +475,7 @@ TF_API tf_status tf_adj_forward(tf_handle* h, const double* rate, const double* 
     a->dt = dt;
     a->device = h->device;
     std::memcpy(a->params, loss_params, sizeof(a->params));
+    CoarseRebuiltEachStep rebuilt(h);
     const tf_status s = adj_forward(h, a, rate, logE);
     if (s != TF_OK && s != TF_NOT_CONVERGED) {
         tf_adj_free(a);
@@ -483,6 +496,7 @@ TF_API tf_status tf_adj_backward(tf_handle* h, tf_adjoint* a, double dloss, doub
         return TF_BAD_INPUT;
     }
     TF_CUDA(cudaSetDevice(h->device));
+    CoarseRebuiltEachStep rebuilt(h);
     return adj_backward(h, a, dloss, grad_rate, grad_logE);
 }
 

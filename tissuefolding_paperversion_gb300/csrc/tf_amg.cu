@@ -273,6 +273,7 @@ struct Amg {
     // level-0 matrix (new assembly, same time step), 2 the whole hierarchy
     int stale = 2;
     bool reused = false;       // the last numeric phase kept the coarse levels
+    long rebuilds = 0;         // full numeric rebuilds so far
 };
 
 void amg_free(Amg* a) {
@@ -1686,6 +1687,8 @@ void amg_mark_stale(tf_handle* h, int level) {
 
 bool amg_reused(const tf_handle* h) { return h->amg && h->amg->reused; }
 
+long amg_rebuilds(const tf_handle* h) { return h->amg ? h->amg->rebuilds : 0; }
+
 bool use_multigrid(const tf_handle* h) { return h->amg != nullptr; }
 
 // Numeric phase for the current matrix.  Within a time step the matrix of
@@ -1731,6 +1734,7 @@ tf_status amg_numeric(tf_handle* h) {
         a->stale = 0;
         return TF_OK;
     }
+    ++a->rebuilds;
     if (a->x_version != h->extra_version) AMG_TRY(amg_extra_symbolic(h));
     // level by level: smoother weight from lambda_max(D^-1 A) (the
     // prolongator smoothing uses it too), prolongator, Galerkin product

@@ -384,6 +384,9 @@ struct tf_handle {
     std::vector<int> bind_slave, bind_master;   // bound DOF couples (NRSolver::slaveMasterList)
     bool bound_applied = false;                 // the couples are applied to the current assembly
     double solve_atol = 0.0;                    // absolute update accuracy of the current solve (0: off)
+    int mg_kept = 0;                            // time steps since the multigrid's last full rebuild
+    int mg_ref_iters = -1;                      // Krylov iterations of the first solve after that rebuild
+    bool mg_force = false;                      // rebuild the coarse levels at the next time step
     tf::BindPlan* bind = nullptr;               // device program of the couples' row/column merges
     std::vector<double> h_xval;                 // their values of the current assembly
     int64_t extra_version = 0;                  // changes with every new extra-block layout
@@ -504,6 +507,7 @@ tf_status sync_extra_to_host(tf_handle* h);      // device extra-block values ->
 void bind_free(tf_handle* h);                     // releases the bound-DOF plan
 tf_status take_check(tf_handle* h);              // checked build: report and clear a failed index check
 bool amg_reused(const tf_handle* h);
+long amg_rebuilds(const tf_handle* h);  // full numeric rebuilds so far
 tf_status launch_adjoint_element(tf_handle* h, const double* lamv, double* carry, double* gr, double* ge, double ndt);
 void destroy_graphs(tf_handle* h);
 
