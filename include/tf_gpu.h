@@ -102,9 +102,11 @@ typedef struct tf_options {
                                 once a step's first solve needs more than 1.25 x (+2) the Krylov
                                 iterations of the first solve after the last rebuild, and at once
                                 when a solve with kept levels does not converge.  Changes Krylov
-                                counts only (every solve meets the same tolerance).  0: the default,
-                                k = 4; negative: rebuilt at every time step.  No reference
-                                counterpart. */
+                                counts only (every solve meets the same tolerance).  tf_set_Fg and
+                                tf_set_dof_bindings drop kept levels; tf_set_positions does not.
+                                The adjoint (tf_adj_forward, tf_adj_backward) rebuilds at every
+                                step.  0: the default, k = 4; negative: rebuilt at every time step.
+                                No reference counterpart. */
 } tf_options;
 
 /* Statistics of one time step (tf_newton_step). */

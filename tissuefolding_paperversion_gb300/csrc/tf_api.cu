@@ -1207,6 +1207,7 @@ tf_status tf_set_dof_bindings(tf_handle* h, int32_t n, const int32_t* slave_dofs
     h->bind_master.assign(master_dofs, master_dofs + n);
     h->bound_applied = false;
     bind_free(h);
+    amg_mark_stale(h, 2);  // a new operator: no kept coarse levels
     return TF_OK;
 }
 
@@ -1453,6 +1454,7 @@ tf_status tf_set_Fg(tf_handle* h, const double* Fg) {
     }
     TF_CUDA(cudaMemcpyAsync(h->d.Fg, f.data(), f.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     TF_CUDA(cudaMemcpyAsync(h->d.invFg, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    amg_mark_stale(h, 2);  // the tangent may differ from the kept coarse levels' by more than a step's change
     return sync(h);
 }
 
