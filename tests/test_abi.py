@@ -2,6 +2,7 @@
 include/tf_gpu.h declares; argument validation needs no GPU."""
 import os
 import re
+import ctypes as C
 import subprocess
 
 import numpy as np
@@ -58,3 +59,30 @@ def test_status_strings():
     L = api.load()
     for code in range(9):
         assert L.tf_status_string(code)
+
+
+def test_ctypes_structs_match_the_header_layout(tmp_path):
+    """Every field of the structs the C ABI takes (tf_mesh, tf_material,
+    tf_options, tf_step_stats) sits at the offset the header gives it, and the
+    sizes agree: a probe compiled against include/tf_gpu.h prints them."""
+    structs = [api.tf_mesh, api.tf_material, api.tf_options, api.tf_step_stats]
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "tf_gpu.h"', "int main(void) {"]
+    for s in structs:
+        n = s.__name__
+        lines.append(f'  printf("{n} size %zu\\n", sizeof({n}));')
+        for f, _ in s._fields_:
+            lines.append(f'  printf("{n} {f} %zu\\n", offsetof({n}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        *key, v = line.split()
+        got[tuple(key)] = int(v)
+    for s in structs:
+        n = s.__name__
+        assert got[(n, "size")] == C.sizeof(s), n
+        for f, _ in s._fields_:
+            assert got[(n, f)] == getattr(s, f).offset, (n, f)
