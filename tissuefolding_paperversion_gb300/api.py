@@ -217,10 +217,16 @@ def _mesh_structs(t):
 
 
 class Solver:
-    """One GPU Newton solver over one tissue (a ``tf_handle``).  ``precond``:
-    0 auto (smoothed-aggregation multigrid from 20,000 nodes on, else
-    block-Jacobi), 1 block-Jacobi, 2 smoothed-aggregation multigrid,
-    3 plain-aggregation multigrid."""
+    """One GPU Newton solver over one tissue (a ``tf_handle``).  The keyword
+    arguments are the fields of ``tf_options``.  ``precond``: 0 auto
+    (smoothed-aggregation multigrid from 20,000 nodes on, else block-Jacobi),
+    1 block-Jacobi, 2 smoothed-aggregation multigrid, 3 plain-aggregation
+    multigrid.  ``update_atol``: the absolute accuracy a Newton update needs
+    (0: newton_tol x 1e-4, negative: every solve to krylov_rtol).
+    ``host_loops``: host-driven Newton iterations and host-checked Krylov
+    chunks instead of the device-side loops (same results).
+    ``multigrid_reuse_steps``: time steps the multigrid's coarse levels are
+    kept for (0: the default, 4; negative: rebuilt at every step)."""
 
     def __init__(self, tissue, newton_tol=1e-8, newton_max_iter=20, krylov_rtol=1e-8, krylov_max_iter=20000,
                  krylov_method=0, deterministic=False, device=0, autotune=True, precond=0, update_atol=0.0,
